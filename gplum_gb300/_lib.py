@@ -1,0 +1,70 @@
+"""Loads the in-tree GB300 library and declares its C ABI (include/*.h)."""
+import ctypes
+import os
+
+from . import build as _build
+
+_HOST = None
+
+VP = ctypes.c_void_p
+I = ctypes.c_int
+D = ctypes.c_double
+
+# name -> (restype, argtypes); every symbol declared in include/gplum_p3t.h
+# and include/p3t_tree.h
+SIGNATURES = {
+    # include/p3t_tree.h
+    "p3t_tree_build": (VP, [I, VP, VP, VP, D, I, I]),
+    "p3t_tree_status": (I, [VP]),
+    "p3t_tree_counts": (None, [VP, VP]),
+    "p3t_tree_export": (None, [VP, VP, VP, VP, VP, VP, VP, VP]),
+    "p3t_tree_free": (None, [VP]),
+    # include/gplum_p3t.h
+    "p3t_init": (I, [I]),
+    "p3t_finalize": (I, []),
+    "p3t_set_params": (I, [VP]),
+    "p3t_set_options": (I, [I, I, I]),
+    "p3t_stream": (VP, []),
+    "p3t_synchronize": (I, []),
+    "p3t_epep": (I, [VP, I, VP, I, VP]),
+    "p3t_epsp": (I, [VP, I, VP, I, VP]),
+    "p3t_soft_dispatch": (I, [I, I, VP, VP, VP, VP, VP, VP]),
+    "p3t_soft_retrieve": (I, [I, I, VP, VP]),
+    "p3t_soft_dispatch_index": (I, [I, I, VP, VP, VP, VP, VP, VP, VP, I, VP, I, I]),
+    "p3t_upload_particles": (I, [I, VP]),
+    "p3t_upload_lists": (I, [I, VP, VP, VP, VP, VP, VP, VP, I]),
+    "p3t_soft_run": (I, [I]),
+    "p3t_download_forces": (I, [VP, I]),
+    "p3t_status": (I, []),
+    "p3t_soft_force_host": (I, [I, VP, I, VP, VP, VP, VP, VP, VP, VP, I, VP]),
+}
+
+
+def lib_path():
+    return _build.LIB
+
+
+def host_lib(build_if_missing=True):
+    """The library handle.  Loading needs no GPU; compute calls do."""
+    global _HOST
+    if _HOST is not None:
+        return _HOST
+    path = lib_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise FileNotFoundError(path)
+        _build.build()
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name, None)
+        if fn is None:
+            continue
+        fn.restype = res
+        fn.argtypes = args
+    _HOST = lib
+    return lib
+
+
+def check(status, what):
+    if status != 0:
+        raise RuntimeError(f"{what} failed with status {status}")

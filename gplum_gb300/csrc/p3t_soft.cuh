@@ -1,0 +1,41 @@
+// Soft-force kernel interface (device side of p3t_soft_* in include/gplum_p3t.h).
+#pragma once
+#include "p3t_common.cuh"
+
+namespace p3t {
+
+struct SoftArgs {
+    // CSR lists (see include/p3t_tree.h)
+    const int *i_off, *i_idx, *j_off, *j_idx, *s_off, *s_idx;
+    const int *group_order;  // optional launch order of groups (nullptr = 0..n_group-1)
+    int n_group;
+    // particles and superparticles: i_idx indexes iptcl, j_idx indexes ptcl
+    // (the same array in the device-resident form)
+    const SoftPtcl *iptcl;
+    const double *i_r_out, *i_r_search;     // FP64 copies (FP64 form)
+    int n_iptcl;
+    const SoftPtcl *ptcl;
+    const double *mass, *r_out, *r_search;  // FP64 copies (FP64 form)
+    int n_ptcl;
+    const SPJRec *spj;
+    int n_spj;
+    // parameters
+    float eps2;
+    double eps2_d;
+    int trace_mode;  // 0: xx+yy+xx (default GPLUM build), 1: xx+yy+zz (PIKG spec)
+    int accumulate;  // 1: add into existing ForceGrav records, 0: overwrite
+    // outputs
+    ForceRec *force;  // indexed like iptcl
+    D4 *acc64;   // FP64 form only: {ax, ay, az, phi}, indexed like iptcl
+    int *cand;        // optional [n_iptcl x cand_cap] table of j indices
+    int cand_cap;
+    int *status;
+};
+
+cudaError_t launch_pack_epj(const EPJRec *in, int n, SoftPtcl *out, double *mass, double *r_out, double *r_search,
+                            cudaStream_t st);
+cudaError_t launch_pack_epi(const EPIRec *in, int n, SoftPtcl *out, double *r_out, double *r_search, cudaStream_t st);
+cudaError_t launch_iota(int *out, int n, int base, cudaStream_t st);
+cudaError_t launch_soft(const SoftArgs &A, int precision, bool emit, cudaStream_t st);
+
+}  // namespace p3t

@@ -1,0 +1,218 @@
+"""ctypes harness over the two CPU checkers.  TEST INFRASTRUCTURE ONLY.
+
+``CpuSystem("orc")`` drives the CPU restatement (oracle/_build/libp3t_oracle.so,
+built by oracle/Makefile on any machine); ``CpuSystem("ref")`` drives GPLUM's
+own headers compiled against the PS shim (oracle/_ref/libgplum_ref.so, only
+where the reference tree was present at build time).  Both expose the same
+surface, so a test runs one scenario through either and compares.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline legs import
+this module.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "libp3t_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libgplum_ref.so")
+REF_SRC = "/root/reference/src"
+
+F64P = ctypes.POINTER(ctypes.c_double)
+I32P = ctypes.POINTER(ctypes.c_int)
+I64P = ctypes.POINTER(ctypes.c_longlong)
+VP = ctypes.c_void_p
+
+# field codes of *_get_f64 / *_get_i64
+VEC_FIELDS = {"pos": 0, "vel": 1, "acc": 2, "acc_d": 3, "jerk_d": 4, "acc_s": 5, "jerk_s": 6}
+SCALAR_FIELDS = {"phi": 10, "phi_d": 11, "phi_s": 12, "mass": 13, "r_out": 14, "r_search": 15,
+                 "dt": 16, "acc0": 17, "time": 18, "r_planet": 19, "v_disp": 20, "r_out_inv": 21}
+INT_FIELDS = {"id": 0, "id_cluster": 1, "number": 2, "n_cluster": 3, "dead": 4, "merged": 5,
+              "rank": 6, "id_min": 7, "id_max": 8}
+
+
+def build_oracle(with_ref=None):
+    """Compiles the restatement (always) and the reference build (when the
+    reference tree exists).  Quick: two translation units."""
+    subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+    if with_ref is None:
+        with_ref = os.path.isdir(REF_SRC)
+    if with_ref:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_SRC={REF_SRC}"], check=True)
+
+
+def ref_available():
+    return os.path.exists(REF_SO)
+
+
+def _ptr(a, t):
+    return a.ctypes.data_as(t)
+
+
+_LIBS = {}
+
+
+def load(kind):
+    if kind in _LIBS:
+        return _LIBS[kind]
+    path = ORACLE_SO if kind == "orc" else REF_SO
+    if not os.path.exists(path):
+        raise FileNotFoundError(path)
+    lib = ctypes.CDLL(path)
+    p = kind + "_"
+    for name, res in [("cutoff_W", ctypes.c_double), ("cutoff_K", ctypes.c_double),
+                      ("cutoff_dKdt", ctypes.c_double), ("solve_kepler", ctypes.c_double),
+                      ("n", ctypes.c_int), ("n_pairs", ctypes.c_int), ("hard", ctypes.c_int),
+                      ("n_cluster", ctypes.c_int), ("n_isolated", ctypes.c_int),
+                      ("n_list_size", ctypes.c_int), ("n_ngb_tot", ctypes.c_int),
+                      ("n_with_ngb", ctypes.c_int)]:
+        getattr(lib, p + name).restype = res
+    getattr(lib, p + "cutoff_W").argtypes = [ctypes.c_double, ctypes.c_double]
+    getattr(lib, p + "cutoff_K").argtypes = [ctypes.c_double, ctypes.c_double]
+    getattr(lib, p + "cutoff_dKdt").argtypes = [ctypes.c_double] * 3
+    getattr(lib, p + "solve_kepler").argtypes = [ctypes.c_double] * 2
+    _LIBS[kind] = lib
+    return lib
+
+
+class CpuSystem:
+    """One particle system inside a checker library (process-global state)."""
+
+    def __init__(self, kind, params):
+        self.kind = kind
+        self.lib = load(kind)
+        self.params = params
+        self.f("set_params")(_ptr(np.ascontiguousarray(params.vector()), F64P))
+
+    def f(self, name):
+        return getattr(self.lib, f"{self.kind}_{name}")
+
+    def load(self, disk):
+        n = len(disk["mass"])
+        self._keep = [np.ascontiguousarray(disk[k]) for k in ("id", "mass", "r_planet", "f", "pos", "vel")]
+        idv, m, rp, f, pos, vel = self._keep
+        self.f("load")(ctypes.c_int(n), _ptr(idv.astype(np.int64), I64P), _ptr(m, F64P), _ptr(rp, F64P),
+                       _ptr(f, F64P), _ptr(pos, F64P), _ptr(vel, F64P))
+
+    @property
+    def n(self):
+        return self.f("n")()
+
+    def get(self, name):
+        n = self.n
+        if name in VEC_FIELDS:
+            out = np.zeros((n, 3))
+            self.f("get_f64")(VEC_FIELDS[name], _ptr(out, F64P))
+        elif name in SCALAR_FIELDS:
+            out = np.zeros(n)
+            self.f("get_f64")(SCALAR_FIELDS[name], _ptr(out, F64P))
+        else:
+            out = np.zeros(n, np.int64)
+            self.f("get_i64")(INT_FIELDS[name], _ptr(out, I64P))
+        return out
+
+    def set(self, name, val):
+        val = np.ascontiguousarray(val, dtype=np.float64)
+        code = VEC_FIELDS.get(name, SCALAR_FIELDS.get(name))
+        self.f("set_f64")(code, _ptr(val, F64P))
+
+    def prepare(self):
+        """setIDLocalAndMyrank + setCutoffRadii."""
+        self.f("set_id_local")()
+        self.f("set_cutoff_radii")()
+
+    def soft_force(self, lists):
+        self.f("soft_force")(ctypes.c_int(lists["n_group"]), _ptr(lists["i_off"], I32P),
+                             _ptr(lists["i_idx"], I32P), _ptr(lists["j_off"], I32P),
+                             _ptr(lists["j_idx"], I32P), _ptr(lists["s_off"], I32P),
+                             _ptr(lists["s_idx"], I32P), lists["spj"].ctypes.data_as(VP))
+
+    def correct(self, initial):
+        self.f("correct")(ctypes.c_int(1 if initial else 0))
+
+    def pairs(self):
+        k = self.f("n_pairs")()
+        out = np.zeros(2 * k, np.int32)
+        self.f("get_pairs")(_ptr(out, I32P))
+        return out.reshape(-1, 2)
+
+    def neighbor_ids(self, i):
+        k = self.f("n_list_size")(ctypes.c_int(i))
+        out = np.zeros(k, np.int64)
+        self.f("n_list")(ctypes.c_int(i), _ptr(out, I64P))
+        return out
+
+    def cluster(self):
+        self.f("cluster")()
+
+    def kick(self):
+        self.f("kick")()
+
+    def hard(self, istep):
+        cols = np.zeros(2 * 4096, np.int64)
+        ed = np.zeros(2)
+        nc = self.f("hard")(ctypes.c_int(istep), _ptr(cols, I64P), ctypes.c_int(4096), _ptr(ed, F64P))
+        if nc < 0:
+            raise RuntimeError("hard part lost particles")
+        return cols[:2 * nc].reshape(-1, 2), ed
+
+    def energy(self):
+        out = np.zeros(5)
+        self.f("energy")(_ptr(out, F64P))
+        return out
+
+    def merge(self, n_col):
+        e = ctypes.c_double(0.0)
+        self.f("merge")(ctypes.c_int(n_col), ctypes.byref(e))
+        return e.value
+
+
+def p3t_init(sysm, disk, lists_fn):
+    """GPLUM's start-up (src/main_p3t.cpp:289-364): radii, then two passes of
+    soft force + correctForceLongInitial (USE_RE_SEARCH_NEIGHBOR)."""
+    sysm.load(disk)
+    sysm.f("set_r_planet")()
+    sysm.prepare()
+    for _ in range(2):
+        sysm.soft_force(lists_fn(sysm))
+        sysm.correct(True)
+    return sysm.energy()
+
+
+def p3t_step(sysm, istep, lists_fn, reset_step=1024):
+    """One tree step (src/main_p3t.cpp:423-717) on a single rank: kick,
+    clusters, hard part, soft force + correction, kick, energy, merge,
+    re-force after collisions.  Returns a dict of what the step produced."""
+    sysm.kick()
+    sysm.cluster()
+    n_cluster = sysm.f("n_cluster")
+    cols, edisp = sysm.hard(istep)
+    n_clusters = sysm.f("n_cluster")()
+    n_iso = sysm.f("n_isolated")()
+    sysm.f("set_id_local")()
+    sysm.soft_force(lists_fn(sysm))
+    sysm.correct(False)
+    sysm.kick()
+    e = sysm.energy()
+    out = dict(cols=cols, edisp=edisp, n_clusters=n_clusters, n_iso=n_iso, energy=e)
+    n_col = len(cols)
+    if n_col:
+        out["edisp_merge"] = sysm.merge(n_col)
+    if n_col or istep % reset_step == reset_step - 1:
+        sysm.prepare()
+        sysm.soft_force(lists_fn(sysm))
+        sysm.correct(True)
+        out["energy"] = sysm.energy()
+    return out
+
+
+def tree_lists_fn(params):
+    """Interaction lists from the package's host tree for a checker system."""
+    from gplum_gb300.tree import build_lists
+
+    def fn(sysm):
+        return build_lists(sysm.get("pos"), sysm.get("mass"), sysm.get("r_search"), params.theta,
+                           params.n_leaf_limit, params.n_group_limit)
+    return fn
