@@ -1,0 +1,304 @@
+"""P3T soft-force step on one GB300: GPLUM's EP-EP + EP-SP interaction pass
+over a 1,048,576-body disk (0.5-1.5 AU, m = 1e-10, theta = 0.5,
+n_group_limit = 256, quadrupole superparticles).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+One step = the fused EP-EP + EP-SP kernel over every i-group of the tree's
+interaction lists (forces, potentials, neighbour counts and the neighbour
+candidates the correction pass reads), inputs resident in HBM.  Prints one
+JSON line.  `--impl reference` times GPLUM's functor arithmetic on the host
+cores instead (the CPU restatement in oracle/, pinned bit-for-bit to GPLUM's
+own code) on a bounded sample of the same groups.
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_BODIES = 1048576
+EPEP_FLOPS = 32  # per pair, FMA = 2, rsqrt/min/max/compare = 1
+EPSP_FLOPS = 70
+
+
+def workload(seed=2):
+    from gplum_gb300.disk import P3TParams, disk_1m_soft
+    from gplum_gb300.radii import cutoff_radii
+    from gplum_gb300.soft import epj_records
+    from gplum_gb300.tree import build_lists
+
+    P = P3TParams(n_group_limit=256)
+    d = disk_1m_soft(N_BODIES, seed=seed)
+    r_out, r_search, _ = cutoff_radii(d["pos"], d["vel"], d["mass"], P)
+    epj = epj_records(d["pos"], d["vel"], d["mass"], r_out, r_search, ids=d["id"])
+    L = build_lists(d["pos"], d["mass"], r_search, P.theta, P.n_leaf_limit, P.n_group_limit)
+    return P, epj, L
+
+
+def pair_counts(L):
+    ni = np.diff(L["i_off"]).astype(np.int64)
+    return int((ni * np.diff(L["j_off"])).sum()), int((ni * np.diff(L["s_off"])).sum())
+
+
+def config(L, extra=None):
+    c = {"workload": "P3T soft force, 1048576-body disk 0.5-1.5 AU, m=1e-10, theta=0.5, "
+                     "n_group_limit=256, quadrupole SPJ",
+         "n_bodies": N_BODIES, "n_groups": int(L["n_group"]), "theta": 0.5, "n_group_limit": 256,
+         "l2": "flushed between timed steps (256 MiB write)", "parallelism": "replicas"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self):
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "100", "-i", os.environ.get("LOCAL_RANK", "0")],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self):
+        if not os.path.exists(self.path):
+            return None
+        rows = [r.split(", ") for r in open(self.path).read().strip().splitlines() if r.strip()]
+        rows = [r for r in rows if len(r) >= 9]
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows]
+        reasons = set()
+        for r in rows:
+            for name, v in zip(["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"],
+                               r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(rows[0][2]), "samples": len(rows),
+                "reasons": sorted(reasons)}
+
+
+def cpu_reference(L, epj, P, budget_s=20.0, threads=None):
+    """GPLUM's functor arithmetic (oracle restatement, FP32 functors) on the
+    host cores over a sample of the groups; returns (steps/s, sample text, cores)."""
+    import ctypes
+
+    from gplum_gb300.layout import cleared_forces
+    from gplum_gb300.soft import epi_records
+    from oracle import harness as H
+
+    harness_sys = H.CpuSystem("orc", P)  # sets the oracle's parameters
+    lib = harness_sys.lib
+    threads = threads or os.cpu_count()
+    epi = epi_records(epj)
+    ng = L["n_group"]
+    vp = ctypes.c_void_p
+
+    def run(groups):
+        sub = {"n_group": len(groups)}
+        for k, idx in (("i", "i_idx"), ("j", "j_idx"), ("s", "s_idx")):
+            off = L[k + "_off"]
+            lens = np.diff(off)[groups]
+            sub[k + "_off"] = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+            sub[idx] = np.concatenate([L[idx][off[g]:off[g + 1]] for g in groups]).astype(np.int32)
+        f = cleared_forces(len(epj))
+        t0 = time.perf_counter()
+        lib.orc_soft_lists(0, 0, sub["n_group"], *(sub[k].ctypes.data_as(vp) for k in
+                                                   ("i_off", "i_idx", "j_off", "j_idx", "s_off", "s_idx")),
+                           epi.ctypes.data_as(vp), epj.ctypes.data_as(vp), L["spj"].ctypes.data_as(vp),
+                           f.ctypes.data_as(vp), None, None, threads)
+        return time.perf_counter() - t0
+
+    rng = np.random.default_rng(0)
+    probe = rng.choice(ng, size=max(1, ng // 200), replace=False)
+    t_probe = run(probe)
+    frac = min(1.0, max(len(probe) / ng, budget_s / max(t_probe, 1e-6) * len(probe) / ng))
+    groups = rng.choice(ng, size=max(1, int(frac * ng)), replace=False)
+    t = run(groups)
+    ni = np.diff(L["i_off"]).astype(np.int64)
+    work = lambda gs: float((ni[gs] * (EPEP_FLOPS * np.diff(L["j_off"])[gs] + EPSP_FLOPS * np.diff(L["s_off"])[gs])).sum())
+    step_s = t * work(np.arange(ng)) / work(groups)
+    return 1.0 / step_s, f"{len(groups)} of {ng} groups ({t:.1f} s), scaled to the full step by pair flops", threads
+
+
+def reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    P, epj, L = workload()
+    steps_s = []
+    for _ in range(args.warmup):
+        cpu_reference(L, epj, P, budget_s=2.0)
+    for _ in range(args.steps):
+        v, sample, cores = cpu_reference(L, epj, P, budget_s=max(2.0, 60.0 / max(args.steps, 1)))
+        steps_s.append(v)
+    v = float(np.mean(steps_s))
+    print(json.dumps({
+        "impl": "reference", "metric": "P3T soft-force steps/s (1M-body disk)", "value": v, "unit": "steps/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 displacements)",
+        "data": "synthetic seeded disk", "config": config(L),
+        "cpu_baseline": {"value": v, "unit": "steps/s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}), flush=True)
+
+
+def gpu_arm(args, rank, world):
+    import torch
+
+    from gplum_gb300 import _lib, soft
+    from gplum_gb300.layout import EPJ_DTYPE, FORCE_DTYPE
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    P, epj, L = workload()
+    n_epep, n_epsp = pair_counts(L)
+    flops = EPEP_FLOPS * n_epep + EPSP_FLOPS * n_epsp
+    lib = _lib.host_lib()
+
+    sf = soft.SoftForce(P, precision=0)
+    sf.upload_particles(epj)
+    sf.upload_lists(L)
+    stream = torch.cuda.ExternalStream(sf.stream())
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def timed_steps(k, precision):
+        soft.configure(P, precision=precision)
+        ms = []
+        for _ in range(k):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                sf.run(emit_candidates=True)
+                e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return ms
+
+    for _ in range(max(3, args.warmup)):
+        sf.run(emit_candidates=True)
+    sf.synchronize()
+    _lib.check(lib.p3t_status(), "warm-up")
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler() as clk:
+        ms = timed_steps(args.steps, 0)
+        torch.cuda.synchronize()
+    clocks = clk.summary()
+    st = lib.p3t_status()
+    if st not in (0,):
+        raise RuntimeError(f"soft kernel reported status {st}")
+    ms_step = float(np.mean(ms))
+    if world > 1:
+        t = torch.tensor([ms_step], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_step = float(t.item())
+    value = world * 1e3 / ms_step
+
+    # plain FP64 form of the same kernel (the accuracy / speed baseline)
+    ms64 = float(np.mean(timed_steps(2, 1)))
+    soft.configure(P, precision=0)
+
+    # FP32 pipe peak of this GPU (project microbenchmark)
+    peak, peak64 = ctypes.c_double(), ctypes.c_double()
+    _lib.check(lib.p3t_probe_fma_peak(0, ctypes.byref(peak)), "fp32 peak probe")
+    _lib.check(lib.p3t_probe_fma_peak(1, ctypes.byref(peak64)), "fp64 peak probe")
+    achieved = flops / (ms_step * 1e-3) / 1e12
+    achieved64 = flops / (ms64 * 1e-3) / 1e12
+
+    # end to end through the C ABI with pinned host buffers
+    def pinned(nbytes):
+        return torch.empty(nbytes, dtype=torch.uint8, pin_memory=True).numpy()
+
+    h_epj = pinned(epj.nbytes).view(EPJ_DTYPE)
+    h_epj[:] = epj
+    h_L = {"n_group": L["n_group"]}
+    for k in ("i_off", "i_idx", "j_off", "j_idx", "s_off", "s_idx", "spj"):
+        h_L[k] = pinned(L[k].nbytes).view(L[k].dtype)
+        h_L[k][:] = L[k]
+    h_force = pinned(len(epj) * FORCE_DTYPE.itemsize).view(FORCE_DTYPE)
+    soft.soft_force_host(P, h_epj, h_L, out=h_force)
+    e2e = []
+    for _ in range(max(2, min(args.steps, 5))):
+        t0 = time.perf_counter()
+        soft.soft_force_host(P, h_epj, h_L, out=h_force)
+        e2e.append(time.perf_counter() - t0)
+    h2d = epj.nbytes + sum(L[k].nbytes for k in ("i_off", "i_idx", "j_off", "j_idx", "s_off", "s_idx", "spj"))
+    d2h = h_force.nbytes
+
+    if rank != 0:
+        return
+    out = {
+        "metric": "P3T soft-force steps/s (1M-body disk)", "value": value, "unit": "steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 displacements, compensated sums)",
+        "data": "synthetic seeded disk", "config": config(L, {"epep_pairs": n_epep, "epsp_pairs": n_epsp}),
+        "fp64_form": {"ms_per_step": ms64, "steps_per_s": 1e3 / ms64, "mixed_speedup": ms64 / ms_step,
+                      "achieved_tflops": achieved64, "fp64_peak_tflops": peak64.value},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
+                     "frac": achieved / peak.value, "peak_source": "measured (FP32 FMA microbenchmark)",
+                     "flops_per_step": flops, "traffic": None},
+        "interactions_per_s": (n_epep + n_epsp) / (ms_step * 1e-3),
+        "e2e": {"value": 1.0 / float(np.median(e2e)), "unit": "steps/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": args.steps,
+        "clocks": clocks,
+    }
+    try:
+        v, sample, cores = cpu_reference(L, epj, P, budget_s=15.0)
+        out["cpu_baseline"] = {"value": v, "unit": "steps/s", "cores": cores, "kind": "port", "sample": sample}
+    except Exception as e:  # the oracle is test infrastructure; report, do not fail the GPU line
+        out["cpu_baseline"] = {"value": None, "unit": "steps/s", "cores": 0, "kind": "port", "sample": str(e)}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        from oracle import harness
+
+        harness.build_oracle(with_ref=False)
+        reference_arm(args, rank, world)
+        return
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    gpu_arm(args, rank, world)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -37,6 +37,7 @@ SIGNATURES = {
     "p3t_download_forces": (I, [VP, I]),
     "p3t_status": (I, []),
     "p3t_soft_force_host": (I, [I, VP, I, VP, VP, VP, VP, VP, VP, VP, I, VP]),
+    "p3t_probe_fma_peak": (I, [I, VP]),
 }
 
 

@@ -50,12 +50,14 @@ __device__ __forceinline__ void fold(float &hi, float &lo, float v) {
 // --------------------------------------------------------------------------
 // mixed precision
 template <int S, int IPT, bool EMIT>
-__device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, float4 *sa, float4 *sb, float4 *sc,
-                                            int *sidx, int *scnt, float *redf, int *redi) {
+__device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, int ni, float4 *sa, float4 *sb,
+                                            float4 *sc, int *sidx, int *scnt, float *redf, int *redi) {
+    // i-particles [ib, ib + ni) of group g (ni <= 2 * SB); the origin is the
+    // group's first i-particle, as in the functor
     constexpr int W = SB / S;
     const int tid = threadIdx.x;
     const int sub = tid / W, lane = tid % W;
-    const int i0 = A.i_off[g], ni = A.i_off[g + 1] - i0;
+    const int i0 = A.i_off[g];
     const int j0 = A.j_off[g], nj = A.j_off[g + 1] - j0;
     const int s0 = A.s_off[g], ns = A.s_off[g + 1] - s0;
     const float eps2 = A.eps2;
@@ -73,7 +75,7 @@ __device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, float4 *sa
     for (int k = 0; k < IPT; k++) {
         li[k] = lane + k * W;
         vi[k] = li[k] < ni;
-        int p = vi[k] ? A.i_idx[i0 + li[k]] : p_first;
+        int p = vi[k] ? A.i_idx[i0 + ib + li[k]] : p_first;
         if ((unsigned)p >= (unsigned)A.n_iptcl) { atomicOr(A.status, ST_BAD_INDEX); p = 0; vi[k] = false; }
         pid[k] = p;
         const SoftPtcl r = A.iptcl[p];
@@ -273,27 +275,32 @@ __global__ void __launch_bounds__(SB, 4) soft_mixed_kernel(SoftArgs A) {
     __shared__ float redf[SB * 8];
     __shared__ int redi[SB * 4];
     const int g = A.group_order ? A.group_order[blockIdx.x] : blockIdx.x;
-    const int ni = A.i_off[g + 1] - A.i_off[g];
-    if (ni <= 0) return;
-    if (ni > 128)
-        group_mixed<1, 2, EMIT>(A, g, sa, sb, sc, sidx, scnt, redf, redi);
-    else if (ni > 64)
-        group_mixed<1, 1, EMIT>(A, g, sa, sb, sc, sidx, scnt, redf, redi);
-    else if (ni > 32)
-        group_mixed<2, 1, EMIT>(A, g, sa, sb, sc, sidx, scnt, redf, redi);
-    else
-        group_mixed<4, 1, EMIT>(A, g, sa, sb, sc, sidx, scnt, redf, redi);
+    const int ni_all = A.i_off[g + 1] - A.i_off[g];
+    // groups above 2 * SB members (not produced by a tree with
+    // n_group_limit <= 256) run as consecutive chunks over the same lists
+    for (int ib = 0; ib < ni_all; ib += 2 * SB) {
+        const int ni = min(2 * SB, ni_all - ib);
+        if (ni > 128)
+            group_mixed<1, 2, EMIT>(A, g, ib, ni, sa, sb, sc, sidx, scnt, redf, redi);
+        else if (ni > 64)
+            group_mixed<1, 1, EMIT>(A, g, ib, ni, sa, sb, sc, sidx, scnt, redf, redi);
+        else if (ni > 32)
+            group_mixed<2, 1, EMIT>(A, g, ib, ni, sa, sb, sc, sidx, scnt, redf, redi);
+        else
+            group_mixed<4, 1, EMIT>(A, g, ib, ni, sa, sb, sc, sidx, scnt, redf, redi);
+        __syncthreads();
+    }
 }
 
 // --------------------------------------------------------------------------
 // plain FP64
 template <int S, int IPT, bool EMIT>
-__device__ __forceinline__ void group_f64(const SoftArgs &A, int g, D4 *da, D4 *db, D4 *dc,
+__device__ __forceinline__ void group_f64(const SoftArgs &A, int g, int ib, int ni, D4 *da, D4 *db, D4 *dc,
                                           int2 *dids, int *sidx, int *scnt, double *redd, int *redi) {
     constexpr int W = SB / S;
     const int tid = threadIdx.x;
     const int sub = tid / W, lane = tid % W;
-    const int i0 = A.i_off[g], ni = A.i_off[g + 1] - i0;
+    const int i0 = A.i_off[g];
     const int j0 = A.j_off[g], nj = A.j_off[g + 1] - j0;
     const int s0 = A.s_off[g], ns = A.s_off[g + 1] - s0;
     const double eps2 = A.eps2_d;
@@ -308,7 +315,7 @@ __device__ __forceinline__ void group_f64(const SoftArgs &A, int g, D4 *da, D4 *
     for (int k = 0; k < IPT; k++) {
         li[k] = lane + k * W;
         vi[k] = li[k] < ni;
-        int p = vi[k] ? A.i_idx[i0 + li[k]] : p_first;
+        int p = vi[k] ? A.i_idx[i0 + ib + li[k]] : p_first;
         if ((unsigned)p >= (unsigned)A.n_iptcl) { atomicOr(A.status, ST_BAD_INDEX); p = 0; vi[k] = false; }
         pid[k] = p;
         xi[k] = A.iptcl[p].x; yi[k] = A.iptcl[p].y; zi[k] = A.iptcl[p].z;
@@ -456,16 +463,19 @@ __global__ void __launch_bounds__(SB, 2) soft_f64_kernel(SoftArgs A) {
     __shared__ double redd[SB * 4];
     __shared__ int redi[SB * 4];
     const int g = A.group_order ? A.group_order[blockIdx.x] : blockIdx.x;
-    const int ni = A.i_off[g + 1] - A.i_off[g];
-    if (ni <= 0) return;
-    if (ni > 128)
-        group_f64<1, 2, EMIT>(A, g, da, db, dc, dids, sidx, scnt, redd, redi);
-    else if (ni > 64)
-        group_f64<1, 1, EMIT>(A, g, da, db, dc, dids, sidx, scnt, redd, redi);
-    else if (ni > 32)
-        group_f64<2, 1, EMIT>(A, g, da, db, dc, dids, sidx, scnt, redd, redi);
-    else
-        group_f64<4, 1, EMIT>(A, g, da, db, dc, dids, sidx, scnt, redd, redi);
+    const int ni_all = A.i_off[g + 1] - A.i_off[g];
+    for (int ib = 0; ib < ni_all; ib += 2 * SB) {
+        const int ni = min(2 * SB, ni_all - ib);
+        if (ni > 128)
+            group_f64<1, 2, EMIT>(A, g, ib, ni, da, db, dc, dids, sidx, scnt, redd, redi);
+        else if (ni > 64)
+            group_f64<1, 1, EMIT>(A, g, ib, ni, da, db, dc, dids, sidx, scnt, redd, redi);
+        else if (ni > 32)
+            group_f64<2, 1, EMIT>(A, g, ib, ni, da, db, dc, dids, sidx, scnt, redd, redi);
+        else
+            group_f64<4, 1, EMIT>(A, g, ib, ni, da, db, dc, dids, sidx, scnt, redd, redi);
+        __syncthreads();
+    }
 }
 
 // --------------------------------------------------------------------------

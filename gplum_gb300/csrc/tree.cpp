@@ -209,7 +209,9 @@ P3TTree *p3t_tree_build(int n, const double *pos, const double *mass, const doub
     t->nodes[0].first = 0;
     t->nodes[0].count = n;
     t->nodes[0].size = size;
-    build_node(*t, 0, 0, pos, mass, r_search, n_leaf_limit);
+    // leaves never exceed the group limit, so every group is a cell of at most
+    // n_group_limit particles (except exactly coincident positions)
+    build_node(*t, 0, 0, pos, mass, r_search, std::min(n_leaf_limit, n_group_limit));
     collect_groups(*t, 0, n_group_limit);
 
     // interaction lists, one walk per group

@@ -96,6 +96,12 @@ int p3t_soft_force_host(int n, const void *epj, int n_group, const int *i_off, c
                         const int *j_off, const int *j_idx, const int *s_off, const int *s_idx,
                         const void *spj, int n_spj, void *force);
 
+/* ---- measurement -------------------------------------------------------------
+ * FMA throughput of this GPU (TFLOP/s, FMA = 2 flops), FP32 (fp64 = 0) or
+ * FP64 (fp64 = 1): the roofline denominators of the soft (FP32-pipe) and
+ * hard (FP64-pipe) kernels.  No counterpart in GPLUM. */
+int p3t_probe_fma_peak(int fp64, double *tflops);
+
 #ifdef __cplusplus
 }
 #endif

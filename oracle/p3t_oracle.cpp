@@ -13,6 +13,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <cstdlib>
 #include <limits>
 #include <map>
 #include <numeric>
@@ -493,6 +494,7 @@ void merge_acc_jerk(std::vector<HPtcl> &c, int t, const std::vector<int> &tw) {
 struct ColRec {
     int64_t id_imp, id_tar;
     double time;
+    double edisp, edisp_d;
 };
 std::vector<ColRec> COLS;
 double EDISP = 0., EDISP_D = 0.;
@@ -531,12 +533,13 @@ void collide(std::vector<HPtcl> &c, std::map<int, std::vector<int>> &twins, int 
     // calcEnergyDissipation
     const double m_i = c[imp].mass + 0.;
     double e_kin = 0.;
+    // (scalar * v) . v, the evaluation order of "s * v * v" with FDPS vectors
     V3 vr = vel_imp - vel_tar;
-    e_kin -= 0.5 * m_imp * m_tar / (m_imp + m_tar) * dot(vr, vr);
+    e_kin -= dot(0.5 * m_imp * m_tar / (m_imp + m_tar) * vr, vr);
     vr = vel_new - vel_g;
-    e_kin += 0.5 * (m_imp - 0.) * dot(vr, vr);
+    e_kin += dot(0.5 * (m_imp - 0.) * vr, vr);
     vr = vel_new - vel_g;
-    e_kin += 0.5 * m_tar * dot(vr, vr);
+    e_kin += dot(0.5 * m_tar * vr, vr);
     double e_int = 0., e_int_d = 0.;
     const V3 dr = pos_imp - pos_tar;
     const double dr2 = dot(dr, dr) + P.eps2;
@@ -564,6 +567,7 @@ void collide(std::vector<HPtcl> &c, std::map<int, std::vector<int>> &twins, int 
     e_sun *= P.m_sun;
     edisp = e_kin + e_int + e_sun;
     edisp_d = e_kin + e_int_d + e_sun;
+    if (getenv("ORC_DEBUG_COL")) fprintf(stderr, "ORC DEkin: %.15e DEint: %.15e DEint_hard: %.15e DEsun: %.15e\n", e_kin, e_int, e_int_d, e_sun);
     // merge_list update, src/hermite.h:413-423
     std::vector<int> &t = twins[tar];
     t.push_back(imp);
@@ -657,6 +661,8 @@ void integrate_cluster(std::vector<HPtcl> &c, double t_end, int &n_col, double &
             double e1 = 0., e2 = 0.;
             ColRec rec;
             collide(c, twins, imp, tar, e1, e2, rec);
+            rec.edisp = e1;
+            rec.edisp_d = e2;
             edisp += e1;
             edisp_d += e2;
             COLS.push_back(rec);
@@ -987,7 +993,14 @@ int hard_all(int istep) {
     COLS.clear();
     EDISP = EDISP_D = 0.;
     int done = 0;
-    for (auto &cl : clusters) {
+    // clusters of 64 or more members first, then the rest, each in cluster
+    // order (src/hard.h:562-575,583,700-701)
+    std::vector<int> order;
+    for (int pass = 0; pass < 2; pass++)
+        for (int k = 0; k < (int)clusters.size(); k++)
+            if ((clusters[k].size() >= 64) == (pass == 0)) order.push_back(k);
+    for (int k : order) {
+        auto &cl = clusters[k];
         std::vector<HPtcl> c;
         for (int i : cl) c.push_back(to_hard(S[i]));
         int nc = 0;
@@ -1323,6 +1336,10 @@ int orc_hard(int istep, long long *col_out, int col_cap, double *edisp_out) {
     edisp_out[1] = EDISP_D;
     return nc;
 }
+void orc_col_edisp(int k, double *out) {
+    out[0] = COLS[k].edisp;
+    out[1] = COLS[k].edisp_d;
+}
 int orc_n_cluster() { return N_CLUSTER; }
 int orc_n_isolated() { return N_ISO; }
 void orc_energy(double *out) {  // Energy::calcEnergy, src/energy.h:29-63
@@ -1354,7 +1371,7 @@ void orc_merge(int n_col, double *edisp) {
                     S[i].vel = (mi * S[i].vel + mj * S[j].vel) / (mi + mj);
                     S[i].phi = (mi * S[i].phi + mj * S[j].phi) / (mi + mj);
                     S[i].phi_d = (mi * S[i].phi_d + mj * S[j].phi_d) / (mi + mj);
-                    e -= 0.5 * mi * mj / (mi + mj) * dot(vrel, vrel);
+                    e -= dot(0.5 * mi * mj / (mi + mj) * vrel, vrel);
                     gone[j] = 1;
                 }
             }

@@ -4,18 +4,27 @@
 // golden-fixture generator.  TEST INFRASTRUCTURE ONLY: nothing in the product
 // links or loads this file's output.
 //
-// The prelude mirrors src/main_p3t.cpp:15-63 of GPLUM (same macros, same
-// constants, same type aliases, same include order) so that the headers see
-// exactly the environment they are written for.
+// The prelude mirrors src/main_p3t.cpp:1-63 of GPLUM (same system headers,
+// macros, constants, type aliases and include order) so that the headers see
+// exactly the environment they are written for.  One consequence: the C++
+// <stdlib.h> brings the floating-point overloads of abs() into the global
+// namespace, so the unqualified abs() of src/kepler.h:23 is the double one.
+#include <iostream>
+#include <fstream>
+#include <vector>
+#include <algorithm>
+#include <stdlib.h>
+#include <unistd.h>
+#include <sys/stat.h>
+#include <map>
+#include <dirent.h>
+#include <ctime>
+#include <cstring>
+
 #define USE_RE_SEARCH_NEIGHBOR
 #define PIKG_USE_FDPS_VECTOR
 
 #include <particle_simulator.hpp>
-#include <cstring>
-#include <sys/stat.h>
-#include <unistd.h>
-#include <dirent.h>
-#include <ctime>
 
 constexpr PS::F64 MY_PI = 3.14159265358979323846L;
 constexpr PS::F64 L_MKS = 149597870700;
@@ -395,6 +404,11 @@ int ref_hard(int istep, long long *col_out, int col_cap, double *edisp_out) {
     edisp_out[0] = g_hard.getEnergyDissipationGlobal();
     edisp_out[1] = g_hard.getHardEnergyDissipationGlobal();
     return nc;
+}
+// per-collision energy changes {edisp, edisp_d} in collision-list order
+void ref_col_edisp(int k, double *out) {
+    out[0] = g_hard.collision_list[k].edisp;
+    out[1] = g_hard.collision_list[k].edisp_d;
 }
 int ref_n_cluster() { return g_hard.getNumberOfClusterLocal(); }
 int ref_n_isolated() { return g_hard.getNumberOfIsolatedParticleLocal(); }

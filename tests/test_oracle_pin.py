@@ -1,0 +1,53 @@
+"""The CPU oracle against GPLUM's own headers compiled here (oracle/_ref),
+on inputs beyond the committed fixtures.  Skipped where the reference tree
+is not mounted (the build of oracle/_ref needs it)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from gplum_gb300.disk import P3TParams, make_disk
+from gplum_gb300.layout import cleared_forces
+from oracle import harness as H
+from tests.common import lists_for, prepared_state, records
+
+pytestmark = pytest.mark.skipif(not H.ref_available(), reason="reference build (oracle/_ref) not available")
+
+
+@pytest.mark.parametrize("trace_mode", [0])
+def test_functors_match_reference(trace_mode):
+    P, d, s = prepared_state(n=2000, seed=21, ecc_hill=4.0, inc_hill=2.0)
+    epi, epj = records(s)
+    L = lists_for(s, P)
+    rl, ol = H.load("ref"), H.load("orc")
+    vp = ctypes.c_void_p
+    for g in range(0, L["n_group"], 3):
+        ii = L["i_idx"][L["i_off"][g]:L["i_off"][g + 1]]
+        ei = np.ascontiguousarray(epi[ii])
+        ej = np.ascontiguousarray(epj[L["j_idx"][L["j_off"][g]:L["j_off"][g + 1]]])
+        sj = np.ascontiguousarray(L["spj"][L["s_idx"][L["s_off"][g]:L["s_off"][g + 1]]])
+        f1, f2 = cleared_forces(len(ii)), cleared_forces(len(ii))
+        rl.ref_epep(ei.ctypes.data_as(vp), len(ei), ej.ctypes.data_as(vp), len(ej), f1.ctypes.data_as(vp))
+        rl.ref_epsp(ei.ctypes.data_as(vp), len(ei), sj.ctypes.data_as(vp), len(sj), f1.ctypes.data_as(vp))
+        ol.orc_epep_f32(ei.ctypes.data_as(vp), len(ei), ej.ctypes.data_as(vp), len(ej), f2.ctypes.data_as(vp))
+        ol.orc_epsp_f32(ei.ctypes.data_as(vp), len(ei), sj.ctypes.data_as(vp), len(sj), f2.ctypes.data_as(vp),
+                        trace_mode)
+        assert f1.tobytes() == f2.tobytes(), g
+
+
+def test_steps_match_reference_with_collisions():
+    P = P3TParams()
+    d = make_disk(800, 1e-9, 0.985, 1.015, ecc_hill=3.0, inc_hill=1.5, seed=31, f=200.0)
+    ref, orc = H.CpuSystem("ref", P), H.CpuSystem("orc", P)
+    lf = H.tree_lists_fn(P)
+    np.testing.assert_array_equal(H.p3t_init(ref, d, lf), H.p3t_init(orc, d, lf))
+    ncol = 0
+    for st in range(1, 7):
+        a, b = H.p3t_step(ref, st, lf), H.p3t_step(orc, st, lf)
+        np.testing.assert_array_equal(a["cols"], b["cols"])
+        np.testing.assert_array_equal(a["energy"], b["energy"])
+        ncol += len(a["cols"])
+        assert ref.n == orc.n
+        for k in ("pos", "vel", "acc", "acc_d", "jerk_d", "dt", "mass", "id_cluster", "number"):
+            np.testing.assert_array_equal(ref.get(k), orc.get(k), err_msg=f"step {st} {k}")
+    assert ncol > 0

@@ -1,0 +1,178 @@
+"""Soft force on the GPU against the CPU oracle (same lists, same records).
+
+Bit-exact: neighbour count, rank sum, id_min, id_max (the FP32 screen of
+src/gravity_kernel.hpp:89-112 reproduced operation for operation).
+Tolerance: accelerations and potentials against the FP64 restatement of the
+functors, per particle |a_gpu - a_64| / |a_64|:
+  mixed form  -- median <= 1e-6 and never worse than GPLUM's own FP32
+                 functor on the same input (max and 99th percentile);
+  FP64 form   -- <= 1e-12.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from gplum_gb300 import soft
+from gplum_gb300.disk import P3TParams
+from gplum_gb300.layout import FORCE_DTYPE, cleared_forces
+from oracle import harness as H
+from tests.common import lists_for, prepared_state, records, rel_err
+
+pytestmark = pytest.mark.gpu
+VP = ctypes.c_void_p
+
+
+def oracle_lists(mode, L, epi, epj, trace_mode=0):
+    lib = H.load("orc")
+    n = len(epj)
+    args = [L[k].ctypes.data_as(VP) for k in ("i_off", "i_idx", "j_off", "j_idx", "s_off", "s_idx")]
+    if mode == 0:
+        f = cleared_forces(n)
+        lib.orc_soft_lists(0, trace_mode, L["n_group"], *args, epi.ctypes.data_as(VP), epj.ctypes.data_as(VP),
+                           L["spj"].ctypes.data_as(VP), f.ctypes.data_as(VP), None, None, 8)
+        return f
+    acc4 = np.zeros(4 * n)
+    ngb4 = np.zeros(4 * n, np.int32)
+    lib.orc_soft_lists(1, trace_mode, L["n_group"], *args, epi.ctypes.data_as(VP), epj.ctypes.data_as(VP),
+                       L["spj"].ctypes.data_as(VP), None, acc4.ctypes.data_as(VP), ngb4.ctypes.data_as(VP), 8)
+    return acc4.reshape(-1, 4), ngb4.reshape(-1, 4)
+
+
+def check_neighbours(got, want):
+    for k in ("number", "rank", "id_max", "id_min"):
+        np.testing.assert_array_equal(got[k], want[k], err_msg=k)
+
+
+def check_mixed_accuracy(got, ref32, a64):
+    e_gpu = rel_err(got["acc"], a64[:, :3])
+    e_ref = rel_err(ref32["acc"], a64[:, :3])
+    assert np.median(e_gpu) <= 1e-6, np.median(e_gpu)
+    assert e_gpu.max() <= max(e_ref.max(), 1e-6), (e_gpu.max(), e_ref.max())
+    assert np.percentile(e_gpu, 99) <= max(np.percentile(e_ref, 99), 1e-6)
+    ep = np.abs(got["phi"] - a64[:, 3]) / np.abs(a64[:, 3])
+    assert ep.max() <= 1e-6, ep.max()
+    return e_gpu, e_ref
+
+
+@pytest.mark.parametrize("n_group_limit", [64, 256, 33, 1])
+def test_resident_mixed_matches_oracle(gpu, n_group_limit):
+    P = P3TParams(n_group_limit=n_group_limit)
+    P, d, s = prepared_state(n=3000 if n_group_limit > 1 else 400, seed=5, ecc_hill=4.0, inc_hill=2.0,
+                             params=P, with_acc_d=True)
+    epi, epj = records(s)
+    L = lists_for(s, P)
+    sf = soft.SoftForce(P, precision=0)
+    sf.upload_particles(epj)
+    sf.upload_lists(L)
+    sf.run()
+    got = sf.download()
+    ref32 = oracle_lists(0, L, epi, epj)
+    a64, _ = oracle_lists(1, L, epi, epj)
+    check_neighbours(got, ref32)
+    check_mixed_accuracy(got, ref32, a64)
+
+
+def test_resident_fp64_form(gpu):
+    P, d, s = prepared_state(n=3000, seed=6, ecc_hill=4.0, inc_hill=2.0, with_acc_d=True)
+    epi, epj = records(s)
+    L = lists_for(s, P)
+    sf = soft.SoftForce(P, precision=1)
+    sf.upload_particles(epj)
+    sf.upload_lists(L)
+    sf.run()
+    got = sf.download()
+    a64, n64 = oracle_lists(1, L, epi, epj)
+    assert rel_err(got["acc"], a64[:, :3]).max() <= 1e-6  # ForceGrav stores float
+    np.testing.assert_array_equal(got["number"], n64[:, 0])
+    soft.configure(P, precision=0)
+
+
+def test_larger_disk_and_both_traces(gpu):
+    """n = 60000 with group limit 256: every work split of the kernel and
+    lists longer than one shared-memory tile; both quadrupole traces."""
+    P = P3TParams(n_group_limit=256)
+    P, d, s = prepared_state(n=60000, seed=7, a_in=0.9, a_out=1.1, m=2e-10, params=P)
+    epi, epj = records(s)
+    L = lists_for(s, P)
+    sizes = np.diff(L["i_off"])
+    assert sizes.max() > 128 and sizes.min() <= 32 and np.diff(L["j_off"]).max() > 128
+    for trace in (0, 1):
+        sf = soft.SoftForce(P, precision=0, trace_mode=trace)
+        sf.upload_particles(epj)
+        sf.upload_lists(L)
+        sf.run()
+        got = sf.download()
+        ref32 = oracle_lists(0, L, epi, epj, trace)
+        a64, _ = oracle_lists(1, L, epi, epj, trace)
+        check_neighbours(got, ref32)
+        check_mixed_accuracy(got, ref32, a64)
+    soft.configure(P, trace_mode=0)
+
+
+def test_functor_calls_accumulate_into_records(gpu):
+    P, d, s = prepared_state(n=2000, seed=8, ecc_hill=4.0, inc_hill=2.0)
+    soft.configure(P)
+    epi, epj = records(s)
+    L = lists_for(s, P)
+    lib = H.load("orc")
+    rng = np.random.default_rng(0)
+    for g in range(0, L["n_group"], 4):
+        ii = L["i_idx"][L["i_off"][g]:L["i_off"][g + 1]]
+        ei = np.ascontiguousarray(epi[ii])
+        ej = np.ascontiguousarray(epj[L["j_idx"][L["j_off"][g]:L["j_off"][g + 1]]])
+        sj = np.ascontiguousarray(L["spj"][L["s_idx"][L["s_off"][g]:L["s_off"][g + 1]]])
+        start = cleared_forces(len(ii))
+        start["acc"] = rng.normal(0, 1e-4, (len(ii), 3))
+        start["number"] = 1
+        start["id_max"] = 5
+        a, b = start.copy(), start.copy()
+        soft.calc_force_epep(ei, ej, a)
+        soft.calc_force_epsp(ei, sj, a)
+        lib.orc_epep_f32(ei.ctypes.data_as(VP), len(ei), ej.ctypes.data_as(VP), len(ej), b.ctypes.data_as(VP))
+        lib.orc_epsp_f32(ei.ctypes.data_as(VP), len(ei), sj.ctypes.data_as(VP), len(sj), b.ctypes.data_as(VP), 0)
+        check_neighbours(a, b)
+        np.testing.assert_allclose(a["acc"], b["acc"], rtol=0, atol=1e-5 * np.abs(b["acc"]).max())
+
+
+def test_multiwalk_forms_equal_resident(gpu):
+    P, d, s = prepared_state(n=5000, seed=9, ecc_hill=4.0, inc_hill=2.0, params=P3TParams(n_group_limit=128))
+    soft.configure(P)
+    epi, epj = records(s)
+    L = lists_for(s, P)
+    sf = soft.SoftForce(P)
+    sf.upload_particles(epj)
+    sf.upload_lists(L)
+    sf.run()
+    want = sf.download()
+    mw = soft.MultiWalk()
+    groups = list(range(L["n_group"]))
+    batches = [groups[k:k + 17] for k in range(0, len(groups), 17)]
+    got = np.zeros(len(epj), FORCE_DTYPE)
+    got_idx = np.zeros(len(epj), FORCE_DTYPE)
+    for bi, batch in enumerate(batches):
+        epis = [epi[L["i_idx"][L["i_off"][g]:L["i_off"][g + 1]]] for g in batch]
+        epjs = [epj[L["j_idx"][L["j_off"][g]:L["j_off"][g + 1]]] for g in batch]
+        spjs = [L["spj"][L["s_idx"][L["s_off"][g]:L["s_off"][g + 1]]] for g in batch]
+        mw.dispatch(bi % 2, epis, epjs, spjs)
+        for g, f in zip(batch, mw.retrieve(bi % 2)):
+            got[L["i_idx"][L["i_off"][g]:L["i_off"][g + 1]]] = f
+        idj = [L["j_idx"][L["j_off"][g]:L["j_off"][g + 1]] for g in batch]
+        ids = [L["s_idx"][L["s_off"][g]:L["s_off"][g + 1]] for g in batch]
+        mw.dispatch_index(bi % 2, epis, idj, ids, epj, L["spj"], send_flag=(bi == 0))
+        for g, f in zip(batch, mw.retrieve(bi % 2)):
+            got_idx[L["i_idx"][L["i_off"][g]:L["i_off"][g + 1]]] = f
+    assert got.tobytes() == want.tobytes()
+    assert got_idx.tobytes() == want.tobytes()
+
+
+def test_host_one_call_equals_resident(gpu):
+    P, d, s = prepared_state(n=3000, seed=10)
+    epi, epj = records(s)
+    L = lists_for(s, P)
+    a = soft.soft_force_host(P, epj, L)
+    sf = soft.SoftForce(P)
+    sf.upload_particles(epj)
+    sf.upload_lists(L)
+    sf.run()
+    assert a.tobytes() == sf.download().tobytes()
