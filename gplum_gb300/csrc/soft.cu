@@ -17,6 +17,9 @@
 // 138-238 of GPLUM, PIKG specs src/gravity_kernel_epep.pikg and
 // src/gravity_kernel_epsp.pikg):
 //   * displacements: FP64 relative to epi[0], rounded to FP32 (as the functor);
+//     for EP-EP the rounding residue is kept as a second FP32 term and added
+//     back for the force arithmetic, so near pairs keep ~1e-7 relative
+//     precision in r however far they sit from the group origin;
 //   * neighbour screen: r2_real = ((rx*rx + ry*ry) + rz*rz) + eps2 in FP32
 //     with every product and sum rounded separately (no FMA), compared with
 //     max(rs2_i, rs2_j) -- bit-identical to the functor, so neighbour counts,
@@ -66,7 +69,7 @@ __device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, in
     if ((unsigned)p_first >= (unsigned)A.n_iptcl) { atomicOr(A.status, ST_BAD_INDEX); p_first = 0; }
     const double ox = A.iptcl[p_first].x, oy = A.iptcl[p_first].y, oz = A.iptcl[p_first].z;
 
-    float xi[IPT], yi[IPT], zi[IPT], ro2i[IPT], rs2i[IPT];
+    float xi[IPT], yi[IPT], zi[IPT], xl[IPT], yl[IPT], zl[IPT], ro2i[IPT], rs2i[IPT];
     int idi[IPT], rki[IPT], pid[IPT], li[IPT];
     bool vi[IPT];
     float ahx[IPT], alx[IPT], ahy[IPT], aly[IPT], ahz[IPT], alz[IPT], ahp[IPT], alp[IPT];
@@ -79,9 +82,13 @@ __device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, in
         if ((unsigned)p >= (unsigned)A.n_iptcl) { atomicOr(A.status, ST_BAD_INDEX); p = 0; vi[k] = false; }
         pid[k] = p;
         const SoftPtcl r = A.iptcl[p];
-        xi[k] = __double2float_rn(r.x - ox);
-        yi[k] = __double2float_rn(r.y - oy);
-        zi[k] = __double2float_rn(r.z - oz);
+        const double dx = r.x - ox, dy = r.y - oy, dz = r.z - oz;
+        xi[k] = __double2float_rn(dx);
+        yi[k] = __double2float_rn(dy);
+        zi[k] = __double2float_rn(dz);
+        xl[k] = __double2float_rn(dx - (double)xi[k]);
+        yl[k] = __double2float_rn(dy - (double)yi[k]);
+        zl[k] = __double2float_rn(dz - (double)zi[k]);
         ro2i[k] = r.ro2;
         rs2i[k] = r.rs2;
         idi[k] = r.id_local;
@@ -101,9 +108,12 @@ __device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, in
             int p = A.j_idx[j0 + base + tid];
             if ((unsigned)p >= (unsigned)A.n_ptcl) { atomicOr(A.status, ST_BAD_INDEX); p = 0; }
             const SoftPtcl r = A.ptcl[p];
-            sa[tid] = make_float4(__double2float_rn(r.x - ox), __double2float_rn(r.y - oy),
-                                  __double2float_rn(r.z - oz), r.m);
+            const double dx = r.x - ox, dy = r.y - oy, dz = r.z - oz;
+            const float hx = __double2float_rn(dx), hy = __double2float_rn(dy), hz = __double2float_rn(dz);
+            sa[tid] = make_float4(hx, hy, hz, r.m);
             sb[tid] = make_float4(r.ro2, r.rs2, __int_as_float(r.id_local), __int_as_float(r.rank));
+            sc[tid] = make_float4(__double2float_rn(dx - (double)hx), __double2float_rn(dy - (double)hy),
+                                  __double2float_rn(dz - (double)hz), 0.f);
             if (EMIT) sidx[tid] = p;
         }
         __syncthreads();
@@ -117,12 +127,17 @@ __device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, in
             for (int jj = c0; jj < c1; jj++) {
                 const float4 a = sa[jj];
                 const float4 b = sb[jj];
+                const float4 c = sc[jj];
 #pragma unroll
                 for (int k = 0; k < IPT; k++) {
-                    const float rx = xi[k] - a.x, ry = yi[k] - a.y, rz = zi[k] - a.z;
+                    // the functor's FP32 displacement (screen) ...
+                    const float hx = xi[k] - a.x, hy = yi[k] - a.y, hz = zi[k] - a.z;
                     const float r2r =
-                        __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(rx, rx), __fmul_rn(ry, ry)), __fmul_rn(rz, rz)), eps2);
-                    const float r2 = fmaxf(r2r, fmaxf(ro2i[k], b.x));
+                        __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(hx, hx), __fmul_rn(hy, hy)), __fmul_rn(hz, hz)), eps2);
+                    // ... and the same displacement with the low parts restored (force)
+                    const float rx = hx + (xl[k] - c.x), ry = hy + (yl[k] - c.y), rz = hz + (zl[k] - c.z);
+                    const float r2f = fmaf(rx, rx, fmaf(ry, ry, fmaf(rz, rz, eps2)));
+                    const float r2 = fmaxf(r2f, fmaxf(ro2i[k], b.x));
                     float ri = rsqrtf(r2);
                     ri = ri * fmaf(-0.5f * r2, ri * ri, 1.5f);
                     const float mr = a.w * ri;
