@@ -38,6 +38,22 @@ SIGNATURES = {
     "p3t_status": (I, []),
     "p3t_soft_force_host": (I, [I, VP, I, VP, VP, VP, VP, VP, VP, VP, I, VP]),
     "p3t_probe_fma_peak": (I, [I, VP]),
+    "p3t_state_load": (I, [I, VP, VP, VP, VP, VP, VP]),
+    "p3t_state_n": (I, []),
+    "p3t_state_get": (I, [I, VP]),
+    "p3t_state_set": (I, [I, VP]),
+    "p3t_set_cutoff_radii": (I, []),
+    "p3t_set_r_planet": (I, []),
+    "p3t_state_soft": (I, [I, VP, VP, VP, VP, VP, VP, VP, I]),
+    "p3t_correct": (I, [I]),
+    "p3t_neighbor_counts": (I, [VP, VP]),
+    "p3t_neighbor_list": (I, [I, VP, I]),
+    "p3t_cluster_label": (I, []),
+    "p3t_cluster_lists": (I, [VP, VP, VP]),
+    "p3t_hard": (I, [I, I, VP, VP]),
+    "p3t_kick": (I, []),
+    "p3t_energy": (I, [VP]),
+    "p3t_merge": (I, [VP]),
 }
 
 

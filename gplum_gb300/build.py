@@ -19,6 +19,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libgplum_p3t.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# FP64 physics kept free of FMA contraction, so it rounds as GPLUM's host build
+NO_FMAD = {"engine.cu", "hard.cu"}
 
 
 def _nvcc():
@@ -51,8 +53,9 @@ def build(force=False, verbose=False):
     jobs = []
     for src in cu:
         obj = os.path.join(OUT, os.path.basename(src) + ".o")
+        extra = ["-fmad=false"] if os.path.basename(src) in NO_FMAD else []
         jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                     "-Xcompiler", "-fno-fast-math", "--expt-relaxed-constexpr", "-c", src, "-o", obj])
+                     "-Xcompiler", "-fno-fast-math", "--expt-relaxed-constexpr", *extra, "-c", src, "-o", obj])
     for src in cpp:
         obj = os.path.join(OUT, os.path.basename(src) + ".o")
         jobs.append(["g++", "-O3", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-c", src,

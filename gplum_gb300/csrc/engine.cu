@@ -1,0 +1,912 @@
+// Device-resident P3T step: particle state, the FP64 cutoff correction and
+// neighbour search, cluster labelling and lists, kicks, energy, merging and
+// cut-off radii.  Compiled with -fmad=false (see p3t_phys.cuh).
+#include <cmath>
+#include <cstdio>
+#include <type_traits>
+#include <cstring>
+#include <vector>
+
+#include "../../include/gplum_p3t.h"
+#include "p3t_capi_internal.cuh"
+#include "p3t_engine.cuh"
+#include "p3t_phys.cuh"
+#include "p3t_soft.cuh"
+
+namespace p3t {
+
+Engine g_eng;
+
+// ---------------------------------------------------------------------------
+// small device helpers
+__global__ void k_fill_i32(int32_t *p, int n, int32_t v) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
+}
+__global__ void k_fill_i64(int64_t *p, int n, int64_t v) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
+}
+__global__ void k_iota(int32_t *p, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = i;
+}
+inline int nb(int n, int t = 256) { return (n + t - 1) / t; }
+
+// Exclusive scan of int32 (block-level Hillis-Steele in shared memory, then
+// block sums scanned recursively).
+__global__ void k_scan_block(const int32_t *in, int32_t *out, int32_t *bsum, int n) {
+    __shared__ int32_t s[1024];
+    const int i = blockIdx.x * 1024 + threadIdx.x;
+    const int32_t v = (i < n) ? in[i] : 0;
+    s[threadIdx.x] = v;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        int32_t t = (threadIdx.x >= off) ? s[threadIdx.x - off] : 0;
+        __syncthreads();
+        s[threadIdx.x] += t;
+        __syncthreads();
+    }
+    if (i < n) out[i] = s[threadIdx.x] - v;
+    if (threadIdx.x == 1023) bsum[blockIdx.x] = s[1023];
+}
+__global__ void k_scan_add(int32_t *out, const int32_t *bscan, int n) {
+    const int i = blockIdx.x * 1024 + threadIdx.x;
+    if (i < n) out[i] += bscan[blockIdx.x];
+}
+
+int Engine::scan(const int32_t *in, int32_t *out, int n, int32_t *total) {
+    // levels of block sums live in scan_tmp
+    std::vector<int> sizes;
+    int m = n;
+    size_t need = 0;
+    while (true) {
+        const int blocks = (m + 1023) / 1024;
+        sizes.push_back(m);
+        need += (size_t)blocks * 2;
+        if (blocks <= 1) break;
+        m = blocks;
+    }
+    int r = scan_tmp.reserve(need + 2);
+    if (r) return r;
+    // recursive scan
+    struct Lvl { const int32_t *in; int32_t *out; int32_t *bsum; int n; };
+    std::vector<Lvl> lv;
+    int32_t *tmp = scan_tmp.p;
+    const int32_t *cur_in = in;
+    int32_t *cur_out = out;
+    int cn = n;
+    while (true) {
+        const int blocks = (cn + 1023) / 1024;
+        int32_t *bsum = tmp;
+        int32_t *bscan = tmp + blocks;
+        tmp += 2 * blocks;
+        lv.push_back({cur_in, cur_out, bsum, cn});
+        k_scan_block<<<blocks, 1024, 0, c->stream>>>(cur_in, cur_out, bsum, cn);
+        if (blocks <= 1) break;
+        cur_in = bsum;
+        cur_out = bscan;
+        cn = blocks;
+    }
+    for (int L = (int)lv.size() - 2; L >= 0; L--) {
+        const int blocks = (lv[L].n + 1023) / 1024;
+        k_scan_add<<<blocks, 1024, 0, c->stream>>>(lv[L].out, lv[L + 1].out, lv[L].n);
+    }
+    if (total) {
+        // total = out[n-1] + in[n-1]
+        int32_t a = 0, b = 0;
+        if (n > 0) {
+            cudaMemcpyAsync(&a, out + n - 1, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream);
+            cudaMemcpyAsync(&b, in + n - 1, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream);
+        }
+        r = cuda_status(cudaStreamSynchronize(c->stream));
+        if (r) return r;
+        *total = a + b;
+    }
+    return cuda_status(cudaGetLastError());
+}
+
+// ---------------------------------------------------------------------------
+// state -> soft-kernel particle records
+__global__ void k_pack_state(State S, SoftPtcl *out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.n) return;
+    SoftPtcl r;
+    r.x = S.pos[3 * i];
+    r.y = S.pos[3 * i + 1];
+    r.z = S.pos[3 * i + 2];
+    r.m = (float)S.mass[i];
+    const float ro = (float)S.r_out[i], rs = (float)S.r_search[i];
+    r.ro2 = __fmul_rn(ro, ro);
+    r.rs2 = __fmul_rn(__fmul_rn(rs, rs), 1.0201f);
+    r.id_local = i;
+    r.rank = 0;
+    r.pad = 0;
+    out[i] = r;
+}
+
+// ---------------------------------------------------------------------------
+// cutoff correction + neighbour search, src/gravity_soft.h:75-528
+struct CorrOut {
+    V3 acc, acc_d, jerk;
+    double phi, phi_d, acc0;
+    int number;
+    int64_t idc;
+};
+
+__device__ __forceinline__ void corr_pair(const State &S, const Params &P, int i, int j, bool initial, V3 pos_i,
+                                          V3 vel_i, V3 accd_i, double ro_i, double roi_i, double rs_i, int cap,
+                                          CorrOut &o) {
+    const double mj = S.mass[j];
+    const double r_out = dmax(ro_i, S.r_out[j]);
+    const double r_out_inv = dmin(roi_i, S.r_out_inv[j]);
+    const double r_search = dmax(rs_i, S.r_search[j]);
+    const V3 dr = ld3(S.pos, j) - pos_i;
+    double dr2 = dot(dr, dr);
+    dr2 += P.eps2;
+    const double rij = sqrt(dr2);
+    const V3 dv = ld3(S.vel, j) - vel_i;
+    const V3 da = ld3(S.acc_d, j) - accd_i;
+    const double drdv = dot(dr, dv);
+    const double dv2 = dot(dv, dv);
+    const double da2 = dot(da, da);
+    const double t_min = dmin(dmax(-drdv / sqrt(dv2), 0.), P.dt_tree);
+    const double dr2_min = dmin(dr2, dr2 + 2. * drdv * t_min + dv2 * t_min * t_min);
+    const double r_crit = P.R_search2 * r_out;
+    const double v_crit_a = P.R_search3 * 0.5 * P.dt_tree;
+    if (dr2_min < r_crit * r_crit || dv2 < v_crit_a * v_crit_a * da2 || (initial && da2 == 0.)) {
+        if (rij < r_search) {
+            // NeighborList::addNeighbor, src/neighbor.h:635-670
+            if (o.number < cap) S.nbr[(size_t)i * cap + o.number] = j;
+            o.number++;
+            o.idc = (S.id[j] < o.idc) ? S.id[j] : o.idc;
+            o.acc0 += r_out * r_out / mj;
+        }
+    }
+    if (rij < r_out) {
+        const double rinv = 1. / rij;
+        const double r2inv = rinv * rinv;
+        const double r3inv = rinv * r2inv;
+        const double W = cut_W(P, rij, r_out_inv);
+        const double K = cut_K(P, rij, r_out_inv);
+        const double r_min = dmin(rinv, r_out_inv);
+        o.phi -= mj * (rinv * W - r_min);
+        addto(o.acc, mj * (r3inv * K - r_min * r_min * r_min) * dr);
+        if (initial) {
+            const double alpha = drdv * r2inv;
+            const double dKdt = cut_dKdt(P, rij, r_out_inv, alpha);
+            const double alpha_c = alpha * (1. - K);
+            o.phi_d -= mj * rinv * (1. - W);
+            addto(o.acc_d, mj * r3inv * (1. - K) * dr);
+            addto(o.jerk, mj * r3inv * ((1. - K) * dv - (3. * alpha_c + dKdt) * dr));
+        }
+    }
+}
+
+__global__ void k_correct(State S, Params P, const ForceRec *__restrict__ F, const int32_t *__restrict__ cand, int cap,
+                          int initial, int32_t *counters, int *status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.n) return;
+    const ForceRec fr = F[i];
+    const V3 pos_i = ld3(S.pos, i), vel_i = ld3(S.vel, i), accd_i = ld3(S.acc_d, i);
+    const double m_i = S.mass[i], ro_i = S.r_out[i], roi_i = S.r_out_inv[i], rs_i = S.r_search[i];
+    const int64_t id_i = S.id[i];
+    V3 acc_s = ld3(S.acc_s, i), jerk_s = ld3(S.jerk_s, i);
+    if (initial) {
+        double phs;
+        sun_force(P, pos_i, vel_i, acc_s, jerk_s, &phs);
+        st3(S.acc_s, i, acc_s);
+        st3(S.jerk_s, i, jerk_s);
+        S.phi_s[i] = phs;
+    }
+    CorrOut o;
+    o.acc = o.acc_d = o.jerk = v3(0., 0., 0.);
+    o.phi = o.phi_d = o.acc0 = 0.;
+    o.number = 0;
+    o.idc = id_i;
+    o.phi += m_i * roi_i;
+    const int k = fr.number;
+    if (k > 0) {
+        // candidates: the soft kernel's screen hits (for k <= 2 exactly the
+        // functor's id_min, id_max), taken in ascending index order
+        const int kc = min(k, cap);
+        if (k > cap) atomicOr(status, ST_CAND_OVERFLOW);
+        int last = -1;
+        for (int t = 0; t < kc; t++) {
+            // next smallest candidate above `last` (lists are short)
+            int best = 0x7fffffff;
+            for (int u = 0; u < kc; u++) {
+                const int c = cand[(size_t)i * cap + u];
+                if (c > last && c < best) best = c;
+            }
+            if (best == 0x7fffffff) break;
+            last = best;
+            if ((unsigned)best >= (unsigned)S.n) {
+                atomicOr(status, ST_BAD_INDEX);
+                continue;
+            }
+            if (S.id[best] == id_i) continue;
+            corr_pair(S, P, i, best, initial != 0, pos_i, vel_i, accd_i, ro_i, roi_i, rs_i, cap, o);
+        }
+        if (o.number > cap) atomicOr(status, ST_CAND_OVERFLOW);
+    }
+    // write back (FPGrav::copyFromForce then the corrections)
+    st3(S.acc, i, v3((double)fr.acc[0], (double)fr.acc[1], (double)fr.acc[2]) + o.acc);
+    S.phi[i] = (double)fr.phi + o.phi;
+    S.acc0[i] = (o.acc0 > 0.) ? o.number / o.acc0 : 0.;
+    S.number[i] = o.number;
+    S.rank[i] = fr.rank;
+    S.id_max[i] = fr.id_max;
+    S.id_min[i] = fr.id_min;
+    S.id_cluster[i] = o.idc;
+    S.nbr_n[i] = min(o.number, cap);
+    if (o.number) {
+        atomicAdd(&counters[0], o.number);
+        atomicAdd(&counters[1], 1);
+    }
+    if (initial) {
+        st3(S.acc_d_new, i, o.acc_d);
+        S.phi_d[i] = o.phi_d;
+        st3(S.jerk_d, i, o.jerk);
+        // calcDeltatInitial reads the pre-pass acc_d (src/gravity_soft.h:388-391,510)
+        S.dt[i] = dt_initial(P, S.time[i], S.dt[i], S.acc0[i], accd_i, o.jerk, acc_s, jerk_s);
+    }
+}
+
+__global__ void k_copy3(double *dst, const double *src, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < 3 * n) dst[i] = src[i];
+}
+
+// ---------------------------------------------------------------------------
+// cluster labelling, src/neighbor.h:800-839: connected components of the
+// local pairs (i < j, j a neighbour of i), each labelled with the minimum
+// id_cluster of its members.  Union-find with hooking to the smaller index.
+__device__ __forceinline__ int uf_find(const int32_t *lab, int x) {
+    for (int k = 0; k < 1 << 20; k++) {
+        const int p = lab[x];
+        if (p == x) return x;
+        x = p;
+    }
+    return x;
+}
+__global__ void k_union(State S, int cap, int *status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.n) return;
+    const int m = S.nbr_n[i];
+    for (int t = 0; t < m; t++) {
+        const int j = S.nbr[(size_t)i * cap + t];
+        if (!(i < j)) continue;
+        int a = i, b = j;
+        int tries = 0;
+        while (true) {
+            a = uf_find(S.label, a);
+            b = uf_find(S.label, b);
+            if (a == b) break;
+            if (a > b) { int t2 = a; a = b; b = t2; }
+            const int old = atomicCAS(&S.label[b], b, a);
+            if (old == b) break;
+            if (++tries > (1 << 20)) { atomicOr(status, ST_ITER_CAP); break; }
+        }
+    }
+}
+__global__ void k_compress(State S, int64_t *cmin) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.n) return;
+    const int r = uf_find(S.label, i);
+    S.label[i] = r;
+    atomicMin((unsigned long long *)&cmin[r], (unsigned long long)S.id_cluster[i]);
+}
+__global__ void k_apply_label(State S, const int64_t *cmin) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.n) return;
+    S.id_cluster[i] = cmin[S.label[i]];
+}
+
+// ---------------------------------------------------------------------------
+// cluster lists, src/hard.h:321-438: members are the particles with
+// neighbours, grouped by component, clusters ordered by their smallest
+// member index, members in ascending index order.
+__global__ void k_head(State S, int32_t *head) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.n) return;
+    if (S.number[i] > 0) atomicMin(&head[S.label[i]], i);
+}
+__global__ void k_head_flag(State S, const int32_t *head, int32_t *flag) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.n) return;
+    flag[i] = (S.number[i] > 0 && head[S.label[i]] == i) ? 1 : 0;
+}
+__global__ void k_member_count(State S, const int32_t *head, const int32_t *cidx, int32_t *cl_of, int32_t *cnt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.n) return;
+    if (S.number[i] > 0) {
+        const int c = cidx[head[S.label[i]]];
+        cl_of[i] = c;
+        atomicAdd(&cnt[c], 1);
+    } else {
+        cl_of[i] = -1;
+    }
+}
+__global__ void k_member_fill(State S, const int32_t *cl_of, const int32_t *off, int32_t *fill, int32_t *members) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.n) return;
+    const int c = cl_of[i];
+    if (c < 0) return;
+    const int s = atomicAdd(&fill[c], 1);
+    members[off[c] + s] = i;
+}
+// one warp per cluster: rank members by index
+__global__ void k_member_sort(int nc, const int32_t *off, const int32_t *cnt, const int32_t *in, int32_t *out) {
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= nc) return;
+    const int o = off[w], m = cnt[w];
+    for (int a = lane; a < m; a += 32) {
+        const int v = in[o + a];
+        int r = 0;
+        for (int b = 0; b < m; b++) r += (in[o + b] < v);
+        out[o + r] = v;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// kicks, energy
+__global__ void k_kick(State S, double half_dt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.n) return;
+    const V3 v = ld3(S.vel, i), a = ld3(S.acc, i);
+    st3(S.vel, i, v + half_dt * a);
+}
+// Energy::calcEnergy, src/energy.h:29-63, per-block partial sums in a fixed
+// order, then one ordered pass over the blocks.
+__global__ void k_energy_partial(State S, double *part) {
+    __shared__ double s[4][256];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double ek = 0., es = 0., ep = 0., ed = 0.;
+    if (i < S.n) {
+        const double m = S.mass[i];
+        const V3 v = ld3(S.vel, i);
+        ek = dot(m * v, v);
+        es = m * S.phi_s[i];
+        ep = m * S.phi[i];
+        ed = m * S.phi_d[i];
+    }
+    s[0][threadIdx.x] = ek; s[1][threadIdx.x] = es; s[2][threadIdx.x] = ep; s[3][threadIdx.x] = ed;
+    __syncthreads();
+    for (int h = 128; h > 0; h >>= 1) {
+        if (threadIdx.x < h)
+            for (int q = 0; q < 4; q++) s[q][threadIdx.x] += s[q][threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x < 4) part[4 * blockIdx.x + threadIdx.x] = s[threadIdx.x][0];
+}
+__global__ void k_energy_final(const double *part, int nblk, double *out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double ek = 0., es = 0., ep = 0., ed = 0.;
+    for (int b = 0; b < nblk; b++) {
+        ek += part[4 * b]; es += part[4 * b + 1]; ep += part[4 * b + 2]; ed += part[4 * b + 3];
+    }
+    ek *= 0.5; ep *= 0.5; ed *= 0.5;
+    out[1] = ek; out[2] = es; out[3] = ep; out[4] = ed;
+    out[0] = ek + es + (ep + ed);
+}
+
+// ---------------------------------------------------------------------------
+// cut-off radii, src/particle.h:713-733,1319-1457 (individual cutoff)
+__global__ void k_rminmax(State S, double *mm) {
+    __shared__ double smax[256], smin[256];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double r2 = 0., r2m = -1.7976931348623157e308;
+    if (i < S.n) {
+        const double x = S.pos[3 * i], y = S.pos[3 * i + 1];
+        r2 = x * x + y * y;
+        r2m = -r2;
+    }
+    smax[threadIdx.x] = r2;
+    smin[threadIdx.x] = r2m;
+    __syncthreads();
+    for (int h = 128; h > 0; h >>= 1) {
+        if (threadIdx.x < h) {
+            smax[threadIdx.x] = dmax(smax[threadIdx.x], smax[threadIdx.x + h]);
+            smin[threadIdx.x] = dmax(smin[threadIdx.x], smin[threadIdx.x + h]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        // non-negative doubles order like their bit patterns: mm[0] = max r^2,
+        // mm[1] = min r^2 (src/particle.h:1324-1333 keeps it as max of -r^2)
+        atomicMax((unsigned long long *)&mm[0], (unsigned long long)__double_as_longlong(smax[0]));
+        atomicMin((unsigned long long *)&mm[1], (unsigned long long)__double_as_longlong(-smin[0]));
+    }
+}
+constexpr int NBIN = 32;
+constexpr int VD_T = 64;
+__global__ void k_vdisp_partial(State S, double r_min, double drinv, double m_sun, double *part, int *cntp) {
+    __shared__ double sv[NBIN][VD_T];
+    __shared__ int sc[NBIN][VD_T];
+    for (int b = 0; b < NBIN; b++) { sv[b][threadIdx.x] = 0.; sc[b][threadIdx.x] = 0; }
+    const int per = (S.n + gridDim.x - 1) / gridDim.x;
+    const int beg = blockIdx.x * per, end = min(S.n, beg + per);
+    for (int i = beg + threadIdx.x; i < end; i += blockDim.x) {
+        const V3 pos = ld3(S.pos, i);
+        const double ri = sqrt(pos.x * pos.x + pos.y * pos.y);
+        int b = (int)((ri - r_min) * drinv);
+        if (b == NBIN) b = NBIN - 1;
+        b = max(0, min(NBIN - 1, b));
+        V3 vk = v3(-pos.y / ri, pos.x / ri, 0.);
+        vk = vk * sqrt(m_sun / sqrt(pos.x * pos.x + pos.y * pos.y));
+        const V3 vr = ld3(S.vel, i) - vk;
+        sv[b][threadIdx.x] += dot(vr, vr);
+        sc[b][threadIdx.x] += 1;
+    }
+    __syncthreads();
+    if (threadIdx.x < NBIN) {
+        double s = 0.;
+        int c = 0;
+        for (int t = 0; t < VD_T; t++) { s += sv[threadIdx.x][t]; c += sc[threadIdx.x][t]; }
+        part[blockIdx.x * NBIN + threadIdx.x] = s;
+        cntp[blockIdx.x * NBIN + threadIdx.x] = c;
+    }
+}
+__global__ void k_vdisp_bins(const double *part, const int *cntp, int nblk, double *vd, int *cnt) {
+    const int b = threadIdx.x;
+    if (b >= NBIN) return;
+    double s = 0.;
+    int c = 0;
+    for (int k = 0; k < nblk; k++) { s += part[k * NBIN + b]; c += cntp[k * NBIN + b]; }
+    vd[b] = (c > 0) ? sqrt(s / c) : 0.;
+    cnt[b] = c;
+}
+__global__ void k_radii(State S, Params P, double r_min, double dr, double drinv, const double *vd, const int *cnt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.n) return;
+    const V3 pos = ld3(S.pos, i), vel = ld3(S.vel, i);
+    const double r2 = pos.x * pos.x + pos.y * pos.y;
+    double vs = 0., ws = 0.;
+    for (int b = 0; b < NBIN; b++) {
+        const double ddr = r_min + (b + 0.5) * dr - sqrt(r2);
+        const double ex = exp(-ddr * ddr * drinv * drinv);
+        vs += vd[b] * ex;
+        ws += (cnt[b] > 0) ? ex : 0.;
+    }
+    const double v_disp = vs / ws;
+    S.v_disp[i] = v_disp;
+    const double r = sqrt(dot(pos, pos));
+    const double rv = dot(pos, vel);
+    double ax = 1.0 / (2.0 / r - dot(vel, vel) / P.m_sun);
+    const double ecccosu = 1. - r / ax;
+    const double eccsinu2 = rv * rv / (P.m_sun * ax);
+    if (!(sqrt(ecccosu * ecccosu + eccsinu2) < 0.6)) ax = r;
+    const double rHill = pow(S.mass[i] / (3. * P.m_sun), 1. / 3.) * ax;
+    const double r_out_i = dmax(P.R_cut0 * pow(ax, -P.p_cut) * rHill, P.R_cut1 * v_disp * P.dt_tree);
+    double ro = dmax(r_out_i, P.r_cut_min);
+    if (P.r_cut_max > 0.) ro = dmin(P.r_cut_max, ro);
+    S.r_out[i] = ro;
+    S.r_out_inv[i] = 1. / ro;
+    S.r_search[i] = P.R_search0 * ro + P.R_search1 * v_disp * P.dt_tree;
+}
+
+// ---------------------------------------------------------------------------
+// MergeParticle, src/func.h:160-207: targets fold in their dead twins (same
+// id, same cluster), twins leave the system (order-preserving).
+__global__ void k_merge_targets(State S, const int32_t *cl_of, const int32_t *off, const int32_t *cnt,
+                                const int32_t *members, int32_t *keep, double *e_t) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.n) return;
+    e_t[i] = 0.;
+    if (!(S.merged[i] && !S.dead[i])) return;
+    const int c = cl_of[i];
+    double e = 0.;
+    if (c >= 0) {
+        for (int t = 0; t < cnt[c]; t++) {
+            const int j = members[off[c] + t];
+            if (S.id[j] == S.id[i] && i != j) {
+                const double mi = S.mass[i], mj = S.mass[j];
+                const V3 vrel = ld3(S.vel, j) - ld3(S.vel, i);
+                S.mass[i] += mj;
+                st3(S.vel, i, (mi * ld3(S.vel, i) + mj * ld3(S.vel, j)) / (mi + mj));
+                S.phi[i] = (mi * S.phi[i] + mj * S.phi[j]) / (mi + mj);
+                S.phi_d[i] = (mi * S.phi_d[i] + mj * S.phi_d[j]) / (mi + mj);
+                e -= dot(0.5 * mi * mj / (mi + mj) * vrel, vrel);
+                keep[j] = 0;
+            }
+        }
+    }
+    S.merged[i] = 0;
+    e_t[i] = e;
+}
+__global__ void k_sum_ordered(const double *v, int n, double *out) {
+    if (threadIdx.x || blockIdx.x) return;
+    double s = 0.;
+    for (int i = 0; i < n; i++) s += v[i];
+    *out = s;
+}
+template <class T>
+__global__ void k_compact(const T *src, T *dst, const int32_t *keep, const int32_t *pos, int n, int w) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !keep[i]) return;
+    for (int k = 0; k < w; k++) dst[(size_t)pos[i] * w + k] = src[(size_t)i * w + k];
+}
+
+// ---------------------------------------------------------------------------
+// Engine host methods
+template <class T>
+static int alloc_field(T **p, size_t n) {
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    return cuda_status(cudaMalloc(p, std::max<size_t>(n, 1) * sizeof(T)));
+}
+
+int Engine::ensure(int n) {
+    if (!c) {
+        c = ctx_get(0);
+        if (!c) return -(int)cudaErrorNoDevice;
+    }
+    if (n <= S.cap && S.nbr && cand_cap_alloc == c->cand_cap) return 0;
+    const int cap = std::max(n, S.cap);
+    int r = 0;
+    State &s = S;
+    for (double **f : {&s.mass, &s.r_planet, &s.f, &s.phi, &s.phi_d, &s.phi_s, &s.r_out, &s.r_out_inv, &s.r_search,
+                       &s.v_disp, &s.time, &s.dt, &s.acc0})
+        if (n > s.cap && (r = alloc_field(f, cap))) return r;
+    for (double **f : {&s.pos, &s.vel, &s.acc, &s.acc_d, &s.jerk_d, &s.acc_s, &s.jerk_s, &s.acc_d_new})
+        if (n > s.cap && (r = alloc_field(f, 3 * (size_t)cap))) return r;
+    for (int64_t **f : {&s.id, &s.id_cluster})
+        if (n > s.cap && (r = alloc_field(f, cap))) return r;
+    for (int32_t **f : {&s.number, &s.rank, &s.id_max, &s.id_min, &s.n_cluster, &s.dead, &s.merged, &s.nbr_n, &s.label})
+        if (n > s.cap && (r = alloc_field(f, cap))) return r;
+    if ((r = alloc_field(&s.nbr, (size_t)cap * c->cand_cap))) return r;
+    cand_cap_alloc = c->cand_cap;
+    s.cap = cap;
+    return 0;
+}
+
+Params Engine::params() const {
+    Params P;
+    const double *p = c->params;
+    P.eps2 = p[0]; P.eps2_sun = p[1]; P.m_sun = p[2]; P.dt_tree = p[3]; P.dt_min = p[4];
+    P.eta = p[5]; P.eta_0 = p[6]; P.eta_sun = p[7]; P.eta_sun0 = p[8]; P.alpha2 = p[9];
+    P.gamma = p[10]; P.R_cut0 = p[11]; P.R_cut1 = p[12]; P.R_search0 = p[13]; P.R_search1 = p[14];
+    P.R_search2 = p[15]; P.R_search3 = p[16]; P.r_cut_min = p[17]; P.r_cut_max = p[18]; P.p_cut = p[19];
+    P.dens = p[20];
+    // FPGrav::setGamma, src/particle.h:619-633 (host libm)
+    const double g = P.gamma;
+    P.g_1_inv = 1. / (g - 1.);
+    const double g2 = g * g;
+    const double gi3 = P.g_1_inv * P.g_1_inv * P.g_1_inv;
+    P.g_1_inv7 = gi3 * gi3 * P.g_1_inv;
+    P.w_y = 7. / 3. * ((((((g - 9.) * g + 45.) * g - 60. * std::log(g)) * g - 45.) * g + 9.) * g - 1.) * P.g_1_inv7;
+    P.f1 = (-10. / 3. + 14. * (g + 1.) - 21. * ((g + 3.) * g + 1.) + 35. / 3. * (((g + 9.) * g + 9.) * g + 1.) -
+            70. * ((g + 3.) * g + 1.) * g + 210. * (g + 1.) * g2 + (((g - 7.) * g + 21.) * g - 35.) * g2 * g2) *
+           P.g_1_inv7;
+    return P;
+}
+
+int Engine::load(int n, const long long *id, const double *mass, const double *r_planet, const double *f,
+                 const double *pos, const double *vel) {
+    int r = ensure(n);
+    if (r) return r;
+    S.n = n;
+    if ((r = h2d(c, S.id, id, n * sizeof(int64_t))) || (r = h2d(c, S.mass, mass, n * sizeof(double))) ||
+        (r = h2d(c, S.r_planet, r_planet, n * sizeof(double))) || (r = h2d(c, S.f, f, n * sizeof(double))) ||
+        (r = h2d(c, S.pos, pos, 3 * n * sizeof(double))) || (r = h2d(c, S.vel, vel, 3 * n * sizeof(double))))
+        return r;
+    // start-up reset, src/main_p3t.cpp:291-303
+    for (double *p : {S.acc, S.acc_d, S.jerk_d, S.acc_s, S.jerk_s})
+        cudaMemsetAsync(p, 0, 3 * (size_t)n * sizeof(double), c->stream);
+    for (double *p : {S.phi, S.phi_d, S.phi_s, S.time, S.dt, S.acc0, S.v_disp, S.r_out, S.r_out_inv, S.r_search})
+        cudaMemsetAsync(p, 0, (size_t)n * sizeof(double), c->stream);
+    for (int32_t *p : {S.number, S.rank, S.n_cluster, S.dead, S.merged, S.nbr_n})
+        cudaMemsetAsync(p, 0, (size_t)n * sizeof(int32_t), c->stream);
+    k_fill_i32<<<nb(n), 256, 0, c->stream>>>(S.id_max, n, -1);
+    k_fill_i32<<<nb(n), 256, 0, c->stream>>>(S.id_min, n, INT32_MAX_);
+    cudaMemcpyAsync(S.id_cluster, S.id, n * sizeof(int64_t), cudaMemcpyDeviceToDevice, c->stream);
+    n_clusters = 0;
+    return cuda_status(cudaStreamSynchronize(c->stream));
+}
+
+int Engine::pack_soft() {
+    DevSet &d = c->res;
+    int r = 0;
+    if ((r = d.ptcl.reserve(S.n)) || (r = d.force.reserve(S.n)) || (r = d.acc64.reserve(S.n)) ||
+        (r = d.mass.reserve(S.n)) || (r = d.r_out.reserve(S.n)) || (r = d.r_search.reserve(S.n)))
+        return r;
+    k_pack_state<<<nb(S.n), 256, 0, c->stream>>>(S, d.ptcl.p);
+    cudaMemcpyAsync(d.mass.p, S.mass, S.n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+    cudaMemcpyAsync(d.r_out.p, S.r_out, S.n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+    cudaMemcpyAsync(d.r_search.p, S.r_search, S.n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+    c->res_n = S.n;
+    return cuda_status(cudaGetLastError());
+}
+
+int Engine::correct(int initial) {
+    const Params P = params();
+    int r = counters.reserve(4);
+    if (r) return r;
+    cudaMemsetAsync(counters.p, 0, 4 * sizeof(int32_t), c->stream);
+    k_correct<<<nb(S.n, 128), 128, 0, c->stream>>>(S, P, c->res.force.p, c->res.cand.p, c->cand_cap, initial,
+                                                     counters.p, c->status);
+    if (initial) k_copy3<<<nb(3 * S.n), 256, 0, c->stream>>>(S.acc_d, S.acc_d_new, S.n);
+    return cuda_status(cudaGetLastError());
+}
+
+int Engine::cluster() {
+    int r = cmin.reserve(S.n);
+    if (r) return r;
+    k_iota<<<nb(S.n), 256, 0, c->stream>>>(S.label, S.n);
+    k_fill_i64<<<nb(S.n), 256, 0, c->stream>>>(cmin.p, S.n, (int64_t)0x7fffffffffffffffLL);
+    k_union<<<nb(S.n), 256, 0, c->stream>>>(S, c->cand_cap, c->status);
+    k_compress<<<nb(S.n), 256, 0, c->stream>>>(S, cmin.p);
+    k_apply_label<<<nb(S.n), 256, 0, c->stream>>>(S, cmin.p);
+    return cuda_status(cudaGetLastError());
+}
+
+int Engine::make_list() {
+    const int n = S.n;
+    int r = 0;
+    if ((r = head.reserve(n)) || (r = flag.reserve(n)) || (r = cidx.reserve(n)) || (r = cl_of.reserve(n)) ||
+        (r = cl_cnt.reserve(n + 1)) || (r = cl_off.reserve(n + 1)) || (r = cl_fill.reserve(n + 1)) ||
+        (r = members_tmp.reserve(n)) || (r = members.reserve(n)))
+        return r;
+    k_fill_i32<<<nb(n), 256, 0, c->stream>>>(head.p, n, 0x7fffffff);
+    k_head<<<nb(n), 256, 0, c->stream>>>(S, head.p);
+    k_head_flag<<<nb(n), 256, 0, c->stream>>>(S, head.p, flag.p);
+    int32_t nc = 0;
+    if ((r = scan(flag.p, cidx.p, n, &nc))) return r;
+    n_clusters = nc;
+    cudaMemsetAsync(cl_cnt.p, 0, (nc + 1) * sizeof(int32_t), c->stream);
+    cudaMemsetAsync(cl_fill.p, 0, (nc + 1) * sizeof(int32_t), c->stream);
+    k_member_count<<<nb(n), 256, 0, c->stream>>>(S, head.p, cidx.p, cl_of.p, cl_cnt.p);
+    int32_t nm = 0;
+    if (nc > 0 && (r = scan(cl_cnt.p, cl_off.p, nc, &nm))) return r;
+    n_members = nm;
+    k_member_fill<<<nb(n), 256, 0, c->stream>>>(S, cl_of.p, cl_off.p, cl_fill.p, members_tmp.p);
+    if (nc > 0) k_member_sort<<<nb(nc * 32), 256, 0, c->stream>>>(nc, cl_off.p, cl_cnt.p, members_tmp.p, members.p);
+    return cuda_status(cudaGetLastError());
+}
+
+int Engine::kick() {
+    k_kick<<<nb(S.n), 256, 0, c->stream>>>(S, 0.5 * c->params[3]);
+    return cuda_status(cudaGetLastError());
+}
+
+int Engine::energy(double *out5) {
+    const int blocks = nb(S.n);
+    int r = 0;
+    if ((r = epart.reserve(4 * (size_t)blocks + 8))) return r;
+    k_energy_partial<<<blocks, 256, 0, c->stream>>>(S, epart.p);
+    k_energy_final<<<1, 32, 0, c->stream>>>(epart.p, blocks, epart.p + 4 * blocks);
+    cudaMemcpyAsync(out5, epart.p + 4 * blocks, 5 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    return cuda_status(cudaStreamSynchronize(c->stream));
+}
+
+int Engine::cutoff_radii() {
+    const Params P = params();
+    int r = 0;
+    const int nblk = 152;
+    if ((r = epart.reserve(2 + 2 * NBIN + (size_t)nblk * NBIN)) || (r = icnt.reserve(NBIN + (size_t)nblk * NBIN)))
+        return r;
+    double *mm = epart.p, *vd = epart.p + 2, *part = epart.p + 2 + 2 * NBIN;
+    int *cnt = icnt.p, *cntp = icnt.p + NBIN;
+    const double init[2] = {0., 1.7976931348623157e308};
+    cudaMemcpyAsync(mm, init, 2 * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+    k_rminmax<<<nb(S.n), 256, 0, c->stream>>>(S, mm);
+    double h[2];
+    cudaMemcpyAsync(h, mm, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if ((r = cuda_status(cudaStreamSynchronize(c->stream)))) return r;
+    // src/particle.h:1324-1339 (r_min tracked as max of -r^2)
+    const double r_max = std::sqrt(h[0]) * 1.01;
+    const double r_min = std::sqrt(h[1]) * 0.99;
+    const double dr = (r_max - r_min) / NBIN, drinv = 1. / dr;
+    k_vdisp_partial<<<nblk, VD_T, 0, c->stream>>>(S, r_min, drinv, P.m_sun, part, cntp);
+    k_vdisp_bins<<<1, 32, 0, c->stream>>>(part, cntp, nblk, vd, cnt);
+    k_radii<<<nb(S.n), 256, 0, c->stream>>>(S, P, r_min, dr, drinv, vd, cnt);
+    return cuda_status(cudaGetLastError());
+}
+
+int Engine::merge(double *edisp) {
+    const int n = S.n;
+    int r = 0;
+    if ((r = keep.reserve(n)) || (r = kpos.reserve(n)) || (r = et.reserve(n + 1))) return r;
+    k_fill_i32<<<nb(n), 256, 0, c->stream>>>(keep.p, n, 1);
+    k_merge_targets<<<nb(n), 256, 0, c->stream>>>(S, cl_of.p, cl_off.p, cl_cnt.p, members.p, keep.p, et.p);
+    k_sum_ordered<<<1, 32, 0, c->stream>>>(et.p, n, et.p + n);
+    double e = 0.;
+    cudaMemcpyAsync(&e, et.p + n, sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    int32_t nk = 0;
+    if ((r = scan(keep.p, kpos.p, n, &nk))) return r;  // synchronizes
+    *edisp = e;
+    if (nk == n) return 0;
+    // order-preserving compaction of every field through a scratch copy
+    auto comp = [&](auto *fld, int w) -> int {
+        using T2 = std::remove_pointer_t<decltype(fld)>;
+        T2 *tmp = nullptr;
+        int rr = cuda_status(cudaMalloc(&tmp, std::max<size_t>((size_t)n * w, 1) * sizeof(T2)));
+        if (rr) return rr;
+        cudaMemcpyAsync(tmp, fld, (size_t)n * w * sizeof(T2), cudaMemcpyDeviceToDevice, c->stream);
+        k_compact<T2><<<nb(n), 256, 0, c->stream>>>(tmp, fld, keep.p, kpos.p, n, w);
+        rr = cuda_status(cudaStreamSynchronize(c->stream));
+        cudaFree(tmp);
+        return rr;
+    };
+    for (double *f : {S.mass, S.r_planet, S.f, S.phi, S.phi_d, S.phi_s, S.r_out, S.r_out_inv, S.r_search, S.v_disp,
+                      S.time, S.dt, S.acc0})
+        if ((r = comp(f, 1))) return r;
+    for (double *f : {S.pos, S.vel, S.acc, S.acc_d, S.jerk_d, S.acc_s, S.jerk_s})
+        if ((r = comp(f, 3))) return r;
+    for (int64_t *f : {S.id, S.id_cluster})
+        if ((r = comp(f, 1))) return r;
+    for (int32_t *f : {S.number, S.rank, S.id_max, S.id_min, S.n_cluster, S.dead, S.merged})
+        if ((r = comp(f, 1))) return r;
+    S.n = nk;
+    n_clusters = 0;
+    return 0;
+}
+
+}  // namespace p3t
+
+using namespace p3t;
+
+extern "C" {
+
+int p3t_state_load(int n, const long long *id, const double *mass, const double *r_planet, const double *f,
+                   const double *pos, const double *vel) {
+    if (n < 0) return ST_BAD_INDEX;
+    return g_eng.load(n, id, mass, r_planet, f, pos, vel);
+}
+
+int p3t_state_n(void) { return g_eng.S.n; }
+
+// field codes: see include/gplum_p3t.h
+static void *field_ptr(int field, int *width, int *kind) {
+    State &S = g_eng.S;
+    *width = 1;
+    *kind = 0;  // 0 double, 1 int64, 2 int32
+    switch (field) {
+        case 0: *width = 3; return S.pos;
+        case 1: *width = 3; return S.vel;
+        case 2: *width = 3; return S.acc;
+        case 3: *width = 3; return S.acc_d;
+        case 4: *width = 3; return S.jerk_d;
+        case 5: *width = 3; return S.acc_s;
+        case 6: *width = 3; return S.jerk_s;
+        case 10: return S.phi;
+        case 11: return S.phi_d;
+        case 12: return S.phi_s;
+        case 13: return S.mass;
+        case 14: return S.r_out;
+        case 15: return S.r_search;
+        case 16: return S.dt;
+        case 17: return S.acc0;
+        case 18: return S.time;
+        case 19: return S.r_planet;
+        case 20: return S.v_disp;
+        case 21: return S.r_out_inv;
+        case 100: *kind = 1; return S.id;
+        case 101: *kind = 1; return S.id_cluster;
+        case 102: *kind = 2; return S.number;
+        case 103: *kind = 2; return S.n_cluster;
+        case 104: *kind = 2; return S.dead;
+        case 105: *kind = 2; return S.merged;
+        case 106: *kind = 2; return S.rank;
+        case 107: *kind = 2; return S.id_min;
+        case 108: *kind = 2; return S.id_max;
+        default: return nullptr;
+    }
+}
+static size_t kind_size(int kind) { return kind == 0 ? 8 : (kind == 1 ? 8 : 4); }
+
+int p3t_state_get(int field, void *out) {
+    Context *c = ctx_get(0);
+    if (!c) return -(int)cudaErrorNoDevice;
+    int w, kind;
+    void *p = field_ptr(field, &w, &kind);
+    if (!p) return ST_BAD_INDEX;
+    const size_t b = (size_t)g_eng.S.n * w * kind_size(kind);
+    int r = cuda_status(cudaMemcpyAsync(out, p, b, cudaMemcpyDeviceToHost, c->stream));
+    if (r) return r;
+    return cuda_status(cudaStreamSynchronize(c->stream));
+}
+
+int p3t_state_set(int field, const void *in) {
+    Context *c = ctx_get(0);
+    if (!c) return -(int)cudaErrorNoDevice;
+    int w, kind;
+    void *p = field_ptr(field, &w, &kind);
+    if (!p) return ST_BAD_INDEX;
+    return h2d(c, p, in, (size_t)g_eng.S.n * w * kind_size(kind));
+}
+
+int p3t_set_cutoff_radii(void) {
+    if (!g_eng.c) return -(int)cudaErrorNoDevice;
+    return g_eng.cutoff_radii();
+}
+
+int p3t_set_r_planet(void) {
+    Context *c = ctx_get(0);
+    if (!c) return -(int)cudaErrorNoDevice;
+    // FPGrav::setRPlanet, src/particle.h:757-759 (host: one pow per body)
+    const int n = g_eng.S.n;
+    std::vector<double> m(n), rp(n);
+    int r = cuda_status(cudaMemcpy(m.data(), g_eng.S.mass, n * sizeof(double), cudaMemcpyDeviceToHost));
+    if (r) return r;
+    for (int i = 0; i < n; i++) rp[i] = std::pow(0.75 * m[i] / (3.14159265358979323846 * c->params[20]), 1. / 3.);
+    return h2d(c, g_eng.S.r_planet, rp.data(), n * sizeof(double));
+}
+
+int p3t_state_soft(int n_group, const int *i_off, const int *i_idx, const int *j_off, const int *j_idx,
+                   const int *s_off, const int *s_idx, const void *spj, int n_spj) {
+    Context *c = ctx_get(0);
+    if (!c) return -(int)cudaErrorNoDevice;
+    int r = g_eng.pack_soft();
+    if (r) return r;
+    if ((r = p3t_upload_lists(n_group, i_off, i_idx, j_off, j_idx, s_off, s_idx, spj, n_spj))) return r;
+    return p3t_soft_run(1);
+}
+
+int p3t_correct(int initial) {
+    if (!g_eng.c) return -(int)cudaErrorNoDevice;
+    int r = g_eng.correct(initial);
+    if (r) return r;
+    return read_status(g_eng.c);
+}
+
+int p3t_neighbor_counts(int *ngb_tot, int *with_ngb) {
+    Context *c = ctx_get(0);
+    if (!c || !g_eng.counters.p) return -(int)cudaErrorNoDevice;
+    int h[2];
+    int r = cuda_status(cudaMemcpy(h, g_eng.counters.p, 2 * sizeof(int), cudaMemcpyDeviceToHost));
+    *ngb_tot = h[0];
+    *with_ngb = h[1];
+    return r;
+}
+
+int p3t_neighbor_list(int i, int *out, int cap) {
+    Context *c = ctx_get(0);
+    if (!c) return -(int)cudaErrorNoDevice;
+    if (i < 0 || i >= g_eng.S.n) return -1;
+    int m = 0;
+    cudaMemcpy(&m, g_eng.S.nbr_n + i, sizeof(int), cudaMemcpyDeviceToHost);
+    m = std::min(m, cap);
+    if (m > 0) cudaMemcpy(out, g_eng.S.nbr + (size_t)i * c->cand_cap, m * sizeof(int), cudaMemcpyDeviceToHost);
+    return m;
+}
+
+int p3t_cluster_label(void) {
+    if (!g_eng.c) return -(int)cudaErrorNoDevice;
+    int r = g_eng.cluster();
+    if (r) return r;
+    if ((r = g_eng.make_list())) return r;
+    return read_status(g_eng.c);
+}
+
+int p3t_cluster_lists(int *n_clusters, int *off, int *members) {
+    Context *c = ctx_get(0);
+    if (!c) return -(int)cudaErrorNoDevice;
+    *n_clusters = g_eng.n_clusters;
+    if (off) {
+        cudaMemcpy(off, g_eng.cl_off.p, g_eng.n_clusters * sizeof(int), cudaMemcpyDeviceToHost);
+        off[g_eng.n_clusters] = g_eng.n_members;
+    }
+    if (members && g_eng.n_members)
+        cudaMemcpy(members, g_eng.members.p, g_eng.n_members * sizeof(int), cudaMemcpyDeviceToHost);
+    return cuda_status(cudaGetLastError());
+}
+
+int p3t_kick(void) {
+    if (!g_eng.c) return -(int)cudaErrorNoDevice;
+    return g_eng.kick();
+}
+
+int p3t_energy(double *out5) {
+    if (!g_eng.c) return -(int)cudaErrorNoDevice;
+    return g_eng.energy(out5);
+}
+
+int p3t_merge(double *edisp) {
+    if (!g_eng.c) return -(int)cudaErrorNoDevice;
+    return g_eng.merge(edisp);
+}
+
+}  // extern "C"

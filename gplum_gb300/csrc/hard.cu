@@ -1,0 +1,751 @@
+// Hard part of the P3T step on the device: every neighbour cluster of the
+// step in one persistent launch, one warp per cluster taken from a device
+// work queue, 4th-order block-timestep Hermite with collision detection and
+// perfect accretion (src/hermite.h:224-479, src/hard.h:554-829,
+// src/collisionA.h:86-706 of GPLUM); isolated bodies take the Kepler drift
+// or the sun-only Hermite (src/hermite.h:734-815, src/kepler.h).
+// Compiled with -fmad=false (see p3t_phys.cuh).
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "../../include/gplum_p3t.h"
+#include "p3t_capi_internal.cuh"
+#include "p3t_engine.cuh"
+#include "p3t_phys.cuh"
+
+namespace p3t {
+
+constexpr int MAX_BLOCK_STEPS = 1 << 22;  // per cluster and tree step
+
+// Per-member working copy of one cluster (FPHard fields), indexed by the
+// member's slot in the cluster lists.
+struct Hard {
+    double *pos, *vel, *acc_s, *jerk_s, *acc_d, *jerk_d;
+    double *x0, *v0, *a0_s, *j0_s, *a0_d, *j0_d, *xp, *vp, *a2_s, *a3_s, *a2_d, *a3_d;
+    double *phi_d, *phi_s, *mass, *r_planet, *f, *r_out_inv, *th, *dt, *acc0, *time_c;
+    int64_t *id;
+    int32_t *dead, *merged, *tw_head, *tw_tail, *tw_next;
+};
+
+struct ColRec {
+    int64_t id_imp, id_tar;
+    double time, edisp, edisp_d;
+    int32_t cluster, seq;
+};
+
+struct HardArgs {
+    State S;
+    Params P;
+    Hard H;
+    const int32_t *off, *cnt, *members, *order;
+    int n_clusters;
+    int32_t *queue;
+    double *cl_edisp;  // [2 * n_clusters]
+    ColRec *cols;
+    int32_t *n_cols;
+    int col_cap;
+    int *status;
+    double t_end;
+};
+
+// ---- FPHard::predict / correct / calcDeltat, src/particle.h:1183-1314 ----
+__device__ __forceinline__ void predict(const Hard &H, int s, double Dt) {
+    const V3 pos = ld3(H.pos, s), vel = ld3(H.vel, s), as = ld3(H.acc_s, s), js = ld3(H.jerk_s, s),
+             ad = ld3(H.acc_d, s), jd = ld3(H.jerk_d, s);
+    st3(H.x0, s, pos); st3(H.v0, s, vel); st3(H.a0_s, s, as); st3(H.j0_s, s, js); st3(H.j0_d, s, jd);
+    st3(H.a0_d, s, ad);
+    const V3 a = as + ad, j = js + jd;
+    st3(H.xp, s, pos + Dt * (vel + Dt * (0.5 * a + 1.6666666666666667e-1 * Dt * j)));
+    st3(H.vp, s, vel + Dt * (a + Dt * 0.5 * j));
+}
+__device__ __forceinline__ void correct(const Hard &H, int s, double Dt) {
+    const double Dt2 = Dt * Dt, Di = 1. / Dt, Di2 = Di * Di, Di3 = Di2 * Di;
+    const V3 Am_s = ld3(H.acc_s, s) - ld3(H.a0_s, s), J0_s = Dt * ld3(H.j0_s, s), J1_s = Dt * ld3(H.jerk_s, s);
+    const V3 A2_s = 3. * Am_s - (J1_s + 2. * J0_s);
+    const V3 A3_s = -2. * Am_s + (J1_s + J0_s);
+    st3(H.a2_s, s, 2. * Di2 * (A2_s + 3. * A3_s));
+    st3(H.a3_s, s, 6. * Di3 * A3_s);
+    const V3 Am_d = ld3(H.acc_d, s) - ld3(H.a0_d, s), J0_d = ld3(H.j0_d, s) * Dt, J1_d = ld3(H.jerk_d, s) * Dt;
+    const V3 A2_d = 3. * Am_d - (J1_d + 2. * J0_d);
+    const V3 A3_d = -2. * Am_d + (J1_d + J0_d);
+    st3(H.a2_d, s, 2. * (A2_d + 3. * A3_d) * Di2);
+    st3(H.a3_d, s, 6. * A3_d * Di3);
+    const V3 A2 = A2_s + A2_d, A3 = A3_s + A3_d;
+    st3(H.pos, s, ld3(H.xp, s) + 1.6666666666666667e-2 * Dt2 * (5. * A2 + 3. * 1.1666666666666667e-3 * A3));
+    st3(H.vel, s, ld3(H.vp, s) + 8.3333333333333333e-2 * Dt * (4. * A2 + 3. * A3));
+}
+__device__ __forceinline__ void dt_hermite(const Params &P, const Hard &H, int s) {
+    double dt_next = dmin(2. * H.dt[s], 0.5 * P.dt_tree);
+    const double dt_1 = dmin(dt4th(P.eta, P.alpha2, H.acc0[s], ld3(H.acc_d, s), ld3(H.jerk_d, s), ld3(H.a2_d, s),
+                                   ld3(H.a3_d, s)),
+                             dt4th(P.eta_sun, P.alpha2, 0., ld3(H.acc_s, s), ld3(H.jerk_s, s), ld3(H.a2_s, s),
+                                   ld3(H.a3_s, s)));
+    const double time = H.th[s];
+    double rem = fmod(time, dt_next);
+    for (int k = 0; rem != 0.0 && k < 1100; k++) {
+        dt_next *= 0.5;
+        rem = fmod(time, dt_next);
+    }
+    for (int k = 0; dt_1 < dt_next && 0.5 * H.dt[s] < dt_next && k < 1100; k++) dt_next *= 0.5;
+    if (dt_next < 2. * P.dt_min) dt_next = P.dt_min;
+    H.dt[s] = dt_next;
+}
+
+// ---- pair sums over a cluster, src/gravity_hard.h:203-367 -------------------
+// mode 0: full (pos/vel, with phi); 1: predicted i and j; 2: corrected i, predicted j
+__device__ void hard_force(const Params &P, const Hard &H, int o, int n, int s, int mode) {
+    V3 xi, vi, as, js;
+    if (mode == 0) {
+        xi = ld3(H.pos, s); vi = ld3(H.vel, s);
+        double phs;
+        sun_force(P, xi, vi, as, js, &phs);
+        H.phi_s[s] = phs;
+    } else if (mode == 1) {
+        xi = ld3(H.xp, s); vi = ld3(H.vp, s);
+        sun_force(P, xi, vi, as, js, nullptr);
+    } else {
+        xi = ld3(H.pos, s); vi = ld3(H.vel, s);
+        sun_force(P, xi, vi, as, js, nullptr);
+    }
+    st3(H.acc_s, s, as);
+    st3(H.jerk_s, s, js);
+    V3 ad = v3(0., 0., 0.), jd = v3(0., 0., 0.);
+    double phd = 0.;
+    const int64_t idi = H.id[s];
+    const double roi = H.r_out_inv[s];
+    for (int k = 0; k < n; k++) {
+        const int t = o + k;
+        if (idi == H.id[t]) continue;
+        const V3 xj = (mode == 0) ? ld3(H.pos, t) : ld3(H.xp, t);
+        const V3 vj = (mode == 0) ? ld3(H.vel, t) : ld3(H.vp, t);
+        const V3 dr = xj - xi;
+        double dr2 = dot(dr, dr);
+        dr2 += P.eps2;
+        const V3 dv = vj - vi;
+        const double rij = sqrt(dr2);
+        const double rinv = 1. / rij;
+        const double r2inv = rinv * rinv;
+        const double r3inv = r2inv * rinv;
+        const double r_out_inv = dmin(roi, H.r_out_inv[t]);
+        const double mj = H.mass[t];
+        const double mr3 = mj * r3inv;
+        const double alpha = dot(dr, dv) * r2inv;
+        double Wc = 0.;
+        if (mode == 0) Wc = 1. - cut_W(P, rij, r_out_inv);
+        const double Kc = 1. - cut_K(P, rij, r_out_inv);
+        const double dKdt = cut_dKdt(P, rij, r_out_inv, alpha);
+        const double alpha_c = alpha * Kc;
+        if (mode == 0) phd -= mj * rinv * Wc;
+        addto(ad, mr3 * Kc * dr);
+        addto(jd, mr3 * (Kc * dv - (3. * alpha_c + dKdt) * dr));
+    }
+    if (mode == 0) H.phi_d[s] = phd;
+    st3(H.acc_d, s, ad);
+    st3(H.jerk_d, s, jd);
+}
+
+// mergeAccJerk for target t, src/hermite.h:36-83 (twins in insertion order)
+__device__ void merge_acc_jerk(const Hard &H, int t) {
+    V3 a = H.mass[t] * ld3(H.acc_d, t), j = H.mass[t] * ld3(H.jerk_d, t);
+    double m = H.mass[t];
+    for (int k = H.tw_head[t], g = 0; k >= 0 && g < 4096; k = H.tw_next[k], g++) {
+        addto(a, H.mass[k] * ld3(H.acc_d, k));
+        addto(j, H.mass[k] * ld3(H.jerk_d, k));
+        m += H.mass[k];
+    }
+    const double mi = 1. / m;
+    a = a * mi;
+    j = j * mi;
+    st3(H.acc_d, t, a);
+    st3(H.jerk_d, t, j);
+    for (int k = H.tw_head[t], g = 0; k >= 0 && g < 4096; k = H.tw_next[k], g++) {
+        st3(H.acc_d, k, a);
+        st3(H.jerk_d, k, j);
+    }
+}
+
+__device__ __forceinline__ double cut_W2(const Params &P, double dr2, double a, double b) {
+    return cut_W(P, sqrt(dr2), dmin(a, b));
+}
+
+// Collision0 perfect accretion: inputPair, collisionOutcome, setParticle,
+// calcEnergyDissipation and the merge-list update (src/collisionA.h:86-706,
+// src/hermite.h:395-423).  One lane.
+__device__ void collide(const Params &P, const Hard &H, int imp, int tar, double &edisp, double &edisp_d,
+                        ColRec &rec) {
+    rec.id_imp = H.id[imp];
+    rec.id_tar = H.id[tar];
+    rec.time = H.time_c[imp] + H.th[imp];
+    const V3 pos_imp = ld3(H.pos, imp), pos_tar = ld3(H.pos, tar), vel_imp = ld3(H.vel, imp),
+             vel_tar = ld3(H.vel, tar);
+    double m_imp = H.mass[imp], m_tar = H.mass[tar];
+    if (H.merged[imp])
+        for (int k = H.tw_head[imp], g = 0; k >= 0 && g < 4096; k = H.tw_next[k], g++) m_imp += H.mass[k];
+    if (H.merged[tar])
+        for (int k = H.tw_head[tar], g = 0; k >= 0 && g < 4096; k = H.tw_next[k], g++) m_tar += H.mass[k];
+    const V3 vel_g = (m_imp * vel_imp + m_tar * vel_tar) / (m_imp + m_tar);
+    const V3 pos_new = (m_imp * pos_imp + m_tar * pos_tar) / (m_imp + m_tar);
+    const V3 vel_new = (m_imp * vel_imp + m_tar * vel_tar) / (m_imp + m_tar);
+    const double m_rem = m_imp + m_tar - 0.;
+    H.r_planet[imp] = 0.;
+    H.r_planet[tar] *= pow(m_rem / m_tar, 1. / 3.);
+    H.mass[imp] -= 0.;
+    H.id[imp] = H.id[tar];
+    H.dead[imp] = 1;
+    for (int k = H.tw_head[imp], g = 0; k >= 0 && g < 4096; k = H.tw_next[k], g++) {
+        H.id[k] = H.id[tar];
+        H.dead[k] = 1;
+    }
+    H.merged[tar] = 1;
+    st3(H.pos, imp, pos_new); st3(H.vel, imp, vel_new);
+    for (int k = H.tw_head[imp], g = 0; k >= 0 && g < 4096; k = H.tw_next[k], g++) {
+        st3(H.pos, k, pos_new); st3(H.vel, k, vel_new);
+    }
+    st3(H.pos, tar, pos_new); st3(H.vel, tar, vel_new);
+    for (int k = H.tw_head[tar], g = 0; k >= 0 && g < 4096; k = H.tw_next[k], g++) {
+        st3(H.pos, k, pos_new); st3(H.vel, k, vel_new);
+    }
+    // energy
+    const double m_i = H.mass[imp] + 0.;
+    double e_kin = 0.;
+    V3 vr = vel_imp - vel_tar;
+    e_kin -= dot(0.5 * m_imp * m_tar / (m_imp + m_tar) * vr, vr);
+    vr = vel_new - vel_g;
+    e_kin += dot(0.5 * (m_imp - 0.) * vr, vr);
+    vr = vel_new - vel_g;
+    e_kin += dot(0.5 * m_tar * vr, vr);
+    double e_int = 0., e_int_d = 0.;
+    const V3 dr = pos_imp - pos_tar;
+    const double dr2 = dot(dr, dr) + P.eps2;
+    const double rinv = sqrt(1. / dr2);
+    double dphi = m_i * rinv;
+    e_int += H.mass[tar] * dphi;
+    e_int_d += H.mass[tar] * dphi * (1. - cut_W2(P, dr2, H.r_out_inv[imp], H.r_out_inv[tar]));
+    for (int k = H.tw_head[tar], g = 0; k >= 0 && g < 4096; k = H.tw_next[k], g++) {
+        e_int += H.mass[k] * dphi;
+        e_int_d += H.mass[k] * dphi * (1. - cut_W2(P, dr2, H.r_out_inv[imp], H.r_out_inv[k]));
+    }
+    for (int ki = H.tw_head[imp], g = 0; ki >= 0 && g < 4096; ki = H.tw_next[ki], g++) {
+        dphi = H.mass[ki] * rinv;
+        e_int += H.mass[tar] * dphi;
+        e_int_d += H.mass[tar] * dphi * (1. - cut_W2(P, dr2, H.r_out_inv[ki], H.r_out_inv[tar]));
+        for (int kj = H.tw_head[tar], h = 0; kj >= 0 && h < 4096; kj = H.tw_next[kj], h++) {
+            e_int += H.mass[kj] * dphi;
+            e_int_d += H.mass[kj] * dphi * (1. - cut_W2(P, dr2, H.r_out_inv[ki], H.r_out_inv[kj]));
+        }
+    }
+    double e_sun = 0.;
+    e_sun += m_imp / sqrt(dot(pos_imp, pos_imp) + P.eps2) + m_tar / sqrt(dot(pos_tar, pos_tar) + P.eps2);
+    const V3 pt = ld3(H.pos, tar), pi = ld3(H.pos, imp);
+    e_sun -= m_tar * sqrt(1. / (dot(pt, pt) + P.eps2));
+    e_sun -= (m_imp - 0.) * sqrt(1. / (dot(pi, pi) + P.eps2));
+    e_sun *= P.m_sun;
+    edisp = e_kin + e_int + e_sun;
+    edisp_d = e_kin + e_int_d + e_sun;
+    rec.edisp = edisp;
+    rec.edisp_d = edisp_d;
+    // merge list: imp, then imp's twins, join tar's list
+    auto append = [&](int k) {
+        H.tw_next[k] = -1;
+        if (H.tw_head[tar] < 0) H.tw_head[tar] = k;
+        else H.tw_next[H.tw_tail[tar]] = k;
+        H.tw_tail[tar] = k;
+    };
+    const int imp_first = H.tw_head[imp];
+    const bool imp_merged = H.merged[imp] != 0;
+    append(imp);
+    if (imp_merged) {
+        for (int k = imp_first, g = 0; k >= 0 && g < 4096; g++) {
+            const int nx = H.tw_next[k];
+            append(k);
+            k = nx;
+        }
+        H.tw_head[imp] = H.tw_tail[imp] = -1;
+        H.merged[imp] = 0;
+    }
+}
+
+__device__ __forceinline__ double warp_min(double v) {
+    for (int o = 16; o > 0; o >>= 1) v = dmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+__global__ void __launch_bounds__(128) k_hard_clusters(HardArgs A) {
+    const int lane = threadIdx.x & 31;
+    const Params &P = A.P;
+    const Hard &H = A.H;
+    for (int guard = 0; guard < (1 << 30); guard++) {
+        int q = 0;
+        if (lane == 0) q = atomicAdd(A.queue, 1);
+        q = __shfl_sync(0xffffffffu, q, 0);
+        if (q >= A.n_clusters) return;
+        const int c = A.order ? A.order[q] : q;
+        const int o = A.off[c], n = A.cnt[c];
+        // FPHard(const FPGrav&), src/particle.h:1096-1116
+        for (int k = lane; k < n; k += 32) {
+            const int s = o + k, i = A.members[s];
+            st3(H.pos, s, ld3(A.S.pos, i)); st3(H.vel, s, ld3(A.S.vel, i));
+            st3(H.acc_s, s, ld3(A.S.acc_s, i)); st3(H.jerk_s, s, ld3(A.S.jerk_s, i));
+            st3(H.acc_d, s, ld3(A.S.acc_d, i)); st3(H.jerk_d, s, ld3(A.S.jerk_d, i));
+            const V3 z = v3(0., 0., 0.);
+            st3(H.x0, s, z); st3(H.v0, s, z); st3(H.a0_s, s, z); st3(H.j0_s, s, z); st3(H.a0_d, s, z);
+            st3(H.j0_d, s, z); st3(H.xp, s, z); st3(H.vp, s, z); st3(H.a2_s, s, z); st3(H.a3_s, s, z);
+            st3(H.a2_d, s, z); st3(H.a3_d, s, z);
+            H.phi_d[s] = A.S.phi_d[i]; H.phi_s[s] = A.S.phi_s[i];
+            H.mass[s] = A.S.mass[i]; H.r_planet[s] = A.S.r_planet[i]; H.f[s] = A.S.f[i];
+            H.r_out_inv[s] = A.S.r_out_inv[i];
+            H.time_c[s] = A.S.time[i]; H.th[s] = 0.; H.dt[s] = A.S.dt[i]; H.acc0[s] = A.S.acc0[i];
+            H.id[s] = A.S.id[i];
+            H.dead[s] = 0; H.merged[s] = 0;
+            H.tw_head[s] = H.tw_tail[s] = H.tw_next[s] = -1;
+        }
+        __syncwarp();
+        for (int k = lane; k < n; k += 32) hard_force(P, H, o, n, o + k, 0);
+        __syncwarp();
+        int n_col = 0;
+        double ed = 0., edd = 0.;
+        double time = 0.;
+        int steps = 0;
+        while (time < A.t_end) {
+            if (++steps > MAX_BLOCK_STEPS) {
+                if (lane == 0) atomicOr(A.status, ST_ITER_CAP);
+                break;
+            }
+            // makeActiveList, src/hermite.h:4-24
+            double ts = 1.e10;
+            for (int k = lane; k < n; k += 32) {
+                const int s = o + k;
+                if (!H.dead[s]) ts = dmin(ts, H.th[s] + H.dt[s]);
+            }
+            ts = warp_min(ts);
+            for (int k = lane; k < n; k += 32) {
+                const int s = o + k;
+                st3(H.xp, s, v3(0., 0., 0.));
+                st3(H.vp, s, v3(0., 0., 0.));
+                predict(H, s, ts - H.th[s]);
+            }
+            __syncwarp();
+            // collisionDetermination, src/hermite.h:98-196: the first ordered
+            // pair (i, j) with the smallest R < 1
+            double Rb = 1.;
+            long long pb = 0x7fffffffffffffffLL;
+            for (int a = lane; a < n; a += 32) {
+                const int si = o + a;
+                if (H.dead[si]) continue;
+                const V3 xi = ld3(H.xp, si);
+                const double ri = H.f[si] * H.r_planet[si];
+                for (int b = 0; b < n; b++) {
+                    const int sj = o + b;
+                    if (a == b || H.dead[sj]) continue;
+                    const V3 dr = xi - ld3(H.xp, sj);
+                    const double r1 = sqrt(dot(dr, dr));
+                    const double r2 = ri + H.f[sj] * H.r_planet[sj];
+                    const double R = r1 / r2;
+                    const long long p = (long long)a * n + b;
+                    if (R < Rb || (R == Rb && R < 1. && p < pb)) { Rb = R; pb = p; }
+                }
+            }
+            for (int sh = 16; sh > 0; sh >>= 1) {
+                const double R2 = __shfl_xor_sync(0xffffffffu, Rb, sh);
+                const long long p2 = __shfl_xor_sync(0xffffffffu, pb, sh);
+                if (R2 < Rb || (R2 == Rb && p2 < pb)) { Rb = R2; pb = p2; }
+            }
+            const bool col = Rb < 1.;
+            int imp = -1, tar = -1;
+            if (col) {
+                const int a = (int)(pb / n), b = (int)(pb % n);
+                if (H.mass[o + a] < H.mass[o + b]) { imp = o + a; tar = o + b; }
+                else { imp = o + b; tar = o + a; }
+                for (int k = lane; k < n; k += 32) H.dt[o + k] = ts - H.th[o + k];
+            }
+            __syncwarp();
+            // correct the active set (all alive on a collision)
+            for (int k = lane; k < n; k += 32) {
+                const int s = o + k;
+                if (H.dead[s]) continue;
+                if (!col && H.th[s] + H.dt[s] != ts) continue;
+                hard_force(P, H, o, n, s, 1);
+                if (H.merged[s]) {
+                    for (int t = H.tw_head[s], g = 0; t >= 0 && g < 4096; t = H.tw_next[t], g++)
+                        hard_force(P, H, o, n, t, 1);
+                    merge_acc_jerk(H, s);
+                }
+                const double tc = ts - H.th[s];
+                for (int it = 0; it < 2; it++) {
+                    correct(H, s, tc);
+                    if (H.merged[s])
+                        for (int t = H.tw_head[s], g = 0; t >= 0 && g < 4096; t = H.tw_next[t], g++)
+                            correct(H, t, tc);
+                    hard_force(P, H, o, n, s, 2);
+                    if (H.merged[s]) {
+                        for (int t = H.tw_head[s], g = 0; t >= 0 && g < 4096; t = H.tw_next[t], g++)
+                            hard_force(P, H, o, n, t, 2);
+                        merge_acc_jerk(H, s);
+                    }
+                }
+                H.th[s] += tc;
+                if (H.merged[s])
+                    for (int t = H.tw_head[s], g = 0; t >= 0 && g < 4096; t = H.tw_next[t], g++) H.th[t] += tc;
+                if (!col) {
+                    dt_hermite(P, H, s);
+                    if (H.merged[s])
+                        for (int t = H.tw_head[s], g = 0; t >= 0 && g < 4096; t = H.tw_next[t], g++)
+                            H.dt[t] = H.dt[s];
+                }
+            }
+            __syncwarp();
+            if (col) {
+                if (lane == 0) {
+                    ColRec rec;
+                    double e1 = 0., e2 = 0.;
+                    collide(P, H, imp, tar, e1, e2, rec);
+                    ed += e1;
+                    edd += e2;
+                    rec.cluster = c;
+                    rec.seq = n_col;
+                    const int slot = atomicAdd(A.n_cols, 1);
+                    if (slot < A.col_cap) A.cols[slot] = rec;
+                    else atomicOr(A.status, ST_QUEUE_OVERFLOW);
+                }
+                n_col++;
+                __syncwarp();
+                for (int k = lane; k < n; k += 32) hard_force(P, H, o, n, o + k, 0);
+                __syncwarp();
+                for (int k = lane; k < n; k += 32)
+                    if (H.merged[o + k] && H.tw_head[o + k] >= 0) merge_acc_jerk(H, o + k);
+                __syncwarp();
+                for (int k = lane; k < n; k += 32) {
+                    const int s = o + k;
+                    if (!H.dead[s])
+                        H.dt[s] = dt_initial(P, H.th[s], H.dt[s], H.acc0[s], ld3(H.acc_d, s), ld3(H.jerk_d, s),
+                                             ld3(H.acc_s, s), ld3(H.jerk_s, s));
+                }
+                __syncwarp();
+                for (int k = lane; k < n; k += 32) {
+                    const int s = o + k;
+                    if (H.merged[s])
+                        for (int t = H.tw_head[s], g = 0; t >= 0 && g < 4096; t = H.tw_next[t], g++) H.dt[t] = H.dt[s];
+                }
+                __syncwarp();
+            }
+            // getSystemTime, src/hermite.h:25-35
+            double tmin = 1.e10;
+            for (int k = lane; k < n; k += 32)
+                if (!H.dead[o + k]) tmin = dmin(tmin, H.th[o + k]);
+            time = warp_min(tmin);
+        }
+        __syncwarp();
+        for (int k = lane; k < n; k += 32) hard_force(P, H, o, n, o + k, 0);
+        __syncwarp();
+        if (n_col > 0)
+            for (int k = lane; k < n; k += 32)
+                if (H.merged[o + k] && H.tw_head[o + k] >= 0) merge_acc_jerk(H, o + k);
+        __syncwarp();
+        // write back to FPGrav, with resetTime (src/hard.h:768-787)
+        for (int k = lane; k < n; k += 32) {
+            const int s = o + k, i = A.members[s];
+            st3(A.S.pos, i, ld3(H.pos, s)); st3(A.S.vel, i, ld3(H.vel, s));
+            st3(A.S.acc_s, i, ld3(H.acc_s, s)); st3(A.S.jerk_s, i, ld3(H.jerk_s, s));
+            st3(A.S.acc_d, i, ld3(H.acc_d, s)); st3(A.S.jerk_d, i, ld3(H.jerk_d, s));
+            A.S.phi_d[i] = H.phi_d[s]; A.S.phi_s[i] = H.phi_s[s];
+            A.S.mass[i] = H.mass[s]; A.S.r_planet[i] = H.r_planet[s];
+            A.S.time[i] = H.time_c[s] + H.th[s]; A.S.dt[i] = H.dt[s];
+            A.S.id[i] = H.id[s];
+            A.S.dead[i] = H.dead[s]; A.S.merged[i] = H.merged[s];
+            A.S.n_cluster[i] = n;
+        }
+        if (lane == 0) {
+            A.cl_edisp[2 * c] = (n_col > 0) ? ed : 0.;
+            A.cl_edisp[2 * c + 1] = (n_col > 0) ? edd : 0.;
+        }
+        __syncwarp();
+    }
+}
+
+// ---- isolated bodies ----------------------------------------------------------
+__device__ __forceinline__ double kepler_eq(double u, double e) { return u - e * sin(u); }
+__device__ double solve_kepler(double l, double e) {  // src/kepler.h:5-38
+    const double e2 = e * e, e3 = e2 * e, e4 = e2 * e2, e5 = e3 * e2, e6 = e3 * e3;
+    double u = l + (e - e3 / 8. + e5 / 192.) * sin(l) + (e2 / 2. - e4 / 6. + e6 / 48.) * sin(2. * l) +
+               (3. * e3 / 8. - 27. * e5 / 128.) * sin(3. * l) + (e4 / 3. - 4. * e6 / 15.) * sin(4. * l) +
+               125. * e5 / 384. * sin(5. * l) + 27. * e6 / 80. * sin(6. * l);
+    if (fabs(kepler_eq(u, e) - l) > 1.e-15) {
+        double u0;
+        int loop = 0;
+        do {
+            u0 = u;
+            const double s = sin(u0), co = cos(u0);
+            u = u0 - ((u0 - e * s - l) / (1. - e * co));
+            loop++;
+        } while (fabs(u - u0) > 1.e-15 && loop < 10);
+    }
+    return u;
+}
+
+struct IsoArgs {
+    State S;
+    Params P;
+    double t0, t1;
+    int *status;
+};
+
+__global__ void k_isolated(IsoArgs A) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const State &S = A.S;
+    const Params &P = A.P;
+    if (i >= S.n || S.number[i] != 0) return;
+    V3 pos = ld3(S.pos, i), vel = ld3(S.vel, i);
+    // getEccentricity, src/particle.h:668-681
+    double ecc;
+    {
+        const double r = sqrt(dot(pos, pos));
+        const double rv = dot(pos, vel);
+        const double ax = 1.0 / (2.0 / r - dot(vel, vel) / P.m_sun);
+        const double ecccosu = 1. - r / ax;
+        const double eccsinu2 = rv * rv / (P.m_sun * ax);
+        ecc = sqrt(ecccosu * ecccosu + eccsinu2);
+    }
+    V3 as, js;
+    double phs;
+    if (ecc < 0.8 && P.eps2_sun == 0.) {
+        // timeIntegrateKepler_isolated, src/hermite.h:787-815
+        const double mu = P.m_sun;
+        const double r2 = dot(pos, pos), r = sqrt(r2), rinv = 1. / r;
+        const double v2 = dot(vel, vel), rv = dot(pos, vel);
+        const double ax = 1.0 / (2.0 * rinv - v2 / mu);
+        const double ecccosu = 1. - r / ax;
+        const double eccsinu = rv / sqrt(mu * ax);
+        const double e = sqrt(ecccosu * ecccosu + eccsinu * eccsinu);
+        const double nm = sqrt(mu / (ax * ax * ax));
+        double u, cosu, sinu;
+        if (e != 0) { u = atan2(eccsinu, ecccosu); cosu = ecccosu / e; sinu = eccsinu / e; }
+        else { u = 0.; cosu = 1.; sinu = 0.; }
+        const double aninv = sqrt(ax / mu);
+        const double ecc_sq = sqrt(1. - e * e);
+        const V3 PP = rinv * cosu * pos - aninv * sinu * vel;
+        const V3 QQ = (rinv * sinu * pos + aninv * (cosu - e) * vel) / ecc_sq;
+        double l = kepler_eq(u, e);
+        l += nm * (A.t1 - A.t0);
+        u = solve_kepler(l, e);
+        const double cu = cos(u), su = sin(u);
+        const double esq = sqrt(1. - e * e);
+        pos = ax * ((cu - e) * PP + esq * su * QQ);
+        const double ri = sqrt(1. / dot(pos, pos));
+        vel = ax * ax * nm * ri * (-su * PP + esq * cu * QQ);
+        st3(S.pos, i, pos);
+        st3(S.vel, i, vel);
+        S.time[i] += (A.t1 - A.t0);
+        S.phi_d[i] = 0.;
+        st3(S.acc_d, i, v3(0., 0., 0.));
+        st3(S.jerk_d, i, v3(0., 0., 0.));
+        sun_force(P, pos, vel, as, js, &phs);
+        st3(S.acc_s, i, as);
+        st3(S.jerk_s, i, js);
+        S.phi_s[i] = phs;
+        S.dt[i] = dt_initial(P, S.time[i], S.dt[i], S.acc0[i], v3(0., 0., 0.), v3(0., 0., 0.), as, js);
+    } else {
+        // timeIntegrate_isolated, src/hermite.h:734-785, on a one-member Hard
+        // view of this body's state arrays
+        const double time_c = S.time[i];
+        double th = 0., dt = S.dt[i];
+        const double acc0 = S.acc0[i];
+        V3 ad = v3(0., 0., 0.), jd = v3(0., 0., 0.);
+        V3 a0s, j0s, a0d, j0d, xp, vp, a2s, a3s, a2d, a3d;
+        sun_force(P, pos, vel, as, js, &phs);
+        ad = ld3(S.acc_d, i);
+        jd = ld3(S.jerk_d, i);
+        int steps = 0;
+        while (th < A.t1 - A.t0) {
+            if (++steps > MAX_BLOCK_STEPS) { atomicOr(A.status, ST_ITER_CAP); break; }
+            // predict
+            a0s = as; j0s = js; j0d = jd; a0d = ad;
+            {
+                const V3 a = as + ad, j = js + jd;
+                xp = pos + dt * (vel + dt * (0.5 * a + 1.6666666666666667e-1 * dt * j));
+                vp = vel + dt * (a + dt * 0.5 * j);
+            }
+            ad = v3(0., 0., 0.);
+            jd = v3(0., 0., 0.);
+            sun_force(P, xp, vp, as, js, nullptr);
+            for (int it = 0; it < 2; it++) {
+                const double Dt = dt, Dt2 = Dt * Dt, Di = 1. / Dt, Di2 = Di * Di, Di3 = Di2 * Di;
+                const V3 Am_s = as - a0s, J0_s = Dt * j0s, J1_s = Dt * js;
+                const V3 A2_s = 3. * Am_s - (J1_s + 2. * J0_s);
+                const V3 A3_s = -2. * Am_s + (J1_s + J0_s);
+                a2s = 2. * Di2 * (A2_s + 3. * A3_s);
+                a3s = 6. * Di3 * A3_s;
+                const V3 Am_d = ad - a0d, J0_d = j0d * Dt, J1_d = jd * Dt;
+                const V3 A2_d = 3. * Am_d - (J1_d + 2. * J0_d);
+                const V3 A3_d = -2. * Am_d + (J1_d + J0_d);
+                a2d = 2. * (A2_d + 3. * A3_d) * Di2;
+                a3d = 6. * A3_d * Di3;
+                const V3 A2 = A2_s + A2_d, A3 = A3_s + A3_d;
+                pos = xp + 1.6666666666666667e-2 * Dt2 * (5. * A2 + 3. * 1.1666666666666667e-3 * A3);
+                vel = vp + 8.3333333333333333e-2 * Dt * (4. * A2 + 3. * A3);
+                sun_force(P, pos, vel, as, js, nullptr);
+            }
+            th += dt;
+            // calcDeltat
+            double dt_next = dmin(2. * dt, 0.5 * P.dt_tree);
+            const double dt_1 = dmin(dt4th(P.eta, P.alpha2, acc0, ad, jd, a2d, a3d),
+                                     dt4th(P.eta_sun, P.alpha2, 0., as, js, a2s, a3s));
+            double rem = fmod(th, dt_next);
+            for (int k = 0; rem != 0.0 && k < 1100; k++) { dt_next *= 0.5; rem = fmod(th, dt_next); }
+            for (int k = 0; dt_1 < dt_next && 0.5 * dt < dt_next && k < 1100; k++) dt_next *= 0.5;
+            if (dt_next < 2. * P.dt_min) dt_next = P.dt_min;
+            dt = dt_next;
+        }
+        sun_force(P, pos, vel, as, js, &phs);
+        st3(S.pos, i, pos);
+        st3(S.vel, i, vel);
+        st3(S.acc_s, i, as);
+        st3(S.jerk_s, i, js);
+        st3(S.acc_d, i, ad);
+        st3(S.jerk_d, i, jd);
+        S.phi_s[i] = phs;
+        S.phi_d[i] = 0.;
+        S.time[i] = time_c + th;
+        S.dt[i] = dt;
+    }
+    S.n_cluster[i] = 1;
+}
+
+__global__ void k_edisp_total(const double *cl_ed, const int32_t *cnt, int nc, double *out) {
+    if (threadIdx.x || blockIdx.x) return;
+    // clusters of 64 or more members first, then the rest (src/hard.h:562-583,700-765)
+    double e = 0., ed = 0.;
+    for (int pass = 0; pass < 2; pass++)
+        for (int c = 0; c < nc; c++)
+            if ((cnt[c] >= 64) == (pass == 0)) { e += cl_ed[2 * c]; ed += cl_ed[2 * c + 1]; }
+    out[0] = e;
+    out[1] = ed;
+}
+
+// ---- host side ------------------------------------------------------------------
+struct HardBufs {
+    DevBuf<double> d;
+    DevBuf<int64_t> id;
+    DevBuf<int32_t> i32, order, queue, n_cols;
+    DevBuf<double> cl_edisp, etot;
+    DevBuf<ColRec> cols;
+    Hard H;
+    int cap = 0;
+    int reserve(int m) {
+        if (m <= cap && d.p) return 0;
+        const int mm = std::max(m, 1);
+        int r = 0;
+        const int nvec = 18, nsc = 10;
+        if ((r = d.reserve((size_t)mm * (3 * nvec + nsc))) || (r = id.reserve(mm)) || (r = i32.reserve((size_t)mm * 5)))
+            return r;
+        double *p = d.p;
+        double **vecs[nvec] = {&H.pos, &H.vel, &H.acc_s, &H.jerk_s, &H.acc_d, &H.jerk_d, &H.x0, &H.v0, &H.a0_s,
+                               &H.j0_s, &H.a0_d, &H.j0_d, &H.xp, &H.vp, &H.a2_s, &H.a3_s, &H.a2_d, &H.a3_d};
+        for (int k = 0; k < nvec; k++) { *vecs[k] = p; p += 3 * (size_t)mm; }
+        double **scs[nsc] = {&H.phi_d, &H.phi_s, &H.mass, &H.r_planet, &H.f, &H.r_out_inv, &H.th, &H.dt, &H.acc0,
+                             &H.time_c};
+        for (int k = 0; k < nsc; k++) { *scs[k] = p; p += mm; }
+        H.id = id.p;
+        int32_t *q = i32.p;
+        H.dead = q; q += mm;
+        H.merged = q; q += mm;
+        H.tw_head = q; q += mm;
+        H.tw_tail = q; q += mm;
+        H.tw_next = q;
+        cap = mm;
+        return 0;
+    }
+};
+static HardBufs g_hb;
+static std::vector<ColRec> g_cols;
+static double g_edisp[2] = {0., 0.};
+
+}  // namespace p3t
+
+using namespace p3t;
+
+extern "C" {
+
+int p3t_hard(int istep, int col_cap, long long *col_pairs, double *edisp) {
+    Engine &E = g_eng;
+    if (!E.c) return -(int)cudaErrorNoDevice;
+    Context *c = E.c;
+    HardBufs &B = g_hb;
+    const int nc = E.n_clusters;
+    int r = 0;
+    if ((r = B.reserve(E.n_members)) || (r = B.order.reserve(nc)) || (r = B.queue.reserve(1)) ||
+        (r = B.n_cols.reserve(1)) || (r = B.cl_edisp.reserve(2 * (size_t)nc + 2)) || (r = B.etot.reserve(2)) ||
+        (r = B.cols.reserve(4096)))
+        return r;
+    // schedule: largest clusters first
+    std::vector<int32_t> cnt(nc), ord(nc);
+    if (nc > 0) {
+        if ((r = cuda_status(cudaMemcpy(cnt.data(), E.cl_cnt.p, nc * sizeof(int32_t), cudaMemcpyDeviceToHost))))
+            return r;
+        for (int k = 0; k < nc; k++) ord[k] = k;
+        std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return cnt[a] > cnt[b]; });
+        if ((r = h2d(c, B.order.p, ord.data(), nc * sizeof(int32_t)))) return r;
+    }
+    cudaMemsetAsync(B.queue.p, 0, sizeof(int32_t), c->stream);
+    cudaMemsetAsync(B.n_cols.p, 0, sizeof(int32_t), c->stream);
+    const Params P = E.params();
+    if (nc > 0) {
+        HardArgs A;
+        A.S = E.S;
+        A.P = P;
+        A.H = B.H;
+        A.off = E.cl_off.p;
+        A.cnt = E.cl_cnt.p;
+        A.members = E.members.p;
+        A.order = B.order.p;
+        A.n_clusters = nc;
+        A.queue = B.queue.p;
+        A.cl_edisp = B.cl_edisp.p;
+        A.cols = B.cols.p;
+        A.n_cols = B.n_cols.p;
+        A.col_cap = 4096;
+        A.status = c->status;
+        A.t_end = P.dt_tree;
+        int sms = 152;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+        const int blocks = std::min((nc + 3) / 4, sms * 8);
+        k_hard_clusters<<<blocks, 128, 0, c->stream>>>(A);
+        if ((r = cuda_status(cudaGetLastError()))) return r;
+    }
+    IsoArgs I;
+    I.S = E.S;
+    I.P = P;
+    I.t0 = (istep - 1) * P.dt_tree;
+    I.t1 = istep * P.dt_tree;
+    I.status = c->status;
+    if (E.S.n > 0) k_isolated<<<(E.S.n + 127) / 128, 128, 0, c->stream>>>(I);
+    if ((r = cuda_status(cudaGetLastError()))) return r;
+    k_edisp_total<<<1, 32, 0, c->stream>>>(B.cl_edisp.p, E.cl_cnt.p, nc, B.etot.p);
+    int ncol = 0;
+    cudaMemcpyAsync(&ncol, B.n_cols.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+    cudaMemcpyAsync(g_edisp, B.etot.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if ((r = cuda_status(cudaStreamSynchronize(c->stream)))) return r;
+    ncol = std::min(ncol, 4096);
+    g_cols.resize(ncol);
+    if (ncol && (r = cuda_status(cudaMemcpy(g_cols.data(), B.cols.p, ncol * sizeof(ColRec), cudaMemcpyDeviceToHost))))
+        return r;
+    // collision-list order of the reference: clusters of 64+ members first,
+    // each group in cluster order, collisions in time order within a cluster
+    std::stable_sort(g_cols.begin(), g_cols.end(), [&](const ColRec &a, const ColRec &b) {
+        const bool la = cnt[a.cluster] >= 64, lb = cnt[b.cluster] >= 64;
+        if (la != lb) return la;
+        if (a.cluster != b.cluster) return a.cluster < b.cluster;
+        return a.seq < b.seq;
+    });
+    for (int k = 0; k < ncol && k < col_cap; k++) {
+        col_pairs[2 * k] = g_cols[k].id_imp;
+        col_pairs[2 * k + 1] = g_cols[k].id_tar;
+    }
+    edisp[0] = g_edisp[0];
+    edisp[1] = g_edisp[1];
+    int st = read_status(c);
+    if (st) return st;
+    return ncol;
+}
+
+}  // extern "C"

@@ -1,0 +1,37 @@
+// Device-resident P3T step engine (one per process, bound to the library's
+// context and stream).
+#pragma once
+#include "p3t_capi_internal.cuh"
+#include "p3t_state.cuh"
+
+namespace p3t {
+
+struct Engine {
+    Context *c = nullptr;
+    State S;
+    int cand_cap_alloc = 0;
+    int n_clusters = 0, n_members = 0;
+    DevBuf<int32_t> counters, head, flag, cidx, cl_of, cl_cnt, cl_off, cl_fill, members_tmp, members, keep, kpos,
+        scan_tmp;
+    DevBuf<int64_t> cmin;
+    DevBuf<double> epart, et;
+    DevBuf<int> icnt;
+
+    int ensure(int n);
+    Params params() const;
+    int load(int n, const long long *id, const double *mass, const double *r_planet, const double *f,
+             const double *pos, const double *vel);
+    int pack_soft();
+    int correct(int initial);
+    int cluster();
+    int make_list();
+    int kick();
+    int energy(double *out5);
+    int cutoff_radii();
+    int merge(double *edisp);
+    int scan(const int32_t *in, int32_t *out, int n, int32_t *total);
+};
+
+extern Engine g_eng;
+
+}  // namespace p3t

@@ -1,0 +1,148 @@
+"""The device-resident P3T step through the C ABI (include/gplum_p3t.h).
+
+:class:`GpuSystem` exposes the phases of GPLUM's tree step
+(src/main_p3t.cpp:423-717) on a particle system that stays in HBM, with the
+same method names as the CPU checkers' harness, so one driver runs a
+scenario on either.  Interaction lists come from the host tree
+(gplum_gb300.tree) built on the current positions.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .soft import configure
+
+VP = ctypes.c_void_p
+VEC_FIELDS = {"pos": 0, "vel": 1, "acc": 2, "acc_d": 3, "jerk_d": 4, "acc_s": 5, "jerk_s": 6}
+SCALAR_FIELDS = {"phi": 10, "phi_d": 11, "phi_s": 12, "mass": 13, "r_out": 14, "r_search": 15, "dt": 16,
+                 "acc0": 17, "time": 18, "r_planet": 19, "v_disp": 20, "r_out_inv": 21}
+I64_FIELDS = {"id": 100, "id_cluster": 101}
+I32_FIELDS = {"number": 102, "n_cluster": 103, "dead": 104, "merged": 105, "rank": 106, "id_min": 107,
+              "id_max": 108}
+
+
+class GpuSystem:
+    kind = "gpu"
+
+    def __init__(self, params, precision=0, trace_mode=0, cand_cap=64):
+        self.lib = configure(params, precision, trace_mode, cand_cap)
+        self.params = params
+        self.cand_cap = cand_cap
+
+    def _chk(self, st, what):
+        _lib.check(st, what)
+
+    def load(self, disk):
+        a = [np.ascontiguousarray(disk[k], dtype=t) for k, t in
+             (("id", np.int64), ("mass", np.float64), ("r_planet", np.float64), ("f", np.float64),
+              ("pos", np.float64), ("vel", np.float64))]
+        self._chk(self.lib.p3t_state_load(len(a[1]), *(x.ctypes.data_as(VP) for x in a)), "p3t_state_load")
+
+    @property
+    def n(self):
+        return self.lib.p3t_state_n()
+
+    def get(self, name):
+        n = self.n
+        if name in VEC_FIELDS:
+            out, code = np.zeros((n, 3)), VEC_FIELDS[name]
+        elif name in SCALAR_FIELDS:
+            out, code = np.zeros(n), SCALAR_FIELDS[name]
+        elif name in I64_FIELDS:
+            out, code = np.zeros(n, np.int64), I64_FIELDS[name]
+        else:
+            out, code = np.zeros(n, np.int32), I32_FIELDS[name]
+        self._chk(self.lib.p3t_state_get(code, out.ctypes.data_as(VP)), "p3t_state_get")
+        return out
+
+    def set(self, name, val):
+        code = VEC_FIELDS.get(name, SCALAR_FIELDS.get(name))
+        dt = np.float64
+        if code is None and name in I64_FIELDS:
+            code, dt = I64_FIELDS[name], np.int64
+        elif code is None:
+            code, dt = I32_FIELDS[name], np.int32
+        val = np.ascontiguousarray(val, dtype=dt)
+        self._chk(self.lib.p3t_state_set(code, val.ctypes.data_as(VP)), "p3t_state_set")
+
+    def set_r_planet(self):
+        self._chk(self.lib.p3t_set_r_planet(), "p3t_set_r_planet")
+
+    def prepare(self):
+        """setIDLocalAndMyrank (implicit: index order) + setCutoffRadii."""
+        self._chk(self.lib.p3t_set_cutoff_radii(), "p3t_set_cutoff_radii")
+
+    def soft_force(self, L):
+        st = self.lib.p3t_state_soft(L["n_group"], *(L[k].ctypes.data_as(VP) for k in
+                                                     ("i_off", "i_idx", "j_off", "j_idx", "s_off", "s_idx")),
+                                     L["spj"].ctypes.data_as(VP), len(L["spj"]))
+        self._chk(st, "p3t_state_soft")
+
+    def correct(self, initial):
+        self._chk(self.lib.p3t_correct(1 if initial else 0), "p3t_correct")
+
+    def neighbor_ids_local(self, i):
+        out = np.zeros(self.cand_cap, np.int32)
+        m = self.lib.p3t_neighbor_list(i, out.ctypes.data_as(VP), self.cand_cap)
+        return out[:max(m, 0)]
+
+    def pairs(self):
+        """(i, j) with i < j, j a neighbour of i (NeighborList::pair_list)."""
+        num = self.get("number")
+        out = []
+        for i in np.nonzero(num)[0]:
+            for j in self.neighbor_ids_local(int(i)):
+                if i < j:
+                    out.append((int(i), int(j)))
+        return np.array(out, dtype=np.int32).reshape(-1, 2)
+
+    def cluster(self):
+        self._chk(self.lib.p3t_cluster_label(), "p3t_cluster_label")
+
+    def cluster_lists(self):
+        nc = ctypes.c_int(0)
+        self._chk(self.lib.p3t_cluster_lists(ctypes.byref(nc), None, None), "p3t_cluster_lists")
+        off = np.zeros(nc.value + 1, np.int32)
+        mem = np.zeros(max(1, self.n), np.int32)
+        self._chk(self.lib.p3t_cluster_lists(ctypes.byref(nc), off.ctypes.data_as(VP), mem.ctypes.data_as(VP)),
+                  "p3t_cluster_lists")
+        return off, mem[:off[-1]]
+
+    def kick(self):
+        self._chk(self.lib.p3t_kick(), "p3t_kick")
+
+    def hard(self, istep, col_cap=4096):
+        cols = np.zeros(2 * col_cap, np.int64)
+        ed = np.zeros(2)
+        nc = self.lib.p3t_hard(istep, col_cap, cols.ctypes.data_as(VP), ed.ctypes.data_as(VP))
+        if nc < 0:
+            raise RuntimeError(f"p3t_hard failed with status {nc}")
+        return cols[:2 * min(nc, col_cap)].reshape(-1, 2), ed
+
+    def energy(self):
+        out = np.zeros(5)
+        self._chk(self.lib.p3t_energy(out.ctypes.data_as(VP)), "p3t_energy")
+        return out
+
+    def merge(self, n_col):
+        e = ctypes.c_double(0.0)
+        self._chk(self.lib.p3t_merge(ctypes.byref(e)), "p3t_merge")
+        return e.value
+
+    def counts(self):
+        a, b = ctypes.c_int(), ctypes.c_int()
+        self._chk(self.lib.p3t_neighbor_counts(ctypes.byref(a), ctypes.byref(b)), "p3t_neighbor_counts")
+        return a.value, b.value
+
+    # interface of the checkers' harness (oracle/harness.py)
+    def f(self, name):
+        if name == "set_r_planet":
+            return self.set_r_planet
+        if name == "set_id_local":
+            return lambda: None
+        if name == "n_cluster":
+            return lambda: len(self.cluster_lists()[0]) - 1
+        if name == "n_isolated":
+            return lambda: int((self.get("number") == 0).sum())
+        raise AttributeError(name)

@@ -96,6 +96,57 @@ int p3t_soft_force_host(int n, const void *epj, int n_group, const int *i_off, c
                         const int *j_off, const int *j_idx, const int *s_off, const int *s_idx,
                         const void *spj, int n_spj, void *force);
 
+/* ---- device-resident P3T step ----------------------------------------------------
+ * The particle system lives in HBM (the FPGrav fields the step touches);
+ * each call below is one phase of GPLUM's tree step (src/main_p3t.cpp:423-717)
+ * on that state.  Field codes of p3t_state_get / p3t_state_set:
+ *   double[n][3]: 0 pos, 1 vel, 2 acc (soft), 3 acc_d, 4 jerk_d, 5 acc_s, 6 jerk_s
+ *   double[n]:   10 phi, 11 phi_d, 12 phi_s, 13 mass, 14 r_out, 15 r_search,
+ *                16 dt, 17 acc0, 18 time, 19 r_planet, 20 v_disp, 21 r_out_inv
+ *   int64[n]:   100 id, 101 id_cluster
+ *   int32[n]:   102 neighbor.number, 103 n_cluster, 104 isDead, 105 isMerged,
+ *               106 neighbor.rank, 107 neighbor.id_min, 108 neighbor.id_max */
+/* Loads n bodies and applies the start-up reset (src/main_p3t.cpp:291-303). */
+int p3t_state_load(int n, const long long *id, const double *mass, const double *r_planet, const double *f,
+                   const double *pos, const double *vel);
+int p3t_state_n(void);
+int p3t_state_get(int field, void *out);
+int p3t_state_set(int field, const void *in);
+/* setCutoffRadii (src/particle.h:1528-1543) on the device. */
+int p3t_set_cutoff_radii(void);
+/* FPGrav::setRPlanet for every body (src/particle.h:757-759). */
+int p3t_set_r_planet(void);
+/* Soft force of the state over caller-supplied lists (the
+ * calcForceAllAndWriteBack pass of src/main_p3t.cpp:583-587), with the
+ * neighbour-candidate table filled for p3t_correct. */
+int p3t_state_soft(int n_group, const int *i_off, const int *i_idx, const int *j_off, const int *j_idx,
+                   const int *s_off, const int *s_idx, const void *spj, int n_spj);
+/* correctForceLong (initial = 0) / correctForceLongInitial (initial = 1),
+ * src/gravity_soft.h:245-528: FP64 cutoff correction, exact neighbour test,
+ * neighbour lists, acc0 (and for initial: sun force, acc_d, jerk_d, phi_d,
+ * first dt). */
+int p3t_correct(int initial);
+int p3t_neighbor_counts(int *n_ngb_tot, int *n_with_ngb);
+/* Neighbour local indices of body i (returns their count, at most cap). */
+int p3t_neighbor_list(int i, int *out, int cap);
+/* NeighborList::createNeighborCluster (src/neighbor.h:800-839) followed by
+ * HardSystem::makeList (src/hard.h:321-438). */
+int p3t_cluster_label(void);
+/* off has n_clusters + 1 entries, members sum(cluster sizes). */
+int p3t_cluster_lists(int *n_clusters, int *off, int *members);
+/* HardSystem::timeIntegrate (src/hard.h:554-829): every cluster in one
+ * persistent launch plus the isolated-body drift.  Returns the number of
+ * collisions (>= 0) and writes (impactor id, target id) pairs and the
+ * dissipated energy {total, hard part}; a negative value is an error. */
+int p3t_hard(int istep, int col_cap, long long *col_pairs, double *edisp);
+/* velKick, src/gravity_soft.h:5-12. */
+int p3t_kick(void);
+/* Energy::calcEnergy, src/energy.h:29-63: {etot, ekin, ephi_sun, ephi, ephi_d}. */
+int p3t_energy(double *out5);
+/* MergeParticle, src/func.h:160-207 (order-preserving removal of the merged
+ * twins); adds the dissipated energy to *edisp. */
+int p3t_merge(double *edisp);
+
 /* ---- measurement -------------------------------------------------------------
  * FMA throughput of this GPU (TFLOP/s, FMA = 2 flops), FP32 (fp64 = 0) or
  * FP64 (fp64 = 1): the roofline denominators of the soft (FP32-pipe) and
