@@ -56,6 +56,10 @@ __global__ void k_scan_add(int32_t *out, const int32_t *bscan, int n) {
 }
 
 int Engine::scan(const int32_t *in, int32_t *out, int n, int32_t *total) {
+    if (n <= 0) {
+        if (total) *total = 0;
+        return 0;
+    }
     // levels of block sums live in scan_tmp
     std::vector<int> sizes;
     int m = n;
@@ -622,8 +626,11 @@ int Engine::pack_soft() {
 
 int Engine::correct(int initial) {
     const Params P = params();
-    int r = counters.reserve(4);
+    int r = ensure(S.n);
     if (r) return r;
+    // the candidate table of a soft pass over this state must exist
+    if (!c->res.cand.p || !c->res.force.p || c->res_n != S.n) return ST_BAD_INDEX;
+    if ((r = counters.reserve(4))) return r;
     cudaMemsetAsync(counters.p, 0, 4 * sizeof(int32_t), c->stream);
     k_correct<<<nb(S.n, 128), 128, 0, c->stream>>>(S, P, c->res.force.p, c->res.cand.p, c->cand_cap, initial,
                                                      counters.p, c->status);

@@ -16,7 +16,7 @@
 
 namespace p3t {
 
-constexpr int MAX_BLOCK_STEPS = 1 << 22;  // per cluster and tree step
+constexpr int MAX_BLOCK_STEPS = 1 << 20;  // per cluster and tree step
 
 // Per-member working copy of one cluster (FPHard fields), indexed by the
 // member's slot in the cluster lists.
