@@ -54,6 +54,7 @@ SIGNATURES = {
     "p3t_kick": (I, []),
     "p3t_energy": (I, [VP]),
     "p3t_merge": (I, [VP]),
+    "p3t_soft_force_noalloc": (I, [I, VP, I, VP, VP, VP, VP, VP, VP, VP, I, D, I, VP, VP]),
 }
 
 

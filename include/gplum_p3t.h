@@ -147,6 +147,30 @@ int p3t_energy(double *out5);
  * twins); adds the dissipated energy to *edisp. */
 int p3t_merge(double *edisp);
 
+/* ---- soft force without allocation ---------------------------------------------
+ * No counterpart in GPLUM.  For callers that cannot allocate device memory
+ * (their device memory comes from another runtime's arena or pool, or their
+ * process may not call cudaMalloc): the same fused EP-EP + EP-SP soft force
+ * as p3t_soft_force_host, mixed precision, on buffers the caller provides.
+ * epj (n EPJGrav records, id_local = index), the CSR lists, spj (n_spj
+ * SPJQuadrupole records) and force (n ForceGrav records, overwritten as
+ * ForceGrav::clear followed by both functors) are device-accessible
+ * pointers; stream is a cudaStream_t (0 for the default stream); the call
+ * returns after the stream has finished its work.  The library allocates
+ * nothing for it: its only scratch is a static per-device array of
+ * P3T_NOALLOC_MAX_BODIES packed bodies (3 MiB, held by every GPU that loads
+ * the library until the process exits) and a status word.  n above
+ * P3T_NOALLOC_MAX_BODIES is rejected with -cudaErrorInvalidValue and a
+ * message on stderr.  The first call on a device looks up the static
+ * array's device address, so make it before any stream capture.  All calls
+ * share the scratch: calls that overlap on the GPU race and must be
+ * serialised by the caller. */
+#define P3T_NOALLOC_MAX_BODIES 65536
+int p3t_soft_force_noalloc(int n, const void *epj, int n_group, const int *i_off, const int *i_idx,
+                           const int *j_off, const int *j_idx, const int *s_off, const int *s_idx,
+                           const void *spj, int n_spj, double eps2, int trace_mode, void *force,
+                           void *stream);
+
 /* ---- measurement -------------------------------------------------------------
  * FMA throughput of this GPU (TFLOP/s, FMA = 2 flops), FP32 (fp64 = 0) or
  * FP64 (fp64 = 1): the roofline denominators of the soft (FP32-pipe) and
