@@ -26,6 +26,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 N_BODIES = 1048576
+METRIC = "P3T steps/s, N=1M: mixed+batched vs plain FP64 on GB300 @ rel force err\u22641e-6"
 EPEP_FLOPS = 32  # per pair, FMA = 2, rsqrt/min/max/compare = 1
 EPSP_FLOPS = 70
 
@@ -102,6 +103,92 @@ class ClockSampler:
                 "reasons": sorted(reasons)}
 
 
+def p3t_step_measure(precision, steps=2, n=N_BODIES):
+    """The whole device P3T tree step (src/main_p3t.cpp:423-717) on the
+    hard-part disk (n bodies, 0.95-1.05 AU, rms e = 6 h): kick, cluster
+    labels + lists, hard part (one persistent launch), host tree + lists, soft
+    force, correction + neighbour search, kick, energy.  Wall-clock per phase
+    with the device synchronised at each phase boundary."""
+    from gplum_gb300.disk import P3TParams, disk_1m_hard
+    from gplum_gb300.p3t import GpuSystem
+    from gplum_gb300.tree import build_lists
+
+    P = P3TParams(n_group_limit=256)
+    d = disk_1m_hard(n)
+    g = GpuSystem(P, precision=precision)
+    ph = {}
+
+    def lists():
+        t0 = time.perf_counter()
+        L = build_lists(g.get("pos"), d["mass"] if g.n == len(d["mass"]) else g.get("mass"), g.get("r_search"),
+                        P.theta, P.n_leaf_limit, P.n_group_limit)
+        ph["tree_host"] = ph.get("tree_host", 0.0) + time.perf_counter() - t0
+        return L
+
+    g.load(d)
+    g.set_r_planet()
+    g.prepare()
+    for _ in range(2):
+        g.soft_force(lists())
+        g.correct(True)
+    e0 = g.energy()
+    ph.clear()
+    clusters = []
+    ncol = 0
+
+    def timed(name, fn):
+        g.lib.p3t_synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        g.lib.p3t_synchronize()
+        ph[name] = ph.get(name, 0.0) + time.perf_counter() - t0
+        return r
+
+    t_all = time.perf_counter()
+    for istep in range(1, steps + 1):
+        timed("kick", g.kick)
+        timed("cluster", g.cluster)
+        cols, _ = timed("hard", lambda: g.hard(istep))
+        ncol += len(cols)
+        off, _m = g.cluster_lists()
+        clusters.append((len(off) - 1, int(np.diff(off).max()) if len(off) > 1 else 0))
+        L = lists()
+        timed("soft", lambda: g.soft_force(L))
+        timed("correct", lambda: g.correct(False))
+        timed("kick", g.kick)
+        e = timed("energy", g.energy)
+        if len(cols):
+            timed("merge", lambda: g.merge(len(cols)))
+            timed("radii", g.prepare)
+            L = lists()
+            timed("soft", lambda: g.soft_force(L))
+            timed("correct", lambda: g.correct(True))
+    total = (time.perf_counter() - t_all) / steps
+    ms = {k: 1e3 * v / steps for k, v in ph.items()}
+    dev = sum(v for k, v in ms.items() if k != "tree_host")
+    return {"n_bodies": n, "steps": steps, "ms_per_step": 1e3 * total, "device_ms_per_step": dev,
+            "phases_ms": ms, "clusters_per_step": [c[0] for c in clusters],
+            "largest_cluster": max(c[1] for c in clusters), "collisions": ncol,
+            "dE_over_E": float((e[0] - e0[0]) / e0[0])}
+
+
+def cpu_step_baseline(n=N_BODIES, steps=1):
+    """The same whole tree step run by GPLUM's arithmetic on the host cores
+    (the oracle port, OpenMP over clusters and bodies as GPLUM's loops are),
+    with the same host tree; start-up not timed."""
+    from gplum_gb300.disk import P3TParams, disk_1m_hard
+    from oracle import harness as H
+
+    P = P3TParams(n_group_limit=256)
+    s = H.CpuSystem("orc", P)
+    lf = H.tree_lists_fn(P)
+    H.p3t_init(s, disk_1m_hard(n), lf)
+    t0 = time.perf_counter()
+    for istep in range(1, steps + 1):
+        H.p3t_step(s, istep, lf)
+    return (time.perf_counter() - t0) / steps
+
+
 def cpu_reference(L, epj, P, budget_s=20.0, threads=None):
     """GPLUM's functor arithmetic (oracle restatement, FP32 functors) on the
     host cores over a sample of the groups; returns (steps/s, sample text, cores)."""
@@ -157,7 +244,7 @@ def reference_arm(args, rank, world):
         steps_s.append(v)
     v = float(np.mean(steps_s))
     print(json.dumps({
-        "impl": "reference", "metric": "P3T soft-force steps/s (1M-body disk)", "value": v, "unit": "steps/s",
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s",
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 displacements)",
         "data": "synthetic seeded disk", "config": config(L),
@@ -253,7 +340,7 @@ def gpu_arm(args, rank, world):
     if rank != 0:
         return
     out = {
-        "metric": "P3T soft-force steps/s (1M-body disk)", "value": value, "unit": "steps/s", "n_gpus": world,
+        "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 displacements, compensated sums)",
         "data": "synthetic seeded disk", "config": config(L, {"epep_pairs": n_epep, "epsp_pairs": n_epsp}),
@@ -268,6 +355,19 @@ def gpu_arm(args, rank, world):
         "gpu_launches": args.steps,
         "clocks": clocks,
     }
+    if not args.skip_step:
+        try:
+            mixed = p3t_step_measure(0)
+            fp64 = p3t_step_measure(1, steps=1)
+            out["p3t_step"] = {"workload": "hard-part disk, 1048576 bodies, 0.95-1.05 AU, m=7e-11, "
+                                           "rms e=6h, rms i=3h, theta=0.5, n_group_limit=256",
+                               "mixed": mixed, "fp64_soft": fp64,
+                               "device_speedup": fp64["device_ms_per_step"] / mixed["device_ms_per_step"]}
+            cpu_s = cpu_step_baseline()
+            out["p3t_step"]["cpu_baseline"] = {"value": 1.0 / cpu_s, "unit": "steps/s", "cores": os.cpu_count(),
+                                               "kind": "port", "sample": "1 tree step, same disk and host tree"}
+        except Exception as e:
+            out["p3t_step"] = {"error": repr(e)}
     try:
         v, sample, cores = cpu_reference(L, epj, P, budget_s=15.0)
         out["cpu_baseline"] = {"value": v, "unit": "steps/s", "cores": cores, "kind": "port", "sample": sample}
@@ -282,6 +382,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--skip-step", action="store_true", help="skip the whole-step measurement")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -120,6 +120,12 @@ def disk_1m_soft(n=1048576, seed=2):
     return make_disk(n, 1e-10, 0.5, 1.5, ecc_hill=2.0, inc_hill=1.0, seed=seed)
 
 
-def disk_1m_hard(n=1048576, seed=3):
-    """Hard-part workload: the 0.95-1.05 AU disk model at n bodies, rms e = 6 h."""
-    return make_disk(n, 1e-9 * 3000.0 / n, 0.95, 1.05, ecc_hill=6.0, inc_hill=3.0, seed=seed)
+def disk_1m_hard(n=1048576, seed=3, m_at_1m=7e-11):
+    """Hard-part workload: the 0.95-1.05 AU disk model at n bodies, rms e = 6 h,
+    rms i = 3 h.  The body mass (7e-11 at n = 1,048,576; scaled as n^-1.5 for
+    smaller n, which keeps the mean neighbour count) puts the neighbour graph
+    just below percolation: tens of thousands of clusters of 2 to ~300 bodies
+    with a power-law tail.  (At m = 1e-9 the annulus percolates into a single
+    cluster at this n.)"""
+    m = m_at_1m * (1048576.0 / n) ** 1.5
+    return make_disk(n, m, 0.95, 1.05, ecc_hill=6.0, inc_hill=3.0, seed=seed)

@@ -579,7 +579,8 @@ void collide(std::vector<HPtcl> &c, std::map<int, std::vector<int>> &twins, int 
 }
 
 // timeIntegrate_multi, src/hermite.h:224-479 (perfect accretion)
-void integrate_cluster(std::vector<HPtcl> &c, double t_end, int &n_col, double &edisp, double &edisp_d) {
+void integrate_cluster(std::vector<HPtcl> &c, double t_end, int &n_col, double &edisp, double &edisp_d,
+                       std::vector<ColRec> &cols) {
     std::map<int, std::vector<int>> twins;  // target -> dead twins, insertion order
     n_col = 0;
     edisp = edisp_d = 0.;
@@ -665,7 +666,7 @@ void integrate_cluster(std::vector<HPtcl> &c, double t_end, int &n_col, double &
             rec.edisp_d = e2;
             edisp += e1;
             edisp_d += e2;
-            COLS.push_back(rec);
+            cols.push_back(rec);
             n_col++;
             for (int i = 0; i < n; i++) hard_force(c[i], c, 0);
             for (auto &kv : twins) merge_acc_jerk(c, kv.first, kv.second);
@@ -999,21 +1000,29 @@ int hard_all(int istep) {
     for (int pass = 0; pass < 2; pass++)
         for (int k = 0; k < (int)clusters.size(); k++)
             if ((clusters[k].size() >= 64) == (pass == 0)) order.push_back(k);
-    for (int k : order) {
-        auto &cl = clusters[k];
+    // clusters are independent: integrate them in parallel, then fold the
+    // per-cluster results in the reference's order
+    const int ncl = (int)order.size();
+    std::vector<std::vector<ColRec>> ccols(ncl);
+    std::vector<double> ce1(ncl, 0.), ce2(ncl, 0.);
+    std::vector<int> cnc(ncl, 0);
+#pragma omp parallel for schedule(dynamic, 2)
+    for (int q = 0; q < ncl; q++) {
+        auto &cl = clusters[order[q]];
         std::vector<HPtcl> c;
         for (int i : cl) c.push_back(to_hard(S[i]));
-        int nc = 0;
-        double e1 = 0., e2 = 0.;
-        integrate_cluster(c, P.dt_tree, nc, e1, e2);
-        if (nc > 0) { EDISP += e1; EDISP_D += e2; }
+        integrate_cluster(c, P.dt_tree, cnc[q], ce1[q], ce2[q], ccols[q]);
         for (size_t k = 0; k < c.size(); k++) {
             c[k].n_cluster = (int)c.size();
             c[k].time = c[k].time_c + c[k].time;  // resetTime
             c[k].time_c = 0.;
             S[cl[k]] = static_cast<Ptcl &>(c[k]);
-            done++;
         }
+    }
+    for (int q = 0; q < ncl; q++) {
+        if (cnc[q] > 0) { EDISP += ce1[q]; EDISP_D += ce2[q]; }
+        COLS.insert(COLS.end(), ccols[q].begin(), ccols[q].end());
+        done += (int)clusters[order[q]].size();
     }
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < n; i++) {
