@@ -51,6 +51,9 @@ SIGNATURES = {
     "p3t_cluster_label": (I, []),
     "p3t_cluster_lists": (I, [VP, VP, VP]),
     "p3t_hard": (I, [I, I, VP, VP]),
+    "p3t_set_hard_tiers": (I, [I, I]),
+    "p3t_set_cluster_priority": (I, [VP, I]),
+    "p3t_hard_costs": (I, [VP, I]),
     "p3t_kick": (I, []),
     "p3t_energy": (I, [VP]),
     "p3t_merge": (I, [VP]),

@@ -726,16 +726,13 @@ int Engine::merge(double *edisp) {
     *edisp = e;
     if (nk == n) return 0;
     // order-preserving compaction of every field through a scratch copy
+    if ((r = compact_tmp.reserve((size_t)n * 3 * sizeof(double)))) return r;
     auto comp = [&](auto *fld, int w) -> int {
         using T2 = std::remove_pointer_t<decltype(fld)>;
-        T2 *tmp = nullptr;
-        int rr = cuda_status(cudaMalloc(&tmp, std::max<size_t>((size_t)n * w, 1) * sizeof(T2)));
-        if (rr) return rr;
+        T2 *tmp = (T2 *)compact_tmp.p;
         cudaMemcpyAsync(tmp, fld, (size_t)n * w * sizeof(T2), cudaMemcpyDeviceToDevice, c->stream);
         k_compact<T2><<<nb(n), 256, 0, c->stream>>>(tmp, fld, keep.p, kpos.p, n, w);
-        rr = cuda_status(cudaStreamSynchronize(c->stream));
-        cudaFree(tmp);
-        return rr;
+        return cuda_status(cudaGetLastError());
     };
     for (double *f : {S.mass, S.r_planet, S.f, S.phi, S.phi_d, S.phi_s, S.r_out, S.r_out_inv, S.r_search, S.v_disp,
                       S.time, S.dt, S.acc0})
@@ -748,7 +745,7 @@ int Engine::merge(double *edisp) {
         if ((r = comp(f, 1))) return r;
     S.n = nk;
     n_clusters = 0;
-    return 0;
+    return cuda_status(cudaStreamSynchronize(c->stream));
 }
 
 }  // namespace p3t

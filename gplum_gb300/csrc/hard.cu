@@ -40,7 +40,9 @@ struct HardArgs {
     Hard H;
     const int32_t *off, *cnt, *members, *order;
     int n_clusters;
-    int32_t *queue;
+    int n_tier[3];       // clusters per tier (CTA, warp, thread), in `order`
+    int32_t *queue;      // [3] tier queue heads
+    long long *cost;     // optional [2 * n_clusters]: block steps, pair sweeps
     double *cl_edisp;  // [2 * n_clusters]
     ColRec *cols;
     int32_t *n_cols;
@@ -94,6 +96,11 @@ __device__ __forceinline__ void dt_hermite(const Params &P, const Hard &H, int s
 
 // ---- pair sums over a cluster, src/gravity_hard.h:203-367 -------------------
 // mode 0: full (pos/vel, with phi); 1: predicted i and j; 2: corrected i, predicted j
+//
+// Pairs at rij >= r_out (here: dr2 * r_out_inv^2 > 1 + 1e-6, a margin far
+// above rounding) have K = W = 1 and dK/dr = 0 exactly, so their terms are
+// exact zeros; they are skipped after the distance test, which leaves every
+// sum bit-identical (the accumulators start at +0 and never become -0).
 __device__ void hard_force(const Params &P, const Hard &H, int o, int n, int s, int mode) {
     V3 xi, vi, as, js;
     if (mode == 0) {
@@ -114,20 +121,21 @@ __device__ void hard_force(const Params &P, const Hard &H, int o, int n, int s, 
     double phd = 0.;
     const int64_t idi = H.id[s];
     const double roi = H.r_out_inv[s];
+    const double *X = (mode == 0) ? H.pos : H.xp;
     for (int k = 0; k < n; k++) {
         const int t = o + k;
         if (idi == H.id[t]) continue;
-        const V3 xj = (mode == 0) ? ld3(H.pos, t) : ld3(H.xp, t);
-        const V3 vj = (mode == 0) ? ld3(H.vel, t) : ld3(H.vp, t);
-        const V3 dr = xj - xi;
+        const V3 dr = ld3(X, t) - xi;
         double dr2 = dot(dr, dr);
         dr2 += P.eps2;
+        const double r_out_inv = dmin(roi, H.r_out_inv[t]);
+        if (dr2 * r_out_inv * r_out_inv > 1.000001) continue;
+        const V3 vj = (mode == 0) ? ld3(H.vel, t) : ld3(H.vp, t);
         const V3 dv = vj - vi;
         const double rij = sqrt(dr2);
         const double rinv = 1. / rij;
         const double r2inv = rinv * rinv;
         const double r3inv = r2inv * rinv;
-        const double r_out_inv = dmin(roi, H.r_out_inv[t]);
         const double mj = H.mass[t];
         const double mr3 = mj * r3inv;
         const double alpha = dot(dr, dv) * r2inv;
@@ -266,200 +274,290 @@ __device__ void collide(const Params &P, const Hard &H, int imp, int tar, double
     }
 }
 
-__device__ __forceinline__ double warp_min(double v) {
-    for (int o = 16; o > 0; o >>= 1) v = dmin(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
-}
+// ---- teams: one thread, one warp or one CTA integrates one cluster ----------
+template <int TEAM>
+struct Team {
+    int rank;
+    double *red_d;      // shared scratch (CTA teams)
+    long long *red_l;
+    __device__ __forceinline__ void sync() const {
+        if constexpr (TEAM == 32) __syncwarp();
+        else if constexpr (TEAM > 32) __syncthreads();
+    }
+    __device__ __forceinline__ double min(double v) const {
+        if constexpr (TEAM == 1) {
+            return v;
+        } else {
+            for (int o = 16; o > 0; o >>= 1) v = dmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+            if constexpr (TEAM == 32) {
+                return v;
+            } else {
+                __syncthreads();
+                if ((rank & 31) == 0) red_d[rank >> 5] = v;
+                __syncthreads();
+                double m = red_d[0];
+                for (int w = 1; w < TEAM / 32; w++) m = dmin(m, red_d[w]);
+                __syncthreads();
+                return m;
+            }
+        }
+    }
+    // lexicographic min of (R, p)
+    __device__ __forceinline__ void argmin(double &R, long long &p) const {
+        if constexpr (TEAM > 1) {
+            for (int sh = 16; sh > 0; sh >>= 1) {
+                const double R2 = __shfl_xor_sync(0xffffffffu, R, sh);
+                const long long p2 = __shfl_xor_sync(0xffffffffu, p, sh);
+                if (R2 < R || (R2 == R && p2 < p)) { R = R2; p = p2; }
+            }
+            if constexpr (TEAM > 32) {
+                __syncthreads();
+                if ((rank & 31) == 0) { red_d[rank >> 5] = R; red_l[rank >> 5] = p; }
+                __syncthreads();
+                R = red_d[0];
+                p = red_l[0];
+                for (int w = 1; w < TEAM / 32; w++)
+                    if (red_d[w] < R || (red_d[w] == R && red_l[w] < p)) { R = red_d[w]; p = red_l[w]; }
+                __syncthreads();
+            }
+        }
+    }
+};
 
-__global__ void __launch_bounds__(128) k_hard_clusters(HardArgs A) {
-    const int lane = threadIdx.x & 31;
+// timeIntegrate_multi, src/hermite.h:224-479, for cluster c by a team.
+template <int TEAM>
+__device__ void run_cluster(const HardArgs &A, int c, const Team<TEAM> &tm) {
     const Params &P = A.P;
     const Hard &H = A.H;
-    for (int guard = 0; guard < (1 << 30); guard++) {
-        int q = 0;
-        if (lane == 0) q = atomicAdd(A.queue, 1);
-        q = __shfl_sync(0xffffffffu, q, 0);
-        if (q >= A.n_clusters) return;
-        const int c = A.order ? A.order[q] : q;
-        const int o = A.off[c], n = A.cnt[c];
-        // FPHard(const FPGrav&), src/particle.h:1096-1116
-        for (int k = lane; k < n; k += 32) {
-            const int s = o + k, i = A.members[s];
-            st3(H.pos, s, ld3(A.S.pos, i)); st3(H.vel, s, ld3(A.S.vel, i));
-            st3(H.acc_s, s, ld3(A.S.acc_s, i)); st3(H.jerk_s, s, ld3(A.S.jerk_s, i));
-            st3(H.acc_d, s, ld3(A.S.acc_d, i)); st3(H.jerk_d, s, ld3(A.S.jerk_d, i));
-            const V3 z = v3(0., 0., 0.);
-            st3(H.x0, s, z); st3(H.v0, s, z); st3(H.a0_s, s, z); st3(H.j0_s, s, z); st3(H.a0_d, s, z);
-            st3(H.j0_d, s, z); st3(H.xp, s, z); st3(H.vp, s, z); st3(H.a2_s, s, z); st3(H.a3_s, s, z);
-            st3(H.a2_d, s, z); st3(H.a3_d, s, z);
-            H.phi_d[s] = A.S.phi_d[i]; H.phi_s[s] = A.S.phi_s[i];
-            H.mass[s] = A.S.mass[i]; H.r_planet[s] = A.S.r_planet[i]; H.f[s] = A.S.f[i];
-            H.r_out_inv[s] = A.S.r_out_inv[i];
-            H.time_c[s] = A.S.time[i]; H.th[s] = 0.; H.dt[s] = A.S.dt[i]; H.acc0[s] = A.S.acc0[i];
-            H.id[s] = A.S.id[i];
-            H.dead[s] = 0; H.merged[s] = 0;
-            H.tw_head[s] = H.tw_tail[s] = H.tw_next[s] = -1;
+    const int rank = tm.rank;
+    const int o = A.off[c], n = A.cnt[c];
+    // FPHard(const FPGrav&), src/particle.h:1096-1116
+    for (int k = rank; k < n; k += TEAM) {
+        const int s = o + k, i = A.members[s];
+        st3(H.pos, s, ld3(A.S.pos, i)); st3(H.vel, s, ld3(A.S.vel, i));
+        st3(H.acc_s, s, ld3(A.S.acc_s, i)); st3(H.jerk_s, s, ld3(A.S.jerk_s, i));
+        st3(H.acc_d, s, ld3(A.S.acc_d, i)); st3(H.jerk_d, s, ld3(A.S.jerk_d, i));
+        const V3 z = v3(0., 0., 0.);
+        st3(H.x0, s, z); st3(H.v0, s, z); st3(H.a0_s, s, z); st3(H.j0_s, s, z); st3(H.a0_d, s, z);
+        st3(H.j0_d, s, z); st3(H.xp, s, z); st3(H.vp, s, z); st3(H.a2_s, s, z); st3(H.a3_s, s, z);
+        st3(H.a2_d, s, z); st3(H.a3_d, s, z);
+        H.phi_d[s] = A.S.phi_d[i]; H.phi_s[s] = A.S.phi_s[i];
+        H.mass[s] = A.S.mass[i]; H.r_planet[s] = A.S.r_planet[i]; H.f[s] = A.S.f[i];
+        H.r_out_inv[s] = A.S.r_out_inv[i];
+        H.time_c[s] = A.S.time[i]; H.th[s] = 0.; H.dt[s] = A.S.dt[i]; H.acc0[s] = A.S.acc0[i];
+        H.id[s] = A.S.id[i];
+        H.dead[s] = 0; H.merged[s] = 0;
+        H.tw_head[s] = H.tw_tail[s] = H.tw_next[s] = -1;
+    }
+    tm.sync();
+    for (int k = rank; k < n; k += TEAM) hard_force(P, H, o, n, o + k, 0);
+    tm.sync();
+    int n_col = 0;
+    double ed = 0., edd = 0.;
+    double time = 0.;
+    int steps = 0;
+    long long work = 0;
+    while (time < A.t_end) {
+        if (++steps > MAX_BLOCK_STEPS) {
+            if (rank == 0) atomicOr(A.status, ST_ITER_CAP);
+            break;
         }
-        __syncwarp();
-        for (int k = lane; k < n; k += 32) hard_force(P, H, o, n, o + k, 0);
-        __syncwarp();
-        int n_col = 0;
-        double ed = 0., edd = 0.;
-        double time = 0.;
-        int steps = 0;
-        while (time < A.t_end) {
-            if (++steps > MAX_BLOCK_STEPS) {
-                if (lane == 0) atomicOr(A.status, ST_ITER_CAP);
-                break;
+        // makeActiveList, src/hermite.h:4-24
+        double ts = 1.e10;
+        for (int k = rank; k < n; k += TEAM) {
+            const int s = o + k;
+            if (!H.dead[s]) ts = dmin(ts, H.th[s] + H.dt[s]);
+        }
+        ts = tm.min(ts);
+        for (int k = rank; k < n; k += TEAM) {
+            const int s = o + k;
+            st3(H.xp, s, v3(0., 0., 0.));
+            st3(H.vp, s, v3(0., 0., 0.));
+            predict(H, s, ts - H.th[s]);
+        }
+        tm.sync();
+        // collisionDetermination, src/hermite.h:98-196: the first ordered pair
+        // (i, j) with the smallest R < 1.  Pairs with |dr|^2 above the squared
+        // radius sum (1e-6 margin) have R > 1 and are skipped after the
+        // distance test.
+        double Rb = 1.;
+        long long pb = 0x7fffffffffffffffLL;
+        for (int a = rank; a < n; a += TEAM) {
+            const int si = o + a;
+            if (H.dead[si]) continue;
+            const V3 xi = ld3(H.xp, si);
+            const double ri = H.f[si] * H.r_planet[si];
+            for (int b = 0; b < n; b++) {
+                const int sj = o + b;
+                if (a == b || H.dead[sj]) continue;
+                const V3 dr = xi - ld3(H.xp, sj);
+                const double d2 = dot(dr, dr);
+                const double r2 = ri + H.f[sj] * H.r_planet[sj];
+                if (d2 > r2 * r2 * 1.000001) continue;
+                const double r1 = sqrt(d2);
+                const double R = r1 / r2;
+                const long long p = (long long)a * n + b;
+                if (R < Rb || (R == Rb && R < 1. && p < pb)) { Rb = R; pb = p; }
             }
-            // makeActiveList, src/hermite.h:4-24
-            double ts = 1.e10;
-            for (int k = lane; k < n; k += 32) {
-                const int s = o + k;
-                if (!H.dead[s]) ts = dmin(ts, H.th[s] + H.dt[s]);
+        }
+        tm.argmin(Rb, pb);
+        const bool col = Rb < 1.;
+        int imp = -1, tar = -1;
+        if (col) {
+            const int a = (int)(pb / n), b = (int)(pb % n);
+            if (H.mass[o + a] < H.mass[o + b]) { imp = o + a; tar = o + b; }
+            else { imp = o + b; tar = o + a; }
+            for (int k = rank; k < n; k += TEAM) H.dt[o + k] = ts - H.th[o + k];
+        }
+        tm.sync();
+        // correct the active set (all alive on a collision)
+        for (int k = rank; k < n; k += TEAM) {
+            const int s = o + k;
+            if (H.dead[s]) continue;
+            if (!col && H.th[s] + H.dt[s] != ts) continue;
+            work += n;
+            hard_force(P, H, o, n, s, 1);
+            if (H.merged[s]) {
+                for (int t = H.tw_head[s], g = 0; t >= 0 && g < 4096; t = H.tw_next[t], g++)
+                    hard_force(P, H, o, n, t, 1);
+                merge_acc_jerk(H, s);
             }
-            ts = warp_min(ts);
-            for (int k = lane; k < n; k += 32) {
-                const int s = o + k;
-                st3(H.xp, s, v3(0., 0., 0.));
-                st3(H.vp, s, v3(0., 0., 0.));
-                predict(H, s, ts - H.th[s]);
-            }
-            __syncwarp();
-            // collisionDetermination, src/hermite.h:98-196: the first ordered
-            // pair (i, j) with the smallest R < 1
-            double Rb = 1.;
-            long long pb = 0x7fffffffffffffffLL;
-            for (int a = lane; a < n; a += 32) {
-                const int si = o + a;
-                if (H.dead[si]) continue;
-                const V3 xi = ld3(H.xp, si);
-                const double ri = H.f[si] * H.r_planet[si];
-                for (int b = 0; b < n; b++) {
-                    const int sj = o + b;
-                    if (a == b || H.dead[sj]) continue;
-                    const V3 dr = xi - ld3(H.xp, sj);
-                    const double r1 = sqrt(dot(dr, dr));
-                    const double r2 = ri + H.f[sj] * H.r_planet[sj];
-                    const double R = r1 / r2;
-                    const long long p = (long long)a * n + b;
-                    if (R < Rb || (R == Rb && R < 1. && p < pb)) { Rb = R; pb = p; }
-                }
-            }
-            for (int sh = 16; sh > 0; sh >>= 1) {
-                const double R2 = __shfl_xor_sync(0xffffffffu, Rb, sh);
-                const long long p2 = __shfl_xor_sync(0xffffffffu, pb, sh);
-                if (R2 < Rb || (R2 == Rb && p2 < pb)) { Rb = R2; pb = p2; }
-            }
-            const bool col = Rb < 1.;
-            int imp = -1, tar = -1;
-            if (col) {
-                const int a = (int)(pb / n), b = (int)(pb % n);
-                if (H.mass[o + a] < H.mass[o + b]) { imp = o + a; tar = o + b; }
-                else { imp = o + b; tar = o + a; }
-                for (int k = lane; k < n; k += 32) H.dt[o + k] = ts - H.th[o + k];
-            }
-            __syncwarp();
-            // correct the active set (all alive on a collision)
-            for (int k = lane; k < n; k += 32) {
-                const int s = o + k;
-                if (H.dead[s]) continue;
-                if (!col && H.th[s] + H.dt[s] != ts) continue;
-                hard_force(P, H, o, n, s, 1);
+            const double tc = ts - H.th[s];
+            for (int it = 0; it < 2; it++) {
+                correct(H, s, tc);
+                if (H.merged[s])
+                    for (int t = H.tw_head[s], g = 0; t >= 0 && g < 4096; t = H.tw_next[t], g++) correct(H, t, tc);
+                hard_force(P, H, o, n, s, 2);
                 if (H.merged[s]) {
                     for (int t = H.tw_head[s], g = 0; t >= 0 && g < 4096; t = H.tw_next[t], g++)
-                        hard_force(P, H, o, n, t, 1);
+                        hard_force(P, H, o, n, t, 2);
                     merge_acc_jerk(H, s);
                 }
-                const double tc = ts - H.th[s];
-                for (int it = 0; it < 2; it++) {
-                    correct(H, s, tc);
-                    if (H.merged[s])
-                        for (int t = H.tw_head[s], g = 0; t >= 0 && g < 4096; t = H.tw_next[t], g++)
-                            correct(H, t, tc);
-                    hard_force(P, H, o, n, s, 2);
-                    if (H.merged[s]) {
-                        for (int t = H.tw_head[s], g = 0; t >= 0 && g < 4096; t = H.tw_next[t], g++)
-                            hard_force(P, H, o, n, t, 2);
-                        merge_acc_jerk(H, s);
-                    }
-                }
-                H.th[s] += tc;
+            }
+            H.th[s] += tc;
+            if (H.merged[s])
+                for (int t = H.tw_head[s], g = 0; t >= 0 && g < 4096; t = H.tw_next[t], g++) H.th[t] += tc;
+            if (!col) {
+                dt_hermite(P, H, s);
                 if (H.merged[s])
-                    for (int t = H.tw_head[s], g = 0; t >= 0 && g < 4096; t = H.tw_next[t], g++) H.th[t] += tc;
-                if (!col) {
-                    dt_hermite(P, H, s);
-                    if (H.merged[s])
-                        for (int t = H.tw_head[s], g = 0; t >= 0 && g < 4096; t = H.tw_next[t], g++)
-                            H.dt[t] = H.dt[s];
-                }
+                    for (int t = H.tw_head[s], g = 0; t >= 0 && g < 4096; t = H.tw_next[t], g++) H.dt[t] = H.dt[s];
             }
-            __syncwarp();
-            if (col) {
-                if (lane == 0) {
-                    ColRec rec;
-                    double e1 = 0., e2 = 0.;
-                    collide(P, H, imp, tar, e1, e2, rec);
-                    ed += e1;
-                    edd += e2;
-                    rec.cluster = c;
-                    rec.seq = n_col;
-                    const int slot = atomicAdd(A.n_cols, 1);
-                    if (slot < A.col_cap) A.cols[slot] = rec;
-                    else atomicOr(A.status, ST_QUEUE_OVERFLOW);
-                }
-                n_col++;
-                __syncwarp();
-                for (int k = lane; k < n; k += 32) hard_force(P, H, o, n, o + k, 0);
-                __syncwarp();
-                for (int k = lane; k < n; k += 32)
-                    if (H.merged[o + k] && H.tw_head[o + k] >= 0) merge_acc_jerk(H, o + k);
-                __syncwarp();
-                for (int k = lane; k < n; k += 32) {
-                    const int s = o + k;
-                    if (!H.dead[s])
-                        H.dt[s] = dt_initial(P, H.th[s], H.dt[s], H.acc0[s], ld3(H.acc_d, s), ld3(H.jerk_d, s),
-                                             ld3(H.acc_s, s), ld3(H.jerk_s, s));
-                }
-                __syncwarp();
-                for (int k = lane; k < n; k += 32) {
-                    const int s = o + k;
-                    if (H.merged[s])
-                        for (int t = H.tw_head[s], g = 0; t >= 0 && g < 4096; t = H.tw_next[t], g++) H.dt[t] = H.dt[s];
-                }
-                __syncwarp();
-            }
-            // getSystemTime, src/hermite.h:25-35
-            double tmin = 1.e10;
-            for (int k = lane; k < n; k += 32)
-                if (!H.dead[o + k]) tmin = dmin(tmin, H.th[o + k]);
-            time = warp_min(tmin);
         }
-        __syncwarp();
-        for (int k = lane; k < n; k += 32) hard_force(P, H, o, n, o + k, 0);
-        __syncwarp();
-        if (n_col > 0)
-            for (int k = lane; k < n; k += 32)
+        tm.sync();
+        if (col) {
+            if (rank == 0) {
+                ColRec rec;
+                double e1 = 0., e2 = 0.;
+                collide(P, H, imp, tar, e1, e2, rec);
+                ed += e1;
+                edd += e2;
+                rec.cluster = c;
+                rec.seq = n_col;
+                const int slot = atomicAdd(A.n_cols, 1);
+                if (slot < A.col_cap) A.cols[slot] = rec;
+                else atomicOr(A.status, ST_QUEUE_OVERFLOW);
+            }
+            n_col++;
+            tm.sync();
+            for (int k = rank; k < n; k += TEAM) hard_force(P, H, o, n, o + k, 0);
+            tm.sync();
+            for (int k = rank; k < n; k += TEAM)
                 if (H.merged[o + k] && H.tw_head[o + k] >= 0) merge_acc_jerk(H, o + k);
-        __syncwarp();
-        // write back to FPGrav, with resetTime (src/hard.h:768-787)
-        for (int k = lane; k < n; k += 32) {
-            const int s = o + k, i = A.members[s];
-            st3(A.S.pos, i, ld3(H.pos, s)); st3(A.S.vel, i, ld3(H.vel, s));
-            st3(A.S.acc_s, i, ld3(H.acc_s, s)); st3(A.S.jerk_s, i, ld3(H.jerk_s, s));
-            st3(A.S.acc_d, i, ld3(H.acc_d, s)); st3(A.S.jerk_d, i, ld3(H.jerk_d, s));
-            A.S.phi_d[i] = H.phi_d[s]; A.S.phi_s[i] = H.phi_s[s];
-            A.S.mass[i] = H.mass[s]; A.S.r_planet[i] = H.r_planet[s];
-            A.S.time[i] = H.time_c[s] + H.th[s]; A.S.dt[i] = H.dt[s];
-            A.S.id[i] = H.id[s];
-            A.S.dead[i] = H.dead[s]; A.S.merged[i] = H.merged[s];
-            A.S.n_cluster[i] = n;
+            tm.sync();
+            for (int k = rank; k < n; k += TEAM) {
+                const int s = o + k;
+                if (!H.dead[s])
+                    H.dt[s] = dt_initial(P, H.th[s], H.dt[s], H.acc0[s], ld3(H.acc_d, s), ld3(H.jerk_d, s),
+                                         ld3(H.acc_s, s), ld3(H.jerk_s, s));
+            }
+            tm.sync();
+            for (int k = rank; k < n; k += TEAM) {
+                const int s = o + k;
+                if (H.merged[s])
+                    for (int t = H.tw_head[s], g = 0; t >= 0 && g < 4096; t = H.tw_next[t], g++) H.dt[t] = H.dt[s];
+            }
+            tm.sync();
         }
-        if (lane == 0) {
-            A.cl_edisp[2 * c] = (n_col > 0) ? ed : 0.;
-            A.cl_edisp[2 * c + 1] = (n_col > 0) ? edd : 0.;
+        // getSystemTime, src/hermite.h:25-35
+        double tmin = 1.e10;
+        for (int k = rank; k < n; k += TEAM)
+            if (!H.dead[o + k]) tmin = dmin(tmin, H.th[o + k]);
+        time = tm.min(tmin);
+    }
+    tm.sync();
+    for (int k = rank; k < n; k += TEAM) hard_force(P, H, o, n, o + k, 0);
+    tm.sync();
+    if (n_col > 0)
+        for (int k = rank; k < n; k += TEAM)
+            if (H.merged[o + k] && H.tw_head[o + k] >= 0) merge_acc_jerk(H, o + k);
+    tm.sync();
+    // write back to FPGrav, with resetTime (src/hard.h:768-787)
+    for (int k = rank; k < n; k += TEAM) {
+        const int s = o + k, i = A.members[s];
+        st3(A.S.pos, i, ld3(H.pos, s)); st3(A.S.vel, i, ld3(H.vel, s));
+        st3(A.S.acc_s, i, ld3(H.acc_s, s)); st3(A.S.jerk_s, i, ld3(H.jerk_s, s));
+        st3(A.S.acc_d, i, ld3(H.acc_d, s)); st3(A.S.jerk_d, i, ld3(H.jerk_d, s));
+        A.S.phi_d[i] = H.phi_d[s]; A.S.phi_s[i] = H.phi_s[s];
+        A.S.mass[i] = H.mass[s]; A.S.r_planet[i] = H.r_planet[s];
+        A.S.time[i] = H.time_c[s] + H.th[s]; A.S.dt[i] = H.dt[s];
+        A.S.id[i] = H.id[s];
+        A.S.dead[i] = H.dead[s]; A.S.merged[i] = H.merged[s];
+        A.S.n_cluster[i] = n;
+    }
+    // per-cluster cost log: block steps and active-body x member pair sweeps
+    if (A.cost) atomicAdd((unsigned long long *)&A.cost[2 * c + 1], (unsigned long long)work);
+    if (rank == 0) {
+        A.cl_edisp[2 * c] = (n_col > 0) ? ed : 0.;
+        A.cl_edisp[2 * c + 1] = (n_col > 0) ? edd : 0.;
+        if (A.cost) A.cost[2 * c] = steps;
+    }
+    tm.sync();
+}
+
+// One persistent launch: clusters of >= cta_min members one per CTA, then
+// clusters of >= warp_min members one per warp, then the rest one per thread.
+// Each tier takes its clusters from its own queue in the order given
+// (largest or costliest first).
+__global__ void __launch_bounds__(128) k_hard_clusters(HardArgs A) {
+    __shared__ double red_d[4];
+    __shared__ long long red_l[4];
+    __shared__ int q_sh;
+    const int tid = threadIdx.x, lane = tid & 31;
+    // tier 1: CTA per cluster
+    {
+        Team<128> tm{tid, red_d, red_l};
+        for (int guard = 0; guard < (1 << 30); guard++) {
+            if (tid == 0) q_sh = atomicAdd(&A.queue[0], 1);
+            __syncthreads();
+            const int q = q_sh;
+            __syncthreads();
+            if (q >= A.n_tier[0]) break;
+            run_cluster<128>(A, A.order[q], tm);
         }
-        __syncwarp();
+    }
+    // tier 2: warp per cluster
+    {
+        Team<32> tm{lane, nullptr, nullptr};
+        for (int guard = 0; guard < (1 << 30); guard++) {
+            int q = 0;
+            if (lane == 0) q = atomicAdd(&A.queue[1], 1);
+            q = __shfl_sync(0xffffffffu, q, 0);
+            if (q >= A.n_tier[1]) break;
+            run_cluster<32>(A, A.order[A.n_tier[0] + q], tm);
+        }
+    }
+    // tier 3: thread per cluster, a warp takes 32 clusters at a time
+    {
+        Team<1> tm{0, nullptr, nullptr};
+        for (int guard = 0; guard < (1 << 30); guard++) {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(&A.queue[2], 32);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base >= A.n_tier[2]) break;
+            const int q = base + lane;
+            if (q < A.n_tier[2]) run_cluster<1>(A, A.order[A.n_tier[0] + A.n_tier[1] + q], tm);
+            __syncwarp();
+        }
     }
 }
 
@@ -629,6 +727,7 @@ struct HardBufs {
     DevBuf<int32_t> i32, order, queue, n_cols;
     DevBuf<double> cl_edisp, etot;
     DevBuf<ColRec> cols;
+    DevBuf<long long> cost;
     Hard H;
     int cap = 0;
     int reserve(int m) {
@@ -659,12 +758,34 @@ struct HardBufs {
 static HardBufs g_hb;
 static std::vector<ColRec> g_cols;
 static double g_edisp[2] = {0., 0.};
+static int g_warp_min = 8, g_cta_min = 64;
+static std::vector<float> g_prio;
 
 }  // namespace p3t
 
 using namespace p3t;
 
 extern "C" {
+
+int p3t_set_hard_tiers(int warp_min, int cta_min) {
+    if (warp_min < 1 || cta_min < warp_min) return ST_BAD_INDEX;
+    g_warp_min = warp_min;
+    g_cta_min = cta_min;
+    return 0;
+}
+
+int p3t_set_cluster_priority(const float *prio, int n) {
+    if (n != g_eng.n_clusters || n < 0) return ST_BAD_INDEX;
+    g_prio.assign(prio, prio + n);
+    return 0;
+}
+
+int p3t_hard_costs(long long *out, int n) {
+    Context *c = ctx_get(0);
+    if (!c) return -(int)cudaErrorNoDevice;
+    if (n != g_eng.n_clusters || !g_hb.cost.p) return ST_BAD_INDEX;
+    return cuda_status(cudaMemcpy(out, g_hb.cost.p, 2 * (size_t)n * sizeof(long long), cudaMemcpyDeviceToHost));
+}
 
 int p3t_hard(int istep, int col_cap, long long *col_pairs, double *edisp) {
     Engine &E = g_eng;
@@ -673,20 +794,35 @@ int p3t_hard(int istep, int col_cap, long long *col_pairs, double *edisp) {
     HardBufs &B = g_hb;
     const int nc = E.n_clusters;
     int r = 0;
-    if ((r = B.reserve(E.n_members)) || (r = B.order.reserve(nc)) || (r = B.queue.reserve(1)) ||
+    if ((r = B.reserve(E.n_members)) || (r = B.order.reserve(nc)) || (r = B.queue.reserve(3)) ||
         (r = B.n_cols.reserve(1)) || (r = B.cl_edisp.reserve(2 * (size_t)nc + 2)) || (r = B.etot.reserve(2)) ||
         (r = B.cols.reserve(4096)))
         return r;
-    // schedule: largest clusters first
-    std::vector<int32_t> cnt(nc), ord(nc);
+    // schedule: three tiers by size (CTA >= g_cta_min > warp >= g_warp_min >
+    // thread), each ordered by the caller's priority when given, else by size,
+    // largest first
+    std::vector<int32_t> cnt(nc), ord;
+    int ntier[3] = {0, 0, 0};
     if (nc > 0) {
         if ((r = cuda_status(cudaMemcpy(cnt.data(), E.cl_cnt.p, nc * sizeof(int32_t), cudaMemcpyDeviceToHost))))
             return r;
+        const bool use_prio = (int)g_prio.size() == nc;
+        auto tier = [&](int k) { return cnt[k] >= g_cta_min ? 0 : (cnt[k] >= g_warp_min ? 1 : 2); };
+        ord.resize(nc);
         for (int k = 0; k < nc; k++) ord[k] = k;
-        std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return cnt[a] > cnt[b]; });
+        std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
+            const int ta = tier(a), tb = tier(b);
+            if (ta != tb) return ta < tb;
+            if (use_prio) return g_prio[a] > g_prio[b];
+            return cnt[a] > cnt[b];
+        });
+        for (int k = 0; k < nc; k++) ntier[tier(k)]++;
         if ((r = h2d(c, B.order.p, ord.data(), nc * sizeof(int32_t)))) return r;
     }
-    cudaMemsetAsync(B.queue.p, 0, sizeof(int32_t), c->stream);
+    g_prio.clear();
+    if ((r = B.cost.reserve(2 * (size_t)nc + 2))) return r;
+    cudaMemsetAsync(B.cost.p, 0, (2 * (size_t)nc + 2) * sizeof(long long), c->stream);
+    cudaMemsetAsync(B.queue.p, 0, 3 * sizeof(int32_t), c->stream);
     cudaMemsetAsync(B.n_cols.p, 0, sizeof(int32_t), c->stream);
     const Params P = E.params();
     if (nc > 0) {
@@ -699,7 +835,9 @@ int p3t_hard(int istep, int col_cap, long long *col_pairs, double *edisp) {
         A.members = E.members.p;
         A.order = B.order.p;
         A.n_clusters = nc;
+        for (int t = 0; t < 3; t++) A.n_tier[t] = ntier[t];
         A.queue = B.queue.p;
+        A.cost = B.cost.p;
         A.cl_edisp = B.cl_edisp.p;
         A.cols = B.cols.p;
         A.n_cols = B.n_cols.p;
@@ -708,7 +846,8 @@ int p3t_hard(int istep, int col_cap, long long *col_pairs, double *edisp) {
         A.t_end = P.dt_tree;
         int sms = 152;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
-        const int blocks = std::min((nc + 3) / 4, sms * 8);
+        const int want = ntier[0] + (ntier[1] + 3) / 4 + (ntier[2] + 127) / 128;
+        const int blocks = std::max(1, std::min(want, sms * 8));
         k_hard_clusters<<<blocks, 128, 0, c->stream>>>(A);
         if ((r = cuda_status(cudaGetLastError()))) return r;
     }

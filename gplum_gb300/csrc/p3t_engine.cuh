@@ -16,6 +16,7 @@ struct Engine {
     DevBuf<int64_t> cmin;
     DevBuf<double> epart, et;
     DevBuf<int> icnt;
+    DevBuf<char> compact_tmp;
 
     int ensure(int n);
     Params params() const;

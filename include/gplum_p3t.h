@@ -139,6 +139,18 @@ int p3t_cluster_lists(int *n_clusters, int *off, int *members);
  * collisions (>= 0) and writes (impactor id, target id) pairs and the
  * dissipated energy {total, hard part}; a negative value is an error. */
 int p3t_hard(int istep, int col_cap, long long *col_pairs, double *edisp);
+/* Size tiers of the hard launch: clusters of >= cta_min members run one per
+ * CTA, of >= warp_min one per warp, smaller ones one per thread (defaults
+ * 8 and 64; GPLUM's own cutoff between its parallel and serial cluster
+ * loops is 64, src/hard.h:562).  No counterpart in GPLUM's interface. */
+int p3t_set_hard_tiers(int warp_min, int cta_min);
+/* Optional priority of each cluster of the current lists (n = cluster
+ * count, higher first within its tier) for the next p3t_hard; without it
+ * clusters go largest first.  Ordering never changes results. */
+int p3t_set_cluster_priority(const float *prio, int n);
+/* Per-cluster cost of the last p3t_hard: {block steps, active-body x member
+ * pair sweeps} for each cluster, in cluster-list order. */
+int p3t_hard_costs(long long *out, int n);
 /* velKick, src/gravity_soft.h:5-12. */
 int p3t_kick(void);
 /* Energy::calcEnergy, src/energy.h:29-63: {etot, ekin, ephi_sun, ephi, ephi_d}. */
