@@ -495,11 +495,13 @@ __global__ void k_radii(State S, Params P, double r_min, double dr, double drinv
 // MergeParticle, src/func.h:160-207: targets fold in their dead twins (same
 // id, same cluster), twins leave the system (order-preserving).
 __global__ void k_merge_targets(State S, const int32_t *cl_of, const int32_t *off, const int32_t *cnt,
-                                const int32_t *members, int32_t *keep, double *e_t) {
+                                const int32_t *members, int32_t *keep, double *e_t, int32_t *tflag) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= S.n) return;
     e_t[i] = 0.;
+    tflag[i] = 0;
     if (!(S.merged[i] && !S.dead[i])) return;
+    tflag[i] = 1;
     const int c = cl_of[i];
     double e = 0.;
     if (c >= 0) {
@@ -519,6 +521,12 @@ __global__ void k_merge_targets(State S, const int32_t *cl_of, const int32_t *of
     }
     S.merged[i] = 0;
     e_t[i] = e;
+}
+// sum of e_t over the targets in ascending index order (the order of the
+// reference's loop); the targets are first gathered by a scan
+__global__ void k_gather_targets(const double *e_t, const int32_t *tflag, const int32_t *tpos, int n, double *tl) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && tflag[i]) tl[tpos[i]] = e_t[i];
 }
 __global__ void k_sum_ordered(const double *v, int n, double *out) {
     if (threadIdx.x || blockIdx.x) return;
@@ -715,12 +723,19 @@ int Engine::cutoff_radii() {
 int Engine::merge(double *edisp) {
     const int n = S.n;
     int r = 0;
-    if ((r = keep.reserve(n)) || (r = kpos.reserve(n)) || (r = et.reserve(n + 1))) return r;
+    if ((r = keep.reserve(n)) || (r = kpos.reserve(n)) || (r = et.reserve(2 * (size_t)n + 1)) ||
+        (r = tflag.reserve(n)) || (r = tpos.reserve(n)))
+        return r;
     k_fill_i32<<<nb(n), 256, 0, c->stream>>>(keep.p, n, 1);
-    k_merge_targets<<<nb(n), 256, 0, c->stream>>>(S, cl_of.p, cl_off.p, cl_cnt.p, members.p, keep.p, et.p);
-    k_sum_ordered<<<1, 32, 0, c->stream>>>(et.p, n, et.p + n);
+    k_merge_targets<<<nb(n), 256, 0, c->stream>>>(S, cl_of.p, cl_off.p, cl_cnt.p, members.p, keep.p, et.p,
+                                                    tflag.p);
+    int32_t nt = 0;
+    if ((r = scan(tflag.p, tpos.p, n, &nt))) return r;
+    double *tl = et.p + n;
+    k_gather_targets<<<nb(n), 256, 0, c->stream>>>(et.p, tflag.p, tpos.p, n, tl);
+    k_sum_ordered<<<1, 32, 0, c->stream>>>(tl, nt, et.p + 2 * (size_t)n);
     double e = 0.;
-    cudaMemcpyAsync(&e, et.p + n, sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    cudaMemcpyAsync(&e, et.p + 2 * (size_t)n, sizeof(double), cudaMemcpyDeviceToHost, c->stream);
     int32_t nk = 0;
     if ((r = scan(keep.p, kpos.p, n, &nk))) return r;  // synchronizes
     *edisp = e;

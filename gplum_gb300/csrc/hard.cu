@@ -26,7 +26,26 @@ struct Hard {
     double *phi_d, *phi_s, *mass, *r_planet, *f, *r_out_inv, *th, *dt, *acc0, *time_c;
     int64_t *id;
     int32_t *dead, *merged, *tw_head, *tw_tail, *tw_next;
+    // FP32 copies of corrected and predicted positions relative to the
+    // cluster's first member, of r_out_inv and of f * r_planet: a cheap
+    // distance prefilter
+    float *pos32, *xp32, *roi32, *fr32;
 };
+
+// Per-cluster prefilter state (uniform across the team).
+struct Pre {
+    bool on;          // prefilter proven safe for this cluster
+    double ref[3];    // origin of the FP32 coordinates
+};
+__device__ __forceinline__ void st32(float *p, int s, V3 x, const Pre &pre) {
+    p[3 * s] = (float)(x.x - pre.ref[0]);
+    p[3 * s + 1] = (float)(x.y - pre.ref[1]);
+    p[3 * s + 2] = (float)(x.z - pre.ref[2]);
+}
+__device__ __forceinline__ float d2_32(const float *a, int s, const float *b, int t) {
+    const float dx = a[3 * s] - b[3 * t], dy = a[3 * s + 1] - b[3 * t + 1], dz = a[3 * s + 2] - b[3 * t + 2];
+    return dx * dx + dy * dy + dz * dz;
+}
 
 struct ColRec {
     int64_t id_imp, id_tar;
@@ -101,7 +120,12 @@ __device__ __forceinline__ void dt_hermite(const Params &P, const Hard &H, int s
 // above rounding) have K = W = 1 and dK/dr = 0 exactly, so their terms are
 // exact zeros; they are skipped after the distance test, which leaves every
 // sum bit-identical (the accumulators start at +0 and never become -0).
-__device__ void hard_force(const Params &P, const Hard &H, int o, int n, int s, int mode) {
+//
+// With the FP32 prefilter on, a pair is first tested on the FP32 relative
+// coordinates: it is skipped when its FP32 distance exceeds twice the cutoff
+// radius, which the prefilter's safety condition (run_cluster) guarantees is
+// beyond the cutoff in exact arithmetic too.
+__device__ void hard_force(const Params &P, const Hard &H, int o, int n, int s, int mode, const Pre &pre) {
     V3 xi, vi, as, js;
     if (mode == 0) {
         xi = ld3(H.pos, s); vi = ld3(H.vel, s);
@@ -122,9 +146,16 @@ __device__ void hard_force(const Params &P, const Hard &H, int o, int n, int s, 
     const int64_t idi = H.id[s];
     const double roi = H.r_out_inv[s];
     const double *X = (mode == 0) ? H.pos : H.xp;
+    const float *xi32 = (mode == 1) ? H.xp32 : H.pos32;
+    const float *xj32 = (mode == 0) ? H.pos32 : H.xp32;
+    const float roi32 = H.roi32[s];
     for (int k = 0; k < n; k++) {
         const int t = o + k;
         if (idi == H.id[t]) continue;
+        if (pre.on) {
+            const float rf = fminf(roi32, H.roi32[t]);
+            if (d2_32(xi32, s, xj32, t) * (rf * rf) > 4.0f) continue;
+        }
         const V3 dr = ld3(X, t) - xi;
         double dr2 = dot(dr, dr);
         dr2 += P.eps2;
@@ -349,8 +380,31 @@ __device__ void run_cluster(const HardArgs &A, int c, const Team<TEAM> &tm) {
         H.dead[s] = 0; H.merged[s] = 0;
         H.tw_head[s] = H.tw_tail[s] = H.tw_next[s] = -1;
     }
+    // FP32 prefilter: coordinates relative to the first member.  Their
+    // distance errors stay below 3.2e-7 (D + motion) with D the cluster's
+    // extent; the prefilter only skips pairs beyond twice a cutoff radius, so
+    // it is exact whenever that error bound is below a quarter of the
+    // smallest radius it is compared with (1e-6 (D + 0.05 AU) below).
+    Pre pre;
+    {
+        const V3 r0 = ld3(A.S.pos, A.members[o]);
+        pre.ref[0] = r0.x; pre.ref[1] = r0.y; pre.ref[2] = r0.z;
+        double ext = 0., rmin = 1.e300;
+        for (int k = rank; k < n; k += TEAM) {
+            const int s = o + k;
+            const V3 d = ld3(H.pos, s) - r0;
+            ext = dmax(ext, dmax(fabs(d.x), dmax(fabs(d.y), fabs(d.z))));
+            rmin = dmin(rmin, dmin(2. * H.f[s] * H.r_planet[s], 1. / H.r_out_inv[s]));
+            st32(H.pos32, s, ld3(H.pos, s), pre);
+            H.roi32[s] = (float)H.r_out_inv[s];
+            H.fr32[s] = (float)(H.f[s] * H.r_planet[s]);
+        }
+        ext = -tm.min(-ext);
+        rmin = tm.min(rmin);
+        pre.on = (ext + 0.05) * 1e-6 < 0.25 * rmin;
+    }
     tm.sync();
-    for (int k = rank; k < n; k += TEAM) hard_force(P, H, o, n, o + k, 0);
+    for (int k = rank; k < n; k += TEAM) hard_force(P, H, o, n, o + k, 0, pre);
     tm.sync();
     int n_col = 0;
     double ed = 0., edd = 0.;
@@ -374,6 +428,7 @@ __device__ void run_cluster(const HardArgs &A, int c, const Team<TEAM> &tm) {
             st3(H.xp, s, v3(0., 0., 0.));
             st3(H.vp, s, v3(0., 0., 0.));
             predict(H, s, ts - H.th[s]);
+            st32(H.xp32, s, ld3(H.xp, s), pre);
         }
         tm.sync();
         // collisionDetermination, src/hermite.h:98-196: the first ordered pair
@@ -387,9 +442,14 @@ __device__ void run_cluster(const HardArgs &A, int c, const Team<TEAM> &tm) {
             if (H.dead[si]) continue;
             const V3 xi = ld3(H.xp, si);
             const double ri = H.f[si] * H.r_planet[si];
+            const float ri32 = H.fr32[si];
             for (int b = 0; b < n; b++) {
                 const int sj = o + b;
                 if (a == b || H.dead[sj]) continue;
+                if (pre.on) {
+                    const float rs = ri32 + H.fr32[sj];
+                    if (d2_32(H.xp32, si, H.xp32, sj) > 4.0f * rs * rs) continue;
+                }
                 const V3 dr = xi - ld3(H.xp, sj);
                 const double d2 = dot(dr, dr);
                 const double r2 = ri + H.f[sj] * H.r_planet[sj];
@@ -416,21 +476,25 @@ __device__ void run_cluster(const HardArgs &A, int c, const Team<TEAM> &tm) {
             if (H.dead[s]) continue;
             if (!col && H.th[s] + H.dt[s] != ts) continue;
             work += n;
-            hard_force(P, H, o, n, s, 1);
+            hard_force(P, H, o, n, s, 1, pre);
             if (H.merged[s]) {
                 for (int t = H.tw_head[s], g = 0; t >= 0 && g < 4096; t = H.tw_next[t], g++)
-                    hard_force(P, H, o, n, t, 1);
+                    hard_force(P, H, o, n, t, 1, pre);
                 merge_acc_jerk(H, s);
             }
             const double tc = ts - H.th[s];
             for (int it = 0; it < 2; it++) {
                 correct(H, s, tc);
+                st32(H.pos32, s, ld3(H.pos, s), pre);
                 if (H.merged[s])
-                    for (int t = H.tw_head[s], g = 0; t >= 0 && g < 4096; t = H.tw_next[t], g++) correct(H, t, tc);
-                hard_force(P, H, o, n, s, 2);
+                    for (int t = H.tw_head[s], g = 0; t >= 0 && g < 4096; t = H.tw_next[t], g++) {
+                        correct(H, t, tc);
+                        st32(H.pos32, t, ld3(H.pos, t), pre);
+                    }
+                hard_force(P, H, o, n, s, 2, pre);
                 if (H.merged[s]) {
                     for (int t = H.tw_head[s], g = 0; t >= 0 && g < 4096; t = H.tw_next[t], g++)
-                        hard_force(P, H, o, n, t, 2);
+                        hard_force(P, H, o, n, t, 2, pre);
                     merge_acc_jerk(H, s);
                 }
             }
@@ -459,7 +523,12 @@ __device__ void run_cluster(const HardArgs &A, int c, const Team<TEAM> &tm) {
             }
             n_col++;
             tm.sync();
-            for (int k = rank; k < n; k += TEAM) hard_force(P, H, o, n, o + k, 0);
+            for (int k = rank; k < n; k += TEAM) {
+                st32(H.pos32, o + k, ld3(H.pos, o + k), pre);
+                H.fr32[o + k] = (float)(H.f[o + k] * H.r_planet[o + k]);
+            }
+            tm.sync();
+            for (int k = rank; k < n; k += TEAM) hard_force(P, H, o, n, o + k, 0, pre);
             tm.sync();
             for (int k = rank; k < n; k += TEAM)
                 if (H.merged[o + k] && H.tw_head[o + k] >= 0) merge_acc_jerk(H, o + k);
@@ -485,7 +554,7 @@ __device__ void run_cluster(const HardArgs &A, int c, const Team<TEAM> &tm) {
         time = tm.min(tmin);
     }
     tm.sync();
-    for (int k = rank; k < n; k += TEAM) hard_force(P, H, o, n, o + k, 0);
+    for (int k = rank; k < n; k += TEAM) hard_force(P, H, o, n, o + k, 0, pre);
     tm.sync();
     if (n_col > 0)
         for (int k = rank; k < n; k += TEAM)
@@ -518,7 +587,7 @@ __device__ void run_cluster(const HardArgs &A, int c, const Team<TEAM> &tm) {
 // clusters of >= warp_min members one per warp, then the rest one per thread.
 // Each tier takes its clusters from its own queue in the order given
 // (largest or costliest first).
-__global__ void __launch_bounds__(128) k_hard_clusters(HardArgs A) {
+__global__ void __launch_bounds__(128, 2) k_hard_clusters(HardArgs A) {
     __shared__ double red_d[4];
     __shared__ long long red_l[4];
     __shared__ int q_sh;
@@ -728,6 +797,7 @@ struct HardBufs {
     DevBuf<double> cl_edisp, etot;
     DevBuf<ColRec> cols;
     DevBuf<long long> cost;
+    DevBuf<float> f32;
     Hard H;
     int cap = 0;
     int reserve(int m) {
@@ -735,8 +805,13 @@ struct HardBufs {
         const int mm = std::max(m, 1);
         int r = 0;
         const int nvec = 18, nsc = 10;
-        if ((r = d.reserve((size_t)mm * (3 * nvec + nsc))) || (r = id.reserve(mm)) || (r = i32.reserve((size_t)mm * 5)))
+        if ((r = d.reserve((size_t)mm * (3 * nvec + nsc))) || (r = id.reserve(mm)) || (r = i32.reserve((size_t)mm * 5)) ||
+            (r = f32.reserve((size_t)mm * 8)))
             return r;
+        H.pos32 = f32.p;
+        H.xp32 = f32.p + 3 * (size_t)mm;
+        H.roi32 = f32.p + 6 * (size_t)mm;
+        H.fr32 = f32.p + 7 * (size_t)mm;
         double *p = d.p;
         double **vecs[nvec] = {&H.pos, &H.vel, &H.acc_s, &H.jerk_s, &H.acc_d, &H.jerk_d, &H.x0, &H.v0, &H.a0_s,
                                &H.j0_s, &H.a0_d, &H.j0_d, &H.xp, &H.vp, &H.a2_s, &H.a3_s, &H.a2_d, &H.a3_d};
@@ -847,7 +922,7 @@ int p3t_hard(int istep, int col_cap, long long *col_pairs, double *edisp) {
         int sms = 152;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
         const int want = ntier[0] + (ntier[1] + 3) / 4 + (ntier[2] + 127) / 128;
-        const int blocks = std::max(1, std::min(want, sms * 8));
+        const int blocks = std::max(1, std::min(want, sms * 2));  // persistent: 2 CTAs per SM
         k_hard_clusters<<<blocks, 128, 0, c->stream>>>(A);
         if ((r = cuda_status(cudaGetLastError()))) return r;
     }

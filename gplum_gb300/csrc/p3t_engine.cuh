@@ -12,7 +12,7 @@ struct Engine {
     int cand_cap_alloc = 0;
     int n_clusters = 0, n_members = 0;
     DevBuf<int32_t> counters, head, flag, cidx, cl_of, cl_cnt, cl_off, cl_fill, members_tmp, members, keep, kpos,
-        scan_tmp;
+        scan_tmp, tflag, tpos;
     DevBuf<int64_t> cmin;
     DevBuf<double> epart, et;
     DevBuf<int> icnt;
