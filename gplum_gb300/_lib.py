@@ -42,6 +42,7 @@ SIGNATURES = {
     "p3t_state_n": (I, []),
     "p3t_state_get": (I, [I, VP]),
     "p3t_state_set": (I, [I, VP]),
+    "p3t_state_snapshot": (I, [I]),
     "p3t_set_cutoff_radii": (I, []),
     "p3t_set_r_planet": (I, []),
     "p3t_state_soft": (I, [I, VP, VP, VP, VP, VP, VP, VP, I]),

@@ -769,6 +769,58 @@ using namespace p3t;
 
 extern "C" {
 
+// Device-to-device copy of every state field (and the cluster lists) into a
+// backup, and back: lets a caller time or retry a phase on the same state.
+static State g_backup;
+static int g_backup_n = -1;
+int p3t_state_snapshot(int restore) {
+    Engine &E = g_eng;
+    if (!E.c) return -(int)cudaErrorNoDevice;
+    State &S = E.S;
+    if (!restore) {
+        if (g_backup.cap < S.cap) {
+            // allocate the backup with the state's capacity
+            State b;
+            b.cap = S.cap;
+            auto al = [&](auto **p, size_t n) -> int {
+                return cuda_status(cudaMalloc((void **)p, std::max<size_t>(n, 1) * sizeof(**p)));
+            };
+            int r = 0;
+            for (double **f : {&b.mass, &b.r_planet, &b.f, &b.phi, &b.phi_d, &b.phi_s, &b.r_out, &b.r_out_inv,
+                               &b.r_search, &b.v_disp, &b.time, &b.dt, &b.acc0})
+                if ((r = al(f, S.cap))) return r;
+            for (double **f : {&b.pos, &b.vel, &b.acc, &b.acc_d, &b.jerk_d, &b.acc_s, &b.jerk_s})
+                if ((r = al(f, 3 * (size_t)S.cap))) return r;
+            for (int64_t **f : {&b.id, &b.id_cluster})
+                if ((r = al(f, S.cap))) return r;
+            for (int32_t **f : {&b.number, &b.rank, &b.id_max, &b.id_min, &b.n_cluster, &b.dead, &b.merged})
+                if ((r = al(f, S.cap))) return r;
+            g_backup = b;
+        }
+        g_backup_n = S.n;
+    } else if (g_backup_n != S.n) {
+        return ST_BAD_INDEX;
+    }
+    State &src = restore ? g_backup : S;
+    State &dst = restore ? S : g_backup;
+    const size_t n = S.n;
+    cudaStream_t st = E.c->stream;
+    auto cp = [&](void *d, const void *s2, size_t b) { cudaMemcpyAsync(d, s2, b, cudaMemcpyDeviceToDevice, st); };
+    cp(dst.mass, src.mass, n * 8); cp(dst.r_planet, src.r_planet, n * 8); cp(dst.f, src.f, n * 8);
+    cp(dst.phi, src.phi, n * 8); cp(dst.phi_d, src.phi_d, n * 8); cp(dst.phi_s, src.phi_s, n * 8);
+    cp(dst.r_out, src.r_out, n * 8); cp(dst.r_out_inv, src.r_out_inv, n * 8); cp(dst.r_search, src.r_search, n * 8);
+    cp(dst.v_disp, src.v_disp, n * 8); cp(dst.time, src.time, n * 8); cp(dst.dt, src.dt, n * 8);
+    cp(dst.acc0, src.acc0, n * 8);
+    cp(dst.pos, src.pos, n * 24); cp(dst.vel, src.vel, n * 24); cp(dst.acc, src.acc, n * 24);
+    cp(dst.acc_d, src.acc_d, n * 24); cp(dst.jerk_d, src.jerk_d, n * 24); cp(dst.acc_s, src.acc_s, n * 24);
+    cp(dst.jerk_s, src.jerk_s, n * 24);
+    cp(dst.id, src.id, n * 8); cp(dst.id_cluster, src.id_cluster, n * 8);
+    cp(dst.number, src.number, n * 4); cp(dst.rank, src.rank, n * 4); cp(dst.id_max, src.id_max, n * 4);
+    cp(dst.id_min, src.id_min, n * 4); cp(dst.n_cluster, src.n_cluster, n * 4); cp(dst.dead, src.dead, n * 4);
+    cp(dst.merged, src.merged, n * 4);
+    return cuda_status(cudaStreamSynchronize(st));
+}
+
 int p3t_state_load(int n, const long long *id, const double *mass, const double *r_planet, const double *f,
                    const double *pos, const double *vel) {
     if (n < 0) return ST_BAD_INDEX;

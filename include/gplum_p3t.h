@@ -112,6 +112,11 @@ int p3t_state_load(int n, const long long *id, const double *mass, const double 
 int p3t_state_n(void);
 int p3t_state_get(int field, void *out);
 int p3t_state_set(int field, const void *in);
+/* restore = 0: copy every state field to a device backup; restore = 1:
+ * copy the backup back (same body count).  Lets a caller time or retry a
+ * phase on one state (tier autotuning, cost logging).  No counterpart in
+ * GPLUM. */
+int p3t_state_snapshot(int restore);
 /* setCutoffRadii (src/particle.h:1528-1543) on the device. */
 int p3t_set_cutoff_radii(void);
 /* FPGrav::setRPlanet for every body (src/particle.h:757-759). */
