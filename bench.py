@@ -383,7 +383,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--skip-step", action="store_true", help="skip the whole-step measurement")
+    ap.add_argument("--step-only", type=int, default=0, metavar="N",
+                    help="only run one whole device step on the N-body hard-part disk and print its phases "
+                         "(a small case for profiling the step's kernels)")
     args = ap.parse_args()
+    if args.step_only:
+        print(json.dumps(p3t_step_measure(0, steps=1, n=args.step_only)))
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":

@@ -55,6 +55,8 @@ SIGNATURES = {
     "p3t_set_hard_tiers": (I, [I, I]),
     "p3t_set_cluster_priority": (I, [VP, I]),
     "p3t_hard_costs": (I, [VP, I]),
+    "p3t_hard_times": (I, [VP, I]),
+    "p3t_set_hard_mode": (I, [I]),
     "p3t_kick": (I, []),
     "p3t_energy": (I, [VP]),
     "p3t_merge": (I, [VP]),

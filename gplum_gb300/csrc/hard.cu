@@ -62,6 +62,7 @@ struct HardArgs {
     int n_tier[3];       // clusters per tier (CTA, warp, thread), in `order`
     int32_t *queue;      // [3] tier queue heads
     long long *cost;     // optional [2 * n_clusters]: block steps, pair sweeps
+    long long *times;    // optional [2 * n_clusters]: start, end (global timer, ns)
     double *cl_edisp;  // [2 * n_clusters]
     ColRec *cols;
     int32_t *n_cols;
@@ -103,10 +104,10 @@ __device__ __forceinline__ void dt_hermite(const Params &P, const Hard &H, int s
                              dt4th(P.eta_sun, P.alpha2, 0., ld3(H.acc_s, s), ld3(H.jerk_s, s), ld3(H.a2_s, s),
                                    ld3(H.a3_s, s)));
     const double time = H.th[s];
-    double rem = fmod(time, dt_next);
+    double rem = rem_pow2(time, dt_next);
     for (int k = 0; rem != 0.0 && k < 1100; k++) {
         dt_next *= 0.5;
-        rem = fmod(time, dt_next);
+        rem = rem_pow2(time, dt_next);
     }
     for (int k = 0; dt_1 < dt_next && 0.5 * H.dt[s] < dt_next && k < 1100; k++) dt_next *= 0.5;
     if (dt_next < 2. * P.dt_min) dt_next = P.dt_min;
@@ -355,9 +356,16 @@ struct Team {
     }
 };
 
+__device__ __forceinline__ long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return (long long)t;
+}
+
 // timeIntegrate_multi, src/hermite.h:224-479, for cluster c by a team.
 template <int TEAM>
 __device__ void run_cluster(const HardArgs &A, int c, const Team<TEAM> &tm) {
+    const long long t_start = (A.times && tm.rank == 0) ? global_ns() : 0;
     const Params &P = A.P;
     const Hard &H = A.H;
     const int rank = tm.rank;
@@ -579,6 +587,10 @@ __device__ void run_cluster(const HardArgs &A, int c, const Team<TEAM> &tm) {
         A.cl_edisp[2 * c] = (n_col > 0) ? ed : 0.;
         A.cl_edisp[2 * c + 1] = (n_col > 0) ? edd : 0.;
         if (A.cost) A.cost[2 * c] = steps;
+        if (A.times) {
+            A.times[2 * c] = t_start;
+            A.times[2 * c + 1] = global_ns();
+        }
     }
     tm.sync();
 }
@@ -629,6 +641,12 @@ __global__ void __launch_bounds__(128, 2) k_hard_clusters(HardArgs A) {
         }
     }
 }
+
+}  // namespace p3t
+
+#include "hard_bundle.cuh"
+
+namespace p3t {
 
 // ---- isolated bodies ----------------------------------------------------------
 __device__ __forceinline__ double kepler_eq(double u, double e) { return u - e * sin(u); }
@@ -757,8 +775,8 @@ __global__ void k_isolated(IsoArgs A) {
             double dt_next = dmin(2. * dt, 0.5 * P.dt_tree);
             const double dt_1 = dmin(dt4th(P.eta, P.alpha2, acc0, ad, jd, a2d, a3d),
                                      dt4th(P.eta_sun, P.alpha2, 0., as, js, a2s, a3s));
-            double rem = fmod(th, dt_next);
-            for (int k = 0; rem != 0.0 && k < 1100; k++) { dt_next *= 0.5; rem = fmod(th, dt_next); }
+            double rem = rem_pow2(th, dt_next);
+            for (int k = 0; rem != 0.0 && k < 1100; k++) { dt_next *= 0.5; rem = rem_pow2(th, dt_next); }
             for (int k = 0; dt_1 < dt_next && 0.5 * dt < dt_next && k < 1100; k++) dt_next *= 0.5;
             if (dt_next < 2. * P.dt_min) dt_next = P.dt_min;
             dt = dt_next;
@@ -796,7 +814,7 @@ struct HardBufs {
     DevBuf<int32_t> i32, order, queue, n_cols;
     DevBuf<double> cl_edisp, etot;
     DevBuf<ColRec> cols;
-    DevBuf<long long> cost;
+    DevBuf<long long> cost, times;
     DevBuf<float> f32;
     Hard H;
     int cap = 0;
@@ -834,6 +852,7 @@ static HardBufs g_hb;
 static std::vector<ColRec> g_cols;
 static double g_edisp[2] = {0., 0.};
 static int g_warp_min = 8, g_cta_min = 64;
+static int g_hard_mode = 0;  // 0: bundles, 1: thread/warp/CTA tiers
 static std::vector<float> g_prio;
 
 }  // namespace p3t
@@ -849,6 +868,12 @@ int p3t_set_hard_tiers(int warp_min, int cta_min) {
     return 0;
 }
 
+int p3t_set_hard_mode(int mode) {
+    if (mode != 0 && mode != 1) return ST_BAD_INDEX;
+    g_hard_mode = mode;
+    return 0;
+}
+
 int p3t_set_cluster_priority(const float *prio, int n) {
     if (n != g_eng.n_clusters || n < 0) return ST_BAD_INDEX;
     g_prio.assign(prio, prio + n);
@@ -860,6 +885,13 @@ int p3t_hard_costs(long long *out, int n) {
     if (!c) return -(int)cudaErrorNoDevice;
     if (n != g_eng.n_clusters || !g_hb.cost.p) return ST_BAD_INDEX;
     return cuda_status(cudaMemcpy(out, g_hb.cost.p, 2 * (size_t)n * sizeof(long long), cudaMemcpyDeviceToHost));
+}
+
+int p3t_hard_times(long long *out, int n) {
+    Context *c = ctx_get(0);
+    if (!c) return -(int)cudaErrorNoDevice;
+    if (n != g_eng.n_clusters || !g_hb.times.p) return ST_BAD_INDEX;
+    return cuda_status(cudaMemcpy(out, g_hb.times.p, 2 * (size_t)n * sizeof(long long), cudaMemcpyDeviceToHost));
 }
 
 int p3t_hard(int istep, int col_cap, long long *col_pairs, double *edisp) {
@@ -882,7 +914,10 @@ int p3t_hard(int istep, int col_cap, long long *col_pairs, double *edisp) {
         if ((r = cuda_status(cudaMemcpy(cnt.data(), E.cl_cnt.p, nc * sizeof(int32_t), cudaMemcpyDeviceToHost))))
             return r;
         const bool use_prio = (int)g_prio.size() == nc;
-        auto tier = [&](int k) { return cnt[k] >= g_cta_min ? 0 : (cnt[k] >= g_warp_min ? 1 : 2); };
+        auto tier = [&](int k) {
+            if (g_hard_mode == 0) return cnt[k] > BCAP ? 0 : 1;
+            return cnt[k] >= g_cta_min ? 0 : (cnt[k] >= g_warp_min ? 1 : 2);
+        };
         ord.resize(nc);
         for (int k = 0; k < nc; k++) ord[k] = k;
         std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
@@ -895,7 +930,7 @@ int p3t_hard(int istep, int col_cap, long long *col_pairs, double *edisp) {
         if ((r = h2d(c, B.order.p, ord.data(), nc * sizeof(int32_t)))) return r;
     }
     g_prio.clear();
-    if ((r = B.cost.reserve(2 * (size_t)nc + 2))) return r;
+    if ((r = B.cost.reserve(2 * (size_t)nc + 2)) || (r = B.times.reserve(2 * (size_t)nc + 2))) return r;
     cudaMemsetAsync(B.cost.p, 0, (2 * (size_t)nc + 2) * sizeof(long long), c->stream);
     cudaMemsetAsync(B.queue.p, 0, 3 * sizeof(int32_t), c->stream);
     cudaMemsetAsync(B.n_cols.p, 0, sizeof(int32_t), c->stream);
@@ -913,6 +948,7 @@ int p3t_hard(int istep, int col_cap, long long *col_pairs, double *edisp) {
         for (int t = 0; t < 3; t++) A.n_tier[t] = ntier[t];
         A.queue = B.queue.p;
         A.cost = B.cost.p;
+        A.times = B.times.p;
         A.cl_edisp = B.cl_edisp.p;
         A.cols = B.cols.p;
         A.n_cols = B.n_cols.p;
@@ -921,9 +957,23 @@ int p3t_hard(int istep, int col_cap, long long *col_pairs, double *edisp) {
         A.t_end = P.dt_tree;
         int sms = 152;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
-        const int want = ntier[0] + (ntier[1] + 3) / 4 + (ntier[2] + 127) / 128;
-        const int blocks = std::max(1, std::min(want, sms * 2));  // persistent: 2 CTAs per SM
-        k_hard_clusters<<<blocks, 128, 0, c->stream>>>(A);
+        if (g_hard_mode == 0) {
+            static bool attr = false;
+            const int smem = (int)sizeof(BundleSmem);
+            if (!attr) {
+                if ((r = cuda_status(cudaFuncSetAttribute(k_hard_bundles, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                          smem))))
+                    return r;
+                attr = true;
+            }
+            const int want = ntier[0] + (ntier[1] + 7) / 8;
+            const int blocks = std::max(1, std::min(want, sms * 2));  // persistent: 2 CTAs per SM
+            k_hard_bundles<<<blocks, BT, smem, c->stream>>>(A);
+        } else {
+            const int want = ntier[0] + (ntier[1] + 3) / 4 + (ntier[2] + 127) / 128;
+            const int blocks = std::max(1, std::min(want, sms * 2));  // persistent: 2 CTAs per SM
+            k_hard_clusters<<<blocks, 128, 0, c->stream>>>(A);
+        }
         if ((r = cuda_status(cudaGetLastError()))) return r;
     }
     IsoArgs I;

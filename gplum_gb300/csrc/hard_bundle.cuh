@@ -1,0 +1,853 @@
+// Lane-dense form of the hard part: one CTA integrates a "bundle" of many
+// clusters at once.
+//
+// FP64 runs at 1/64 of the FP32 rate on this GPU, and a warp instruction
+// occupies the FP64 pipe for all 32 lanes whether or not they are active.  A
+// warp (or thread) per cluster leaves most lanes idle: a cluster has a few
+// active members per block step, and a serial pair loop per member has one
+// live partner in several.  Here the CTA keeps up to BCAP members of up to
+// BMAXCL clusters in shared memory and advances every cluster by one block
+// step per iteration, so each phase runs over the union of the bundle's
+// work items:
+//   - member phases (predict, correct, time steps) over all members or all
+//     active members of all clusters;
+//   - pair phases over (target, partner) items: an FP32 distance prefilter
+//     (with a per-cluster margin proven below) packs the live pairs into a
+//     ring in (target, partner) order; their FP64 terms are computed one pair
+//     per thread; the terms are then added to each target's accumulators in
+//     partner order, which is the summation order of the reference loop
+//     (src/gravity_hard.h:203-367), so the sums are bit-identical;
+//   - collision detection over unordered member pairs, FP32 prefilter, FP64
+//     R for the survivors and a per-cluster lexicographic (R, pair) minimum.
+// Finished clusters leave the bundle and the queue refills it, so the CTA
+// stays full until the queue is empty.  Clusters larger than BCAP take the
+// one-cluster-per-CTA form (run_cluster<128>) first.
+//
+// The global per-slot arrays (struct Hard) stay the state of record; shared
+// memory mirrors the fields that other members read (positions, velocities,
+// predicted state, masses, radii, ids, flags) and is refreshed after every
+// phase that changes them.
+//
+// Prefilter margins.  FP32 coordinates are taken relative to the cluster's
+// first member, u = fl32(x - ref).  While every stored |x - ref| component
+// stays below E (checked at every store; a violation switches the cluster to
+// exact FP64 tests for good), a computed FP32 distance exceeds the exact one
+// by at most err = 3e-7 E plus 1.6e-7 relative.  A pair whose exact cutoff
+// test passes (|dr|^2 r_out_inv^2 <= 1.000001) then has an FP32 value
+// <= (1.000001 + err r_out_inv_max)^2 * 1.000001 =: thr_f, and a pair with
+// exact R < 1 has FP32 d^2 <= thr_c (r_i + r_j)_32^2 with
+// thr_c = (1.000001 + err / (2 min f r_p))^2 * 1.000001 (both rounded up to
+// FP32).  Pairs above the thresholds are therefore beyond the cutoff (their
+// terms are exact zeros) or have R > 1, so skipping them is exact; pairs below
+// them but beyond the cutoff contribute exact +-0 terms to accumulators that
+// start at +0, which leaves every sum unchanged.
+#pragma once
+
+namespace p3t {
+
+constexpr int BT = 128;      // threads of a bundle (one CTA)
+constexpr int BCAP = 256;    // member slots of a bundle
+constexpr int BMAXCL = 128;  // clusters in a bundle at once
+constexpr int BSURV = 64;    // colliding-pair candidates kept per block step
+constexpr int BCLAIM = 8;    // clusters claimed from the queue at a time
+
+enum : int { CF_COL = 1, CF_FIN = 2, CF_FRESH = 4, CF_EXACT = 8 };
+enum : unsigned char { MF_ACT = 1, MF_TGT = 2 };
+
+struct BundleSmem {
+    // member mirror (pool slot p)
+    double pos[3 * BCAP], vel[3 * BCAP], xp[3 * BCAP], vp[3 * BCAP];
+    double mass[BCAP], roi[BCAP], fr[BCAP];
+    double acc[7 * BCAP];  // force accumulators of the running pair phase
+    double term[7 * BT];   // FP64 pair terms of one drain
+    long long id[BCAP];
+    float pos32[3 * BCAP], xp32[3 * BCAP], roi32[BCAP], fr32[BCAP];
+    int gslot[BCAP];
+    int pfx[BCAP + 1];
+    int ring[2 * BT];
+    int seg[BT + 1];
+    short tgt[BCAP], cl[BCAP], owner[BCAP];
+    unsigned char dead[BCAP], merged[BCAP], flag[BCAP];
+    // clusters (bundle index k)
+    double c_ts[BMAXCL], c_ref[3 * BMAXCL], c_ed[BMAXCL], c_edd[BMAXCL];
+    unsigned long long c_key[BMAXCL], c_red[4 * BMAXCL];
+    long long c_pb[BMAXCL], c_work[BMAXCL], c_t0[BMAXCL];
+    float c_thrf[BMAXCL], c_thrc[BMAXCL], c_E32[BMAXCL];
+    int c_idx[BMAXCL], c_off[BMAXCL], c_n[BMAXCL], c_goff[BMAXCL], c_steps[BMAXCL], c_ncol[BMAXCL];
+    int c_flags[BMAXCL], c_imp[BMAXCL], c_tar[BMAXCL];
+    // colliding-pair candidates
+    double sv_R[BSURV];
+    long long sv_p[BSURV];
+    int sv_k[BSURV];
+    // claimed, not yet admitted clusters
+    int pend_c[BCLAIM], pend_n[BCLAIM];
+    int ws[BT / 32];
+    int used, ncl, fresh_k, fresh_p, n_sv, n_pend, i_pend, exhausted, any;
+};
+
+__device__ __forceinline__ unsigned long long dbits(double x) {
+    return (unsigned long long)__double_as_longlong(x);
+}
+__device__ __forceinline__ double bitsd(unsigned long long b) { return __longlong_as_double((long long)b); }
+
+// exclusive block-wide prefix sum of v; all threads must call
+__device__ __forceinline__ int bscan(int v, int *ws, int &total) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[w] = x;
+    __syncthreads();
+    int off = 0, tot = 0;
+#pragma unroll
+    for (int k = 0; k < BT / 32; k++) {
+        const int c = ws[k];
+        off += (k < w) ? c : 0;
+        tot += c;
+    }
+    __syncthreads();
+    total = tot;
+    return off + x - v;
+}
+
+// FP32 copy of a position relative to the cluster origin, with the bound check
+__device__ __forceinline__ void st32b(BundleSmem &B, float *dst, int p, V3 x, int k) {
+    const float u0 = (float)(x.x - B.c_ref[3 * k]), u1 = (float)(x.y - B.c_ref[3 * k + 1]),
+                u2 = (float)(x.z - B.c_ref[3 * k + 2]);
+    dst[3 * p] = u0;
+    dst[3 * p + 1] = u1;
+    dst[3 * p + 2] = u2;
+    const float E = B.c_E32[k];
+    if (!(fabsf(u0) < E && fabsf(u1) < E && fabsf(u2) < E)) atomicOr(&B.c_flags[k], CF_EXACT);
+}
+
+// mirror every field of slot p from the state of record (global slot g)
+__device__ __forceinline__ void mirror_all(BundleSmem &B, const Hard &H, int p, int g, int k, bool with32) {
+    const V3 x = ld3(H.pos, g);
+    st3(B.pos, p, x);
+    st3(B.vel, p, ld3(H.vel, g));
+    st3(B.xp, p, ld3(H.xp, g));
+    st3(B.vp, p, ld3(H.vp, g));
+    B.mass[p] = H.mass[g];
+    B.roi[p] = H.r_out_inv[g];
+    const double fr = H.f[g] * H.r_planet[g];
+    B.fr[p] = fr;
+    B.fr32[p] = (float)fr;
+    B.roi32[p] = (float)H.r_out_inv[g];
+    B.id[p] = H.id[g];
+    B.dead[p] = (unsigned char)H.dead[g];
+    B.merged[p] = (unsigned char)H.merged[g];
+    B.gslot[p] = g;
+    B.cl[p] = (short)k;
+    if (with32) {
+        st32b(B, B.pos32, p, x, k);
+        st32b(B, B.xp32, p, ld3(H.xp, g), k);
+    }
+}
+
+// ---- pair phases ------------------------------------------------------------
+// ordered list of the occupied slots whose flag has `bit`
+__device__ int bundle_list(BundleSmem &B, unsigned char bit) {
+    constexpr int PER = BCAP / BT;
+    const int base = threadIdx.x * PER;
+    int c = 0;
+#pragma unroll
+    for (int j = 0; j < PER; j++) {
+        const int p = base + j;
+        if (p < B.used && (B.flag[p] & bit)) c++;
+    }
+    int tot;
+    int off = bscan(c, B.ws, tot);
+#pragma unroll
+    for (int j = 0; j < PER; j++) {
+        const int p = base + j;
+        if (p < B.used && (B.flag[p] & bit)) B.tgt[off++] = (short)p;
+    }
+    __syncthreads();
+    return tot;
+}
+
+// the seven terms (acc_d xyz, jerk_d xyz, -phi_d) of target s from partner t,
+// the arithmetic of hard_force for one pair
+__device__ __forceinline__ void pair_terms(const Params &P, const BundleSmem &B, int mode, int s, int t, double *o) {
+    V3 xi, vi, xj, vj;
+    if (mode == 1) { xi = ld3(B.xp, s); vi = ld3(B.vp, s); }
+    else { xi = ld3(B.pos, s); vi = ld3(B.vel, s); }
+    if (mode == 0) { xj = ld3(B.pos, t); vj = ld3(B.vel, t); }
+    else { xj = ld3(B.xp, t); vj = ld3(B.vp, t); }
+    const V3 dr = xj - xi;
+    double dr2 = dot(dr, dr);
+    dr2 += P.eps2;
+    const double r_out_inv = dmin(B.roi[s], B.roi[t]);
+    const V3 dv = vj - vi;
+    const double rij = sqrt(dr2);
+    const double rinv = 1. / rij;
+    const double r2inv = rinv * rinv;
+    const double r3inv = r2inv * rinv;
+    const double mj = B.mass[t];
+    const double mr3 = mj * r3inv;
+    const double alpha = dot(dr, dv) * r2inv;
+    double Wc = 0.;
+    if (mode == 0) Wc = 1. - cut_W(P, rij, r_out_inv);
+    const double Kc = 1. - cut_K(P, rij, r_out_inv);
+    const double dKdt = cut_dKdt(P, rij, r_out_inv, alpha);
+    const double alpha_c = alpha * Kc;
+    const V3 a = mr3 * Kc * dr;
+    const V3 j = mr3 * (Kc * dv - (3. * alpha_c + dKdt) * dr);
+    o[0] = a.x; o[1] = a.y; o[2] = a.z;
+    o[3] = j.x; o[4] = j.y; o[5] = j.z;
+    o[6] = (mode == 0) ? -(mj * rinv * Wc) : 0.;
+}
+
+// terms of ring[0..m), then in-order addition into the targets' accumulators
+__device__ void bundle_drain(const Params &P, BundleSmem &B, int mode, int m) {
+    const int q = threadIdx.x;
+    int sq = -1;
+    if (q < m) {
+        const int e = B.ring[q];
+        sq = e >> 16;
+        double o[7];
+        pair_terms(P, B, mode, sq, e & 0xffff, o);
+#pragma unroll
+        for (int c = 0; c < 7; c++) B.term[c * BT + q] = o[c];
+    }
+    const int head = (q < m) && (q == 0 || (B.ring[q - 1] >> 16) != sq);
+    int nseg;
+    const int off = bscan(head, B.ws, nseg);
+    if (head) B.seg[off] = q;
+    if (q == 0) B.seg[nseg] = m;
+    __syncthreads();
+    const int ncomp = (mode == 0) ? 7 : 6;
+    for (int it = q; it < ncomp * nseg; it += BT) {
+        const int j = it / ncomp, c = it - ncomp * j;
+        const int a = B.seg[j], b = B.seg[j + 1];
+        const int s = B.ring[a] >> 16;
+        double acc = B.acc[c * BCAP + s];
+        for (int k = a; k < b; k++) acc += B.term[c * BT + k];
+        B.acc[c * BCAP + s] = acc;
+    }
+    __syncthreads();
+}
+
+// mode 0: full (pos/vel, with phi); 1: predicted i and j; 2: corrected i,
+// predicted j -- for the nt targets in B.tgt
+__device__ void bundle_pairs(const HardArgs &A, BundleSmem &B, int mode, int nt) {
+    const int tid = threadIdx.x;
+    constexpr int PER = BCAP / BT;
+    for (int i = tid; i < nt; i += BT) {
+        const int s = B.tgt[i];
+#pragma unroll
+        for (int c = 0; c < 7; c++) B.acc[c * BCAP + s] = 0.;
+    }
+    // partner-count prefix over the targets
+    int total;
+    {
+        const int base = tid * PER;
+        int c = 0;
+#pragma unroll
+        for (int j = 0; j < PER; j++)
+            if (base + j < nt) c += B.c_n[B.cl[B.tgt[base + j]]];
+        int off = bscan(c, B.ws, total);
+#pragma unroll
+        for (int j = 0; j < PER; j++)
+            if (base + j < nt) {
+                B.pfx[base + j] = off;
+                off += B.c_n[B.cl[B.tgt[base + j]]];
+            }
+        if (tid == 0) B.pfx[nt] = total;
+        __syncthreads();
+    }
+    const float *xi32 = (mode == 1) ? B.xp32 : B.pos32;
+    const float *xj32 = (mode == 0) ? B.pos32 : B.xp32;
+    int ring_n = 0;
+    for (int base = 0; base < total; base += BT) {
+        const int f = base + tid;
+        int live = 0, e = 0;
+        if (f < total) {
+            int lo = 0, hi = nt - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (B.pfx[mid] <= f) lo = mid;
+                else hi = mid - 1;
+            }
+            const int s = B.tgt[lo], k = B.cl[s];
+            const int t = B.c_off[k] + (f - B.pfx[lo]);
+            if (B.id[s] != B.id[t]) {
+                if (!(B.c_flags[k] & CF_EXACT)) {
+                    const float rf = fminf(B.roi32[s], B.roi32[t]);
+                    live = d2_32(xi32, s, xj32, t) * (rf * rf) <= B.c_thrf[k];
+                } else {
+                    const V3 xi = ld3((mode == 1) ? B.xp : B.pos, s);
+                    const V3 dr = ld3((mode == 0) ? B.pos : B.xp, t) - xi;
+                    double dr2 = dot(dr, dr);
+                    dr2 += A.P.eps2;
+                    const double r = dmin(B.roi[s], B.roi[t]);
+                    live = !(dr2 * r * r > 1.000001);
+                }
+            }
+            e = (s << 16) | t;
+        }
+        int cnt;
+        const int off = bscan(live, B.ws, cnt);
+        if (live) B.ring[ring_n + off] = e;
+        ring_n += cnt;
+        __syncthreads();
+        if (ring_n >= BT) {
+            bundle_drain(A.P, B, mode, BT);
+            const int rest = ring_n - BT;
+            if (tid < rest) B.ring[tid] = B.ring[BT + tid];
+            ring_n = rest;
+            __syncthreads();
+        }
+    }
+    if (ring_n > 0) bundle_drain(A.P, B, mode, ring_n);
+}
+
+// sun force and the accumulated pair sums of the targets to the state of
+// record, then mergeAccJerk for the merged targets (merge_sel 1: active
+// phase, merged alive targets; 2: all merged targets with twins)
+__device__ void bundle_finalize(const HardArgs &A, BundleSmem &B, int mode, int nt, int merge_sel) {
+    const Hard &H = A.H;
+    for (int i = threadIdx.x; i < nt; i += BT) {
+        const int s = B.tgt[i], g = B.gslot[s];
+        V3 xi, vi, as, js;
+        if (mode == 1) { xi = ld3(B.xp, s); vi = ld3(B.vp, s); }
+        else { xi = ld3(B.pos, s); vi = ld3(B.vel, s); }
+        if (mode == 0) {
+            double phs;
+            sun_force(A.P, xi, vi, as, js, &phs);
+            H.phi_s[g] = phs;
+            H.phi_d[g] = B.acc[6 * BCAP + s];
+        } else {
+            sun_force(A.P, xi, vi, as, js, nullptr);
+        }
+        st3(H.acc_s, g, as);
+        st3(H.jerk_s, g, js);
+        st3(H.acc_d, g, v3(B.acc[s], B.acc[BCAP + s], B.acc[2 * BCAP + s]));
+        st3(H.jerk_d, g, v3(B.acc[3 * BCAP + s], B.acc[4 * BCAP + s], B.acc[5 * BCAP + s]));
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nt; i += BT) {
+        const int s = B.tgt[i], g = B.gslot[s];
+        const bool m = (merge_sel == 1) ? (!B.dead[s] && B.merged[s]) : (B.merged[s] && H.tw_head[g] >= 0);
+        if (m) merge_acc_jerk(H, g);
+    }
+    __syncthreads();
+}
+
+// ---- collision detection ------------------------------------------------------
+// unordered pairs {a, b} of each cluster, balanced over members: member a
+// takes b = a + d (mod n) for d = 1..n/2 (the pair at distance n/2 once)
+__device__ void bundle_detect(const HardArgs &A, BundleSmem &B, bool second) {
+    for (int p = threadIdx.x; p < B.used; p += BT) {
+        if (B.dead[p]) continue;
+        const int k = B.cl[p];
+        const int o = B.c_off[k], n = B.c_n[k], a = p - o;
+        const bool exact = (B.c_flags[k] & CF_EXACT) != 0;
+        const float thr = B.c_thrc[k];
+        for (int d = 1; 2 * d <= n; d++) {
+            if (2 * d == n && a >= d) break;
+            int b = a + d;
+            if (b >= n) b -= n;
+            const int q = o + b;
+            if (B.dead[q]) continue;
+            if (!exact) {
+                const float rs = B.fr32[p] + B.fr32[q];
+                if (d2_32(B.xp32, p, B.xp32, q) > thr * (rs * rs)) continue;
+            }
+            const int lo = (a < b) ? a : b, hi = (a < b) ? b : a;
+            const V3 dr = ld3(B.xp, o + lo) - ld3(B.xp, o + hi);
+            const double d2 = dot(dr, dr);
+            const double r2 = B.fr[o + lo] + B.fr[o + hi];
+            if (d2 > r2 * r2 * 1.000001) continue;
+            const double R = sqrt(d2) / r2;
+            if (!(R < 1.)) continue;
+            const long long pp = (long long)lo * n + hi;
+            if (!second) {
+                atomicMin(&B.c_key[k], dbits(R));
+                const int i = atomicAdd(&B.n_sv, 1);
+                if (i < BSURV) {
+                    B.sv_k[i] = k;
+                    B.sv_R[i] = R;
+                    B.sv_p[i] = pp;
+                }
+            } else if (dbits(R) == B.c_key[k]) {
+                atomicMin(&B.c_pb[k], pp);
+            }
+        }
+    }
+}
+
+// ---- bundle lifecycle ---------------------------------------------------------------
+// warp 0: claim clusters from the queue and admit them while they fit (lane
+// 0 decides, the decisions are broadcast so the warp's control flow stays
+// uniform)
+__device__ void bundle_refill(const HardArgs &A, BundleSmem &B) {
+    const int lane = threadIdx.x & 31;
+    if (threadIdx.x < 32) {
+        for (int guard = 0; guard < (1 << 20); guard++) {
+            int stop = 0, claim = 0;
+            if (lane == 0 && B.i_pend >= B.n_pend) {
+                if (B.exhausted) stop = 1;
+                else claim = 1;
+            }
+            stop = __shfl_sync(0xffffffffu, stop, 0);
+            claim = __shfl_sync(0xffffffffu, claim, 0);
+            if (stop) break;
+            if (claim) {
+                int q = 0;
+                if (lane == 0) q = atomicAdd(&A.queue[1], BCLAIM);
+                q = __shfl_sync(0xffffffffu, q, 0);
+                const int qi = q + lane;
+                const bool ok = lane < BCLAIM && qi < A.n_tier[1];
+                const unsigned m = __ballot_sync(0xffffffffu, ok);
+                if (ok) {
+                    const int c = A.order[A.n_tier[0] + qi];
+                    B.pend_c[lane] = c;
+                    B.pend_n[lane] = A.cnt[c];
+                }
+                __syncwarp();
+                if (lane == 0) {
+                    B.n_pend = __popc(m);
+                    B.i_pend = 0;
+                    if (__popc(m) < BCLAIM) B.exhausted = 1;
+                }
+                __syncwarp();
+                if (m == 0u) break;
+            }
+            // admit in queue order
+            int full = 0;
+            if (lane == 0) {
+                while (B.i_pend < B.n_pend) {
+                    const int c = B.pend_c[B.i_pend], n = B.pend_n[B.i_pend];
+                    if (B.used + n > BCAP || B.ncl >= BMAXCL) break;
+                    const int k = B.ncl++;
+                    B.c_idx[k] = c;
+                    B.c_off[k] = B.used;
+                    B.c_n[k] = n;
+                    B.c_flags[k] = CF_FRESH;
+                    B.used += n;
+                    B.i_pend++;
+                }
+                full = B.i_pend < B.n_pend;
+            }
+            full = __shfl_sync(0xffffffffu, full, 0);
+            __syncwarp();
+            if (full) break;  // the next claimed cluster waits for space
+        }
+    }
+    __syncthreads();
+}
+
+// load the fresh clusters (bundle indices fresh_k..ncl-1, slots fresh_p..used-1)
+__device__ void bundle_load(const HardArgs &A, BundleSmem &B) {
+    const Hard &H = A.H;
+    const int tid = threadIdx.x;
+    const int k0 = B.fresh_k, k1 = B.ncl, p0 = B.fresh_p, p1 = B.used;
+    for (int k = k0 + tid; k < k1; k += BT) {
+        const int c = B.c_idx[k];
+        const int goff = A.off[c];
+        B.c_goff[k] = goff;
+        const V3 r0 = ld3(A.S.pos, A.members[goff]);
+        B.c_ref[3 * k] = r0.x; B.c_ref[3 * k + 1] = r0.y; B.c_ref[3 * k + 2] = r0.z;
+        B.c_steps[k] = 0; B.c_ncol[k] = 0; B.c_work[k] = 0;
+        B.c_ed[k] = 0.; B.c_edd[k] = 0.;
+        B.c_t0[k] = A.times ? global_ns() : 0;
+        B.c_red[4 * k] = 0ULL;                 // max |x - ref| component
+        B.c_red[4 * k + 1] = 0ULL;             // max |v| component
+        B.c_red[4 * k + 2] = 0ULL;             // max r_out_inv
+        B.c_red[4 * k + 3] = dbits(1.e300);    // min f r_planet
+    }
+    __syncthreads();
+    for (int p = p0 + tid; p < p1; p += BT) {
+        int lo = k0, hi = k1 - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (B.c_off[mid] <= p) lo = mid;
+            else hi = mid - 1;
+        }
+        const int k = lo, g = B.c_goff[k] + (p - B.c_off[k]), i = A.members[g];
+        // FPHard(const FPGrav&), src/particle.h:1096-1116
+        st3(H.pos, g, ld3(A.S.pos, i)); st3(H.vel, g, ld3(A.S.vel, i));
+        st3(H.acc_s, g, ld3(A.S.acc_s, i)); st3(H.jerk_s, g, ld3(A.S.jerk_s, i));
+        st3(H.acc_d, g, ld3(A.S.acc_d, i)); st3(H.jerk_d, g, ld3(A.S.jerk_d, i));
+        const V3 z = v3(0., 0., 0.);
+        st3(H.x0, g, z); st3(H.v0, g, z); st3(H.a0_s, g, z); st3(H.j0_s, g, z); st3(H.a0_d, g, z);
+        st3(H.j0_d, g, z); st3(H.xp, g, z); st3(H.vp, g, z); st3(H.a2_s, g, z); st3(H.a3_s, g, z);
+        st3(H.a2_d, g, z); st3(H.a3_d, g, z);
+        H.phi_d[g] = A.S.phi_d[i]; H.phi_s[g] = A.S.phi_s[i];
+        H.mass[g] = A.S.mass[i]; H.r_planet[g] = A.S.r_planet[i]; H.f[g] = A.S.f[i];
+        H.r_out_inv[g] = A.S.r_out_inv[i];
+        H.time_c[g] = A.S.time[i]; H.th[g] = 0.; H.dt[g] = A.S.dt[i]; H.acc0[g] = A.S.acc0[i];
+        H.id[g] = A.S.id[i];
+        H.dead[g] = 0; H.merged[g] = 0;
+        H.tw_head[g] = H.tw_tail[g] = H.tw_next[g] = -1;
+        mirror_all(B, H, p, g, k, false);
+        B.owner[p] = -1;
+        B.flag[p] = 0;
+        const V3 x = ld3(H.pos, g), v = ld3(H.vel, g);
+        const double ext = dmax(fabs(x.x - B.c_ref[3 * k]), dmax(fabs(x.y - B.c_ref[3 * k + 1]),
+                                                                  fabs(x.z - B.c_ref[3 * k + 2])));
+        const double vm = dmax(fabs(v.x), dmax(fabs(v.y), fabs(v.z)));
+        atomicMax(&B.c_red[4 * k], dbits(ext));
+        atomicMax(&B.c_red[4 * k + 1], dbits(vm));
+        atomicMax(&B.c_red[4 * k + 2], dbits(B.roi[p]));
+        atomicMin(&B.c_red[4 * k + 3], dbits(B.fr[p]));
+    }
+    __syncthreads();
+    for (int k = k0 + tid; k < k1; k += BT) {
+        // coordinate bound, then the prefilter thresholds (see the header)
+        const double E = (bitsd(B.c_red[4 * k]) + 2. * bitsd(B.c_red[4 * k + 1]) * A.t_end) * 1.0001 + 1.e-30;
+        const double err = 3.e-7 * E;
+        const double rmax = bitsd(B.c_red[4 * k + 2]), frmin = bitsd(B.c_red[4 * k + 3]);
+        const double tf = 1.000001 + 1.0001 * err * rmax;
+        const double tc = 1.000001 + 1.0001 * err / (2. * frmin);
+        B.c_thrf[k] = __double2float_ru(tf * tf * 1.000001);
+        B.c_thrc[k] = (frmin > 0.) ? __double2float_ru(tc * tc * 1.000001) : __int_as_float(0x7f800000);
+        B.c_E32[k] = __double2float_rd(E);
+    }
+    __syncthreads();
+    for (int p = tid; p < p1; p += BT) {
+        if (p < p0) {
+            B.flag[p] = 0;
+            continue;
+        }
+        st32b(B, B.pos32, p, ld3(B.pos, p), B.cl[p]);
+        B.flag[p] = MF_TGT;
+    }
+    __syncthreads();
+}
+
+// member-parallel loop over the occupied slots
+#define FOR_SLOTS(p) for (int p = threadIdx.x; p < B.used; p += BT)
+#define FOR_CLUSTERS(k) for (int k = threadIdx.x; k < B.ncl; k += BT)
+
+// one block step of every cluster in the bundle (timeIntegrate_multi body,
+// src/hermite.h:224-479)
+__device__ void bundle_step(const HardArgs &A, BundleSmem &B) {
+    const Params &P = A.P;
+    const Hard &H = A.H;
+    // makeActiveList: ts = min over alive members of th + dt
+    FOR_CLUSTERS(k) {
+        B.c_steps[k]++;
+        B.c_key[k] = dbits(1.e10);
+    }
+    __syncthreads();
+    FOR_SLOTS(p) {
+        if (B.dead[p]) continue;
+        const int g = B.gslot[p];
+        atomicMin(&B.c_key[B.cl[p]], dbits(H.th[g] + H.dt[g]));
+    }
+    __syncthreads();
+    FOR_CLUSTERS(k) {
+        B.c_ts[k] = bitsd(B.c_key[k]);
+        B.c_key[k] = dbits(1.);
+        B.c_pb[k] = 0x7fffffffffffffffLL;
+    }
+    if (threadIdx.x == 0) B.n_sv = 0;
+    __syncthreads();
+    // predict every member
+    FOR_SLOTS(p) {
+        const int g = B.gslot[p], k = B.cl[p];
+        predict(H, g, B.c_ts[k] - H.th[g]);
+        const V3 xp = ld3(H.xp, g);
+        st3(B.xp, p, xp);
+        st3(B.vp, p, ld3(H.vp, g));
+        st32b(B, B.xp32, p, xp, k);
+    }
+    __syncthreads();
+    // collisionDetermination, src/hermite.h:98-196
+    bundle_detect(A, B, false);
+    __syncthreads();
+    if (B.n_sv <= BSURV) {
+        for (int i = threadIdx.x; i < B.n_sv; i += BT)
+            if (dbits(B.sv_R[i]) == B.c_key[B.sv_k[i]]) atomicMin(&B.c_pb[B.sv_k[i]], B.sv_p[i]);
+    } else {
+        bundle_detect(A, B, true);
+    }
+    __syncthreads();
+    FOR_CLUSTERS(k) {
+        int fl = B.c_flags[k] & ~CF_COL;
+        if (B.c_key[k] < dbits(1.)) {
+            fl |= CF_COL;
+            const int o = B.c_off[k], n = B.c_n[k];
+            const int a = (int)(B.c_pb[k] / n), b = (int)(B.c_pb[k] % n);
+            if (B.mass[o + a] < B.mass[o + b]) { B.c_imp[k] = o + a; B.c_tar[k] = o + b; }
+            else { B.c_imp[k] = o + b; B.c_tar[k] = o + a; }
+        }
+        B.c_flags[k] = fl;
+    }
+    __syncthreads();
+    // the active set (every alive member on a collision) and the twins of
+    // active merged members
+    FOR_SLOTS(p) {
+        const int k = B.cl[p], g = B.gslot[p];
+        const bool col = (B.c_flags[k] & CF_COL) != 0;
+        if (col) H.dt[g] = B.c_ts[k] - H.th[g];
+        unsigned char f = 0;
+        if (!B.dead[p] && (col || H.th[g] + H.dt[g] == B.c_ts[k])) {
+            f = MF_ACT | MF_TGT;
+            atomicAdd((unsigned long long *)&B.c_work[k], (unsigned long long)B.c_n[k]);
+        }
+        B.flag[p] = f;
+    }
+    __syncthreads();
+    FOR_SLOTS(p) {
+        const int ow = B.owner[p];
+        if (B.dead[p] && ow >= 0 && (B.flag[ow] & MF_ACT)) B.flag[p] |= MF_TGT;
+    }
+    __syncthreads();
+    const int nt = bundle_list(B, MF_TGT);
+    bundle_pairs(A, B, 1, nt);
+    bundle_finalize(A, B, 1, nt, 1);
+    for (int it = 0; it < 2; it++) {
+        for (int i = threadIdx.x; i < nt; i += BT) {
+            const int s = B.tgt[i], g = B.gslot[s], k = B.cl[s];
+            correct(H, g, B.c_ts[k] - H.th[g]);
+            const V3 x = ld3(H.pos, g);
+            st3(B.pos, s, x);
+            st3(B.vel, s, ld3(H.vel, g));
+            st32b(B, B.pos32, s, x, k);
+        }
+        __syncthreads();
+        bundle_pairs(A, B, 2, nt);
+        bundle_finalize(A, B, 2, nt, 1);
+    }
+    for (int i = threadIdx.x; i < nt; i += BT) {
+        const int s = B.tgt[i], g = B.gslot[s], k = B.cl[s];
+        H.th[g] += B.c_ts[k] - H.th[g];
+        if (!(B.c_flags[k] & CF_COL) && !B.dead[s]) dt_hermite(P, H, g);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nt; i += BT) {
+        const int s = B.tgt[i], k = B.cl[s];
+        if (B.dead[s] && B.owner[s] >= 0 && !(B.c_flags[k] & CF_COL)) H.dt[B.gslot[s]] = H.dt[B.gslot[B.owner[s]]];
+    }
+    if (threadIdx.x == 0) B.any = 0;
+    __syncthreads();
+    // collisions: one thread per colliding cluster
+    FOR_CLUSTERS(k) {
+        if (!(B.c_flags[k] & CF_COL)) continue;
+        B.any = 1;
+        ColRec rec;
+        double e1 = 0., e2 = 0.;
+        collide(P, H, B.gslot[B.c_imp[k]], B.gslot[B.c_tar[k]], e1, e2, rec);
+        B.c_ed[k] += e1;
+        B.c_edd[k] += e2;
+        rec.cluster = B.c_idx[k];
+        rec.seq = B.c_ncol[k]++;
+        const int slot = atomicAdd(A.n_cols, 1);
+        if (slot < A.col_cap) A.cols[slot] = rec;
+        else atomicOr(A.status, ST_QUEUE_OVERFLOW);
+        // twin owners (pool slots) from the merge lists
+        const int o = B.c_off[k], n = B.c_n[k], go = B.c_goff[k];
+        for (int j = 0; j < n; j++) B.owner[o + j] = -1;
+        for (int j = 0; j < n; j++)
+            if (H.merged[go + j])
+                for (int t = H.tw_head[go + j], gg = 0; t >= 0 && gg < 4096; t = H.tw_next[t], gg++)
+                    if (t >= go && t < go + n) B.owner[o + (t - go)] = (short)(o + j);
+    }
+    __syncthreads();
+    if (B.any) {
+        FOR_SLOTS(p) {
+            const int k = B.cl[p];
+            B.flag[p] = 0;
+            if (!(B.c_flags[k] & CF_COL)) continue;
+            mirror_all(B, H, p, B.gslot[p], k, true);
+            B.flag[p] = MF_TGT;
+        }
+        __syncthreads();
+        const int nc = bundle_list(B, MF_TGT);
+        bundle_pairs(A, B, 0, nc);
+        bundle_finalize(A, B, 0, nc, 2);
+        for (int i = threadIdx.x; i < nc; i += BT) {
+            const int s = B.tgt[i], g = B.gslot[s];
+            if (!B.dead[s])
+                H.dt[g] = dt_initial(P, H.th[g], H.dt[g], H.acc0[g], ld3(H.acc_d, g), ld3(H.jerk_d, g),
+                                     ld3(H.acc_s, g), ld3(H.jerk_s, g));
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < nc; i += BT) {
+            const int s = B.tgt[i], g = B.gslot[s];
+            if (B.merged[s])
+                for (int t = H.tw_head[g], gg = 0; t >= 0 && gg < 4096; t = H.tw_next[t], gg++) H.dt[t] = H.dt[g];
+        }
+        __syncthreads();
+    }
+    // getSystemTime, src/hermite.h:25-35
+    FOR_CLUSTERS(k) B.c_key[k] = dbits(1.e10);
+    __syncthreads();
+    FOR_SLOTS(p) {
+        if (!B.dead[p]) atomicMin(&B.c_key[B.cl[p]], dbits(H.th[B.gslot[p]]));
+    }
+    if (threadIdx.x == 0) B.any = 0;
+    __syncthreads();
+    FOR_CLUSTERS(k) {
+        const double time = bitsd(B.c_key[k]);
+        if (time < A.t_end && B.c_steps[k] >= MAX_BLOCK_STEPS) atomicOr(A.status, ST_ITER_CAP);
+        if (!(time < A.t_end) || B.c_steps[k] >= MAX_BLOCK_STEPS) {
+            B.c_flags[k] |= CF_FIN;
+            B.any = 1;
+        }
+    }
+    __syncthreads();
+}
+
+// final forces, write-back and removal of the finished clusters
+__device__ void bundle_retire(const HardArgs &A, BundleSmem &B) {
+    const Hard &H = A.H;
+    const int tid = threadIdx.x;
+    FOR_SLOTS(p) B.flag[p] = (B.c_flags[B.cl[p]] & CF_FIN) ? MF_TGT : 0;
+    __syncthreads();
+    const int nt = bundle_list(B, MF_TGT);
+    bundle_pairs(A, B, 0, nt);
+    bundle_finalize(A, B, 0, nt, 2);
+    // write back to FPGrav, with resetTime (src/hard.h:768-787)
+    for (int i = tid; i < nt; i += BT) {
+        const int s = B.tgt[i], g = B.gslot[s], k = B.cl[s], idx = A.members[g];
+        st3(A.S.pos, idx, ld3(H.pos, g)); st3(A.S.vel, idx, ld3(H.vel, g));
+        st3(A.S.acc_s, idx, ld3(H.acc_s, g)); st3(A.S.jerk_s, idx, ld3(H.jerk_s, g));
+        st3(A.S.acc_d, idx, ld3(H.acc_d, g)); st3(A.S.jerk_d, idx, ld3(H.jerk_d, g));
+        A.S.phi_d[idx] = H.phi_d[g]; A.S.phi_s[idx] = H.phi_s[g];
+        A.S.mass[idx] = H.mass[g]; A.S.r_planet[idx] = H.r_planet[g];
+        A.S.time[idx] = H.time_c[g] + H.th[g]; A.S.dt[idx] = H.dt[g];
+        A.S.id[idx] = H.id[g];
+        A.S.dead[idx] = H.dead[g]; A.S.merged[idx] = H.merged[g];
+        A.S.n_cluster[idx] = B.c_n[k];
+    }
+    FOR_CLUSTERS(k) {
+        if (!(B.c_flags[k] & CF_FIN)) continue;
+        const int c = B.c_idx[k];
+        A.cl_edisp[2 * c] = (B.c_ncol[k] > 0) ? B.c_ed[k] : 0.;
+        A.cl_edisp[2 * c + 1] = (B.c_ncol[k] > 0) ? B.c_edd[k] : 0.;
+        if (A.cost) {
+            A.cost[2 * c] = B.c_steps[k];
+            A.cost[2 * c + 1] = B.c_work[k];
+        }
+        if (A.times) {
+            A.times[2 * c] = B.c_t0[k];
+            A.times[2 * c + 1] = global_ns();
+        }
+    }
+    __syncthreads();
+    // compaction: kept clusters move down, in order
+    int keep = 0, nk = 0, nkeep = 0, noff = 0, tot = 0;
+    int t_idx = 0, t_n = 0, t_goff = 0, t_steps = 0, t_ncol = 0, t_flags = 0;
+    double t_ref0 = 0., t_ref1 = 0., t_ref2 = 0., t_ed = 0., t_edd = 0.;
+    long long t_work = 0, t_t0 = 0;
+    float t_thrf = 0.f, t_thrc = 0.f, t_E = 0.f;
+    if (tid < B.ncl) {
+        keep = !(B.c_flags[tid] & CF_FIN);
+        t_idx = B.c_idx[tid]; t_n = B.c_n[tid]; t_goff = B.c_goff[tid];
+        t_steps = B.c_steps[tid]; t_ncol = B.c_ncol[tid]; t_flags = B.c_flags[tid];
+        t_ref0 = B.c_ref[3 * tid]; t_ref1 = B.c_ref[3 * tid + 1]; t_ref2 = B.c_ref[3 * tid + 2];
+        t_ed = B.c_ed[tid]; t_edd = B.c_edd[tid]; t_work = B.c_work[tid]; t_t0 = B.c_t0[tid];
+        t_thrf = B.c_thrf[tid]; t_thrc = B.c_thrc[tid]; t_E = B.c_E32[tid];
+    }
+    static_assert(BMAXCL <= BT, "one thread per bundle cluster");
+    nk = bscan(keep, B.ws, nkeep);
+    noff = bscan(keep ? t_n : 0, B.ws, tot);
+    // slots: read the old placement before anything moves
+    constexpr int PER = BCAP / BT;
+    int mv_new[PER], mv_g[PER], mv_k[PER], mv_own[PER];
+    __syncthreads();
+    if (keep) {
+        // old -> new offset per kept cluster, through c_key (free here)
+        B.c_key[tid] = (unsigned long long)(unsigned)noff | ((unsigned long long)(unsigned)nk << 32);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < PER; j++) {
+        const int p = tid + j * BT;
+        mv_new[j] = -1;
+        if (p < B.used) {
+            const int k = B.cl[p];
+            if (!(B.c_flags[k] & CF_FIN)) {
+                const int no = (int)(B.c_key[k] & 0xffffffffULL), kk = (int)(B.c_key[k] >> 32);
+                mv_new[j] = no + (p - B.c_off[k]);
+                mv_g[j] = B.gslot[p];
+                mv_k[j] = kk;
+                mv_own[j] = (B.owner[p] >= 0) ? no + (B.owner[p] - B.c_off[k]) : -1;
+            }
+        }
+    }
+    __syncthreads();
+    if (keep) {
+        B.c_idx[nk] = t_idx; B.c_off[nk] = noff; B.c_n[nk] = t_n; B.c_goff[nk] = t_goff;
+        B.c_steps[nk] = t_steps; B.c_ncol[nk] = t_ncol; B.c_flags[nk] = t_flags;
+        B.c_ref[3 * nk] = t_ref0; B.c_ref[3 * nk + 1] = t_ref1; B.c_ref[3 * nk + 2] = t_ref2;
+        B.c_ed[nk] = t_ed; B.c_edd[nk] = t_edd; B.c_work[nk] = t_work; B.c_t0[nk] = t_t0;
+        B.c_thrf[nk] = t_thrf; B.c_thrc[nk] = t_thrc; B.c_E32[nk] = t_E;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < PER; j++) {
+        const int p = tid + j * BT;
+        if (mv_new[j] >= 0 && mv_new[j] != p) {
+            mirror_all(B, H, mv_new[j], mv_g[j], mv_k[j], true);
+            B.owner[mv_new[j]] = (short)mv_own[j];
+        } else if (mv_new[j] >= 0) {
+            B.cl[p] = (short)mv_k[j];
+            B.owner[p] = (short)mv_own[j];
+        }
+    }
+    if (tid == 0) {
+        B.ncl = nkeep;
+        B.used = tot;
+    }
+    __syncthreads();
+}
+
+// one CTA: the huge clusters one at a time, then bundles until the queue is empty
+__global__ void __launch_bounds__(BT, 2) k_hard_bundles(HardArgs A) {
+    extern __shared__ __align__(16) unsigned char bundle_smem[];
+    BundleSmem &B = *reinterpret_cast<BundleSmem *>(bundle_smem);
+    __shared__ double red_d[4];
+    __shared__ long long red_l[4];
+    __shared__ int q_sh;
+    const int tid = threadIdx.x;
+    {
+        Team<128> tm{tid, red_d, red_l};
+        for (int guard = 0; guard < (1 << 30); guard++) {
+            if (tid == 0) q_sh = atomicAdd(&A.queue[0], 1);
+            __syncthreads();
+            const int q = q_sh;
+            __syncthreads();
+            if (q >= A.n_tier[0]) break;
+            run_cluster<128>(A, A.order[q], tm);
+        }
+    }
+    if (tid == 0) {
+        B.used = 0;
+        B.ncl = 0;
+        B.n_pend = 0;
+        B.i_pend = 0;
+        B.exhausted = 0;
+    }
+    __syncthreads();
+    for (int guard = 0; guard < (1 << 30); guard++) {
+        if (tid == 0) {
+            B.fresh_k = B.ncl;
+            B.fresh_p = B.used;
+        }
+        __syncthreads();
+        bundle_refill(A, B);
+        if (B.ncl == 0) break;
+        if (B.fresh_k < B.ncl) {
+            bundle_load(A, B);
+            const int nt = bundle_list(B, MF_TGT);
+            bundle_pairs(A, B, 0, nt);
+            bundle_finalize(A, B, 0, nt, 2);
+        }
+        bundle_step(A, B);
+        if (B.any) bundle_retire(A, B);
+    }
+}
+
+#undef FOR_SLOTS
+#undef FOR_CLUSTERS
+
+}  // namespace p3t

@@ -93,16 +93,29 @@ __device__ __forceinline__ double dt4th(double eta, double alpha2, double acc0, 
     return (Jerk > 0.) ? eta * sqrt((Acc * Snap + Jerk2) / (Jerk * Crac + Snap2)) : 1.7976931348623157e308;
 }
 
+// fmod(t, d) for the time-step quantisation.  d is a power of two there
+// (dt_tree, dt_min and every halving of them); then t - floor(t/d)*d is
+// computed exactly (scaling by a power of two, floor and the product are
+// exact, and the difference is representable), which is the exact value
+// IEEE fmod returns for t >= 0.  Any other d takes the library fmod.
+__device__ __forceinline__ double rem_pow2(double t, double d) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    const bool pow2 = d > 0. && (b & 0x000fffffffffffffULL) == 0ULL && ((b >> 52) & 0x7ff) != 0 &&
+                      ((b >> 52) & 0x7ff) != 0x7ff;
+    if (!pow2 || !(t >= 0.) || t >= 1e300) return fmod(t, d);
+    return t - floor(t / d) * d;
+}
+
 // FPGrav::calcDeltatInitial, src/particle.h:886-914.  The fmod loops are
 // bounded (time and dt are commensurate powers of two within 64 halvings).
 __device__ __forceinline__ double dt_initial(const Params &P, double time, double dt_old, double acc0, V3 acc_d,
                                              V3 jerk_d, V3 acc_s, V3 jerk_s) {
     double dt_next = 0.5 * P.dt_tree;
     const double dt_1 = dmin(dt2nd(P.eta_0, P.alpha2, acc0, acc_d, jerk_d), dt2nd(P.eta_sun0, P.alpha2, 0., acc_s, jerk_s));
-    double rem = fmod(time, dt_next);
+    double rem = rem_pow2(time, dt_next);
     for (int k = 0; rem != 0.0 && k < 1100; k++) {
         dt_next *= 0.5;
-        rem = fmod(time, dt_next);
+        rem = rem_pow2(time, dt_next);
     }
     if (dt_old > 0.)
         for (int k = 0; 2. * dt_old < dt_next && k < 1100; k++) dt_next *= 0.5;

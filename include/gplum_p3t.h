@@ -149,6 +149,12 @@ int p3t_hard(int istep, int col_cap, long long *col_pairs, double *edisp);
  * 8 and 64; GPLUM's own cutoff between its parallel and serial cluster
  * loops is 64, src/hard.h:562).  No counterpart in GPLUM's interface. */
 int p3t_set_hard_tiers(int warp_min, int cta_min);
+/* Execution form of the hard launch: 0 (default) bundles -- each CTA holds
+ * the members of many clusters in shared memory and advances them together,
+ * so FP64 work is spread over all lanes; clusters above the bundle capacity
+ * (256 members) run one per CTA.  1: the size tiers of p3t_set_hard_tiers.
+ * Both give identical results.  No counterpart in GPLUM's interface. */
+int p3t_set_hard_mode(int mode);
 /* Optional priority of each cluster of the current lists (n = cluster
  * count, higher first within its tier) for the next p3t_hard; without it
  * clusters go largest first.  Ordering never changes results. */
@@ -156,6 +162,9 @@ int p3t_set_cluster_priority(const float *prio, int n);
 /* Per-cluster cost of the last p3t_hard: {block steps, active-body x member
  * pair sweeps} for each cluster, in cluster-list order. */
 int p3t_hard_costs(long long *out, int n);
+/* Per-cluster timeline of the last p3t_hard: {start, end} of each cluster's
+ * integration on the device's global timer (ns), in cluster-list order. */
+int p3t_hard_times(long long *out, int n);
 /* velKick, src/gravity_soft.h:5-12. */
 int p3t_kick(void);
 /* Energy::calcEnergy, src/energy.h:29-63: {etot, ekin, ephi_sun, ephi, ephi_d}. */
