@@ -57,6 +57,14 @@ SIGNATURES = {
     "p3t_hard_costs": (I, [VP, I]),
     "p3t_hard_times": (I, [VP, I]),
     "p3t_set_hard_mode": (I, [I]),
+    "p3t_mlp_set": (I, [VP, VP]),
+    "p3t_mlp_get": (I, [VP, VP]),
+    "p3t_mlp_reset": (I, []),
+    "p3t_mlp_predict": (I, [VP, I, VP]),
+    "p3t_mlp_loss_grad": (I, [VP, VP, I, VP, VP]),
+    "p3t_mlp_train": (I, [VP, VP, I, I, I, ctypes.c_float, ctypes.c_ulonglong, VP]),
+    "p3t_cluster_features": (I, [VP, I]),
+    "p3t_set_schedule": (I, [I]),
     "p3t_kick": (I, []),
     "p3t_energy": (I, [VP]),
     "p3t_merge": (I, [VP]),

@@ -124,6 +124,13 @@ struct Uploader {
     }
 };
 
+int d2h(Context *c, void *dst, const void *src, size_t bytes) {
+    if (bytes == 0) return 0;
+    int r = cuda_status(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream));
+    if (r) return r;
+    return cuda_status(cudaStreamSynchronize(c->stream));
+}
+
 int h2d(Context *c, void *dst, const void *src, size_t bytes) {
     Uploader u(c);
     u.add(dst, src, bytes);

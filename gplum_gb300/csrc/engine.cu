@@ -900,7 +900,7 @@ int p3t_set_r_planet(void) {
     // FPGrav::setRPlanet, src/particle.h:757-759 (host: one pow per body)
     const int n = g_eng.S.n;
     std::vector<double> m(n), rp(n);
-    int r = cuda_status(cudaMemcpy(m.data(), g_eng.S.mass, n * sizeof(double), cudaMemcpyDeviceToHost));
+    int r = d2h(g_eng.c, m.data(), g_eng.S.mass, n * sizeof(double));
     if (r) return r;
     for (int i = 0; i < n; i++) rp[i] = std::pow(0.75 * m[i] / (3.14159265358979323846 * c->params[20]), 1. / 3.);
     return h2d(c, g_eng.S.r_planet, rp.data(), n * sizeof(double));
@@ -927,7 +927,7 @@ int p3t_neighbor_counts(int *ngb_tot, int *with_ngb) {
     Context *c = ctx_get(0);
     if (!c || !g_eng.counters.p) return -(int)cudaErrorNoDevice;
     int h[2];
-    int r = cuda_status(cudaMemcpy(h, g_eng.counters.p, 2 * sizeof(int), cudaMemcpyDeviceToHost));
+    int r = d2h(g_eng.c, h, g_eng.counters.p, 2 * sizeof(int));
     *ngb_tot = h[0];
     *with_ngb = h[1];
     return r;
@@ -938,9 +938,9 @@ int p3t_neighbor_list(int i, int *out, int cap) {
     if (!c) return -(int)cudaErrorNoDevice;
     if (i < 0 || i >= g_eng.S.n) return -1;
     int m = 0;
-    cudaMemcpy(&m, g_eng.S.nbr_n + i, sizeof(int), cudaMemcpyDeviceToHost);
+    d2h(g_eng.c, &m, g_eng.S.nbr_n + i, sizeof(int));
     m = std::min(m, cap);
-    if (m > 0) cudaMemcpy(out, g_eng.S.nbr + (size_t)i * c->cand_cap, m * sizeof(int), cudaMemcpyDeviceToHost);
+    if (m > 0) d2h(g_eng.c, out, g_eng.S.nbr + (size_t)i * c->cand_cap, m * sizeof(int));
     return m;
 }
 
@@ -957,11 +957,11 @@ int p3t_cluster_lists(int *n_clusters, int *off, int *members) {
     if (!c) return -(int)cudaErrorNoDevice;
     *n_clusters = g_eng.n_clusters;
     if (off) {
-        cudaMemcpy(off, g_eng.cl_off.p, g_eng.n_clusters * sizeof(int), cudaMemcpyDeviceToHost);
+        d2h(g_eng.c, off, g_eng.cl_off.p, g_eng.n_clusters * sizeof(int));
         off[g_eng.n_clusters] = g_eng.n_members;
     }
     if (members && g_eng.n_members)
-        cudaMemcpy(members, g_eng.members.p, g_eng.n_members * sizeof(int), cudaMemcpyDeviceToHost);
+        d2h(g_eng.c, members, g_eng.members.p, g_eng.n_members * sizeof(int));
     return cuda_status(cudaGetLastError());
 }
 

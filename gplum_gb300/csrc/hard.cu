@@ -50,7 +50,7 @@ __device__ __forceinline__ float d2_32(const float *a, int s, const float *b, in
 struct ColRec {
     int64_t id_imp, id_tar;
     double time, edisp, edisp_d;
-    int32_t cluster, seq;
+    int32_t cluster, seq, n;  // cluster index, collision number within it, cluster size
 };
 
 struct HardArgs {
@@ -59,7 +59,7 @@ struct HardArgs {
     Hard H;
     const int32_t *off, *cnt, *members, *order;
     int n_clusters;
-    int n_tier[3];       // clusters per tier (CTA, warp, thread), in `order`
+    const int *n_tier;   // [3] clusters per tier, in `order` (device)
     int32_t *queue;      // [3] tier queue heads
     long long *cost;     // optional [2 * n_clusters]: block steps, pair sweeps
     long long *times;    // optional [2 * n_clusters]: start, end (global timer, ns)
@@ -525,6 +525,7 @@ __device__ void run_cluster(const HardArgs &A, int c, const Team<TEAM> &tm) {
                 edd += e2;
                 rec.cluster = c;
                 rec.seq = n_col;
+                rec.n = n;
                 const int slot = atomicAdd(A.n_cols, 1);
                 if (slot < A.col_cap) A.cols[slot] = rec;
                 else atomicOr(A.status, ST_QUEUE_OVERFLOW);
@@ -796,15 +797,78 @@ __global__ void k_isolated(IsoArgs A) {
     S.n_cluster[i] = 1;
 }
 
-__global__ void k_edisp_total(const double *cl_ed, const int32_t *cnt, int nc, double *out) {
-    if (threadIdx.x || blockIdx.x) return;
-    // clusters of 64 or more members first, then the rest (src/hard.h:562-583,700-765)
-    double e = 0., ed = 0.;
-    for (int pass = 0; pass < 2; pass++)
-        for (int c = 0; c < nc; c++)
-            if ((cnt[c] >= 64) == (pass == 0)) { e += cl_ed[2 * c]; ed += cl_ed[2 * c + 1]; }
-    out[0] = e;
-    out[1] = ed;
+
+// ---- work-queue order ------------------------------------------------------------
+// A counting sort of the clusters by (tier, priority bucket): bins ascend with
+// the tier and descend with the priority.  The order within a bin is
+// arbitrary; no result depends on the order, only the makespan does.
+constexpr int ORDER_NB = 4096;
+
+__global__ void k_order_bins(const int32_t *cnt, const float *prio, int nc, int mode, int warp_min, int cta_min,
+                             float pmin, float pscale, int32_t *bin, int32_t *hist) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nc) return;
+    const int n = cnt[k];
+    const int tier = (mode == 0) ? (n > BCAP ? 0 : 1) : (n >= cta_min ? 0 : (n >= warp_min ? 1 : 2));
+    int key = n < ORDER_NB - 1 ? n : ORDER_NB - 1;
+    if (prio) {
+        const float v = (prio[k] - pmin) * pscale;
+        key = (v >= 0.f) ? (v < (float)(ORDER_NB - 1) ? (int)v : ORDER_NB - 1) : 0;  // NaN -> 0
+    }
+    const int b = tier * ORDER_NB + (ORDER_NB - 1 - key);
+    bin[k] = b;
+    atomicAdd(&hist[b], 1);
+}
+
+// exclusive offsets of the 3 x ORDER_NB bins (one block of 1024) and the
+// clusters per tier
+__global__ void k_order_scan(int32_t *hist, int32_t *n_tier) {
+    constexpr int NBIN = 3 * ORDER_NB, PER = NBIN / 1024;
+    __shared__ int ws[32];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    int loc[PER], sum = 0;
+#pragma unroll
+    for (int j = 0; j < PER; j++) {
+        loc[j] = hist[tid * PER + j];
+        sum += loc[j];
+    }
+    int x = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        int v = ws[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v += y;
+        }
+        ws[lane] = v;  // inclusive
+    }
+    __syncthreads();
+    int off = x - sum + (w > 0 ? ws[w - 1] : 0);
+    const int total = ws[31];
+#pragma unroll
+    for (int j = 0; j < PER; j++) {
+        hist[tid * PER + j] = off;
+        off += loc[j];
+    }
+    __syncthreads();
+    if (tid == 0) {
+        n_tier[0] = hist[ORDER_NB];
+        n_tier[1] = hist[2 * ORDER_NB] - hist[ORDER_NB];
+        n_tier[2] = total - hist[2 * ORDER_NB];
+    }
+}
+
+__global__ void k_order_scatter(const int32_t *bin, int nc, int32_t *offs, int32_t *order) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nc) return;
+    order[atomicAdd(&offs[bin[k]], 1)] = k;
 }
 
 // ---- host side ------------------------------------------------------------------
@@ -812,10 +876,11 @@ struct HardBufs {
     DevBuf<double> d;
     DevBuf<int64_t> id;
     DevBuf<int32_t> i32, order, queue, n_cols;
-    DevBuf<double> cl_edisp, etot;
+    DevBuf<double> cl_edisp;
     DevBuf<ColRec> cols;
     DevBuf<long long> cost, times;
-    DevBuf<float> f32;
+    DevBuf<float> f32, prio;
+    DevBuf<int32_t> bin, hist, ntier;
     Hard H;
     int cap = 0;
     int reserve(int m) {
@@ -884,14 +949,14 @@ int p3t_hard_costs(long long *out, int n) {
     Context *c = ctx_get(0);
     if (!c) return -(int)cudaErrorNoDevice;
     if (n != g_eng.n_clusters || !g_hb.cost.p) return ST_BAD_INDEX;
-    return cuda_status(cudaMemcpy(out, g_hb.cost.p, 2 * (size_t)n * sizeof(long long), cudaMemcpyDeviceToHost));
+    return d2h(c, out, g_hb.cost.p, 2 * (size_t)n * sizeof(long long));
 }
 
 int p3t_hard_times(long long *out, int n) {
     Context *c = ctx_get(0);
     if (!c) return -(int)cudaErrorNoDevice;
     if (n != g_eng.n_clusters || !g_hb.times.p) return ST_BAD_INDEX;
-    return cuda_status(cudaMemcpy(out, g_hb.times.p, 2 * (size_t)n * sizeof(long long), cudaMemcpyDeviceToHost));
+    return d2h(c, out, g_hb.times.p, 2 * (size_t)n * sizeof(long long));
 }
 
 int p3t_hard(int istep, int col_cap, long long *col_pairs, double *edisp) {
@@ -902,32 +967,32 @@ int p3t_hard(int istep, int col_cap, long long *col_pairs, double *edisp) {
     const int nc = E.n_clusters;
     int r = 0;
     if ((r = B.reserve(E.n_members)) || (r = B.order.reserve(nc)) || (r = B.queue.reserve(3)) ||
-        (r = B.n_cols.reserve(1)) || (r = B.cl_edisp.reserve(2 * (size_t)nc + 2)) || (r = B.etot.reserve(2)) ||
+        (r = B.n_cols.reserve(1)) || (r = B.cl_edisp.reserve(2 * (size_t)nc + 2)) ||
         (r = B.cols.reserve(4096)))
         return r;
-    // schedule: three tiers by size (CTA >= g_cta_min > warp >= g_warp_min >
-    // thread), each ordered by the caller's priority when given, else by size,
-    // largest first
-    std::vector<int32_t> cnt(nc), ord;
-    int ntier[3] = {0, 0, 0};
+    // schedule, on the device: clusters binned by tier (bundle mode: above
+    // the bundle capacity first; tier mode: CTA >= g_cta_min > warp >=
+    // g_warp_min > thread), then by priority (the caller's, the learned cost
+    // model's, else the size), highest first
+    if ((r = B.bin.reserve(nc + 1)) || (r = B.hist.reserve(3 * ORDER_NB)) || (r = B.ntier.reserve(3))) return r;
+    cudaMemsetAsync(B.hist.p, 0, 3 * ORDER_NB * sizeof(int32_t), c->stream);
     if (nc > 0) {
-        if ((r = cuda_status(cudaMemcpy(cnt.data(), E.cl_cnt.p, nc * sizeof(int32_t), cudaMemcpyDeviceToHost))))
-            return r;
-        const bool use_prio = (int)g_prio.size() == nc;
-        auto tier = [&](int k) {
-            if (g_hard_mode == 0) return cnt[k] > BCAP ? 0 : 1;
-            return cnt[k] >= g_cta_min ? 0 : (cnt[k] >= g_warp_min ? 1 : 2);
-        };
-        ord.resize(nc);
-        for (int k = 0; k < nc; k++) ord[k] = k;
-        std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
-            const int ta = tier(a), tb = tier(b);
-            if (ta != tb) return ta < tb;
-            if (use_prio) return g_prio[a] > g_prio[b];
-            return cnt[a] > cnt[b];
-        });
-        for (int k = 0; k < nc; k++) ntier[tier(k)]++;
-        if ((r = h2d(c, B.order.p, ord.data(), nc * sizeof(int32_t)))) return r;
+        const float *prio = nullptr;
+        float pmin = 0.f, pscale = 1.f;
+        if ((int)g_prio.size() == nc) {
+            if ((r = B.prio.reserve(nc)) || (r = h2d(c, B.prio.p, g_prio.data(), nc * sizeof(float)))) return r;
+            const auto mm = std::minmax_element(g_prio.begin(), g_prio.end());
+            pmin = *mm.first;
+            pscale = (*mm.second > *mm.first) ? (ORDER_NB - 1) / (*mm.second - *mm.first) : 0.f;
+            prio = B.prio.p;
+        } else {
+            prio = sched_priority(c, nc, &pmin, &pscale);
+        }
+        k_order_bins<<<(nc + 255) / 256, 256, 0, c->stream>>>(E.cl_cnt.p, prio, nc, g_hard_mode, g_warp_min, g_cta_min,
+                                                              pmin, pscale, B.bin.p, B.hist.p);
+        k_order_scan<<<1, 1024, 0, c->stream>>>(B.hist.p, B.ntier.p);
+        k_order_scatter<<<(nc + 255) / 256, 256, 0, c->stream>>>(B.bin.p, nc, B.hist.p, B.order.p);
+        if ((r = cuda_status(cudaGetLastError()))) return r;
     }
     g_prio.clear();
     if ((r = B.cost.reserve(2 * (size_t)nc + 2)) || (r = B.times.reserve(2 * (size_t)nc + 2))) return r;
@@ -945,7 +1010,7 @@ int p3t_hard(int istep, int col_cap, long long *col_pairs, double *edisp) {
         A.members = E.members.p;
         A.order = B.order.p;
         A.n_clusters = nc;
-        for (int t = 0; t < 3; t++) A.n_tier[t] = ntier[t];
+        A.n_tier = B.ntier.p;
         A.queue = B.queue.p;
         A.cost = B.cost.p;
         A.times = B.times.p;
@@ -966,12 +1031,11 @@ int p3t_hard(int istep, int col_cap, long long *col_pairs, double *edisp) {
                     return r;
                 attr = true;
             }
-            const int want = ntier[0] + (ntier[1] + 7) / 8;
-            const int blocks = std::max(1, std::min(want, sms * 2));  // persistent: 2 CTAs per SM
+            // persistent: 2 CTAs per SM (fewer when there are few clusters)
+            const int blocks = std::max(1, std::min(sms * 2, (nc + 3) / 4));
             k_hard_bundles<<<blocks, BT, smem, c->stream>>>(A);
         } else {
-            const int want = ntier[0] + (ntier[1] + 3) / 4 + (ntier[2] + 127) / 128;
-            const int blocks = std::max(1, std::min(want, sms * 2));  // persistent: 2 CTAs per SM
+            const int blocks = std::max(1, std::min(sms * 2, (nc + 3) / 4));
             k_hard_clusters<<<blocks, 128, 0, c->stream>>>(A);
         }
         if ((r = cuda_status(cudaGetLastError()))) return r;
@@ -984,19 +1048,16 @@ int p3t_hard(int istep, int col_cap, long long *col_pairs, double *edisp) {
     I.status = c->status;
     if (E.S.n > 0) k_isolated<<<(E.S.n + 127) / 128, 128, 0, c->stream>>>(I);
     if ((r = cuda_status(cudaGetLastError()))) return r;
-    k_edisp_total<<<1, 32, 0, c->stream>>>(B.cl_edisp.p, E.cl_cnt.p, nc, B.etot.p);
     int ncol = 0;
-    cudaMemcpyAsync(&ncol, B.n_cols.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
-    cudaMemcpyAsync(g_edisp, B.etot.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
-    if ((r = cuda_status(cudaStreamSynchronize(c->stream)))) return r;
+    if ((r = d2h(c, &ncol, B.n_cols.p, sizeof(int)))) return r;
     ncol = std::min(ncol, 4096);
     g_cols.resize(ncol);
-    if (ncol && (r = cuda_status(cudaMemcpy(g_cols.data(), B.cols.p, ncol * sizeof(ColRec), cudaMemcpyDeviceToHost))))
+    if (ncol && (r = d2h(c, g_cols.data(), B.cols.p, ncol * sizeof(ColRec))))
         return r;
     // collision-list order of the reference: clusters of 64+ members first,
     // each group in cluster order, collisions in time order within a cluster
     std::stable_sort(g_cols.begin(), g_cols.end(), [&](const ColRec &a, const ColRec &b) {
-        const bool la = cnt[a.cluster] >= 64, lb = cnt[b.cluster] >= 64;
+        const bool la = a.n >= 64, lb = b.n >= 64;
         if (la != lb) return la;
         if (a.cluster != b.cluster) return a.cluster < b.cluster;
         return a.seq < b.seq;
@@ -1004,6 +1065,22 @@ int p3t_hard(int istep, int col_cap, long long *col_pairs, double *edisp) {
     for (int k = 0; k < ncol && k < col_cap; k++) {
         col_pairs[2 * k] = g_cols[k].id_imp;
         col_pairs[2 * k + 1] = g_cols[k].id_tar;
+    }
+    // dissipated energy in the reference's order (src/hard.h:562-583,700-765):
+    // per cluster the sum of its collisions in time order, then over clusters
+    // of 64+ members in cluster order, then the rest in cluster order.  Clusters
+    // without a collision add exact zeros, so only the listed ones are summed.
+    g_edisp[0] = g_edisp[1] = 0.;
+    for (int k = 0; k < ncol;) {
+        double e = 0., ed = 0.;
+        int j = k;
+        for (; j < ncol && g_cols[j].cluster == g_cols[k].cluster; j++) {
+            e += g_cols[j].edisp;
+            ed += g_cols[j].edisp_d;
+        }
+        g_edisp[0] += e;
+        g_edisp[1] += ed;
+        k = j;
     }
     edisp[0] = g_edisp[0];
     edisp[1] = g_edisp[1];

@@ -639,6 +639,7 @@ __device__ void bundle_step(const HardArgs &A, BundleSmem &B) {
         B.c_edd[k] += e2;
         rec.cluster = B.c_idx[k];
         rec.seq = B.c_ncol[k]++;
+        rec.n = B.c_n[k];
         const int slot = atomicAdd(A.n_cols, 1);
         if (slot < A.col_cap) A.cols[slot] = rec;
         else atomicOr(A.status, ST_QUEUE_OVERFLOW);

@@ -106,6 +106,9 @@ int read_status(Context *c);
 // Async host->device copy; pinned sources go straight to the DMA engine,
 // pageable ones through the context's pinned staging buffer.
 int h2d(Context *c, void *dst, const void *src, size_t bytes);
+// Device -> host copy ordered after the work queued on the library's
+// stream (a non-blocking stream, which plain cudaMemcpy does not wait for).
+int d2h(Context *c, void *dst, const void *src, size_t bytes);
 
 struct SoftArgs;
 SoftArgs make_args(Context *c, DevSet &d, int n_group, int n_ptcl, int n_spj, bool accumulate);

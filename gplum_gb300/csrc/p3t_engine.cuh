@@ -35,4 +35,9 @@ struct Engine {
 
 extern Engine g_eng;
 
+// Device priorities (higher first) of the current clusters from the learned
+// cost model, with the scale that maps them to the order's bins, or nullptr
+// when the size order applies (sched.cu).
+const float *sched_priority(Context *c, int nc, float *pmin, float *pscale);
+
 }  // namespace p3t

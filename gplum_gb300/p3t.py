@@ -120,6 +120,27 @@ class GpuSystem:
             raise RuntimeError(f"p3t_hard failed with status {nc}")
         return cols[:2 * min(nc, col_cap)].reshape(-1, 2), ed
 
+    def hard_costs(self):
+        """(block steps, pair sweeps) of each cluster of the last hard launch."""
+        nc = len(self.cluster_lists()[0]) - 1
+        out = np.zeros(2 * max(nc, 1), np.int64)
+        self._chk(self.lib.p3t_hard_costs(out.ctypes.data_as(VP), nc), "p3t_hard_costs")
+        return out[:2 * nc].reshape(-1, 2)
+
+    def hard_times(self):
+        """(start, end) of each cluster's integration, device global timer (ns)."""
+        nc = len(self.cluster_lists()[0]) - 1
+        out = np.zeros(2 * max(nc, 1), np.int64)
+        self._chk(self.lib.p3t_hard_times(out.ctypes.data_as(VP), nc), "p3t_hard_times")
+        return out[:2 * nc].reshape(-1, 2)
+
+    def cluster_features(self):
+        """The learned scheduler's four features of each current cluster."""
+        nc = len(self.cluster_lists()[0]) - 1
+        out = np.zeros((max(nc, 1), 4), np.float32)
+        self._chk(self.lib.p3t_cluster_features(out.ctypes.data_as(VP), nc), "p3t_cluster_features")
+        return out[:nc]
+
     def energy(self):
         out = np.zeros(5)
         self._chk(self.lib.p3t_energy(out.ctypes.data_as(VP)), "p3t_energy")

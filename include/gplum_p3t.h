@@ -155,6 +155,37 @@ int p3t_set_hard_tiers(int warp_min, int cta_min);
  * (256 members) run one per CTA.  1: the size tiers of p3t_set_hard_tiers.
  * Both give identical results.  No counterpart in GPLUM's interface. */
 int p3t_set_hard_mode(int mode);
+
+/* ---- learned work-queue order (no counterpart in GPLUM) ------------------
+ * A 4-32-32-1 FP32 MLP (tanh) predicts log2(1 + block steps) of each cluster
+ * from four features: log2 n, log2 min |dr|/r_out over neighbour pairs,
+ * log2(1e-6 + max |dv| dt_tree / r_out), log2(dt_tree / min member dt).
+ * Parameters: W1[32][4], b1[32], W2[32][32], b2[32], w3[32], b3 (1249
+ * floats); norm: feature mean[4], feature scale[4], target mean, target
+ * scale (inputs enter as (x - mean) * scale, the output leaves as
+ * out / scale + mean).  The order never changes any result. */
+#define P3T_MLP_PARAMS 1249
+#define P3T_MLP_NORM 10
+/* Install / read the model (host arrays). */
+int p3t_mlp_set(const float *params, const float *norm);
+int p3t_mlp_get(float *params, float *norm);
+/* Forget the model (the next p3t_mlp_train starts from fresh weights). */
+int p3t_mlp_reset(void);
+/* Predictions for n raw feature rows (host arrays [n][4] -> [n]). */
+int p3t_mlp_predict(const float *x, int n, float *out);
+/* Loss 0.5 mean((f(x) - y)^2) of the standardised target and its gradient
+ * with respect to the parameters (host arrays), under the installed model. */
+int p3t_mlp_loss_grad(const float *x, const float *y, int n, float *loss, float *grad);
+/* Minibatch Adam on the device; without an installed model the weights
+ * start from a seeded uniform draw and the standardisation is fitted to the
+ * data.  loss_per_epoch[epochs] may be NULL. */
+int p3t_mlp_train(const float *x, const float *y, int n, int epochs, int batch, float lr, unsigned long long seed,
+                  float *loss_per_epoch);
+/* Features of the current clusters (after p3t_cluster_label), [n][4]. */
+int p3t_cluster_features(float *out, int n);
+/* 0: size order (default); 1: the installed model's order (size order
+ * while no model is installed). */
+int p3t_set_schedule(int mode);
 /* Optional priority of each cluster of the current lists (n = cluster
  * count, higher first within its tier) for the next p3t_hard; without it
  * clusters go largest first.  Ordering never changes results. */
