@@ -65,6 +65,10 @@ SIGNATURES = {
     "p3t_mlp_train": (I, [VP, VP, I, I, I, ctypes.c_float, ctypes.c_ulonglong, VP]),
     "p3t_cluster_features": (I, [VP, I]),
     "p3t_set_schedule": (I, [I]),
+    "p3t_state_tree": (I, [D, I, I]),
+    "p3t_state_tree_soft": (I, [D, I, I]),
+    "p3t_tree_lists_counts": (I, [VP]),
+    "p3t_tree_lists_get": (I, [VP] * 7),
     "p3t_kick": (I, []),
     "p3t_energy": (I, [VP]),
     "p3t_merge": (I, [VP]),

@@ -20,7 +20,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libgplum_p3t.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # FP64 physics kept free of FMA contraction, so it rounds as GPLUM's host build
-NO_FMAD = {"engine.cu", "hard.cu"}
+NO_FMAD = {"engine.cu", "hard.cu", "dtree.cu"}
 
 
 def _nvcc():

@@ -1,0 +1,626 @@
+// Device octree and interaction lists for the soft force.
+//
+// The caller side of the soft-force path, on the device: the contract of the
+// host builder (csrc/tree.cpp, include/p3t_tree.h; in GPLUM, FDPS's
+// TreeForForce with LONG_SYMMETRY search and quadrupole moments, called at
+// src/main_p3t.cpp:344-355,581-587,672-676):
+//   * 63-bit Morton keys on the root cube (side = 1.0001 x the largest
+//     extent), bodies in key order (ties by index);
+//   * a node splits into one child per occupied octant while it holds more
+//     than min(n_leaf_limit, n_group_limit) bodies (21 levels at most);
+//   * i-groups are the highest nodes with at most n_group_limit bodies (or
+//     leaves), in Morton order;
+//   * a cell is opened when its search box (bodies +- 1.1 r_search) overlaps
+//     the group's body box, or the group's search box overlaps the cell's
+//     body box, or size^2 > theta^2 d^2 (d: cell centre of mass to the
+//     group's body box); opened leaves give EPJ entries, unopened cells SPJ
+//     entries (quadrupole about the centre of mass).
+// Steps: bounding box (two-stage reduction); keys; a stable LSD radix sort of
+// (key, index) in 8 passes of 8 bits; the tree one level at a time (a scan of
+// "a new 3-bit digit starts here" over the sorted keys gives the children,
+// contiguous, in level order); moments and boxes bottom-up (leaves sum their
+// bodies in key order, as the host builder; inner nodes combine children by
+// the parallel-axis rule); groups; and one thread per group walking the tree
+// twice (count, then fill) with the host builder's stack discipline, so the
+// lists equal the host builder's entry for entry (SPJ entries name the same
+// cells; node numbers are in level order here).  The lists go straight into
+// the resident soft-force buffers.  Compiled with -fmad=false so the box and
+// opening arithmetic rounds as the host builder's (-ffp-contract=off).
+#include <algorithm>
+#include <cstdint>
+#include <vector>
+
+#include "../../include/gplum_p3t.h"
+#include "p3t_capi_internal.cuh"
+#include "p3t_engine.cuh"
+
+namespace p3t {
+
+struct TNode {
+    double ilo[3], ihi[3], olo[3], ohi[3];  // body box, search box (bodies +- 1.1 r_search)
+    double com[3], size;
+    int first, count, child0, nchild;
+};
+
+constexpr int RADIX_TILE = 4096;  // keys per radix block (256 threads x 16)
+constexpr int WALK_STACK = 256;
+
+// ---- bounding box and keys ------------------------------------------------------
+__global__ void k_bbox_partial(const double *pos, int n, double *part) {
+    __shared__ double s[6][256];
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        for (int d = 0; d < 3; d++) {
+            lo[d] = fmin(lo[d], pos[3 * i + d]);
+            hi[d] = fmax(hi[d], pos[3 * i + d]);
+        }
+    for (int d = 0; d < 3; d++) {
+        s[d][threadIdx.x] = lo[d];
+        s[3 + d][threadIdx.x] = hi[d];
+    }
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o)
+            for (int d = 0; d < 3; d++) {
+                s[d][threadIdx.x] = fmin(s[d][threadIdx.x], s[d][threadIdx.x + o]);
+                s[3 + d][threadIdx.x] = fmax(s[3 + d][threadIdx.x], s[3 + d][threadIdx.x + o]);
+            }
+        __syncthreads();
+    }
+    if (threadIdx.x < 6) part[6 * blockIdx.x + threadIdx.x] = s[threadIdx.x][0];
+}
+
+// root cube as the host builder: out = {base.xyz, size, scale}
+__global__ void k_bbox_root(const double *part, int nblk, double *out) {
+    if (threadIdx.x || blockIdx.x) return;
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int b = 0; b < nblk; b++)
+        for (int d = 0; d < 3; d++) {
+            lo[d] = fmin(lo[d], part[6 * b + d]);
+            hi[d] = fmax(hi[d], part[6 * b + 3 + d]);
+        }
+    double size = 0.;
+    for (int d = 0; d < 3; d++) size = fmax(size, hi[d] - lo[d]);
+    size = size * 1.0001 + 1e-300;
+    for (int d = 0; d < 3; d++) {
+        const double cen = 0.5 * (lo[d] + hi[d]);
+        out[d] = cen - 0.5 * size;
+    }
+    out[3] = size;
+    out[4] = double(1 << 21) / size;
+}
+
+__device__ __forceinline__ unsigned long long spread21(unsigned long long v) {
+    v &= 0x1fffffULL;
+    v = (v | v << 32) & 0x1f00000000ffffULL;
+    v = (v | v << 16) & 0x1f0000ff0000ffULL;
+    v = (v | v << 8) & 0x100f00f00f00f00fULL;
+    v = (v | v << 4) & 0x10c30c30c30c30c3ULL;
+    v = (v | v << 2) & 0x1249249249249249ULL;
+    return v;
+}
+
+__global__ void k_keys(const double *pos, int n, const double *root, unsigned long long *key, int *idx) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    unsigned long long c[3];
+    for (int d = 0; d < 3; d++) {
+        const double u = (pos[3 * i + d] - root[d]) * root[4];
+        long long v = (long long)u;
+        v = v < 0 ? 0 : (v > (1 << 21) - 1 ? (1 << 21) - 1 : v);
+        c[d] = (unsigned long long)v;
+    }
+    key[i] = (spread21(c[0]) << 2) | (spread21(c[1]) << 1) | spread21(c[2]);
+    idx[i] = i;
+}
+
+// ---- stable LSD radix sort of (key, index) -----------------------------------------
+__global__ void __launch_bounds__(256) k_radix_hist(const unsigned long long *key, int n, int shift, int nblk,
+                                                    int *hist) {
+    __shared__ int h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const int base = blockIdx.x * RADIX_TILE;
+    for (int j = threadIdx.x; j < RADIX_TILE; j += 256) {
+        const int k = base + j;
+        if (k < n) atomicAdd(&h[(key[k] >> shift) & 255], 1);
+    }
+    __syncthreads();
+    hist[threadIdx.x * nblk + blockIdx.x] = h[threadIdx.x];  // digit-major
+}
+
+// scatter of one tile in 16 rounds of 256 keys; within a round, keys with the
+// same digit keep their order (warp match + per-warp counts)
+__global__ void __launch_bounds__(256) k_radix_scatter(const unsigned long long *key, const int *idx, int n,
+                                                       int shift, int nblk, const int *offs,
+                                                       unsigned long long *key_out, int *idx_out) {
+    __shared__ int cnt[8][256];
+    __shared__ int run[256];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    for (int j = 0; j < 8; j++) cnt[j][tid] = 0;
+    run[tid] = offs[tid * nblk + blockIdx.x];
+    __syncthreads();
+    const int base = blockIdx.x * RADIX_TILE;
+    for (int r = 0; r < RADIX_TILE / 256; r++) {
+        const int k = base + r * 256 + tid;
+        const bool valid = k < n;
+        unsigned long long kv = 0;
+        int iv = 0, d = 256;
+        if (valid) {
+            kv = key[k];
+            iv = idx[k];
+            d = (int)((kv >> shift) & 255);
+        }
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const int rank = __popc(peers & ((1u << lane) - 1u));
+        if (valid && rank == 0) cnt[w][d] = __popc(peers);
+        __syncthreads();
+        if (valid) {
+            int off = run[d] + rank;
+            for (int ww = 0; ww < w; ww++) off += cnt[ww][d];
+            key_out[off] = kv;
+            idx_out[off] = iv;
+        }
+        __syncthreads();
+        int add = 0;
+        for (int ww = 0; ww < 8; ww++) {
+            add += cnt[ww][tid];
+            cnt[ww][tid] = 0;
+        }
+        run[tid] += add;
+        __syncthreads();
+    }
+}
+
+// ---- tree, one level at a time -------------------------------------------------------
+__global__ void k_root_node(TNode *nd, int *parent, const double *root, int n, int limit, int *enode) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k == 0) {
+        nd[0].first = 0;
+        nd[0].count = n;
+        nd[0].child0 = -1;
+        nd[0].nchild = 0;
+        nd[0].size = root[3];
+        parent[0] = -1;
+    }
+    if (k < n) enode[k] = (n > limit) ? 0 : -1;
+}
+
+__global__ void k_lvl_heads(const unsigned long long *key, const int *enode, const TNode *nd, int n, int shift,
+                            int *head) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int p = enode[k];
+    int h = 0;
+    if (p >= 0) h = (k == nd[p].first) || (((key[k] >> shift) & 7ULL) != ((key[k - 1] >> shift) & 7ULL));
+    head[k] = h;
+}
+
+__global__ void k_lvl_make(const int *enode, const int *head, const int *hs, int n, int base, TNode *nd,
+                           int *parent, int *enode_next) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int p = enode[k];
+    if (p < 0) {
+        enode_next[k] = -1;
+        return;
+    }
+    const int c = base + hs[k] + head[k] - 1;
+    enode_next[k] = c;
+    if (head[k]) {
+        nd[c].first = k;
+        nd[c].size = nd[p].size * 0.5;
+        nd[c].child0 = -1;
+        nd[c].nchild = 0;
+        parent[c] = p;
+        if (k == nd[p].first) nd[p].child0 = c;
+    }
+}
+
+__global__ void k_lvl_count(int base, int m, TNode *nd, const int *parent) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= m) return;
+    const int c = base + t, p = parent[c];
+    const int end = (t + 1 < m && parent[c + 1] == p) ? nd[c + 1].first : nd[p].first + nd[p].count;
+    nd[c].count = end - nd[c].first;
+    if (nd[p].child0 == c) {
+        int j = 1;
+        while (t + j < m && parent[c + j] == p && j < 8) j++;
+        nd[p].nchild = j;
+    }
+}
+
+__global__ void k_lvl_split(int n, int level, int limit, const TNode *nd, int *enode) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int c = enode[k];
+    if (c >= 0 && !(nd[c].count > limit && level < 21)) enode[k] = -1;
+}
+
+// ---- moments and boxes, bottom-up -------------------------------------------------------
+__global__ void k_moments(int lo, int hi, TNode *nd, SPJRec *spj, const int *order, const double *pos,
+                          const double *mass, const double *rs) {
+    const int c = lo + blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= hi) return;
+    TNode &N = nd[c];
+    double m = 0., cx = 0., cy = 0., cz = 0., q[6] = {0., 0., 0., 0., 0., 0.};
+    double ilo[3] = {1e300, 1e300, 1e300}, ihi[3] = {-1e300, -1e300, -1e300};
+    double olo[3] = {1e300, 1e300, 1e300}, ohi[3] = {-1e300, -1e300, -1e300};
+    if (N.nchild == 0) {
+        // the host builder's sums, in key order
+        for (int k = N.first; k < N.first + N.count; k++) {
+            const int p = order[k];
+            const double x = pos[3 * p], y = pos[3 * p + 1], z = pos[3 * p + 2], mp = mass[p];
+            m += mp;
+            cx += mp * x;
+            cy += mp * y;
+            cz += mp * z;
+            const double r = 1.1 * rs[p];
+            const double v[3] = {x, y, z};
+            for (int d = 0; d < 3; d++) {
+                ilo[d] = fmin(ilo[d], v[d] - 0.);
+                ihi[d] = fmax(ihi[d], v[d] + 0.);
+                olo[d] = fmin(olo[d], v[d] - r);
+                ohi[d] = fmax(ohi[d], v[d] + r);
+            }
+        }
+        if (m != 0.) {
+            cx /= m;
+            cy /= m;
+            cz /= m;
+        }
+        for (int k = N.first; k < N.first + N.count; k++) {
+            const int p = order[k];
+            const double dx = pos[3 * p] - cx, dy = pos[3 * p + 1] - cy, dz = pos[3 * p + 2] - cz, mp = mass[p];
+            q[0] += mp * dx * dx; q[1] += mp * dy * dy; q[2] += mp * dz * dz;
+            q[3] += mp * dx * dy; q[4] += mp * dx * dz; q[5] += mp * dy * dz;
+        }
+    } else {
+        for (int j = 0; j < N.nchild; j++) {
+            const int ch = N.child0 + j;
+            const double mc = spj[ch].mass;
+            m += mc;
+            cx += mc * spj[ch].pos[0];
+            cy += mc * spj[ch].pos[1];
+            cz += mc * spj[ch].pos[2];
+            for (int d = 0; d < 3; d++) {
+                ilo[d] = fmin(ilo[d], nd[ch].ilo[d]);
+                ihi[d] = fmax(ihi[d], nd[ch].ihi[d]);
+                olo[d] = fmin(olo[d], nd[ch].olo[d]);
+                ohi[d] = fmax(ohi[d], nd[ch].ohi[d]);
+            }
+        }
+        if (m != 0.) {
+            cx /= m;
+            cy /= m;
+            cz /= m;
+        }
+        for (int j = 0; j < N.nchild; j++) {
+            const SPJRec &S = spj[N.child0 + j];
+            const double dx = S.pos[0] - cx, dy = S.pos[1] - cy, dz = S.pos[2] - cz, mc = S.mass;
+            q[0] += S.xx + mc * dx * dx; q[1] += S.yy + mc * dy * dy; q[2] += S.zz + mc * dz * dz;
+            q[3] += S.xy + mc * dx * dy; q[4] += S.xz + mc * dx * dz; q[5] += S.yz + mc * dy * dz;
+        }
+    }
+    for (int d = 0; d < 3; d++) {
+        N.ilo[d] = ilo[d];
+        N.ihi[d] = ihi[d];
+        N.olo[d] = olo[d];
+        N.ohi[d] = ohi[d];
+    }
+    N.com[0] = cx;
+    N.com[1] = cy;
+    N.com[2] = cz;
+    SPJRec &S = spj[c];
+    S.mass = m;
+    S.pos[0] = cx;
+    S.pos[1] = cy;
+    S.pos[2] = cz;
+    S.xx = q[0]; S.yy = q[1]; S.zz = q[2]; S.xy = q[3]; S.xz = q[4]; S.yz = q[5];
+}
+
+// ---- groups ---------------------------------------------------------------------------------
+__global__ void k_group_mark(int nn, const TNode *nd, const int *parent, int ngl, int *gmark) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nn) return;
+    const TNode &N = nd[c];
+    const bool cand = N.count <= ngl || N.nchild == 0;
+    const bool top = (c == 0) || nd[parent[c]].count > ngl;
+    if (cand && top) gmark[N.first] = c + 1;
+}
+
+__global__ void k_group_flag(const int *gmark, int n, int *flag) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) flag[k] = gmark[k] > 0;
+}
+
+__global__ void k_group_fill(const int *gmark, const int *gpos, int n, int ng, int *gnode, int *i_off) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n && gmark[k] > 0) {
+        gnode[gpos[k]] = gmark[k] - 1;
+        i_off[gpos[k]] = k;
+    }
+    if (k == 0) i_off[ng] = n;
+}
+
+// ---- walk --------------------------------------------------------------------------------------
+__device__ __forceinline__ bool box_overlap(const double *alo, const double *ahi, const double *blo,
+                                            const double *bhi) {
+    for (int d = 0; d < 3; d++)
+        if (ahi[d] < blo[d] || bhi[d] < alo[d]) return false;
+    return true;
+}
+
+__device__ __forceinline__ double box_dist2(const double *lo, const double *hi, const double *x) {
+    double s = 0.;
+    for (int d = 0; d < 3; d++) {
+        double e = 0.;
+        if (x[d] < lo[d]) e = lo[d] - x[d];
+        else if (x[d] > hi[d]) e = x[d] - hi[d];
+        s += e * e;
+    }
+    return s;
+}
+
+// fill == 0: counts per group into jcnt/scnt; fill == 1: entries at j_off/s_off
+__global__ void k_walk(const TNode *nd, const int *gnode, int ng, double theta2, const int *order, int fill,
+                       int *jcnt, int *scnt, const int *j_off, const int *s_off, int *j_idx, int *s_idx,
+                       int *status) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= ng) return;
+    const TNode &G = nd[gnode[g]];
+    double gilo[3], gihi[3], golo[3], gohi[3];
+    for (int d = 0; d < 3; d++) {
+        gilo[d] = G.ilo[d];
+        gihi[d] = G.ihi[d];
+        golo[d] = G.olo[d];
+        gohi[d] = G.ohi[d];
+    }
+    int stack[WALK_STACK];
+    int sp = 0;
+    stack[sp++] = 0;
+    int nj = 0, ns = 0;
+    const int jo = fill ? j_off[g] : 0, so = fill ? s_off[g] : 0;
+    for (int guard = 0; sp > 0 && guard < (1 << 26); guard++) {
+        const int c = stack[--sp];
+        const TNode &C = nd[c];
+        const bool near = box_overlap(C.olo, C.ohi, gilo, gihi) || box_overlap(golo, gohi, C.ilo, C.ihi);
+        const bool open = near || (C.size * C.size > theta2 * box_dist2(gilo, gihi, C.com));
+        if (!open) {
+            if (fill) s_idx[so + ns] = c;
+            ns++;
+        } else if (C.nchild == 0) {
+            if (fill)
+                for (int k = 0; k < C.count; k++) j_idx[jo + nj + k] = order[C.first + k];
+            nj += C.count;
+        } else {
+            if (sp + C.nchild > WALK_STACK) {
+                atomicOr(status, ST_QUEUE_OVERFLOW);
+                break;
+            }
+            for (int ch = C.nchild - 1; ch >= 0; ch--) stack[sp++] = C.child0 + ch;
+        }
+    }
+    if (!fill) {
+        jcnt[g] = nj;
+        scnt[g] = ns;
+    }
+}
+
+// launch order of the soft kernel: largest groups first (key: weight desc, group asc)
+__global__ void k_group_weight(int ng, const int *i_off, const int *j_off, const int *s_off,
+                               unsigned long long *key, int *idx) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= ng) return;
+    const long long ni = i_off[g + 1] - i_off[g];
+    const long long nj = (j_off[g + 1] - j_off[g]) + 2LL * (s_off[g + 1] - s_off[g]);
+    const long long w = ((ni + 31) / 32) * 32 * nj;
+    const unsigned long long wc = (unsigned long long)(w < (1LL << 43) ? w : (1LL << 43) - 1);
+    key[g] = (((1ULL << 43) - 1 - wc) << 20) | (unsigned long long)g;
+    idx[g] = g;
+}
+
+// ---- host side ----------------------------------------------------------------------------------
+struct DTree {
+    DevBuf<double> part, root;
+    DevBuf<unsigned long long> key, key2;
+    DevBuf<int> idx, idx2, hist, hoff, head, hs, enode, enode2, parent, gmark, gflag, gpos, gnode, cnt;
+    DevBuf<TNode> nd;
+    size_t node_cap = 0;
+    std::vector<int> level_start;
+    int n_nodes = 0, n_groups = 0;
+};
+static DTree g_dt;
+
+// (key, idx) sorted in place by key, stably (8 passes of 8 bits over `bits`)
+static int radix_sort(Context *c, DTree &T, unsigned long long *&key, int *&idx, unsigned long long *&key2,
+                      int *&idx2, int n, int bits) {
+    const int nblk = (n + RADIX_TILE - 1) / RADIX_TILE;
+    int r = 0;
+    if ((r = T.hist.reserve(256 * (size_t)nblk)) || (r = T.hoff.reserve(256 * (size_t)nblk + 1))) return r;
+    for (int shift = 0; shift < bits; shift += 8) {
+        k_radix_hist<<<nblk, 256, 0, c->stream>>>(key, n, shift, nblk, T.hist.p);
+        int tot = 0;
+        if ((r = g_eng.scan(T.hist.p, T.hoff.p, 256 * nblk, &tot))) return r;
+        k_radix_scatter<<<nblk, 256, 0, c->stream>>>(key, idx, n, shift, nblk, T.hoff.p, key2, idx2);
+        std::swap(key, key2);
+        std::swap(idx, idx2);
+    }
+    return cuda_status(cudaGetLastError());
+}
+
+// node storage that keeps its contents when it grows
+static int grow_nodes(Context *c, DTree &T, size_t need) {
+    if (need <= T.node_cap) return 0;
+    const size_t cap = std::max(need, T.node_cap * 2);
+    TNode *np = nullptr;
+    int *pp = nullptr;
+    int r = cuda_status(cudaMalloc(&np, cap * sizeof(TNode)));
+    if (r) return r;
+    if ((r = cuda_status(cudaMalloc(&pp, cap * sizeof(int))))) {
+        cudaFree(np);
+        return r;
+    }
+    if (T.node_cap) {
+        cudaMemcpyAsync(np, T.nd.p, T.node_cap * sizeof(TNode), cudaMemcpyDeviceToDevice, c->stream);
+        cudaMemcpyAsync(pp, T.parent.p, T.node_cap * sizeof(int), cudaMemcpyDeviceToDevice, c->stream);
+        cudaStreamSynchronize(c->stream);
+    }
+    T.nd.release();
+    T.parent.release();
+    T.nd.p = np;
+    T.nd.cap = cap * sizeof(TNode);
+    T.parent.p = pp;
+    T.parent.cap = cap * sizeof(int);
+    T.node_cap = cap;
+    return 0;
+}
+
+static inline int nblocks(long long n, int t = 256) { return (int)std::max<long long>(1, (n + t - 1) / t); }
+
+// Builds the tree of the state's bodies and writes the group lists and the
+// SPJ array into the resident soft-force set.
+static int device_tree(Context *c, double theta, int n_leaf_limit, int n_group_limit) {
+    Engine &E = g_eng;
+    DTree &T = g_dt;
+    DevSet &d = c->res;
+    const int n = E.S.n;
+    if (n <= 0 || theta <= 0. || n_leaf_limit < 1 || n_group_limit < 1) return ST_BAD_INDEX;
+    const int limit = std::min(n_leaf_limit, n_group_limit);
+    int r = 0;
+    const int pb = std::min(1024, nblocks(n));
+    if ((r = T.part.reserve(6 * (size_t)pb)) || (r = T.root.reserve(8)) || (r = T.key.reserve(n)) ||
+        (r = T.key2.reserve(n)) || (r = T.idx.reserve(n)) || (r = T.idx2.reserve(n)) || (r = T.head.reserve(n)) ||
+        (r = T.hs.reserve(n)) || (r = T.enode.reserve(n)) || (r = T.enode2.reserve(n)) ||
+        (r = T.gmark.reserve(n)) || (r = T.gflag.reserve(n)) || (r = T.gpos.reserve(n)))
+        return r;
+    // 1. root cube, keys, sort
+    k_bbox_partial<<<pb, 256, 0, c->stream>>>(E.S.pos, n, T.part.p);
+    k_bbox_root<<<1, 32, 0, c->stream>>>(T.part.p, pb, T.root.p);
+    k_keys<<<nblocks(n), 256, 0, c->stream>>>(E.S.pos, n, T.root.p, T.key.p, T.idx.p);
+    unsigned long long *key = T.key.p, *key2 = T.key2.p;
+    int *idx = T.idx.p, *idx2 = T.idx2.p;
+    if ((r = radix_sort(c, T, key, idx, key2, idx2, n, 64))) return r;  // 8 passes: back in T.key / T.idx
+    // 2. levels
+    if ((r = grow_nodes(c, T, (size_t)n / 4 + 1024))) return r;
+    k_root_node<<<nblocks(n), 256, 0, c->stream>>>(T.nd.p, T.parent.p, T.root.p, n, limit, T.enode.p);
+    T.level_start.assign(1, 0);
+    int base = 1;
+    int *en = T.enode.p, *en2 = T.enode2.p;
+    for (int level = 0; level < 21; level++) {
+        k_lvl_heads<<<nblocks(n), 256, 0, c->stream>>>(key, en, T.nd.p, n, 3 * (20 - level), T.head.p);
+        int m = 0;
+        if ((r = E.scan(T.head.p, T.hs.p, n, &m))) return r;
+        if (m == 0) break;
+        if ((r = grow_nodes(c, T, (size_t)base + m))) return r;
+        T.level_start.push_back(base);
+        k_lvl_make<<<nblocks(n), 256, 0, c->stream>>>(en, T.head.p, T.hs.p, n, base, T.nd.p, T.parent.p, en2);
+        k_lvl_count<<<nblocks(m), 256, 0, c->stream>>>(base, m, T.nd.p, T.parent.p);
+        k_lvl_split<<<nblocks(n), 256, 0, c->stream>>>(n, level + 1, limit, T.nd.p, en2);
+        std::swap(en, en2);
+        base += m;
+    }
+    T.level_start.push_back(base);
+    T.n_nodes = base;
+    if ((r = d.spj.reserve(base))) return r;
+    // 3. moments, deepest level first
+    for (int L = (int)T.level_start.size() - 2; L >= 0; L--) {
+        const int lo = T.level_start[L], hi = T.level_start[L + 1];
+        k_moments<<<nblocks(hi - lo, 128), 128, 0, c->stream>>>(lo, hi, T.nd.p, d.spj.p, idx, E.S.pos, E.S.mass,
+                                                                E.S.r_search);
+    }
+    // 4. groups in Morton order
+    cudaMemsetAsync(T.gmark.p, 0, n * sizeof(int), c->stream);
+    k_group_mark<<<nblocks(base), 256, 0, c->stream>>>(base, T.nd.p, T.parent.p, n_group_limit, T.gmark.p);
+    k_group_flag<<<nblocks(n), 256, 0, c->stream>>>(T.gmark.p, n, T.gflag.p);
+    int ng = 0;
+    if ((r = E.scan(T.gflag.p, T.gpos.p, n, &ng))) return r;
+    T.n_groups = ng;
+    if ((r = T.gnode.reserve(ng + 1)) || (r = d.i_off.reserve(ng + 1)) || (r = d.j_off.reserve(ng + 1)) ||
+        (r = d.s_off.reserve(ng + 1)) || (r = d.i_idx.reserve(n)) || (r = T.cnt.reserve(2 * (size_t)ng + 2)))
+        return r;
+    k_group_fill<<<nblocks(n), 256, 0, c->stream>>>(T.gmark.p, T.gpos.p, n, ng, T.gnode.p, d.i_off.p);
+    cudaMemcpyAsync(d.i_idx.p, idx, n * sizeof(int), cudaMemcpyDeviceToDevice, c->stream);
+    // 5. walks: counts, offsets, entries
+    int *jcnt = T.cnt.p, *scnt = T.cnt.p + ng + 1;
+    k_walk<<<nblocks(ng, 64), 64, 0, c->stream>>>(T.nd.p, T.gnode.p, ng, theta * theta, idx, 0, jcnt, scnt,
+                                                  nullptr, nullptr, nullptr, nullptr, c->status);
+    int nj = 0, ns = 0;
+    if ((r = E.scan(jcnt, d.j_off.p, ng, &nj)) || (r = E.scan(scnt, d.s_off.p, ng, &ns))) return r;
+    cudaMemcpyAsync(d.j_off.p + ng, &nj, sizeof(int), cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(d.s_off.p + ng, &ns, sizeof(int), cudaMemcpyHostToDevice, c->stream);
+    if ((r = d.j_idx.reserve(nj)) || (r = d.s_idx.reserve(ns))) return r;
+    k_walk<<<nblocks(ng, 64), 64, 0, c->stream>>>(T.nd.p, T.gnode.p, ng, theta * theta, idx, 1, jcnt, scnt,
+                                                  d.j_off.p, d.s_off.p, d.j_idx.p, d.s_idx.p, c->status);
+    // 6. the soft kernel's launch order (the bodies' key buffers and the
+    // group-scan scratch are free by now)
+    if ((r = d.order.reserve(ng))) return r;
+    if (ng > 0) {
+        unsigned long long *k1 = T.key.p, *k2 = T.key2.p;
+        int *i1 = T.gflag.p, *i2 = T.head.p;
+        k_group_weight<<<nblocks(ng), 256, 0, c->stream>>>(ng, d.i_off.p, d.j_off.p, d.s_off.p, k1, i1);
+        if ((r = radix_sort(c, T, k1, i1, k2, i2, ng, 64))) return r;
+        cudaMemcpyAsync(d.order.p, i1, ng * sizeof(int), cudaMemcpyDeviceToDevice, c->stream);
+    }
+    d.order_valid = true;
+    c->res_groups = ng;
+    c->res_spj = base;
+    c->res_n = n;
+    return cuda_status(cudaGetLastError());
+}
+
+}  // namespace p3t
+
+using namespace p3t;
+
+extern "C" {
+
+int p3t_state_tree(double theta, int n_leaf_limit, int n_group_limit) {
+    Context *c = ctx_get(0);
+    if (!c || !g_eng.c) return -(int)cudaErrorNoDevice;
+    int r = g_eng.pack_soft();
+    if (r) return r;
+    if ((r = device_tree(c, theta, n_leaf_limit, n_group_limit))) return r;
+    return read_status(c);
+}
+
+int p3t_state_tree_soft(double theta, int n_leaf_limit, int n_group_limit) {
+    int r = p3t_state_tree(theta, n_leaf_limit, n_group_limit);
+    if (r) return r;
+    return p3t_soft_run(1);
+}
+
+int p3t_tree_lists_counts(long long *counts) {
+    Context *c = ctx_get(0);
+    if (!c) return -(int)cudaErrorNoDevice;
+    const int ng = c->res_groups;
+    counts[0] = ng;
+    counts[1] = c->res_n;
+    int nj = 0, ns = 0;
+    if (ng > 0) {
+        int r = d2h(c, &nj, c->res.j_off.p + ng, sizeof(int));
+        if (r || (r = d2h(c, &ns, c->res.s_off.p + ng, sizeof(int)))) return r;
+    }
+    counts[2] = nj;
+    counts[3] = ns;
+    counts[4] = c->res_spj;
+    return 0;
+}
+
+int p3t_tree_lists_get(int *i_off, int *i_idx, int *j_off, int *j_idx, int *s_off, int *s_idx, void *spj) {
+    Context *c = ctx_get(0);
+    if (!c) return -(int)cudaErrorNoDevice;
+    long long k[5];
+    int r = p3t_tree_lists_counts(k);
+    if (r) return r;
+    DevSet &d = c->res;
+    const int ng = (int)k[0];
+    if ((r = d2h(c, i_off, d.i_off.p, (ng + 1) * sizeof(int))) || (r = d2h(c, j_off, d.j_off.p, (ng + 1) * sizeof(int))) ||
+        (r = d2h(c, s_off, d.s_off.p, (ng + 1) * sizeof(int))) || (r = d2h(c, i_idx, d.i_idx.p, k[1] * sizeof(int))) ||
+        (r = d2h(c, j_idx, d.j_idx.p, k[2] * sizeof(int))) || (r = d2h(c, s_idx, d.s_idx.p, k[3] * sizeof(int))))
+        return r;
+    if (spj && (r = d2h(c, spj, d.spj.p, k[4] * sizeof(SPJRec)))) return r;
+    return 0;
+}
+
+}  // extern "C"

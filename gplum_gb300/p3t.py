@@ -120,6 +120,30 @@ class GpuSystem:
             raise RuntimeError(f"p3t_hard failed with status {nc}")
         return cols[:2 * min(nc, col_cap)].reshape(-1, 2), ed
 
+    def tree_soft(self):
+        """Device octree + interaction lists from the current state, then the
+        soft force (replaces a host build_lists + soft_force pair)."""
+        P = self.params
+        self._chk(self.lib.p3t_state_tree_soft(P.theta, P.n_leaf_limit, P.n_group_limit), "p3t_state_tree_soft")
+
+    def tree_lists(self, build=True):
+        """The resident lists as a dict in build_lists' layout (optionally
+        building them on the device first)."""
+        from .layout import SPJ_DTYPE
+        P = self.params
+        if build:
+            self._chk(self.lib.p3t_state_tree(P.theta, P.n_leaf_limit, P.n_group_limit), "p3t_state_tree")
+        c = np.zeros(5, np.int64)
+        self._chk(self.lib.p3t_tree_lists_counts(c.ctypes.data_as(VP)), "p3t_tree_lists_counts")
+        ng, ni, nj, ns, nn = (int(x) for x in c)
+        out = dict(n_group=ng, i_off=np.zeros(ng + 1, np.int32), i_idx=np.zeros(ni, np.int32),
+                   j_off=np.zeros(ng + 1, np.int32), j_idx=np.zeros(nj, np.int32),
+                   s_off=np.zeros(ng + 1, np.int32), s_idx=np.zeros(ns, np.int32), spj=np.zeros(nn, SPJ_DTYPE))
+        self._chk(self.lib.p3t_tree_lists_get(*(out[k].ctypes.data_as(VP) for k in
+                                                ("i_off", "i_idx", "j_off", "j_idx", "s_off", "s_idx", "spj"))),
+                  "p3t_tree_lists_get")
+        return out
+
     def hard_costs(self):
         """(block steps, pair sweeps) of each cluster of the last hard launch."""
         nc = len(self.cluster_lists()[0]) - 1

@@ -126,6 +126,20 @@ int p3t_set_r_planet(void);
  * neighbour-candidate table filled for p3t_correct. */
 int p3t_state_soft(int n_group, const int *i_off, const int *i_idx, const int *j_off, const int *j_idx,
                    const int *s_off, const int *s_idx, const void *spj, int n_spj);
+/* The same step with the lists built on the device from the state's own
+ * positions, masses and search radii (no host round trip): the octree and
+ * interaction lists of include/p3t_tree.h's builder (FDPS's TreeForForce as
+ * GPLUM drives it, src/main_p3t.cpp:344-355,581-587,672-676), written into
+ * the resident soft-force buffers.  p3t_state_tree builds only;
+ * p3t_state_tree_soft builds and runs the soft force (with candidates). */
+int p3t_state_tree(double theta, int n_leaf_limit, int n_group_limit);
+int p3t_state_tree_soft(double theta, int n_leaf_limit, int n_group_limit);
+/* The resident lists (from p3t_state_tree or an upload): counts[0..4] =
+ * groups, i entries, EPJ entries, SPJ entries, SPJ records; then the CSR
+ * arrays and the SPJ records (80-byte SPJQuadrupole each) in the layout of
+ * include/p3t_tree.h. */
+int p3t_tree_lists_counts(long long *counts);
+int p3t_tree_lists_get(int *i_off, int *i_idx, int *j_off, int *j_idx, int *s_off, int *s_idx, void *spj);
 /* correctForceLong (initial = 0) / correctForceLongInitial (initial = 1),
  * src/gravity_soft.h:245-528: FP64 cutoff correction, exact neighbour test,
  * neighbour lists, acc0 (and for initial: sun force, acc_d, jerk_d, phi_d,
