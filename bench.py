@@ -103,12 +103,19 @@ class ClockSampler:
                 "reasons": sorted(reasons)}
 
 
-def p3t_step_measure(precision, steps=2, n=N_BODIES):
+def p3t_step_measure(precision, steps=2, n=N_BODIES, hard_mode=0, learned=True, device_tree=True):
     """The whole device P3T tree step (src/main_p3t.cpp:423-717) on the
     hard-part disk (n bodies, 0.95-1.05 AU, rms e = 6 h): kick, cluster
-    labels + lists, hard part (one persistent launch), host tree + lists, soft
-    force, correction + neighbour search, kick, energy.  Wall-clock per phase
-    with the device synchronised at each phase boundary."""
+    labels + lists, hard part (one persistent launch), tree + interaction
+    lists + soft force, correction + neighbour search, kick, energy.  Wall-clock per phase
+    with the device synchronised at each phase boundary.  The octree and
+    interaction lists are built on the device (tree_soft: tree + lists + soft
+    force); device_tree=False builds them on the host instead.
+
+    precision 0/1: mixed / FP64 soft force; hard_mode 0/1: bundles / one
+    cluster per thread, warp or CTA; learned: queue in the order of the
+    committed cost model (else size order)."""
+    from gplum_gb300 import scheduler
     from gplum_gb300.disk import P3TParams, disk_1m_hard
     from gplum_gb300.p3t import GpuSystem
     from gplum_gb300.tree import build_lists
@@ -116,6 +123,9 @@ def p3t_step_measure(precision, steps=2, n=N_BODIES):
     P = P3TParams(n_group_limit=256)
     d = disk_1m_hard(n)
     g = GpuSystem(P, precision=precision)
+    g.lib.p3t_set_hard_mode(hard_mode)
+    model = scheduler.load(lib=g.lib) if learned else None
+    g.lib.p3t_set_schedule(1 if model is not None else 0)
     ph = {}
 
     def lists():
@@ -128,8 +138,16 @@ def p3t_step_measure(precision, steps=2, n=N_BODIES):
     g.load(d)
     g.set_r_planet()
     g.prepare()
+
+    def tree_soft():
+        if device_tree:
+            g.tree_soft()
+        else:
+            L = lists()
+            g.soft_force(L)
+
     for _ in range(2):
-        g.soft_force(lists())
+        tree_soft()
         g.correct(True)
     e0 = g.energy()
     ph.clear()
@@ -152,21 +170,26 @@ def p3t_step_measure(precision, steps=2, n=N_BODIES):
         ncol += len(cols)
         off, _m = g.cluster_lists()
         clusters.append((len(off) - 1, int(np.diff(off).max()) if len(off) > 1 else 0))
-        L = lists()
-        timed("soft", lambda: g.soft_force(L))
+        timed("tree_soft", tree_soft)
         timed("correct", lambda: g.correct(False))
         timed("kick", g.kick)
         e = timed("energy", g.energy)
         if len(cols):
             timed("merge", lambda: g.merge(len(cols)))
             timed("radii", g.prepare)
-            L = lists()
-            timed("soft", lambda: g.soft_force(L))
+            timed("tree_soft", tree_soft)
             timed("correct", lambda: g.correct(True))
     total = (time.perf_counter() - t_all) / steps
+    g.lib.p3t_set_hard_mode(0)
+    g.lib.p3t_set_schedule(0)
     ms = {k: 1e3 * v / steps for k, v in ph.items()}
-    dev = sum(v for k, v in ms.items() if k != "tree_host")
-    return {"n_bodies": n, "steps": steps, "ms_per_step": 1e3 * total, "device_ms_per_step": dev,
+    # tree_host (host list build) is nested inside tree_soft when the tree is on the host
+    dev = sum(ms.values()) - 2.0 * ms.get("tree_host", 0.0)
+    return {"n_bodies": n, "steps": steps, "soft": "mixed" if precision == 0 else "fp64",
+            "hard": "bundles" if hard_mode == 0 else "cluster per thread/warp/CTA",
+            "queue": "learned cost model" if model is not None else "size",
+            "tree": "device" if device_tree else "host",
+            "ms_per_step": 1e3 * total, "device_ms_per_step": dev,
             "phases_ms": ms, "clusters_per_step": [c[0] for c in clusters],
             "largest_cluster": max(c[1] for c in clusters), "collisions": ncol,
             "dE_over_E": float((e[0] - e0[0]) / e0[0])}
@@ -358,11 +381,12 @@ def gpu_arm(args, rank, world):
     if not args.skip_step:
         try:
             mixed = p3t_step_measure(0)
-            fp64 = p3t_step_measure(1, steps=1)
+            plain = p3t_step_measure(1, steps=1, hard_mode=1, learned=False)
             out["p3t_step"] = {"workload": "hard-part disk, 1048576 bodies, 0.95-1.05 AU, m=7e-11, "
                                            "rms e=6h, rms i=3h, theta=0.5, n_group_limit=256",
-                               "mixed": mixed, "fp64_soft": fp64,
-                               "device_speedup": fp64["device_ms_per_step"] / mixed["device_ms_per_step"]}
+                               "mixed_batched": mixed, "plain_fp64": plain,
+                               "device_speedup": plain["device_ms_per_step"] / mixed["device_ms_per_step"],
+                               "hard_speedup": plain["phases_ms"]["hard"] / mixed["phases_ms"]["hard"]}
             cpu_s = cpu_step_baseline()
             out["p3t_step"]["cpu_baseline"] = {"value": 1.0 / cpu_s, "unit": "steps/s", "cores": os.cpu_count(),
                                                "kind": "port", "sample": "1 tree step, same disk and host tree"}

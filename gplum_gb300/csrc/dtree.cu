@@ -20,10 +20,11 @@
 // "a new 3-bit digit starts here" over the sorted keys gives the children,
 // contiguous, in level order); moments and boxes bottom-up (leaves sum their
 // bodies in key order, as the host builder; inner nodes combine children by
-// the parallel-axis rule); groups; and one thread per group walking the tree
-// twice (count, then fill) with the host builder's stack discipline, so the
-// lists equal the host builder's entry for entry (SPJ entries name the same
-// cells; node numbers are in level order here).  The lists go straight into
+// the parallel-axis rule); groups; and the walks, split into (group, node of
+// the upper three levels) tasks taken in pre-order, each walking its subtree
+// with the host builder's stack discipline (count, then fill), so the
+// concatenated lists equal the host builder's entry for entry (SPJ entries
+// name the same cells; node numbers are in level order here).  The lists go straight into
 // the resident soft-force buffers.  Compiled with -fmad=false so the box and
 // opening arithmetic rounds as the host builder's (-ffp-contract=off).
 #include <algorithm>
@@ -39,6 +40,13 @@ namespace p3t {
 struct TNode {
     double ilo[3], ihi[3], olo[3], ohi[3];  // body box, search box (bodies +- 1.1 r_search)
     double com[3], size;
+    int first, count, child0, nchild;
+};
+
+// FP32 copy of the walk's fields (rounded to nearest), for the ternary
+// opening test below
+struct TNodeF {
+    float ilo[3], ihi[3], olo[3], ohi[3], com[3], size;
     int first, count, child0, nchild;
 };
 
@@ -70,20 +78,34 @@ __global__ void k_bbox_partial(const double *pos, int n, double *part) {
     if (threadIdx.x < 6) part[6 * blockIdx.x + threadIdx.x] = s[threadIdx.x][0];
 }
 
-// root cube as the host builder: out = {base.xyz, size, scale}
+// root cube as the host builder: out = {base.xyz, size, scale} (one block of 256)
 __global__ void k_bbox_root(const double *part, int nblk, double *out) {
-    if (threadIdx.x || blockIdx.x) return;
+    __shared__ double s[6][256];
     double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-    for (int b = 0; b < nblk; b++)
+    for (int b = threadIdx.x; b < nblk; b += 256)
         for (int d = 0; d < 3; d++) {
             lo[d] = fmin(lo[d], part[6 * b + d]);
             hi[d] = fmax(hi[d], part[6 * b + 3 + d]);
         }
+    for (int d = 0; d < 3; d++) {
+        s[d][threadIdx.x] = lo[d];
+        s[3 + d][threadIdx.x] = hi[d];
+    }
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o)
+            for (int d = 0; d < 3; d++) {
+                s[d][threadIdx.x] = fmin(s[d][threadIdx.x], s[d][threadIdx.x + o]);
+                s[3 + d][threadIdx.x] = fmax(s[3 + d][threadIdx.x], s[3 + d][threadIdx.x + o]);
+            }
+        __syncthreads();
+    }
+    if (threadIdx.x) return;
     double size = 0.;
-    for (int d = 0; d < 3; d++) size = fmax(size, hi[d] - lo[d]);
+    for (int d = 0; d < 3; d++) size = fmax(size, s[3 + d][0] - s[d][0]);
     size = size * 1.0001 + 1e-300;
     for (int d = 0; d < 3; d++) {
-        const double cen = 0.5 * (lo[d] + hi[d]);
+        const double cen = 0.5 * (s[d][0] + s[3 + d][0]);
         out[d] = cen - 0.5 * size;
     }
     out[3] = size;
@@ -362,49 +384,215 @@ __device__ __forceinline__ double box_dist2(const double *lo, const double *hi, 
     return s;
 }
 
-// fill == 0: counts per group into jcnt/scnt; fill == 1: entries at j_off/s_off
-__global__ void k_walk(const TNode *nd, const int *gnode, int ng, double theta2, const int *order, int fill,
-                       int *jcnt, int *scnt, const int *j_off, const int *s_off, int *j_idx, int *s_idx,
-                       int *status) {
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= ng) return;
-    const TNode &G = nd[gnode[g]];
-    double gilo[3], gihi[3], golo[3], gohi[3];
+// The walk split into tasks: pair (group g, top node t) for each of the
+// ntop nodes of the upper `depth` levels, taken in the tree's pre-order.  The
+// open test of every pair goes first (k_walk_open); then a pair is reached
+// when all its top-node ancestors are open for g, and it contributes: an SPJ
+// entry (reached, not open), its bodies (reached, open leaf), nothing
+// (reached, open, above the split depth: its children are pairs of their
+// own), or the depth-first walk of its subtree (reached, open, at the split
+// depth).  Pairs in (group, pre-order) order concatenate to the single walk's
+// output, entry for entry.
+__device__ __forceinline__ bool cell_open(const TNode &C, const double *gilo, const double *gihi,
+                                          const double *golo, const double *gohi, double theta2) {
+    const bool near = box_overlap(C.olo, C.ohi, gilo, gihi) || box_overlap(golo, gohi, C.ilo, C.ihi);
+    return near || (C.size * C.size > theta2 * box_dist2(gilo, gihi, C.com));
+}
+
+__global__ void k_node_f32(const TNode *nd, int nn, TNodeF *nf) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nn) return;
+    const TNode &N = nd[c];
+    TNodeF F;
     for (int d = 0; d < 3; d++) {
-        gilo[d] = G.ilo[d];
-        gihi[d] = G.ihi[d];
-        golo[d] = G.olo[d];
-        gohi[d] = G.ohi[d];
+        F.ilo[d] = (float)N.ilo[d];
+        F.ihi[d] = (float)N.ihi[d];
+        F.olo[d] = (float)N.olo[d];
+        F.ohi[d] = (float)N.ohi[d];
+        F.com[d] = (float)N.com[d];
     }
-    int stack[WALK_STACK];
-    int sp = 0;
-    stack[sp++] = 0;
-    int nj = 0, ns = 0;
-    const int jo = fill ? j_off[g] : 0, so = fill ? s_off[g] : 0;
-    for (int guard = 0; sp > 0 && guard < (1 << 26); guard++) {
-        const int c = stack[--sp];
+    F.size = (float)N.size;
+    F.first = N.first;
+    F.count = N.count;
+    F.child0 = N.child0;
+    F.nchild = N.nchild;
+    nf[c] = F;
+}
+
+// Ternary comparisons on FP32 copies of doubles (each within 2^-24 relative
+// of its double): +1 when a < b certainly holds for the doubles, -1 when
+// a >= b certainly holds, 0 when the copies cannot tell.  b - a differs from
+// the FP32 difference of the copies by less than 1.8e-7 (|a| + |b|) (two
+// conversions and one rounded subtraction); the margin is 2.5e-7.
+__device__ __forceinline__ int lt3(float a, float b) {
+    const float d = b - a, e = 2.5e-7f * (fabsf(a) + fabsf(b)) + 1e-30f;
+    return d > e ? 1 : (d < -e ? -1 : 0);
+}
+// box overlap (no dimension separated): +1 yes, -1 no, 0 unknown
+__device__ __forceinline__ int overlap3(const float *alo, const float *ahi, const float *blo, const float *bhi) {
+    int res = 1;
+    for (int d = 0; d < 3; d++) {
+        const int s1 = lt3(ahi[d], blo[d]), s2 = lt3(bhi[d], alo[d]);
+        if (s1 == 1 || s2 == 1) return -1;  // separated for sure
+        if (s1 == 0 || s2 == 0) res = 0;
+    }
+    return res;
+}
+// The cell test of the host builder on the FP32 copies: +1 open, -1 closed,
+// 0 unknown.  The distance from the group box carries an absolute error
+// below E_d = 2.5e-7 (|x| + |lo or hi|) per dimension, so d^2 is within
+// B = sum(2 |e_d| E_d + E_d^2) + 4e-7 d^2; sizes and theta^2 carry 2e-7
+// relative, covered by the 4e-7 factors.
+__device__ __forceinline__ int open3(const TNodeF &C, const float *gilo, const float *gihi, const float *golo,
+                                     const float *gohi, float theta2) {
+    const int a = overlap3(C.olo, C.ohi, gilo, gihi);
+    if (a == 1) return 1;
+    const int b = overlap3(golo, gohi, C.ilo, C.ihi);
+    if (b == 1) return 1;
+    if (a == 0 || b == 0) return 0;
+    float d2 = 0.f, bnd = 0.f;
+    for (int d = 0; d < 3; d++) {
+        const float x = C.com[d];
+        float e = 0.f, E = 0.f;
+        if (x < gilo[d]) {
+            e = gilo[d] - x;
+            E = 2.5e-7f * (fabsf(x) + fabsf(gilo[d]));
+        } else if (x > gihi[d]) {
+            e = x - gihi[d];
+            E = 2.5e-7f * (fabsf(x) + fabsf(gihi[d]));
+        } else {
+            E = 2.5e-7f * (fabsf(x) + fmaxf(fabsf(gilo[d]), fabsf(gihi[d])));
+        }
+        d2 += e * e;
+        bnd += 2.f * e * E + E * E;
+    }
+    bnd += 4e-7f * d2 + 1e-37f;
+    const float s2 = C.size * C.size;
+    if (s2 * (1.f - 4e-7f) > theta2 * (d2 + bnd) * (1.f + 4e-7f)) return 1;
+    if (s2 * (1.f + 4e-7f) < theta2 * fmaxf(d2 - bnd, 0.f) * (1.f - 4e-7f)) return -1;
+    return 0;
+}
+
+__global__ void k_walk_open(const TNode *nd, const TNodeF *nf, const int *gnode, int ng, const int *top, int ntop,
+                            double theta2, float theta2f, unsigned char *ostat) {
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= (long long)ng * ntop) return;
+    const int g = (int)(p / ntop), t = (int)(p - (long long)g * ntop);
+    const TNodeF &G = nf[gnode[g]];
+    int o = open3(nf[top[t]], G.ilo, G.ihi, G.olo, G.ohi, theta2f);
+    if (o == 0) {
+        const TNode &Gd = nd[gnode[g]];
+        o = cell_open(nd[top[t]], Gd.ilo, Gd.ihi, Gd.olo, Gd.ohi, theta2) ? 1 : -1;
+    }
+    ostat[p] = o > 0 ? 1 : 0;
+}
+
+// Class of each pair and its entry counts: not reached or an open node above
+// the split depth (no entries), unopened (one SPJ entry), open leaf (its
+// bodies), open node at the split depth (a subtree task, counted later).
+// fill == 1 writes the entries of the first three kinds.
+__global__ void k_walk_class(const TNode *nd, const int *top, const int *top_anc, const int *top_lvl, long long np,
+                             int ntop, int depth, const unsigned char *ostat, const int *order, int fill, int *jc,
+                             int *sc, int *task_flag, const int *jo, const int *so, int *j_idx, int *s_idx) {
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    const int g = (int)(p / ntop), t = (int)(p - (long long)g * ntop);
+    const unsigned char *os = ostat + (long long)g * ntop;
+    bool reached = true;
+    for (int a = 0; a < depth; a++) {
+        const int ta = top_anc[t * depth + a];
+        if (ta >= 0 && !os[ta]) reached = false;
+    }
+    int nj = 0, ns = 0, task = 0;
+    const int c = top[t];
+    if (reached) {
         const TNode &C = nd[c];
-        const bool near = box_overlap(C.olo, C.ohi, gilo, gihi) || box_overlap(golo, gohi, C.ilo, C.ihi);
-        const bool open = near || (C.size * C.size > theta2 * box_dist2(gilo, gihi, C.com));
-        if (!open) {
-            if (fill) s_idx[so + ns] = c;
-            ns++;
+        if (!os[t]) {
+            if (fill) s_idx[so[p]] = c;
+            ns = 1;
         } else if (C.nchild == 0) {
             if (fill)
-                for (int k = 0; k < C.count; k++) j_idx[jo + nj + k] = order[C.first + k];
-            nj += C.count;
-        } else {
-            if (sp + C.nchild > WALK_STACK) {
-                atomicOr(status, ST_QUEUE_OVERFLOW);
-                break;
-            }
-            for (int ch = C.nchild - 1; ch >= 0; ch--) stack[sp++] = C.child0 + ch;
+                for (int k = 0; k < C.count; k++) j_idx[jo[p] + k] = order[C.first + k];
+            nj = C.count;
+        } else if (top_lvl[t] == depth) {
+            task = 1;
         }
     }
     if (!fill) {
-        jcnt[g] = nj;
-        scnt[g] = ns;
+        jc[p] = nj;
+        sc[p] = ns;
+        task_flag[p] = task;
     }
+}
+
+// the subtree walks of the compacted tasks (pair indices), one per thread;
+// the opening test runs on the FP32 copies and falls back to the doubles
+// only when the copies cannot decide
+__global__ void k_walk_tasks(const TNode *nd, const TNodeF *nf, const int *gnode, const int *top, int ntop,
+                             const int *tasks, int ntask, double theta2, float theta2f, const int *order, int fill,
+                             int *jc, int *sc, const int *jo, const int *so, int *j_idx, int *s_idx, int *status) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= ntask) return;
+    const long long p = tasks[q];
+    const int g = (int)(p / ntop), t = (int)(p - (long long)g * ntop);
+    const int gn = gnode[g];
+    float fil[3], fih[3], fol[3], foh[3];
+    {
+        const TNodeF &G = nf[gn];
+        for (int d = 0; d < 3; d++) {
+            fil[d] = G.ilo[d];
+            fih[d] = G.ihi[d];
+            fol[d] = G.olo[d];
+            foh[d] = G.ohi[d];
+        }
+    }
+    const TNodeF &C = nf[top[t]];
+    int stack[WALK_STACK];
+    int sp = 0;
+    for (int ch = C.nchild - 1; ch >= 0; ch--) stack[sp++] = C.child0 + ch;
+    int nj = 0, ns = 0;
+    const int jbase = fill ? jo[p] : 0, sbase = fill ? so[p] : 0;
+    for (int guard = 0; sp > 0 && guard < (1 << 26); guard++) {
+        const int c = stack[--sp];
+        const TNodeF &Q = nf[c];
+        int o = open3(Q, fil, fih, fol, foh, theta2f);
+        if (o == 0) {
+            const TNode &Gd = nd[gn];
+            o = cell_open(nd[c], Gd.ilo, Gd.ihi, Gd.olo, Gd.ohi, theta2) ? 1 : -1;
+        }
+        if (o < 0) {
+            if (fill) s_idx[sbase + ns] = c;
+            ns++;
+        } else if (Q.nchild == 0) {
+            if (fill)
+                for (int k = 0; k < Q.count; k++) j_idx[jbase + nj + k] = order[Q.first + k];
+            nj += Q.count;
+        } else {
+            if (sp + Q.nchild > WALK_STACK) {
+                atomicOr(status, ST_QUEUE_OVERFLOW);
+                break;
+            }
+            for (int ch = Q.nchild - 1; ch >= 0; ch--) stack[sp++] = Q.child0 + ch;
+        }
+    }
+    if (!fill) {
+        jc[p] = nj;
+        sc[p] = ns;
+    }
+}
+
+__global__ void k_task_list(const int *flag, const int *pos, long long np, int *tasks) {
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < np && flag[p]) tasks[pos[p]] = (int)p;
+}
+
+// per-group list offsets from the per-pair offsets
+__global__ void k_walk_group_off(const int *jo, const int *so, int ng, int ntop, int nj, int ns, int *j_off,
+                                 int *s_off) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g > ng) return;
+    j_off[g] = (g < ng) ? jo[(long long)g * ntop] : nj;
+    s_off[g] = (g < ng) ? so[(long long)g * ntop] : ns;
 }
 
 // launch order of the soft kernel: largest groups first (key: weight desc, group asc)
@@ -424,13 +612,17 @@ __global__ void k_group_weight(int ng, const int *i_off, const int *j_off, const
 struct DTree {
     DevBuf<double> part, root;
     DevBuf<unsigned long long> key, key2;
-    DevBuf<int> idx, idx2, hist, hoff, head, hs, enode, enode2, parent, gmark, gflag, gpos, gnode, cnt;
+    DevBuf<int> idx, idx2, hist, hoff, head, hs, enode, enode2, parent, gmark, gflag, gpos, gnode;
     DevBuf<TNode> nd;
+    DevBuf<TNodeF> nf;
+    DevBuf<int> top, pc, tasks;
+    DevBuf<unsigned char> ostat;
     size_t node_cap = 0;
     std::vector<int> level_start;
     int n_nodes = 0, n_groups = 0;
 };
 static DTree g_dt;
+static int g_walk_depth = 3;  // levels above the walk's task split
 
 // (key, idx) sorted in place by key, stably (8 passes of 8 bits over `bits`)
 static int radix_sort(Context *c, DTree &T, unsigned long long *&key, int *&idx, unsigned long long *&key2,
@@ -496,7 +688,7 @@ static int device_tree(Context *c, double theta, int n_leaf_limit, int n_group_l
         return r;
     // 1. root cube, keys, sort
     k_bbox_partial<<<pb, 256, 0, c->stream>>>(E.S.pos, n, T.part.p);
-    k_bbox_root<<<1, 32, 0, c->stream>>>(T.part.p, pb, T.root.p);
+    k_bbox_root<<<1, 256, 0, c->stream>>>(T.part.p, pb, T.root.p);
     k_keys<<<nblocks(n), 256, 0, c->stream>>>(E.S.pos, n, T.root.p, T.key.p, T.idx.p);
     unsigned long long *key = T.key.p, *key2 = T.key2.p;
     int *idx = T.idx.p, *idx2 = T.idx2.p;
@@ -537,21 +729,80 @@ static int device_tree(Context *c, double theta, int n_leaf_limit, int n_group_l
     if ((r = E.scan(T.gflag.p, T.gpos.p, n, &ng))) return r;
     T.n_groups = ng;
     if ((r = T.gnode.reserve(ng + 1)) || (r = d.i_off.reserve(ng + 1)) || (r = d.j_off.reserve(ng + 1)) ||
-        (r = d.s_off.reserve(ng + 1)) || (r = d.i_idx.reserve(n)) || (r = T.cnt.reserve(2 * (size_t)ng + 2)))
+        (r = d.s_off.reserve(ng + 1)) || (r = d.i_idx.reserve(n)))
         return r;
     k_group_fill<<<nblocks(n), 256, 0, c->stream>>>(T.gmark.p, T.gpos.p, n, ng, T.gnode.p, d.i_off.p);
     cudaMemcpyAsync(d.i_idx.p, idx, n * sizeof(int), cudaMemcpyDeviceToDevice, c->stream);
-    // 5. walks: counts, offsets, entries
-    int *jcnt = T.cnt.p, *scnt = T.cnt.p + ng + 1;
-    k_walk<<<nblocks(ng, 64), 64, 0, c->stream>>>(T.nd.p, T.gnode.p, ng, theta * theta, idx, 0, jcnt, scnt,
-                                                  nullptr, nullptr, nullptr, nullptr, c->status);
-    int nj = 0, ns = 0;
-    if ((r = E.scan(jcnt, d.j_off.p, ng, &nj)) || (r = E.scan(scnt, d.s_off.p, ng, &ns))) return r;
-    cudaMemcpyAsync(d.j_off.p + ng, &nj, sizeof(int), cudaMemcpyHostToDevice, c->stream);
-    cudaMemcpyAsync(d.s_off.p + ng, &ns, sizeof(int), cudaMemcpyHostToDevice, c->stream);
-    if ((r = d.j_idx.reserve(nj)) || (r = d.s_idx.reserve(ns))) return r;
-    k_walk<<<nblocks(ng, 64), 64, 0, c->stream>>>(T.nd.p, T.gnode.p, ng, theta * theta, idx, 1, jcnt, scnt,
-                                                  d.j_off.p, d.s_off.p, d.j_idx.p, d.s_idx.p, c->status);
+    // 5. walks: the top levels in pre-order (host, from the node table), then
+    // (group, top node) pairs: open tests, counts, offsets, entries
+    {
+        const int nlev = (int)T.level_start.size() - 1;
+        const int depth = std::min(g_walk_depth, nlev - 1);
+        const int ntop_nodes = T.level_start[depth + 1];
+        std::vector<TNode> tn(ntop_nodes);
+        if ((r = d2h(c, tn.data(), T.nd.p, ntop_nodes * sizeof(TNode)))) return r;
+        std::vector<int> top, anc, lvl;
+        std::vector<int> path;
+        std::vector<int> pos_of(ntop_nodes, -1);
+        // pre-order from the root, levels 0..depth
+        std::vector<std::pair<int, int>> st{{0, 0}};
+        std::vector<int> par_top(ntop_nodes, -1);
+        while (!st.empty()) {
+            const int nd_id = st.back().first, L = st.back().second;
+            st.pop_back();
+            pos_of[nd_id] = (int)top.size();
+            top.push_back(nd_id);
+            lvl.push_back(L);
+            if (L < depth)
+                for (int ch = tn[nd_id].nchild - 1; ch >= 0; ch--) {
+                    par_top[tn[nd_id].child0 + ch] = nd_id;
+                    st.push_back({tn[nd_id].child0 + ch, L + 1});
+                }
+        }
+        const int ntop = (int)top.size();
+        anc.assign((size_t)ntop * std::max(depth, 1), -1);
+        for (int t = 0; t < ntop; t++) {
+            int a = par_top[top[t]], k = 0;
+            while (a >= 0 && k < depth) {
+                anc[(size_t)t * depth + k++] = pos_of[a];
+                a = par_top[a];
+            }
+        }
+        const long long np = (long long)ng * ntop;
+        if (np > 2000000000LL) return ST_QUEUE_OVERFLOW;
+        if ((r = T.top.reserve(3 * (size_t)ntop + (size_t)ntop * std::max(depth, 1))) ||
+            (r = T.ostat.reserve(np)) || (r = T.pc.reserve(6 * np + 6)))
+            return r;
+        int *top_d = T.top.p, *lvl_d = T.top.p + ntop, *anc_d = T.top.p + 2 * ntop;
+        if ((r = h2d(c, top_d, top.data(), ntop * sizeof(int))) || (r = h2d(c, lvl_d, lvl.data(), ntop * sizeof(int))) ||
+            (r = h2d(c, anc_d, anc.data(), anc.size() * sizeof(int))))
+            return r;
+        int *jc = T.pc.p, *sc = T.pc.p + np, *jo = T.pc.p + 2 * np, *so = T.pc.p + 3 * np;
+        int *tflag = T.pc.p + 4 * np, *tpos = T.pc.p + 5 * np;
+        const int wb = (int)std::min<long long>((np + 127) / 128, 1LL << 30);
+        if ((r = T.nf.reserve(T.n_nodes))) return r;
+        k_node_f32<<<nblocks(T.n_nodes), 256, 0, c->stream>>>(T.nd.p, T.n_nodes, T.nf.p);
+        const float th2f = (float)(theta * theta);
+        k_walk_open<<<wb, 128, 0, c->stream>>>(T.nd.p, T.nf.p, T.gnode.p, ng, top_d, ntop, theta * theta, th2f,
+                                               T.ostat.p);
+        k_walk_class<<<wb, 128, 0, c->stream>>>(T.nd.p, top_d, anc_d, lvl_d, np, ntop, depth, T.ostat.p, idx, 0, jc,
+                                                sc, tflag, nullptr, nullptr, nullptr, nullptr);
+        int ntask = 0;
+        if ((r = E.scan(tflag, tpos, (int)np, &ntask)) || (r = T.tasks.reserve(ntask + 1))) return r;
+        k_task_list<<<wb, 128, 0, c->stream>>>(tflag, tpos, np, T.tasks.p);
+        k_walk_tasks<<<nblocks(ntask, 128), 128, 0, c->stream>>>(T.nd.p, T.nf.p, T.gnode.p, top_d, ntop, T.tasks.p,
+                                                                 ntask, theta * theta, th2f, idx, 0, jc, sc, nullptr,
+                                                                 nullptr, nullptr, nullptr, c->status);
+        int nj = 0, ns = 0;
+        if ((r = E.scan(jc, jo, (int)np, &nj)) || (r = E.scan(sc, so, (int)np, &ns))) return r;
+        k_walk_group_off<<<nblocks(ng + 1), 256, 0, c->stream>>>(jo, so, ng, ntop, nj, ns, d.j_off.p, d.s_off.p);
+        if ((r = d.j_idx.reserve(nj)) || (r = d.s_idx.reserve(ns))) return r;
+        k_walk_class<<<wb, 128, 0, c->stream>>>(T.nd.p, top_d, anc_d, lvl_d, np, ntop, depth, T.ostat.p, idx, 1, jc,
+                                                sc, tflag, jo, so, d.j_idx.p, d.s_idx.p);
+        k_walk_tasks<<<nblocks(ntask, 128), 128, 0, c->stream>>>(T.nd.p, T.nf.p, T.gnode.p, top_d, ntop, T.tasks.p,
+                                                                 ntask, theta * theta, th2f, idx, 1, jc, sc, jo, so,
+                                                                 d.j_idx.p, d.s_idx.p, c->status);
+    }
     // 6. the soft kernel's launch order (the bodies' key buffers and the
     // group-scan scratch are free by now)
     if ((r = d.order.reserve(ng))) return r;

@@ -385,13 +385,23 @@ __global__ void k_energy_partial(State S, double *part) {
     }
     if (threadIdx.x < 4) part[4 * blockIdx.x + threadIdx.x] = s[threadIdx.x][0];
 }
+// one block of 256: each thread sums a contiguous run of block partials in
+// order, then a fixed tree over the threads (deterministic)
 __global__ void k_energy_final(const double *part, int nblk, double *out) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double ek = 0., es = 0., ep = 0., ed = 0.;
-    for (int b = 0; b < nblk; b++) {
-        ek += part[4 * b]; es += part[4 * b + 1]; ep += part[4 * b + 2]; ed += part[4 * b + 3];
+    __shared__ double s[4][256];
+    const int t = threadIdx.x, per = (nblk + 255) / 256;
+    double q[4] = {0., 0., 0., 0.};
+    for (int b = t * per; b < min(nblk, (t + 1) * per); b++)
+        for (int k = 0; k < 4; k++) q[k] += part[4 * b + k];
+    for (int k = 0; k < 4; k++) s[k][t] = q[k];
+    __syncthreads();
+    for (int h = 128; h > 0; h >>= 1) {
+        if (t < h)
+            for (int k = 0; k < 4; k++) s[k][t] += s[k][t + h];
+        __syncthreads();
     }
-    ek *= 0.5; ep *= 0.5; ed *= 0.5;
+    if (t) return;
+    const double ek = 0.5 * s[0][0], es = s[1][0], ep = 0.5 * s[2][0], ed = 0.5 * s[3][0];
     out[1] = ek; out[2] = es; out[3] = ep; out[4] = ed;
     out[0] = ek + es + (ep + ed);
 }
@@ -691,7 +701,7 @@ int Engine::energy(double *out5) {
     int r = 0;
     if ((r = epart.reserve(4 * (size_t)blocks + 8))) return r;
     k_energy_partial<<<blocks, 256, 0, c->stream>>>(S, epart.p);
-    k_energy_final<<<1, 32, 0, c->stream>>>(epart.p, blocks, epart.p + 4 * blocks);
+    k_energy_final<<<1, 256, 0, c->stream>>>(epart.p, blocks, epart.p + 4 * blocks);
     cudaMemcpyAsync(out5, epart.p + 4 * blocks, 5 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
     return cuda_status(cudaStreamSynchronize(c->stream));
 }

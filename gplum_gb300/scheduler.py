@@ -32,7 +32,14 @@ VP = ctypes.c_void_p
 def run_steps(g, lists, istep0, steps, log=None):
     """`steps` device tree steps (src/main_p3t.cpp:423-717) of GpuSystem g;
     with `log` a list, appends (features, block steps) of each step's
-    clusters."""
+    clusters.  lists: a host list builder, or None for the device tree."""
+
+    def tree_soft():
+        if lists is None:
+            g.tree_soft()
+        else:
+            g.soft_force(lists())
+
     ncol = 0
     for istep in range(istep0, istep0 + steps):
         g.kick()
@@ -42,15 +49,13 @@ def run_steps(g, lists, istep0, steps, log=None):
         ncol += len(cols)
         if log is not None:
             log.append((X, g.hard_costs()[:, 0].copy()))
-        L = lists()
-        g.soft_force(L)
+        tree_soft()
         g.correct(False)
         g.kick()
         if len(cols):
             g.merge(len(cols))
             g.prepare()
-            L = lists()
-            g.soft_force(L)
+            tree_soft()
             g.correct(True)
     return ncol
 
@@ -116,7 +121,6 @@ def load(path=MODEL, lib=None, schedule=True):
 def main():
     from .disk import P3TParams, disk_1m_hard
     from .p3t import GpuSystem
-    from .tree import build_lists
 
     ap = argparse.ArgumentParser()
     ap.add_argument("--n", type=int, default=1048576)
@@ -127,17 +131,15 @@ def main():
     P = P3TParams(n_group_limit=256)
     d = disk_1m_hard(args.n)
     g = GpuSystem(P)
-    lists = lambda: build_lists(g.get("pos"), g.get("mass"), g.get("r_search"), P.theta, P.n_leaf_limit,
-                                P.n_group_limit)
     g.load(d)
     g.set_r_planet()
     g.prepare()
     for _ in range(2):
-        g.soft_force(lists())
+        g.tree_soft()
         g.correct(True)
     log = []
     t0 = time.perf_counter()
-    run_steps(g, lists, 1, args.steps, log)
+    run_steps(g, None, 1, args.steps, log)
     X = np.concatenate([a for a, _ in log])
     y = target(np.concatenate([b for _, b in log]))
     t1 = time.perf_counter()
