@@ -410,9 +410,12 @@ def main():
     ap.add_argument("--step-only", type=int, default=0, metavar="N",
                     help="only run one whole device step on the N-body hard-part disk and print its phases "
                          "(a small case for profiling the step's kernels)")
+    ap.add_argument("--hard-mode", type=int, default=0, choices=[0, 1],
+                    help="with --step-only: 0 bundled hard launch (default), 1 one cluster per thread/warp/CTA")
     args = ap.parse_args()
     if args.step_only:
-        print(json.dumps(p3t_step_measure(0, steps=1, n=args.step_only)))
+        print(json.dumps(p3t_step_measure(0, steps=1, n=args.step_only, hard_mode=args.hard_mode,
+                                          learned=args.hard_mode == 0)))
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
