@@ -255,6 +255,26 @@ def cpu_reference(L, epj, P, budget_s=20.0, threads=None):
     return 1.0 / step_s, f"{len(groups)} of {ng} groups ({t:.1f} s), scaled to the full step by pair flops", threads
 
 
+def max_over_ranks(x, world):
+    """The largest x over the ranks (every rank receives it); x itself on one
+    rank.  NCCL tensors live on the rank's GPU, gloo tensors on the host."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(ms_step, world):
+    """Whole-job steps/s of `world` independent replicas, each step timed as
+    the slowest rank's (replicas only: no data-path collective)."""
+    return world * 1e3 / ms_step
+
+
 def reference_arm(args, rank, world):
     if rank != 0:
         return
@@ -323,11 +343,8 @@ def gpu_arm(args, rank, world):
     if st not in (0,):
         raise RuntimeError(f"soft kernel reported status {st}")
     ms_step = float(np.mean(ms))
-    if world > 1:
-        t = torch.tensor([ms_step], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_step = float(t.item())
-    value = world * 1e3 / ms_step
+    ms_step = max_over_ranks(ms_step, world)
+    value = replica_rate(ms_step, world)
 
     # plain FP64 form of the same kernel (the accuracy / speed baseline)
     ms64 = float(np.mean(timed_steps(2, 1)))

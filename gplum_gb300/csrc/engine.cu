@@ -933,6 +933,8 @@ int p3t_correct(int initial) {
     return read_status(g_eng.c);
 }
 
+int p3t_correct_and_search(int initial) { return p3t_correct(initial); }
+
 int p3t_neighbor_counts(int *ngb_tot, int *with_ngb) {
     Context *c = ctx_get(0);
     if (!c || !g_eng.counters.p) return -(int)cudaErrorNoDevice;

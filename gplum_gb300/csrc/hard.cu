@@ -959,7 +959,11 @@ int p3t_hard_times(long long *out, int n) {
     return d2h(c, out, g_hb.times.p, 2 * (size_t)n * sizeof(long long));
 }
 
-int p3t_hard(int istep, int col_cap, long long *col_pairs, double *edisp) {
+// Stage 1 of the hard part: buffers and the work-queue order (device only,
+// queued on the library stream).
+static int g_enqueued = -1;  // cluster count of the enqueued lists
+
+int p3t_hard_enqueue(void) {
     Engine &E = g_eng;
     if (!E.c) return -(int)cudaErrorNoDevice;
     Context *c = E.c;
@@ -999,6 +1003,21 @@ int p3t_hard(int istep, int col_cap, long long *col_pairs, double *edisp) {
     cudaMemsetAsync(B.cost.p, 0, (2 * (size_t)nc + 2) * sizeof(long long), c->stream);
     cudaMemsetAsync(B.queue.p, 0, 3 * sizeof(int32_t), c->stream);
     cudaMemsetAsync(B.n_cols.p, 0, sizeof(int32_t), c->stream);
+    g_enqueued = nc;
+    return cuda_status(cudaGetLastError());
+}
+
+// Stage 2: the persistent cluster launch and the isolated-body drift of tree
+// step istep (queued, no host synchronisation).
+int p3t_hard_integrate(int istep) {
+    Engine &E = g_eng;
+    if (!E.c) return -(int)cudaErrorNoDevice;
+    Context *c = E.c;
+    HardBufs &B = g_hb;
+    const int nc = E.n_clusters;
+    if (g_enqueued != nc) return ST_BAD_INDEX;
+    g_enqueued = -1;
+    int r = 0;
     const Params P = E.params();
     if (nc > 0) {
         HardArgs A;
@@ -1047,7 +1066,17 @@ int p3t_hard(int istep, int col_cap, long long *col_pairs, double *edisp) {
     I.t1 = istep * P.dt_tree;
     I.status = c->status;
     if (E.S.n > 0) k_isolated<<<(E.S.n + 127) / 128, 128, 0, c->stream>>>(I);
-    if ((r = cuda_status(cudaGetLastError()))) return r;
+    return cuda_status(cudaGetLastError());
+}
+
+// Stage 3: wait for the launch, then the collision list in the reference's
+// order and the dissipated energy; returns the number of collisions.
+int p3t_hard_fetch(int col_cap, long long *col_pairs, double *edisp) {
+    Engine &E = g_eng;
+    if (!E.c) return -(int)cudaErrorNoDevice;
+    Context *c = E.c;
+    HardBufs &B = g_hb;
+    int r = 0;
     int ncol = 0;
     if ((r = d2h(c, &ncol, B.n_cols.p, sizeof(int)))) return r;
     ncol = std::min(ncol, 4096);
@@ -1087,6 +1116,12 @@ int p3t_hard(int istep, int col_cap, long long *col_pairs, double *edisp) {
     int st = read_status(c);
     if (st) return st;
     return ncol;
+}
+
+int p3t_hard(int istep, int col_cap, long long *col_pairs, double *edisp) {
+    int r = p3t_hard_enqueue();
+    if (r || (r = p3t_hard_integrate(istep))) return r;
+    return p3t_hard_fetch(col_cap, col_pairs, edisp);
 }
 
 }  // extern "C"

@@ -145,6 +145,9 @@ int p3t_tree_lists_get(int *i_off, int *i_idx, int *j_off, int *j_idx, int *s_of
  * neighbour lists, acc0 (and for initial: sun force, acc_d, jerk_d, phi_d,
  * first dt). */
 int p3t_correct(int initial);
+/* The same call under the name of the hot-path contract: correctForceLong /
+ * correctForceLongInitial with the neighbour search (src/gravity_soft.h:245-528). */
+int p3t_correct_and_search(int initial);
 int p3t_neighbor_counts(int *n_ngb_tot, int *n_with_ngb);
 /* Neighbour local indices of body i (returns their count, at most cap). */
 int p3t_neighbor_list(int i, int *out, int cap);
@@ -158,6 +161,15 @@ int p3t_cluster_lists(int *n_clusters, int *off, int *members);
  * collisions (>= 0) and writes (impactor id, target id) pairs and the
  * dissipated energy {total, hard part}; a negative value is an error. */
 int p3t_hard(int istep, int col_cap, long long *col_pairs, double *edisp);
+/* p3t_hard in three stages (HardSystem::makeList / timeIntegrate / the
+ * collision records, src/hard.h:321-438,554-829): enqueue orders the
+ * clusters of the last p3t_cluster_label into the work queue and integrate
+ * queues the launches for tree step istep, both without waiting; fetch
+ * waits and returns the collision count with the pairs and the dissipated
+ * energy as p3t_hard does. */
+int p3t_hard_enqueue(void);
+int p3t_hard_integrate(int istep);
+int p3t_hard_fetch(int col_cap, long long *col_pairs, double *edisp);
 /* Size tiers of the hard launch: clusters of >= cta_min members run one per
  * CTA, of >= warp_min one per warp, smaller ones one per thread (defaults
  * 8 and 64; GPLUM's own cutoff between its parallel and serial cluster
