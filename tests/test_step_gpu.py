@@ -145,3 +145,39 @@ def test_full_steps_track_the_oracle(gpu):
         dEo = (a["energy"][0] - e0o[0]) / e0o[0]
         dEg = (b["energy"][0] - e0g[0]) / e0g[0]
         assert abs(dEg - dEo) < 1e-9, (dEg, dEo)
+
+
+def test_isolated_bodies_take_the_sun_hermite(gpu):
+    """With a softened sun (eps2_sun > 0) isolated bodies are integrated by the
+    sun-only block-step Hermite (src/hermite.h:734-785) instead of the Kepler
+    drift (src/hard.h:803-811); cluster members feel the softened sun too."""
+    P = P3TParams(eps2_sun=1e-6)
+    d = make_disk(3000, 1e-9, 0.95, 1.05, ecc_hill=2.0, inc_hill=1.0, seed=24)
+    orc, g, lf = both(d, P)
+    H.p3t_init(orc, d, lf)
+    H.p3t_init(g, d, lf)
+    for istep in (1, 2):
+        orc.kick()
+        g.kick()
+        orc.cluster()
+        g.cluster()
+        sync_state(orc, g)
+        g.set("id", orc.get("id"))
+        c1, _ = orc.hard(istep)
+        c2, _ = g.hard(istep)
+        np.testing.assert_array_equal(c2, c1)
+        iso = orc.get("n_cluster") == 1
+        assert iso.sum() > 1000
+        for k in ("pos", "vel"):
+            assert rel_err(g.get(k), orc.get(k)).max() < 1e-13, k
+        np.testing.assert_array_equal(g.get("dt")[iso], orc.get("dt")[iso])
+        np.testing.assert_array_equal(g.get("time"), orc.get("time"))
+        for s in (orc, g):
+            s.f("set_id_local")()
+        L = lf(orc)
+        sync_state(orc, g)
+        for s in (orc, g):
+            s.soft_force(L)
+            s.correct(False)
+            s.kick()
+        sync_state(orc, g)
