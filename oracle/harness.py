@@ -18,6 +18,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libp3t_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libgplum_ref.so")
+REF_KOM_SO = os.path.join(HERE, "_ref", "libgplum_ref_kominami.so")
 REF_SRC = "/root/reference/src"
 
 F64P = ctypes.POINTER(ctypes.c_double)
@@ -55,13 +56,15 @@ _LIBS = {}
 
 
 def load(kind):
+    """kind: "orc" (restatement), "ref" (reference build), "ref_kominami"
+    (reference build with the KOMINAMI fragmentation model; symbols ref_*)."""
     if kind in _LIBS:
         return _LIBS[kind]
-    path = ORACLE_SO if kind == "orc" else REF_SO
+    path = {"orc": ORACLE_SO, "ref": REF_SO, "ref_kominami": REF_KOM_SO}[kind]
     if not os.path.exists(path):
         raise FileNotFoundError(path)
     lib = ctypes.CDLL(path)
-    p = kind + "_"
+    p = kind.split("_")[0] + "_"
     for name, res in [("cutoff_W", ctypes.c_double), ("cutoff_K", ctypes.c_double),
                       ("cutoff_dKdt", ctypes.c_double), ("solve_kepler", ctypes.c_double),
                       ("n", ctypes.c_int), ("n_pairs", ctypes.c_int), ("hard", ctypes.c_int),
@@ -216,3 +219,46 @@ def tree_lists_fn(params):
         return build_lists(sysm.get("pos"), sysm.get("mass"), sysm.get("r_search"), params.theta,
                            params.n_leaf_limit, params.n_group_limit)
     return fn
+
+
+# One collision in isolation (orc_collide_unit / ref_collide_unit): 26 doubles
+# per FPHard record, in this order.
+UNIT_FIELDS = ("x", "y", "z", "vx", "vy", "vz", "mass", "r_planet", "f", "r_out", "r_out_inv", "r_search",
+               "v_disp", "time", "time_c", "dt", "phi", "phi_d", "phi_s", "acc0", "id", "id_cluster",
+               "number", "dead", "merged", "spare")
+
+
+def collide_unit(kind, params, frag, records, twins, imp, tar, id_next=0, seed=12345):
+    """Runs one collision through the restatement ("orc", fragment phase
+    from drand48 seeded with `seed`) or a reference build ("ref" /
+    "ref_kominami", srand48(seed) first).  frag = (a_frag, N_frag, m_min).
+    Returns (records after, n_frag, edisp[2], id_next after)."""
+    lib = load(kind)
+    pre = kind.split("_")[0] + "_"
+    getattr(lib, pre + "set_params")(_ptr(np.ascontiguousarray(params.vector()), F64P))
+    a_frag, n_frag, m_min = frag
+    if kind == "orc":
+        lib.orc_set_frag(ctypes.c_double(a_frag), ctypes.c_int(n_frag), ctypes.c_double(m_min), ctypes.c_int(1),
+                         ctypes.c_ulonglong(seed))
+    else:
+        lib.ref_set_frag(ctypes.c_double(a_frag), ctypes.c_int(n_frag), ctypes.c_double(m_min))
+        lib.ref_srand48(ctypes.c_long(seed))
+    rec = np.ascontiguousarray(records, np.float64)
+    n = len(rec)
+    tw = np.ascontiguousarray(np.array(twins, np.int32).reshape(-1, 2))
+    cap = n + 64
+    out = np.zeros((cap, 26))
+    ed = np.zeros(2)
+    idn = ctypes.c_longlong(id_next)
+    fn = getattr(lib, pre + "collide_unit")
+    fn.restype = ctypes.c_int
+    try:
+        nf = fn(ctypes.c_int(n), _ptr(rec, F64P), ctypes.c_int(len(tw)), _ptr(tw, I32P), ctypes.c_int(imp),
+                ctypes.c_int(tar), ctypes.byref(idn), _ptr(out, F64P), ctypes.c_int(cap), _ptr(ed, F64P))
+    finally:  # back to perfect accretion for whatever runs next in this process
+        if kind == "orc":
+            lib.orc_set_frag(ctypes.c_double(0.0), ctypes.c_int(10), ctypes.c_double(9.426627927538057e-12),
+                             ctypes.c_int(0), ctypes.c_ulonglong(0))
+        else:
+            lib.ref_set_frag(ctypes.c_double(0.0), ctypes.c_int(10), ctypes.c_double(9.426627927538057e-12))
+    return out[:n + nf], nf, ed, idn.value

@@ -495,14 +495,52 @@ struct ColRec {
     int64_t id_imp, id_tar;
     double time;
     double edisp, edisp_d;
+    int n_frag;       // fragments made by this collision
+    int64_t id_frag;  // temporary id of its first fragment (the others count down)
 };
 std::vector<ColRec> COLS;
 double EDISP = 0., EDISP_D = 0.;
 
-// Collision0 perfect accretion: inputPair + collisionOutcome + setParticle +
-// calcEnergyDissipation, src/collisionA.h:86-706 (no fragments).
-void collide(std::vector<HPtcl> &c, std::map<int, std::vector<int>> &twins, int imp, int tar,
-             double &edisp, double &edisp_d, ColRec &rec) {
+// KOMINAMI fragmentation (src/collisionB.h:7-93; m_min src/collisionA.h:57,152).
+// a_frag = 0 gives no fragments, the perfect accretion of Collision0.
+double A_FRAG = 0.0;
+int N_FRAG = 10;
+double M_MIN = 9.426627927538057e-12;
+// Fragment-circle phase: GPLUM draws drand48() (src/collisionA.h:727), whose
+// sequence depends on the order OpenMP threads reach their collisions.  Mode
+// 0 (default) draws from a counter-based generator keyed by (tree step,
+// impactor id, target id, seed), the same on every device; mode 1 calls
+// drand48() in the reference's processing order, for pinning against it.
+int FRAG_RNG = 0;
+uint64_t FRAG_SEED = 0;
+int CUR_STEP = 0;
+int64_t ID_NEXT = 0;  // next particle id (src/main_p3t.cpp:233,295-305)
+constexpr double MY_PI = 3.14159265358979323846;  // src/main_p3t.cpp:25
+
+uint64_t mix64(uint64_t z) {  // splitmix64 finaliser
+    z += 0x9e3779b97f4a7c15ULL;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+    return z ^ (z >> 31);
+}
+double frag_uniform(int64_t id_imp, int64_t id_tar) {
+    if (FRAG_RNG == 1) return drand48();
+    uint64_t h = mix64(FRAG_SEED ^ 0x5851f42d4c957f2dULL);
+    h = mix64(h ^ (uint64_t)(int64_t)CUR_STEP);
+    h = mix64(h ^ (uint64_t)id_imp);
+    h = mix64(h ^ (uint64_t)id_tar);
+    return (double)(h >> 11) * 0x1.0p-53;
+}
+
+// One collision: Collision0::inputPair (src/collisionA.h:156-213), the
+// KOMINAMI collisionOutcome with setFragmentCircle (src/collisionB.h:43-93,
+// src/collisionA.h:708-742), Collision0::setParticle, calcEnergyDissipation
+// and setNeighbors (src/collisionA.h:220-706).  Fragments are appended to the
+// cluster c (their temporary ids count down from -(128 id_cluster + id_next
+// + 1)); id_next is the cluster's fragment counter (src/hermite.h:243).
+// Returns the number of fragments.
+int collide(std::vector<HPtcl> &c, std::map<int, std::vector<int>> &twins, int imp, int tar,
+            double &edisp, double &edisp_d, ColRec &rec, int64_t &id_next) {
     const std::vector<int> tw_imp = twins.count(imp) ? twins[imp] : std::vector<int>();
     const std::vector<int> tw_tar = twins.count(tar) ? twins[tar] : std::vector<int>();
     rec.id_imp = c[imp].id;
@@ -514,36 +552,107 @@ void collide(std::vector<HPtcl> &c, std::map<int, std::vector<int>> &twins, int 
         for (int k : tw_imp) m_imp += c[k].mass;
     if (c[tar].merged)
         for (int k : tw_tar) m_tar += c[k].mass;
+    const double r_planet_tar = c[tar].r_planet, f_imp = c[imp].f, f_tar = c[tar].f;
+    const V3 pos_g = (m_imp * pos_imp + m_tar * pos_tar) / (m_imp + m_tar);
     const V3 vel_g = (m_imp * vel_imp + m_tar * vel_tar) / (m_imp + m_tar);
-    const V3 pos_new = (m_imp * pos_imp + m_tar * pos_tar) / (m_imp + m_tar);
-    const V3 vel_new = (m_imp * vel_imp + m_tar * vel_tar) / (m_imp + m_tar);
-    // setParticle
-    const double m_rem = m_imp + m_tar - 0.;
+    // collisionOutcome (KOMINAMI)
+    int n_frag = (int)std::floor(A_FRAG * m_imp / M_MIN);
+    if (n_frag < 2) n_frag = 0;
+    if (n_frag > N_FRAG) n_frag = N_FRAG;
+    const double mass_frag = n_frag ? (A_FRAG * m_imp) : 0.;
+    const double mass_rem = m_imp + m_tar - mass_frag;
+    V3 masspos = ZERO, massvel = ZERO;
+    std::vector<HPtcl> F;
+    if (n_frag) {
+        const V3 ximp = pos_imp - pos_tar, vimp = vel_imp - vel_tar;
+        const double f_frag = f_imp;
+        const double r_planet_frag = std::pow(0.75 * mass_frag / n_frag / (MY_PI * P.dens), 1. / 3.);
+        const double r_planet_rem = std::pow(mass_rem / m_tar, 1. / 3.) * r_planet_tar;
+        const double r_frag = 2. * std::max(f_tar, f_frag) * (r_planet_frag + r_planet_rem);
+        const double r2_frag = r_frag * r_frag + P.eps2;
+        const double r_frag_inv = std::sqrt(1. / r2_frag);
+        const double v_frag = 1.05 * std::sqrt(2. * mass_rem * r_frag_inv);
+        const double m_f = mass_frag / n_frag;
+        // setFragmentCircle
+        V3 e0 = ximp;
+        V3 e1 = vimp - (dot(vimp, ximp) / dot(ximp, ximp)) * ximp;
+        e0 = e0 / std::sqrt(dot(e0, e0));
+        e1 = e1 / std::sqrt(dot(e1, e1));
+        const double theta0 = 2. * M_PI * frag_uniform(rec.id_imp, rec.id_tar);
+        for (int i = 0; i < n_frag; i++) {
+            HPtcl h;
+            std::memset((void *)&h, 0, sizeof(HPtcl));
+            h.mass = m_f;
+            const double theta = theta0 + 2. * M_PI * i / n_frag;
+            h.pos = pos_g + r_frag * (std::cos(theta) * e0 + std::sin(theta) * e1);
+            h.vel = vel_g + v_frag * (std::cos(theta) * e0 + std::sin(theta) * e1);
+            masspos += h.mass * h.pos;
+            massvel += h.mass * h.vel;
+            F.push_back(h);
+        }
+    }
+    const V3 pos_new = (m_imp * pos_imp + m_tar * pos_tar - masspos) / mass_rem;
+    const V3 vel_new = (m_imp * vel_imp + m_tar * vel_tar - massvel) / mass_rem;
+    // setParticle (flag_merge)
     c[imp].r_planet = 0.;
-    c[tar].r_planet *= std::pow(m_rem / m_tar, 1. / 3.);
-    c[imp].mass -= 0.;
+    c[tar].r_planet *= std::pow(mass_rem / m_tar, 1. / 3.);
+    c[imp].mass -= mass_frag;
     c[imp].id = c[tar].id;
     c[imp].dead = true;
     for (int k : tw_imp) { c[k].id = c[tar].id; c[k].dead = true; }
     c[tar].merged = true;
+    const int id_c_frag = n_frag ? (int)c.size() : 0;
+    const int64_t id_frag = n_frag ? (-(128 * c[imp].id_cluster + id_next + 1)) : 0;
+    for (int i = 0; i < n_frag; i++) {
+        HPtcl &h = F[i];
+        h.r_planet = std::pow(0.75 * h.mass / (MY_PI * P.dens), 1. / 3.);  // setRPlanet
+        h.f = c[imp].f;
+        h.r_out = c[imp].r_out;
+        h.r_out_inv = c[imp].r_out_inv;
+        h.r_search = c[imp].r_search;
+        h.v_disp = c[imp].v_disp;
+        h.time = c[imp].time;
+        h.time_c = c[imp].time_c;
+        h.dt = c[imp].dt;
+        h.phi = c[imp].phi;
+        h.phi_d = c[imp].phi_d;
+        h.phi_s = c[imp].phi_s;
+        // GPLUM leaves acc0 of a fragment unset (FPHard() does not initialise
+        // it); the reference build showed a denormal there, whose square --
+        // the only way acc0 enters calcDeltatInitial -- is 0
+        h.acc0 = 0.;
+        h.id = id_frag - i;
+        h.id_cluster = c[imp].id_cluster;
+        h.dead = false;
+        h.merged = false;
+        h.number = c[imp].number;  // setNeighbors
+        h.rank = 0; h.id_max = -1; h.id_min = INT_MAX;
+        id_next++;
+    }
+    c.insert(c.end(), F.begin(), F.end());
     c[imp].pos = pos_new; c[imp].vel = vel_new;
     for (int k : tw_imp) { c[k].pos = pos_new; c[k].vel = vel_new; }
     c[tar].pos = pos_new; c[tar].vel = vel_new;
     for (int k : tw_tar) { c[k].pos = pos_new; c[k].vel = vel_new; }
     // calcEnergyDissipation
-    const double m_i = c[imp].mass + 0.;
+    const double m_i = c[imp].mass + mass_frag;
     double e_kin = 0.;
     // (scalar * v) . v, the evaluation order of "s * v * v" with FDPS vectors
     V3 vr = vel_imp - vel_tar;
     e_kin -= dot(0.5 * m_imp * m_tar / (m_imp + m_tar) * vr, vr);
     vr = vel_new - vel_g;
-    e_kin += dot(0.5 * (m_imp - 0.) * vr, vr);
+    e_kin += dot(0.5 * (m_imp - mass_frag) * vr, vr);
     vr = vel_new - vel_g;
     e_kin += dot(0.5 * m_tar * vr, vr);
+    for (int i = 0; i < n_frag; i++) {
+        const HPtcl &h = c[id_c_frag + i];
+        vr = h.vel - vel_g;
+        e_kin += dot(0.5 * h.mass * vr, vr);
+    }
     double e_int = 0., e_int_d = 0.;
-    const V3 dr = pos_imp - pos_tar;
-    const double dr2 = dot(dr, dr) + P.eps2;
-    const double rinv = std::sqrt(1. / dr2);
+    V3 dr = pos_imp - pos_tar;
+    double dr2 = dot(dr, dr) + P.eps2;
+    double rinv = std::sqrt(1. / dr2), rinv_new;
     double dphi = m_i * rinv;
     e_int += c[tar].mass * dphi;
     e_int_d += c[tar].mass * dphi * (1. - cut_W2(dr2, c[imp].r_out_inv, c[tar].r_out_inv));
@@ -560,14 +669,92 @@ void collide(std::vector<HPtcl> &c, std::map<int, std::vector<int>> &twins, int 
             e_int_d += c[kj].mass * dphi * (1. - cut_W2(dr2, c[ki].r_out_inv, c[kj].r_out_inv));
         }
     }
+    for (int i = 0; i < n_frag; i++) {
+        const int f0 = id_c_frag + i;
+        dr = c[f0].pos - c[imp].pos;
+        dr2 = dot(dr, dr) + P.eps2;
+        rinv_new = std::sqrt(1. / dr2);
+        dphi = -c[f0].mass * rinv_new;
+        e_int += c[imp].mass * dphi;
+        e_int_d += c[imp].mass * dphi * (1. - cut_W2(dr2, c[imp].r_out_inv, c[f0].r_out_inv));
+        for (int k : tw_imp) {
+            e_int += c[k].mass * dphi;
+            e_int_d += c[k].mass * dphi * (1. - cut_W2(dr2, c[k].r_out_inv, c[f0].r_out_inv));
+        }
+        dr = c[f0].pos - c[tar].pos;
+        dr2 = dot(dr, dr) + P.eps2;
+        rinv_new = std::sqrt(1. / dr2);
+        dphi = -c[f0].mass * rinv_new;
+        e_int += c[tar].mass * dphi;
+        e_int_d += c[tar].mass * dphi * (1. - cut_W2(dr2, c[tar].r_out_inv, c[f0].r_out_inv));
+        for (int k : tw_tar) {
+            e_int += c[k].mass * dphi;
+            e_int_d += c[k].mass * dphi * (1. - cut_W2(dr2, c[k].r_out_inv, c[f0].r_out_inv));
+        }
+        for (int j = 0; j < i; j++) {
+            const int f1 = id_c_frag + j;
+            dr = c[f0].pos - c[f1].pos;
+            dr2 = dot(dr, dr) + P.eps2;
+            rinv_new = std::sqrt(1. / dr2);
+            dphi = -c[f0].mass * c[f1].mass * rinv_new;
+            e_int += dphi;
+            e_int_d += dphi * (1. - cut_W2(dr2, c[f0].r_out_inv, c[f1].r_out_inv));
+        }
+    }
+    for (int i = 0; i < id_c_frag; i++) {
+        if (c[i].id == c[imp].id || c[i].id == c[tar].id) continue;
+        const double m_nei = c[i].mass;
+        dr = pos_imp - c[i].pos;
+        dr2 = dot(dr, dr) + P.eps2;
+        rinv = std::sqrt(1. / dr2);
+        dr = c[imp].pos - c[i].pos;
+        dr2 = dot(dr, dr) + P.eps2;
+        rinv_new = std::sqrt(1. / dr2);
+        dphi = m_nei * (rinv - rinv_new);
+        e_int += m_nei * (m_i * rinv - c[imp].mass * rinv_new);
+        e_int_d += m_nei * (m_i * rinv - c[imp].mass * rinv_new) *
+                   (1. - cut_W2(dr2, c[imp].r_out_inv, c[i].r_out_inv));
+        for (int k : tw_imp) {
+            e_int += c[k].mass * dphi;
+            e_int_d += c[k].mass * dphi * (1. - cut_W2(dr2, c[k].r_out_inv, c[i].r_out_inv));
+        }
+        for (int j = 0; j < n_frag; j++) {
+            const int fj = id_c_frag + j;
+            dr = c[fj].pos - c[i].pos;
+            dr2 = dot(dr, dr) + P.eps2;
+            rinv_new = std::sqrt(1. / dr2);
+            dphi = -m_nei * c[fj].mass * rinv_new;
+            e_int += dphi;
+            e_int_d += dphi * (1. - cut_W2(dr2, c[fj].r_out_inv, c[i].r_out_inv));
+        }
+        dr = pos_tar - c[i].pos;
+        dr2 = dot(dr, dr) + P.eps2;
+        rinv = std::sqrt(1. / dr2);
+        dr = c[tar].pos - c[i].pos;
+        dr2 = dot(dr, dr) + P.eps2;
+        rinv_new = std::sqrt(1. / dr2);
+        dphi = m_nei * (rinv - rinv_new);
+        e_int += c[tar].mass * dphi;
+        e_int_d += c[tar].mass * dphi * (1. - cut_W2(dr2, c[tar].r_out_inv, c[i].r_out_inv));
+        for (int k : tw_tar) {
+            e_int += c[k].mass * dphi;
+            e_int_d += c[k].mass * dphi * (1. - cut_W2(dr2, c[k].r_out_inv, c[i].r_out_inv));
+        }
+    }
     double e_sun = 0.;
     e_sun += m_imp / std::sqrt(dot(pos_imp, pos_imp) + P.eps2) + m_tar / std::sqrt(dot(pos_tar, pos_tar) + P.eps2);
     e_sun -= m_tar * std::sqrt(1. / (dot(c[tar].pos, c[tar].pos) + P.eps2));
-    e_sun -= (m_imp - 0.) * std::sqrt(1. / (dot(c[imp].pos, c[imp].pos) + P.eps2));
+    e_sun -= (m_imp - mass_frag) * std::sqrt(1. / (dot(c[imp].pos, c[imp].pos) + P.eps2));
+    for (int i = 0; i < n_frag; i++) {
+        const HPtcl &h = c[id_c_frag + i];
+        e_sun -= h.mass * std::sqrt(1. / (dot(h.pos, h.pos) + P.eps2));
+    }
     e_sun *= P.m_sun;
     edisp = e_kin + e_int + e_sun;
     edisp_d = e_kin + e_int_d + e_sun;
     if (getenv("ORC_DEBUG_COL")) fprintf(stderr, "ORC DEkin: %.15e DEint: %.15e DEint_hard: %.15e DEsun: %.15e\n", e_kin, e_int, e_int_d, e_sun);
+    rec.n_frag = n_frag;
+    rec.id_frag = id_frag;
     // merge_list update, src/hermite.h:413-423
     std::vector<int> &t = twins[tar];
     t.push_back(imp);
@@ -576,6 +763,7 @@ void collide(std::vector<HPtcl> &c, std::map<int, std::vector<int>> &twins, int 
         twins.erase(imp);
         c[imp].merged = false;
     }
+    return n_frag;
 }
 
 // timeIntegrate_multi, src/hermite.h:224-479 (perfect accretion)
@@ -584,7 +772,8 @@ void integrate_cluster(std::vector<HPtcl> &c, double t_end, int &n_col, double &
     std::map<int, std::vector<int>> twins;  // target -> dead twins, insertion order
     n_col = 0;
     edisp = edisp_d = 0.;
-    const int n = (int)c.size();
+    int64_t id_next = 0;  // fragments made in this cluster
+    int n = (int)c.size();
     for (int i = 0; i < n; i++) hard_force(c[i], c, 0);
     for (int i = 0; i < n; i++) c[i].dead = c[i].merged = false;
     double time = 0.;
@@ -661,7 +850,8 @@ void integrate_cluster(std::vector<HPtcl> &c, double t_end, int &n_col, double &
         if (col) {
             double e1 = 0., e2 = 0.;
             ColRec rec;
-            collide(c, twins, imp, tar, e1, e2, rec);
+            collide(c, twins, imp, tar, e1, e2, rec, id_next);
+            n = (int)c.size();
             rec.edisp = e1;
             rec.edisp_d = e2;
             edisp += e1;
@@ -993,6 +1183,7 @@ int hard_all(int istep) {
     N_ISO = niso;
     COLS.clear();
     EDISP = EDISP_D = 0.;
+    CUR_STEP = istep;
     int done = 0;
     // clusters of 64 or more members first, then the rest, each in cluster
     // order (src/hard.h:562-575,583,700-701)
@@ -1006,7 +1197,9 @@ int hard_all(int istep) {
     std::vector<std::vector<ColRec>> ccols(ncl);
     std::vector<double> ce1(ncl, 0.), ce2(ncl, 0.);
     std::vector<int> cnc(ncl, 0);
-#pragma omp parallel for schedule(dynamic, 2)
+    std::vector<std::vector<Ptcl>> cfrag(ncl);  // fragments of each cluster, in creation order
+    // (drand48 fragment phases follow the reference's sequential order)
+#pragma omp parallel for schedule(dynamic, 2) if (FRAG_RNG == 0)
     for (int q = 0; q < ncl; q++) {
         auto &cl = clusters[order[q]];
         std::vector<HPtcl> c;
@@ -1016,13 +1209,33 @@ int hard_all(int istep) {
             c[k].n_cluster = (int)c.size();
             c[k].time = c[k].time_c + c[k].time;  // resetTime
             c[k].time_c = 0.;
-            S[cl[k]] = static_cast<Ptcl &>(c[k]);
+            if (k < cl.size()) S[cl[k]] = static_cast<Ptcl &>(c[k]);
+            else cfrag[q].push_back(static_cast<Ptcl &>(c[k]));
         }
     }
     for (int q = 0; q < ncl; q++) {
         if (cnc[q] > 0) { EDISP += ce1[q]; EDISP_D += ce2[q]; }
         COLS.insert(COLS.end(), ccols[q].begin(), ccols[q].end());
         done += (int)clusters[order[q]].size();
+    }
+    // rewriteFragmentID + addFragment2ParticleSystem (src/hard.h:832-943):
+    // new ids in collision-list order, then the fragments join the system in
+    // cluster order; dead members that merged into a fragment take its new id
+    {
+        std::map<int64_t, int64_t> o2n;
+        for (const ColRec &r : COLS)
+            for (int j = 0; j < r.n_frag; j++) o2n[r.id_frag - j] = ID_NEXT++;
+        for (int q = 0; q < ncl; q++) {
+            const auto &cl = clusters[order[q]];
+            for (Ptcl h : cfrag[q]) {
+                const int64_t old = h.id, nid = (old < 0) ? o2n.at(old) : old;
+                if (h.merged)
+                    for (int i : cl)
+                        if (S[i].id == old) S[i].id = nid;
+                h.id = nid;
+                S.push_back(h);
+            }
+        }
     }
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < n; i++) {
@@ -1198,6 +1411,7 @@ void orc_load(int n, const long long *id, const double *mass, const double *r_pl
         p.number = 0; p.rank = 0; p.id_max = -1; p.id_min = INT_MAX;
         p.id_cluster = p.id;
         p.n_cluster = 1;
+        if (i == 0 || p.id + 1 > ID_NEXT) ID_NEXT = p.id + 1;
     }
 }
 int orc_n() { return (int)S.size(); }
@@ -1335,6 +1549,55 @@ void orc_n_list(int i, long long *out) {
     for (size_t k = 0; k < NLIST[i].size(); k++) out[k] = NLIST[i][k];
 }
 void orc_cluster() { cluster_all(); }
+// KOMINAMI fragmentation parameters (a_frag = 0: perfect accretion) and the
+// fragment-phase generator (0 keyed, 1 drand48 seeded here)
+void orc_set_frag(double a_frag, int n_frag, double m_min, int rng_mode, unsigned long long seed) {
+    A_FRAG = a_frag;
+    N_FRAG = n_frag;
+    M_MIN = m_min;
+    FRAG_RNG = rng_mode;
+    FRAG_SEED = seed;
+    if (rng_mode == 1) srand48((long)seed);
+}
+long long orc_id_next() { return ID_NEXT; }
+// One collision in isolation (the counterpart of ref_collide_unit in
+// oracle/ref_build/ref_wrap.cpp; record layout UNIT_FIELDS of harness.py).
+int orc_collide_unit(int n, const double *in, int n_tw, const int *tw, int imp, int tar, long long *id_next,
+                     double *out, int cap, double *edisp) {
+    std::vector<HPtcl> c(n);
+    for (int i = 0; i < n; i++) {
+        const double *r = in + 26 * i;
+        HPtcl &p = c[i];
+        std::memset((void *)&p, 0, sizeof(HPtcl));
+        p.pos = v3(r[0], r[1], r[2]);
+        p.vel = v3(r[3], r[4], r[5]);
+        p.mass = r[6]; p.r_planet = r[7]; p.f = r[8]; p.r_out = r[9]; p.r_out_inv = r[10];
+        p.r_search = r[11]; p.v_disp = r[12]; p.time = r[13]; p.time_c = r[14]; p.dt = r[15];
+        p.phi = r[16]; p.phi_d = r[17]; p.phi_s = r[18]; p.acc0 = r[19];
+        p.id = (int64_t)r[20]; p.id_cluster = (int64_t)r[21]; p.number = (int32_t)r[22];
+        p.dead = r[23] != 0.; p.merged = r[24] != 0.;
+    }
+    std::map<int, std::vector<int>> twins;
+    for (int k = 0; k < n_tw; k++) twins[tw[2 * k]].push_back(tw[2 * k + 1]);
+    ColRec rec;
+    double e1 = 0., e2 = 0.;
+    int64_t idn = *id_next;
+    const int nf = collide(c, twins, imp, tar, e1, e2, rec, idn);
+    *id_next = idn;
+    edisp[0] = e1;
+    edisp[1] = e2;
+    for (int i = 0; i < (int)c.size() && i < cap; i++) {
+        double *r = out + 26 * i;
+        const HPtcl &p = c[i];
+        r[0] = p.pos.x; r[1] = p.pos.y; r[2] = p.pos.z; r[3] = p.vel.x; r[4] = p.vel.y; r[5] = p.vel.z;
+        r[6] = p.mass; r[7] = p.r_planet; r[8] = p.f; r[9] = p.r_out; r[10] = p.r_out_inv;
+        r[11] = p.r_search; r[12] = p.v_disp; r[13] = p.time; r[14] = p.time_c; r[15] = p.dt;
+        r[16] = p.phi; r[17] = p.phi_d; r[18] = p.phi_s; r[19] = p.acc0;
+        r[20] = (double)p.id; r[21] = (double)p.id_cluster; r[22] = p.number;
+        r[23] = p.dead; r[24] = p.merged; r[25] = 0.;
+    }
+    return nf;
+}
 void orc_kick() {
     for (Ptcl &p : S) p.vel += 0.5 * P.dt_tree * p.acc;
 }

@@ -428,3 +428,64 @@ void ref_energy(double *out) {
 void ref_merge(int n_col, double *edisp) { MergeParticle(g_pp, n_col, *edisp); }
 
 }  // extern "C"
+
+// One collision in isolation, for pinning the fragmentation model: a cluster
+// of n FPHard records (26 doubles each, layout of oracle/harness.py
+// UNIT_FIELDS), its merge list as (target, twin) pairs in insertion order,
+// and the colliding pair; runs Collision::inputPair, collisionOutcome,
+// setParticle, calcEnergyDissipation and setNeighbors (src/collisionA.h,
+// src/collisionB.h; KOMINAMI when built with it, drand48 seeded by the
+// caller through ref_srand48), then clears the impactor's merged flag as the
+// Hermite loop does.  Writes the n + n_frag records, the energy
+// changes {edisp, edisp_d} and the fragment counter; returns n_frag.
+extern "C" void ref_srand48(long seed) { srand48(seed); }
+extern "C" void ref_set_frag(double a_frag, int n_frag, double m_min) {
+#ifdef KOMINAMI
+    Collision::a_frag = a_frag;
+    Collision::N_frag = n_frag;
+#else
+    (void)a_frag;
+    (void)n_frag;
+#endif
+    Collision0::m_min = m_min;
+}
+extern "C" int ref_collide_unit(int n, const double *in, int n_tw, const int *tw, int imp, int tar,
+                                long long *id_next, double *out, int cap, double *edisp) {
+    std::vector<FPHard> pp(n);
+    for (int i = 0; i < n; i++) {
+        const double *r = in + 26 * i;
+        FPHard &p = pp[i];
+        p.pos = PS::F64vec(r[0], r[1], r[2]);
+        p.vel = PS::F64vec(r[3], r[4], r[5]);
+        p.mass = r[6]; p.r_planet = r[7]; p.f = r[8]; p.r_out = r[9]; p.r_out_inv = r[10];
+        p.r_search = r[11]; p.v_disp = r[12]; p.time = r[13]; p.time_c = r[14]; p.dt = r[15];
+        p.phi = r[16]; p.phi_d = r[17]; p.phi_s = r[18]; p.acc0 = r[19];
+        p.id = (PS::S64)r[20]; p.id_cluster = (PS::S64)r[21]; p.neighbor.number = (PS::S32)r[22];
+        p.isDead = r[23] != 0.; p.isMerged = r[24] != 0.;
+    }
+    std::multimap<PS::S32, PS::S32> merge_list;
+    for (int k = 0; k < n_tw; k++) merge_list.insert(std::make_pair(tw[2 * k], tw[2 * k + 1]));
+    Collision col;
+    std::vector<FPHard> pfrag;
+    col.inputPair(pp, merge_list, std::make_pair(imp, tar));
+    PS::S64 idn = *id_next;
+    const int nf = col.collisionOutcome(pfrag);
+    col.setParticle(pp, pfrag, merge_list, idn);
+    edisp[0] = col.calcEnergyDissipation(pp, merge_list);
+    edisp[1] = col.getHardEnergyDissipation();
+    col.setNeighbors(pp);
+    // the merge-list bookkeeping that follows in src/hermite.h:413-423
+    if (col.flag_merge && pp[imp].isMerged) pp[imp].isMerged = false;
+    *id_next = idn;
+    for (int i = 0; i < (int)pp.size() && i < cap; i++) {
+        double *r = out + 26 * i;
+        const FPHard &p = pp[i];
+        r[0] = p.pos.x; r[1] = p.pos.y; r[2] = p.pos.z; r[3] = p.vel.x; r[4] = p.vel.y; r[5] = p.vel.z;
+        r[6] = p.mass; r[7] = p.r_planet; r[8] = p.f; r[9] = p.r_out; r[10] = p.r_out_inv;
+        r[11] = p.r_search; r[12] = p.v_disp; r[13] = p.time; r[14] = p.time_c; r[15] = p.dt;
+        r[16] = p.phi; r[17] = p.phi_d; r[18] = p.phi_s; r[19] = p.acc0;
+        r[20] = (double)p.id; r[21] = (double)p.id_cluster; r[22] = p.neighbor.number;
+        r[23] = p.isDead; r[24] = p.isMerged; r[25] = 0.;
+    }
+    return nf;
+}

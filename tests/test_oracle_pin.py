@@ -21,6 +21,9 @@ def test_functors_match_reference(trace_mode):
     L = lists_for(s, P)
     rl, ol = H.load("ref"), H.load("orc")
     vp = ctypes.c_void_p
+    pv = np.ascontiguousarray(P.vector())
+    rl.ref_set_params(pv.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))  # the functors read FPGrav::eps2
+    ol.orc_set_params(pv.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
     for g in range(0, L["n_group"], 3):
         ii = L["i_idx"][L["i_off"][g]:L["i_off"][g + 1]]
         ei = np.ascontiguousarray(epi[ii])
