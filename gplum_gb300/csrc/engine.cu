@@ -503,30 +503,33 @@ __global__ void k_radii(State S, Params P, double r_min, double dr, double drinv
 
 // ---------------------------------------------------------------------------
 // MergeParticle, src/func.h:160-207: targets fold in their dead twins (same
-// id, same cluster), twins leave the system (order-preserving).
+// id; twins share the target's cluster or are fragments made by the last
+// hard part), twins leave the system (order-preserving).
 __global__ void k_merge_targets(State S, const int32_t *cl_of, const int32_t *off, const int32_t *cnt,
-                                const int32_t *members, int32_t *keep, double *e_t, int32_t *tflag) {
+                                const int32_t *members, int32_t *keep, double *e_t, int32_t *tflag, int frag_lo,
+                                int frag_hi, const int32_t *frag_cl) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= S.n) return;
     e_t[i] = 0.;
     tflag[i] = 0;
     if (!(S.merged[i] && !S.dead[i])) return;
     tflag[i] = 1;
-    const int c = cl_of[i];
+    // twins: the cluster's members (ascending index), then the fragments the
+    // hard part appended (higher indices, ascending)
+    const int c = (i < frag_lo) ? cl_of[i] : (i < frag_hi ? frag_cl[i - frag_lo] : -1);
     double e = 0.;
-    if (c >= 0) {
-        for (int t = 0; t < cnt[c]; t++) {
-            const int j = members[off[c] + t];
-            if (S.id[j] == S.id[i] && i != j) {
-                const double mi = S.mass[i], mj = S.mass[j];
-                const V3 vrel = ld3(S.vel, j) - ld3(S.vel, i);
-                S.mass[i] += mj;
-                st3(S.vel, i, (mi * ld3(S.vel, i) + mj * ld3(S.vel, j)) / (mi + mj));
-                S.phi[i] = (mi * S.phi[i] + mj * S.phi[j]) / (mi + mj);
-                S.phi_d[i] = (mi * S.phi_d[i] + mj * S.phi_d[j]) / (mi + mj);
-                e -= dot(0.5 * mi * mj / (mi + mj) * vrel, vrel);
-                keep[j] = 0;
-            }
+    const int nm = (c >= 0) ? cnt[c] : 0;
+    for (int t = 0; t < nm + (frag_hi - frag_lo); t++) {
+        const int j = (t < nm) ? members[off[c] + t] : frag_lo + (t - nm);
+        if (S.id[j] == S.id[i] && i != j) {
+            const double mi = S.mass[i], mj = S.mass[j];
+            const V3 vrel = ld3(S.vel, j) - ld3(S.vel, i);
+            S.mass[i] += mj;
+            st3(S.vel, i, (mi * ld3(S.vel, i) + mj * ld3(S.vel, j)) / (mi + mj));
+            S.phi[i] = (mi * S.phi[i] + mj * S.phi[j]) / (mi + mj);
+            S.phi_d[i] = (mi * S.phi_d[i] + mj * S.phi_d[j]) / (mi + mj);
+            e -= dot(0.5 * mi * mj / (mi + mj) * vrel, vrel);
+            keep[j] = 0;
         }
     }
     S.merged[i] = 0;
@@ -584,6 +587,38 @@ int Engine::ensure(int n) {
     return 0;
 }
 
+// Capacity for n bodies keeping the first S.n of every field (new
+// particles from fragmentation).
+int Engine::grow(int n) {
+    if (n <= S.cap) return 0;
+    const int cap = n + n / 8 + 1024;
+    int r = 0;
+    if ((r = cuda_status(cudaStreamSynchronize(c->stream)))) return r;
+    auto move = [&](auto **f, size_t w) -> int {
+        using T = std::remove_pointer_t<std::remove_pointer_t<decltype(f)>>;
+        T *np = nullptr;
+        int rr = cuda_status(cudaMalloc(&np, std::max<size_t>((size_t)cap * w, 1) * sizeof(T)));
+        if (rr) return rr;
+        if (*f && S.n > 0) cudaMemcpy(np, *f, (size_t)S.n * w * sizeof(T), cudaMemcpyDeviceToDevice);
+        if (*f) cudaFree(*f);
+        *f = np;
+        return 0;
+    };
+    State &s = S;
+    for (double **f : {&s.mass, &s.r_planet, &s.f, &s.phi, &s.phi_d, &s.phi_s, &s.r_out, &s.r_out_inv, &s.r_search,
+                       &s.v_disp, &s.time, &s.dt, &s.acc0})
+        if ((r = move(f, 1))) return r;
+    for (double **f : {&s.pos, &s.vel, &s.acc, &s.acc_d, &s.jerk_d, &s.acc_s, &s.jerk_s, &s.acc_d_new})
+        if ((r = move(f, 3))) return r;
+    for (int64_t **f : {&s.id, &s.id_cluster})
+        if ((r = move(f, 1))) return r;
+    for (int32_t **f : {&s.number, &s.rank, &s.id_max, &s.id_min, &s.n_cluster, &s.dead, &s.merged, &s.nbr_n, &s.label})
+        if ((r = move(f, 1))) return r;
+    if ((r = alloc_field(&s.nbr, (size_t)cap * c->cand_cap))) return r;
+    s.cap = cap;
+    return 0;
+}
+
 Params Engine::params() const {
     Params P;
     const double *p = c->params;
@@ -625,6 +660,10 @@ int Engine::load(int n, const long long *id, const double *mass, const double *r
     k_fill_i32<<<nb(n), 256, 0, c->stream>>>(S.id_min, n, INT32_MAX_);
     cudaMemcpyAsync(S.id_cluster, S.id, n * sizeof(int64_t), cudaMemcpyDeviceToDevice, c->stream);
     n_clusters = 0;
+    frag_lo = frag_hi = n;
+    id_next = 0;
+    for (int i = 0; i < n; i++)
+        if (i == 0 || id[i] + 1 > id_next) id_next = id[i] + 1;
     return cuda_status(cudaStreamSynchronize(c->stream));
 }
 
@@ -738,7 +777,7 @@ int Engine::merge(double *edisp) {
         return r;
     k_fill_i32<<<nb(n), 256, 0, c->stream>>>(keep.p, n, 1);
     k_merge_targets<<<nb(n), 256, 0, c->stream>>>(S, cl_of.p, cl_off.p, cl_cnt.p, members.p, keep.p, et.p,
-                                                    tflag.p);
+                                                    tflag.p, frag_lo, frag_hi, frag_cl.p);
     int32_t nt = 0;
     if ((r = scan(tflag.p, tpos.p, n, &nt))) return r;
     double *tl = et.p + n;
@@ -749,6 +788,7 @@ int Engine::merge(double *edisp) {
     int32_t nk = 0;
     if ((r = scan(keep.p, kpos.p, n, &nk))) return r;  // synchronizes
     *edisp = e;
+    frag_lo = frag_hi = n;
     if (nk == n) return 0;
     // order-preserving compaction of every field through a scratch copy
     if ((r = compact_tmp.reserve((size_t)n * 3 * sizeof(double)))) return r;
@@ -770,6 +810,7 @@ int Engine::merge(double *edisp) {
         if ((r = comp(f, 1))) return r;
     S.n = nk;
     n_clusters = 0;
+    frag_lo = frag_hi = nk;
     return cuda_status(cudaStreamSynchronize(c->stream));
 }
 

@@ -51,6 +51,25 @@ struct ColRec {
     int64_t id_imp, id_tar;
     double time, edisp, edisp_d;
     int32_t cluster, seq, n;  // cluster index, collision number within it, cluster size
+    int32_t n_frag, frag0;    // fragments made (KOMINAMI) and the first one's fragment index
+    int64_t id_frag;          // temporary id of the first fragment (the others count down)
+};
+
+// One fragment (KOMINAMI), in creation order within its cluster: the FPGrav
+// fields the hard part does not carry, copied from the impactor
+// (src/collisionA.h:293-316), and where its hard state lives.
+struct FragRec {
+    int32_t cluster, seq, gslot, n_cl;  // cluster, creation number in it, hard slot, final cluster size
+    double r_out, r_search, v_disp, phi;
+    int32_t number, n0;  // impactor's neighbour count (setNeighbors); its cluster's size at admission
+    int64_t id_cluster;
+};
+
+// KOMINAMI fragmentation (src/collisionB.h:7-93); a_frag = 0 turns it off
+struct FragParams {
+    double a_frag, m_min;
+    int n_frag_max, istep;
+    unsigned long long seed;
 };
 
 struct HardArgs {
@@ -69,6 +88,10 @@ struct HardArgs {
     int col_cap;
     int *status;
     double t_end;
+    FragParams frag;
+    FragRec *frags;      // [frag_cap] fragments of this launch
+    int32_t *n_frags;    // fragments made so far
+    int frag_base, frag_cap;  // hard slots frag_base + k hold fragment k
 };
 
 // ---- FPHard::predict / correct / calcDeltat, src/particle.h:1183-1314 ----
@@ -209,14 +232,49 @@ __device__ __forceinline__ double cut_W2(const Params &P, double dr2, double a, 
     return cut_W(P, sqrt(dr2), dmin(a, b));
 }
 
-// Collision0 perfect accretion: inputPair, collisionOutcome, setParticle,
-// calcEnergyDissipation and the merge-list update (src/collisionA.h:86-706,
-// src/hermite.h:395-423).  One lane.
-__device__ void collide(const Params &P, const Hard &H, int imp, int tar, double &edisp, double &edisp_d,
-                        ColRec &rec) {
+// The fragment-circle phase: a counter-based draw keyed by (tree step,
+// impactor id, target id, seed) -- GPLUM draws drand48() from OpenMP threads
+// (src/collisionA.h:727), whose order is not reproducible; the oracle uses
+// the same keyed draw.  splitmix64 finaliser, 53-bit uniform in [0, 1).
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+    z += 0x9e3779b97f4a7c15ULL;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+    return z ^ (z >> 31);
+}
+__device__ __forceinline__ double frag_uniform(const FragParams &F, long long id_imp, long long id_tar) {
+    unsigned long long h = mix64(F.seed ^ 0x5851f42d4c957f2dULL);
+    h = mix64(h ^ (unsigned long long)(long long)F.istep);
+    h = mix64(h ^ (unsigned long long)id_imp);
+    h = mix64(h ^ (unsigned long long)id_tar);
+    return (double)(h >> 11) * 0x1.0p-53;
+}
+
+// Where one cluster's fragments go and what they inherit (bundle form only).
+struct FragCtx {
+    const HardArgs *A;
+    const int *mem;      // hard slots of the cluster's members, in member order
+    int n;               // members (earlier fragments included)
+    int cluster;
+    long long label;     // the cluster's id_cluster
+    long long *id_next;  // fragments made in this cluster so far (src/hermite.h:243)
+    int *out_slots;      // [n_frag_max]: hard slots of the new fragments
+};
+
+// Collision0::inputPair, the KOMINAMI collisionOutcome with setFragmentCircle
+// (src/collisionB.h:43-93, src/collisionA.h:708-742), Collision0::setParticle,
+// calcEnergyDissipation and setNeighbors (src/collisionA.h:86-706) with the
+// merge-list update (src/hermite.h:395-423).  One lane.  Without a fragment
+// context (or with a_frag = 0) this is perfect accretion.  Returns the
+// number of fragments, whose hard slots are written to X->out_slots.
+__device__ int collide(const Params &P, const Hard &H, int imp, int tar, double &edisp, double &edisp_d,
+                       ColRec &rec, const FragCtx *X) {
     rec.id_imp = H.id[imp];
     rec.id_tar = H.id[tar];
     rec.time = H.time_c[imp] + H.th[imp];
+    rec.n_frag = 0;
+    rec.frag0 = -1;
+    rec.id_frag = 0;
     const V3 pos_imp = ld3(H.pos, imp), pos_tar = ld3(H.pos, tar), vel_imp = ld3(H.vel, imp),
              vel_tar = ld3(H.vel, tar);
     double m_imp = H.mass[imp], m_tar = H.mass[tar];
@@ -224,13 +282,73 @@ __device__ void collide(const Params &P, const Hard &H, int imp, int tar, double
         for (int k = H.tw_head[imp], g = 0; k >= 0 && g < 4096; k = H.tw_next[k], g++) m_imp += H.mass[k];
     if (H.merged[tar])
         for (int k = H.tw_head[tar], g = 0; k >= 0 && g < 4096; k = H.tw_next[k], g++) m_tar += H.mass[k];
+    const double r_planet_tar = H.r_planet[tar], f_imp = H.f[imp], f_tar = H.f[tar];
     const V3 vel_g = (m_imp * vel_imp + m_tar * vel_tar) / (m_imp + m_tar);
-    const V3 pos_new = (m_imp * pos_imp + m_tar * pos_tar) / (m_imp + m_tar);
-    const V3 vel_new = (m_imp * vel_imp + m_tar * vel_tar) / (m_imp + m_tar);
-    const double m_rem = m_imp + m_tar - 0.;
+    const V3 pos_g = (m_imp * pos_imp + m_tar * pos_tar) / (m_imp + m_tar);
+    // collisionOutcome (KOMINAMI)
+    int n_frag = 0;
+    const FragParams *F = X ? &X->A->frag : nullptr;
+    if (F && F->a_frag > 0.) {
+        n_frag = (int)floor(F->a_frag * m_imp / F->m_min);
+        if (n_frag < 2) n_frag = 0;
+        if (n_frag > F->n_frag_max) n_frag = F->n_frag_max;
+    }
+    const double mass_frag = n_frag ? (F->a_frag * m_imp) : 0.;
+    const double mass_rem = m_imp + m_tar - mass_frag;
+    V3 masspos = v3(0., 0., 0.), massvel = v3(0., 0., 0.);
+    int f0 = 0;
+    if (n_frag && !X->mem) {  // the one-cluster-per-CTA form does not place fragments
+        atomicOr(X->A->status, ST_CLUSTER_TOO_BIG);
+        n_frag = 0;
+    }
+    if (n_frag) {
+        f0 = atomicAdd(X->A->n_frags, n_frag);
+        if (f0 + n_frag > X->A->frag_cap) {
+            atomicOr(X->A->status, ST_QUEUE_OVERFLOW);
+            n_frag = 0;
+        }
+    }
+    const double mass_frag_k = n_frag ? mass_frag : 0.;
+    const double mass_rem_k = n_frag ? mass_rem : m_imp + m_tar - 0.;
+    if (n_frag) {
+        const V3 ximp = pos_imp - pos_tar, vimp = vel_imp - vel_tar;
+        const double f_frag = f_imp;
+        const double r_planet_frag = pow(0.75 * mass_frag / n_frag / (3.14159265358979323846 * P.dens), 1. / 3.);
+        const double r_planet_rem = pow(mass_rem / m_tar, 1. / 3.) * r_planet_tar;
+        const double r_frag = 2. * dmax(f_tar, f_frag) * (r_planet_frag + r_planet_rem);
+        const double r2_frag = r_frag * r_frag + P.eps2;
+        const double r_frag_inv = sqrt(1. / r2_frag);
+        const double v_frag = 1.05 * sqrt(2. * mass_rem * r_frag_inv);
+        const double m_f = mass_frag / n_frag;
+        // setFragmentCircle
+        V3 e0 = ximp;
+        V3 e1 = vimp - (dot(vimp, ximp) / dot(ximp, ximp)) * ximp;
+        e0 = e0 / sqrt(dot(e0, e0));
+        e1 = e1 / sqrt(dot(e1, e1));
+        const double theta0 = 2. * 3.14159265358979323846 * frag_uniform(*F, rec.id_imp, rec.id_tar);
+        for (int i = 0; i < n_frag; i++) {
+            const int gf = X->A->frag_base + f0 + i;
+            const double theta = theta0 + 2. * 3.14159265358979323846 * i / n_frag;
+            const double ct = cos(theta), st = sin(theta);
+            const V3 fp = pos_g + r_frag * (ct * e0 + st * e1);
+            const V3 fv = vel_g + v_frag * (ct * e0 + st * e1);
+            H.mass[gf] = m_f;
+            st3(H.pos, gf, fp);
+            st3(H.vel, gf, fv);
+            // (the predicted state is rebuilt before it is next read; starting
+            // it at the position keeps the bundle's coordinate bound)
+            st3(H.xp, gf, fp);
+            st3(H.vp, gf, fv);
+            masspos = masspos + m_f * fp;
+            massvel = massvel + m_f * fv;
+        }
+    }
+    const V3 pos_new = (m_imp * pos_imp + m_tar * pos_tar - masspos) / mass_rem_k;
+    const V3 vel_new = (m_imp * vel_imp + m_tar * vel_tar - massvel) / mass_rem_k;
+    // setParticle (flag_merge)
     H.r_planet[imp] = 0.;
-    H.r_planet[tar] *= pow(m_rem / m_tar, 1. / 3.);
-    H.mass[imp] -= 0.;
+    H.r_planet[tar] *= pow(mass_rem_k / m_tar, 1. / 3.);
+    H.mass[imp] -= mass_frag_k;
     H.id[imp] = H.id[tar];
     H.dead[imp] = 1;
     for (int k = H.tw_head[imp], g = 0; k >= 0 && g < 4096; k = H.tw_next[k], g++) {
@@ -238,6 +356,66 @@ __device__ void collide(const Params &P, const Hard &H, int imp, int tar, double
         H.dead[k] = 1;
     }
     H.merged[tar] = 1;
+    long long id_frag = 0;
+    if (n_frag) {
+        id_frag = -(128LL * X->label + *X->id_next + 1);
+        // the impactor's FPGrav fields the hard part does not carry
+        double ro = 0., rs = 0., vd = 0., phi = 0.;
+        int num = 0;
+        if (imp < X->A->frag_base) {
+            const int si = X->A->members[imp];
+            ro = X->A->S.r_out[si];
+            rs = X->A->S.r_search[si];
+            vd = X->A->S.v_disp[si];
+            phi = X->A->S.phi[si];
+            num = X->A->S.number[si];
+        } else {
+            const FragRec &R = X->A->frags[imp - X->A->frag_base];
+            ro = R.r_out;
+            rs = R.r_search;
+            vd = R.v_disp;
+            phi = R.phi;
+            num = R.number;
+        }
+        for (int i = 0; i < n_frag; i++) {
+            const int gf = X->A->frag_base + f0 + i;
+            H.r_planet[gf] = pow(0.75 * H.mass[gf] / (3.14159265358979323846 * P.dens), 1. / 3.);  // setRPlanet
+            H.f[gf] = H.f[imp];
+            H.r_out_inv[gf] = H.r_out_inv[imp];
+            H.time_c[gf] = H.time_c[imp];
+            H.th[gf] = H.th[imp];
+            H.dt[gf] = H.dt[imp];
+            H.phi_d[gf] = H.phi_d[imp];
+            H.phi_s[gf] = H.phi_s[imp];
+            H.acc0[gf] = 0.;  // unset by GPLUM (FPHard()); it enters the time step only squared
+            H.id[gf] = id_frag - i;
+            H.dead[gf] = 0;
+            H.merged[gf] = 0;
+            H.tw_head[gf] = H.tw_tail[gf] = H.tw_next[gf] = -1;
+            const V3 z = v3(0., 0., 0.);
+            st3(H.acc_s, gf, z); st3(H.jerk_s, gf, z); st3(H.acc_d, gf, z); st3(H.jerk_d, gf, z);
+            st3(H.x0, gf, z); st3(H.v0, gf, z); st3(H.a0_s, gf, z); st3(H.j0_s, gf, z); st3(H.a0_d, gf, z);
+            st3(H.j0_d, gf, z); st3(H.a2_s, gf, z); st3(H.a3_s, gf, z);
+            st3(H.a2_d, gf, z); st3(H.a3_d, gf, z);
+            FragRec &R = X->A->frags[f0 + i];
+            R.cluster = X->cluster;
+            R.seq = (int)*X->id_next;
+            R.gslot = gf;
+            R.n_cl = 0;
+            R.r_out = ro;
+            R.r_search = rs;
+            R.v_disp = vd;
+            R.phi = phi;
+            R.number = num;  // setNeighbors
+            R.n0 = 0;
+            R.id_cluster = X->label;
+            X->out_slots[i] = gf;
+            (*X->id_next)++;
+        }
+        rec.n_frag = n_frag;
+        rec.frag0 = f0;
+        rec.id_frag = id_frag;
+    }
     st3(H.pos, imp, pos_new); st3(H.vel, imp, vel_new);
     for (int k = H.tw_head[imp], g = 0; k >= 0 && g < 4096; k = H.tw_next[k], g++) {
         st3(H.pos, k, pos_new); st3(H.vel, k, vel_new);
@@ -246,19 +424,24 @@ __device__ void collide(const Params &P, const Hard &H, int imp, int tar, double
     for (int k = H.tw_head[tar], g = 0; k >= 0 && g < 4096; k = H.tw_next[k], g++) {
         st3(H.pos, k, pos_new); st3(H.vel, k, vel_new);
     }
-    // energy
-    const double m_i = H.mass[imp] + 0.;
+    // calcEnergyDissipation
+    const double m_i = H.mass[imp] + mass_frag_k;
     double e_kin = 0.;
     V3 vr = vel_imp - vel_tar;
     e_kin -= dot(0.5 * m_imp * m_tar / (m_imp + m_tar) * vr, vr);
     vr = vel_new - vel_g;
-    e_kin += dot(0.5 * (m_imp - 0.) * vr, vr);
+    e_kin += dot(0.5 * (m_imp - mass_frag_k) * vr, vr);
     vr = vel_new - vel_g;
     e_kin += dot(0.5 * m_tar * vr, vr);
+    for (int i = 0; i < n_frag; i++) {
+        const int gf = X->A->frag_base + f0 + i;
+        vr = ld3(H.vel, gf) - vel_g;
+        e_kin += dot(0.5 * H.mass[gf] * vr, vr);
+    }
     double e_int = 0., e_int_d = 0.;
-    const V3 dr = pos_imp - pos_tar;
-    const double dr2 = dot(dr, dr) + P.eps2;
-    const double rinv = sqrt(1. / dr2);
+    V3 dr = pos_imp - pos_tar;
+    double dr2 = dot(dr, dr) + P.eps2;
+    double rinv = sqrt(1. / dr2), rinv_new;
     double dphi = m_i * rinv;
     e_int += H.mass[tar] * dphi;
     e_int_d += H.mass[tar] * dphi * (1. - cut_W2(P, dr2, H.r_out_inv[imp], H.r_out_inv[tar]));
@@ -275,11 +458,92 @@ __device__ void collide(const Params &P, const Hard &H, int imp, int tar, double
             e_int_d += H.mass[kj] * dphi * (1. - cut_W2(P, dr2, H.r_out_inv[ki], H.r_out_inv[kj]));
         }
     }
+    if (n_frag) {
+        const int fb = X->A->frag_base + f0;
+        for (int i = 0; i < n_frag; i++) {
+            const int a = fb + i;
+            dr = ld3(H.pos, a) - ld3(H.pos, imp);
+            dr2 = dot(dr, dr) + P.eps2;
+            rinv_new = sqrt(1. / dr2);
+            dphi = -H.mass[a] * rinv_new;
+            e_int += H.mass[imp] * dphi;
+            e_int_d += H.mass[imp] * dphi * (1. - cut_W2(P, dr2, H.r_out_inv[imp], H.r_out_inv[a]));
+            for (int k = H.tw_head[imp], g = 0; k >= 0 && g < 4096; k = H.tw_next[k], g++) {
+                e_int += H.mass[k] * dphi;
+                e_int_d += H.mass[k] * dphi * (1. - cut_W2(P, dr2, H.r_out_inv[k], H.r_out_inv[a]));
+            }
+            dr = ld3(H.pos, a) - ld3(H.pos, tar);
+            dr2 = dot(dr, dr) + P.eps2;
+            rinv_new = sqrt(1. / dr2);
+            dphi = -H.mass[a] * rinv_new;
+            e_int += H.mass[tar] * dphi;
+            e_int_d += H.mass[tar] * dphi * (1. - cut_W2(P, dr2, H.r_out_inv[tar], H.r_out_inv[a]));
+            for (int k = H.tw_head[tar], g = 0; k >= 0 && g < 4096; k = H.tw_next[k], g++) {
+                e_int += H.mass[k] * dphi;
+                e_int_d += H.mass[k] * dphi * (1. - cut_W2(P, dr2, H.r_out_inv[k], H.r_out_inv[a]));
+            }
+            for (int j = 0; j < i; j++) {
+                const int b = fb + j;
+                dr = ld3(H.pos, a) - ld3(H.pos, b);
+                dr2 = dot(dr, dr) + P.eps2;
+                rinv_new = sqrt(1. / dr2);
+                dphi = -H.mass[a] * H.mass[b] * rinv_new;
+                e_int += dphi;
+                e_int_d += dphi * (1. - cut_W2(P, dr2, H.r_out_inv[a], H.r_out_inv[b]));
+            }
+        }
+        // the other members of the cluster, before the new fragments
+        for (int q = 0; q < X->n; q++) {
+            const int i = X->mem[q];
+            if (H.id[i] == H.id[imp] || H.id[i] == H.id[tar]) continue;
+            const double m_nei = H.mass[i];
+            dr = pos_imp - ld3(H.pos, i);
+            dr2 = dot(dr, dr) + P.eps2;
+            rinv = sqrt(1. / dr2);
+            dr = ld3(H.pos, imp) - ld3(H.pos, i);
+            dr2 = dot(dr, dr) + P.eps2;
+            rinv_new = sqrt(1. / dr2);
+            dphi = m_nei * (rinv - rinv_new);
+            e_int += m_nei * (m_i * rinv - H.mass[imp] * rinv_new);
+            e_int_d += m_nei * (m_i * rinv - H.mass[imp] * rinv_new) *
+                       (1. - cut_W2(P, dr2, H.r_out_inv[imp], H.r_out_inv[i]));
+            for (int k = H.tw_head[imp], g = 0; k >= 0 && g < 4096; k = H.tw_next[k], g++) {
+                e_int += H.mass[k] * dphi;
+                e_int_d += H.mass[k] * dphi * (1. - cut_W2(P, dr2, H.r_out_inv[k], H.r_out_inv[i]));
+            }
+            for (int j = 0; j < n_frag; j++) {
+                const int b = fb + j;
+                dr = ld3(H.pos, b) - ld3(H.pos, i);
+                dr2 = dot(dr, dr) + P.eps2;
+                rinv_new = sqrt(1. / dr2);
+                dphi = -m_nei * H.mass[b] * rinv_new;
+                e_int += dphi;
+                e_int_d += dphi * (1. - cut_W2(P, dr2, H.r_out_inv[b], H.r_out_inv[i]));
+            }
+            dr = pos_tar - ld3(H.pos, i);
+            dr2 = dot(dr, dr) + P.eps2;
+            rinv = sqrt(1. / dr2);
+            dr = ld3(H.pos, tar) - ld3(H.pos, i);
+            dr2 = dot(dr, dr) + P.eps2;
+            rinv_new = sqrt(1. / dr2);
+            dphi = m_nei * (rinv - rinv_new);
+            e_int += H.mass[tar] * dphi;
+            e_int_d += H.mass[tar] * dphi * (1. - cut_W2(P, dr2, H.r_out_inv[tar], H.r_out_inv[i]));
+            for (int k = H.tw_head[tar], g = 0; k >= 0 && g < 4096; k = H.tw_next[k], g++) {
+                e_int += H.mass[k] * dphi;
+                e_int_d += H.mass[k] * dphi * (1. - cut_W2(P, dr2, H.r_out_inv[k], H.r_out_inv[i]));
+            }
+        }
+    }
     double e_sun = 0.;
     e_sun += m_imp / sqrt(dot(pos_imp, pos_imp) + P.eps2) + m_tar / sqrt(dot(pos_tar, pos_tar) + P.eps2);
     const V3 pt = ld3(H.pos, tar), pi = ld3(H.pos, imp);
     e_sun -= m_tar * sqrt(1. / (dot(pt, pt) + P.eps2));
-    e_sun -= (m_imp - 0.) * sqrt(1. / (dot(pi, pi) + P.eps2));
+    e_sun -= (m_imp - mass_frag_k) * sqrt(1. / (dot(pi, pi) + P.eps2));
+    for (int i = 0; i < n_frag; i++) {
+        const V3 fp = ld3(H.pos, X->A->frag_base + f0 + i);
+        e_sun -= H.mass[X->A->frag_base + f0 + i] * sqrt(1. / (dot(fp, fp) + P.eps2));
+    }
     e_sun *= P.m_sun;
     edisp = e_kin + e_int + e_sun;
     edisp_d = e_kin + e_int_d + e_sun;
@@ -304,6 +568,7 @@ __device__ void collide(const Params &P, const Hard &H, int imp, int tar, double
         H.tw_head[imp] = H.tw_tail[imp] = -1;
         H.merged[imp] = 0;
     }
+    return n_frag;
 }
 
 // ---- teams: one thread, one warp or one CTA integrates one cluster ----------
@@ -520,7 +785,8 @@ __device__ void run_cluster(const HardArgs &A, int c, const Team<TEAM> &tm) {
             if (rank == 0) {
                 ColRec rec;
                 double e1 = 0., e2 = 0.;
-                collide(P, H, imp, tar, e1, e2, rec);
+                FragCtx X{&A, nullptr, 0, c, 0, nullptr, nullptr};
+                collide(P, H, imp, tar, e1, e2, rec, A.frag.a_frag > 0. ? &X : nullptr);
                 ed += e1;
                 edd += e2;
                 rec.cluster = c;
@@ -881,6 +1147,9 @@ struct HardBufs {
     DevBuf<long long> cost, times;
     DevBuf<float> f32, prio;
     DevBuf<int32_t> bin, hist, ntier;
+    DevBuf<FragRec> frags;
+    DevBuf<int32_t> n_frags, fgslot, fidx;
+    DevBuf<long long> fmap;
     Hard H;
     int cap = 0;
     int reserve(int m) {
@@ -918,6 +1187,62 @@ static std::vector<ColRec> g_cols;
 static double g_edisp[2] = {0., 0.};
 static int g_warp_min = 8, g_cta_min = 64;
 static int g_hard_mode = 0;  // 0: bundles, 1: thread/warp/CTA tiers
+static FragParams g_frag = {0., 9.426627927538057e-12, 10, 0, 0ULL};  // off (a_frag = 0)
+static int g_frag_cap = 0;  // fragment slots of the current launch
+
+// Fragments made by a launch join the particle system (addFragment2ParticleSystem,
+// src/hard.h:858-943): the r-th new body is the fragment in hard slot
+// gslot[r] (record fidx[r]); temporary (negative) ids map through
+// old[k] -> new[k].
+__device__ __forceinline__ long long frag_new_id(long long id, const long long *map, int nmap) {
+    if (id >= 0) return id;
+    for (int k = 0; k < nmap; k++)
+        if (map[2 * k] == id) return map[2 * k + 1];
+    return id;
+}
+__global__ void k_frag_append(State S, Hard H, const FragRec *fr, const int32_t *gslot, const int32_t *fidx, int nf,
+                              int n0, const long long *map, int nmap, int32_t *frag_cl) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nf) return;
+    const int g = gslot[r], i = n0 + r;
+    const FragRec &R = fr[fidx[r]];
+    st3(S.pos, i, ld3(H.pos, g));
+    st3(S.vel, i, ld3(H.vel, g));
+    st3(S.acc, i, v3(0., 0., 0.));
+    st3(S.acc_d, i, ld3(H.acc_d, g));
+    st3(S.jerk_d, i, ld3(H.jerk_d, g));
+    st3(S.acc_s, i, ld3(H.acc_s, g));
+    st3(S.jerk_s, i, ld3(H.jerk_s, g));
+    S.phi[i] = R.phi;
+    S.phi_d[i] = H.phi_d[g];
+    S.phi_s[i] = H.phi_s[g];
+    S.mass[i] = H.mass[g];
+    S.r_planet[i] = H.r_planet[g];
+    S.f[i] = H.f[g];
+    S.r_out[i] = R.r_out;
+    S.r_out_inv[i] = H.r_out_inv[g];
+    S.r_search[i] = R.r_search;
+    S.v_disp[i] = R.v_disp;
+    S.time[i] = H.time_c[g] + H.th[g];  // resetTime
+    S.dt[i] = H.dt[g];
+    S.acc0[i] = H.acc0[g];
+    S.number[i] = R.number;
+    S.rank[i] = 0;
+    S.id_max[i] = -1;
+    S.id_min[i] = 2147483647;
+    S.n_cluster[i] = R.n_cl;
+    S.nbr_n[i] = 0;
+    S.dead[i] = H.dead[g];
+    S.merged[i] = H.merged[g];
+    S.id[i] = frag_new_id(H.id[g], map, nmap);
+    S.id_cluster[i] = R.id_cluster;
+    frag_cl[r] = R.cluster;
+}
+// dead members that merged into a fragment carry its temporary id
+__global__ void k_frag_ids(State S, int n, const long long *map, int nmap) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && S.id[i] < 0) S.id[i] = frag_new_id(S.id[i], map, nmap);
+}
 static std::vector<float> g_prio;
 
 }  // namespace p3t
@@ -932,6 +1257,17 @@ int p3t_set_hard_tiers(int warp_min, int cta_min) {
     g_cta_min = cta_min;
     return 0;
 }
+
+int p3t_set_fragmentation(double a_frag, int n_frag, double m_min, unsigned long long seed) {
+    if (a_frag < 0. || n_frag < 0 || n_frag > 32 || !(m_min > 0.)) return ST_BAD_INDEX;
+    g_frag.a_frag = a_frag;
+    g_frag.n_frag_max = n_frag;
+    g_frag.m_min = m_min;
+    g_frag.seed = seed;
+    return 0;
+}
+
+long long p3t_id_next(void) { return g_eng.id_next; }
 
 int p3t_set_hard_mode(int mode) {
     if (mode != 0 && mode != 1) return ST_BAD_INDEX;
@@ -970,10 +1306,13 @@ int p3t_hard_enqueue(void) {
     HardBufs &B = g_hb;
     const int nc = E.n_clusters;
     int r = 0;
-    if ((r = B.reserve(E.n_members)) || (r = B.order.reserve(nc)) || (r = B.queue.reserve(3)) ||
+    if (g_frag.a_frag > 0. && g_hard_mode != 0) return ST_BAD_INDEX;  // fragments need the bundle form
+    g_frag_cap = (g_frag.a_frag > 0.) ? std::max(1024, g_frag.n_frag_max * 4096) : 0;
+    if ((r = B.reserve(E.n_members + g_frag_cap)) || (r = B.order.reserve(nc)) || (r = B.queue.reserve(3)) ||
         (r = B.n_cols.reserve(1)) || (r = B.cl_edisp.reserve(2 * (size_t)nc + 2)) ||
-        (r = B.cols.reserve(4096)))
+        (r = B.cols.reserve(4096)) || (r = B.frags.reserve(g_frag_cap + 1)) || (r = B.n_frags.reserve(1)))
         return r;
+    cudaMemsetAsync(B.n_frags.p, 0, sizeof(int32_t), c->stream);
     // schedule, on the device: clusters binned by tier (bundle mode: above
     // the bundle capacity first; tier mode: CTA >= g_cta_min > warp >=
     // g_warp_min > thread), then by priority (the caller's, the learned cost
@@ -1039,6 +1378,12 @@ int p3t_hard_integrate(int istep) {
         A.col_cap = 4096;
         A.status = c->status;
         A.t_end = P.dt_tree;
+        A.frag = g_frag;
+        A.frag.istep = istep;
+        A.frags = B.frags.p;
+        A.n_frags = B.n_frags.p;
+        A.frag_base = E.n_members;
+        A.frag_cap = g_frag_cap;
         int sms = 152;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
         if (g_hard_mode == 0) {
@@ -1113,6 +1458,47 @@ int p3t_hard_fetch(int col_cap, long long *col_pairs, double *edisp) {
     }
     edisp[0] = g_edisp[0];
     edisp[1] = g_edisp[1];
+    // fragments join the system (rewriteFragmentID + addFragment2ParticleSystem,
+    // src/hard.h:832-943): ids in collision-list order, bodies in cluster
+    // order (clusters of 64+ members first), fragments in creation order
+    int nfr = 0;
+    if (g_frag_cap > 0 && (r = d2h(c, &nfr, B.n_frags.p, sizeof(int)))) return r;
+    nfr = std::min(nfr, g_frag_cap);
+    if (nfr > 0) {
+        std::vector<FragRec> fr(nfr);
+        if ((r = d2h(c, fr.data(), B.frags.p, nfr * sizeof(FragRec)))) return r;
+        std::vector<long long> map;
+        for (const ColRec &cr : g_cols)
+            for (int j = 0; j < cr.n_frag; j++) {
+                map.push_back(cr.id_frag - j);
+                map.push_back(E.id_next++);
+            }
+        std::vector<int> ord(nfr);
+        for (int k = 0; k < nfr; k++) ord[k] = k;
+        std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
+            const bool la = fr[a].n0 >= 64, lb = fr[b].n0 >= 64;
+            if (la != lb) return la;
+            if (fr[a].cluster != fr[b].cluster) return fr[a].cluster < fr[b].cluster;
+            return fr[a].seq < fr[b].seq;
+        });
+        std::vector<int> gs(nfr);
+        for (int k = 0; k < nfr; k++) gs[k] = fr[ord[k]].gslot;
+        const int n0 = E.S.n, nmap = (int)map.size() / 2;
+        if ((r = E.grow(n0 + nfr)) || (r = B.fgslot.reserve(nfr)) || (r = B.fidx.reserve(nfr)) ||
+            (r = B.fmap.reserve(map.size() + 2)) || (r = E.frag_cl.reserve(nfr)))
+            return r;
+        if ((r = h2d(c, B.fgslot.p, gs.data(), nfr * sizeof(int))) || (r = h2d(c, B.fidx.p, ord.data(), nfr * sizeof(int))) ||
+            (map.size() && (r = h2d(c, B.fmap.p, map.data(), map.size() * sizeof(long long)))))
+            return r;
+        k_frag_append<<<(nfr + 127) / 128, 128, 0, c->stream>>>(E.S, B.H, B.frags.p, B.fgslot.p, B.fidx.p, nfr, n0,
+                                                                B.fmap.p, nmap, E.frag_cl.p);
+        k_frag_ids<<<(n0 + 255) / 256, 256, 0, c->stream>>>(E.S, n0, B.fmap.p, nmap);
+        if ((r = cuda_status(cudaGetLastError()))) return r;
+        E.S.n = n0 + nfr;
+        E.frag_lo = n0;
+        E.frag_hi = n0 + nfr;
+        if ((r = cuda_status(cudaStreamSynchronize(c->stream)))) return r;
+    }
     int st = read_status(c);
     if (st) return st;
     return ncol;

@@ -72,6 +72,8 @@ struct BundleSmem {
     double c_ts[BMAXCL], c_ref[3 * BMAXCL], c_ed[BMAXCL], c_edd[BMAXCL];
     unsigned long long c_key[BMAXCL], c_red[4 * BMAXCL];
     long long c_pb[BMAXCL], c_work[BMAXCL], c_t0[BMAXCL];
+    long long c_label[BMAXCL], c_fragn[BMAXCL];  // id_cluster, fragments made (KOMINAMI)
+    int c_n0[BMAXCL], c_addn[BMAXCL], c_addg[BMAXCL];  // members at admission; new fragments (count, first slot)
     float c_thrf[BMAXCL], c_thrc[BMAXCL], c_E32[BMAXCL];
     int c_idx[BMAXCL], c_off[BMAXCL], c_n[BMAXCL], c_goff[BMAXCL], c_steps[BMAXCL], c_ncol[BMAXCL];
     int c_flags[BMAXCL], c_imp[BMAXCL], c_tar[BMAXCL];
@@ -82,7 +84,7 @@ struct BundleSmem {
     // claimed, not yet admitted clusters
     int pend_c[BCLAIM], pend_n[BCLAIM];
     int ws[BT / 32];
-    int used, ncl, fresh_k, fresh_p, n_sv, n_pend, i_pend, exhausted, any;
+    int used, ncl, fresh_k, fresh_p, n_sv, n_pend, i_pend, exhausted, any, grew;
 };
 
 __device__ __forceinline__ unsigned long long dbits(double x) {
@@ -423,7 +425,9 @@ __device__ void bundle_refill(const HardArgs &A, BundleSmem &B) {
             if (lane == 0) {
                 while (B.i_pend < B.n_pend) {
                     const int c = B.pend_c[B.i_pend], n = B.pend_n[B.i_pend];
-                    if (B.used + n > BCAP || B.ncl >= BMAXCL) break;
+                    // with fragmentation, keep room for the fragments of a collision
+                    const int room = (A.frag.a_frag > 0.) ? 2 * A.frag.n_frag_max : 0;
+                    if (B.used + n + room > BCAP || B.ncl >= BMAXCL) break;
                     const int k = B.ncl++;
                     B.c_idx[k] = c;
                     B.c_off[k] = B.used;
@@ -454,6 +458,10 @@ __device__ void bundle_load(const HardArgs &A, BundleSmem &B) {
         const V3 r0 = ld3(A.S.pos, A.members[goff]);
         B.c_ref[3 * k] = r0.x; B.c_ref[3 * k + 1] = r0.y; B.c_ref[3 * k + 2] = r0.z;
         B.c_steps[k] = 0; B.c_ncol[k] = 0; B.c_work[k] = 0;
+        B.c_label[k] = A.S.id_cluster[A.members[goff]];
+        B.c_fragn[k] = 0;
+        B.c_n0[k] = B.c_n[k];
+        B.c_addn[k] = 0;
         B.c_ed[k] = 0.; B.c_edd[k] = 0.;
         B.c_t0[k] = A.times ? global_ns() : 0;
         B.c_red[4 * k] = 0ULL;                 // max |x - ref| component
@@ -524,6 +532,69 @@ __device__ void bundle_load(const HardArgs &A, BundleSmem &B) {
 // member-parallel loop over the occupied slots
 #define FOR_SLOTS(p) for (int p = threadIdx.x; p < B.used; p += BT)
 #define FOR_CLUSTERS(k) for (int k = threadIdx.x; k < B.ncl; k += BT)
+
+// A cluster made fragments (KOMINAMI): its member range grows by them, the
+// clusters after it move up, and every slot is mirrored again from the
+// state of record (fragments are rare; owners are remapped).
+__device__ void bundle_grow(const HardArgs &A, BundleSmem &B) {
+    const Hard &H = A.H;
+    const int tid = threadIdx.x;
+    static_assert(BMAXCL <= BT, "one thread per bundle cluster");
+    const int add = (tid < B.ncl) ? B.c_addn[tid] : 0;
+    const int nn = (tid < B.ncl) ? B.c_n[tid] + add : 0;
+    int tot;
+    const int noff = bscan(nn, B.ws, tot);
+    constexpr int PER = BCAP / BT;
+    int mv_new[PER], mv_g[PER], mv_k[PER], mv_own[PER];
+    int my_old_n = 0, my_addg = 0;
+    if (tid < B.ncl) {
+        my_old_n = B.c_n[tid];
+        my_addg = B.c_addg[tid];
+    }
+    __syncthreads();
+    if (tot > BCAP) {  // no room: the fragments cannot be integrated here
+        if (tid == 0) atomicOr(A.status, ST_CLUSTER_TOO_BIG);
+        return;
+    }
+    if (tid < B.ncl) B.c_key[tid] = (unsigned long long)(unsigned)noff;  // new offsets, by cluster
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < PER; j++) {
+        const int p = tid + j * BT;
+        mv_new[j] = -1;
+        if (p < B.used) {
+            const int k = B.cl[p];
+            const int no = (int)B.c_key[k];
+            mv_new[j] = no + (p - B.c_off[k]);
+            mv_g[j] = B.gslot[p];
+            mv_k[j] = k;
+            mv_own[j] = (B.owner[p] >= 0) ? no + (B.owner[p] - B.c_off[k]) : -1;
+        }
+    }
+    __syncthreads();
+    if (tid < B.ncl) {
+        B.c_off[tid] = noff;
+        B.c_n[tid] = nn;
+        // fragments are smaller than the members the prefilter margins were
+        // set for: exact FP64 tests for this cluster from here on
+        if (add > 0) B.c_flags[tid] |= CF_EXACT;
+    }
+    if (tid == 0) B.used = tot;
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < PER; j++) {
+        if (mv_new[j] < 0) continue;
+        mirror_all(B, H, mv_new[j], mv_g[j], mv_k[j], true);
+        B.owner[mv_new[j]] = (short)mv_own[j];
+    }
+    if (tid < B.ncl)
+        for (int i = 0; i < add; i++) {
+            const int q = noff + my_old_n + i;
+            mirror_all(B, H, q, my_addg + i, tid, true);
+            B.owner[q] = -1;
+        }
+    __syncthreads();
+}
 
 // one block step of every cluster in the bundle (timeIntegrate_multi body,
 // src/hermite.h:224-479)
@@ -629,28 +700,47 @@ __device__ void bundle_step(const HardArgs &A, BundleSmem &B) {
     if (threadIdx.x == 0) B.any = 0;
     __syncthreads();
     // collisions: one thread per colliding cluster
+    if (threadIdx.x == 0) B.grew = 0;
+    __syncthreads();
     FOR_CLUSTERS(k) {
+        B.c_addn[k] = 0;
         if (!(B.c_flags[k] & CF_COL)) continue;
         B.any = 1;
         ColRec rec;
         double e1 = 0., e2 = 0.;
-        collide(P, H, B.gslot[B.c_imp[k]], B.gslot[B.c_tar[k]], e1, e2, rec);
+        const int o = B.c_off[k], n = B.c_n[k];
+        int fs[32];
+        FragCtx X{&A, &B.gslot[o], n, B.c_idx[k], B.c_label[k], &B.c_fragn[k], fs};
+        const int nf = collide(P, H, B.gslot[B.c_imp[k]], B.gslot[B.c_tar[k]], e1, e2, rec, &X);
         B.c_ed[k] += e1;
         B.c_edd[k] += e2;
         rec.cluster = B.c_idx[k];
         rec.seq = B.c_ncol[k]++;
-        rec.n = B.c_n[k];
+        rec.n = B.c_n0[k];
         const int slot = atomicAdd(A.n_cols, 1);
         if (slot < A.col_cap) A.cols[slot] = rec;
         else atomicOr(A.status, ST_QUEUE_OVERFLOW);
+        if (nf > 0) {
+            B.c_addn[k] = nf;
+            B.c_addg[k] = fs[0];  // a collision's fragments have consecutive slots
+            B.grew = 1;
+            for (int i = 0; i < nf; i++) A.frags[fs[i] - A.frag_base].n0 = B.c_n0[k];
+        }
         // twin owners (pool slots) from the merge lists
-        const int o = B.c_off[k], n = B.c_n[k], go = B.c_goff[k];
         for (int j = 0; j < n; j++) B.owner[o + j] = -1;
-        for (int j = 0; j < n; j++)
-            if (H.merged[go + j])
-                for (int t = H.tw_head[go + j], gg = 0; t >= 0 && gg < 4096; t = H.tw_next[t], gg++)
-                    if (t >= go && t < go + n) B.owner[o + (t - go)] = (short)(o + j);
+        for (int j = 0; j < n; j++) {
+            const int gj = B.gslot[o + j];
+            if (!H.merged[gj]) continue;
+            for (int t = H.tw_head[gj], gg = 0; t >= 0 && gg < 4096; t = H.tw_next[t], gg++)
+                for (int q = 0; q < n; q++)
+                    if (B.gslot[o + q] == t) {
+                        B.owner[o + q] = (short)(o + j);
+                        break;
+                    }
+        }
     }
+    __syncthreads();
+    if (B.grew) bundle_grow(A, B);
     __syncthreads();
     if (B.any) {
         FOR_SLOTS(p) {
@@ -708,7 +798,12 @@ __device__ void bundle_retire(const HardArgs &A, BundleSmem &B) {
     bundle_finalize(A, B, 0, nt, 2);
     // write back to FPGrav, with resetTime (src/hard.h:768-787)
     for (int i = tid; i < nt; i += BT) {
-        const int s = B.tgt[i], g = B.gslot[s], k = B.cl[s], idx = A.members[g];
+        const int s = B.tgt[i], g = B.gslot[s], k = B.cl[s];
+        if (g >= A.frag_base) {  // a fragment: joins the system after the launch
+            A.frags[g - A.frag_base].n_cl = B.c_n[k];
+            continue;
+        }
+        const int idx = A.members[g];
         st3(A.S.pos, idx, ld3(H.pos, g)); st3(A.S.vel, idx, ld3(H.vel, g));
         st3(A.S.acc_s, idx, ld3(H.acc_s, g)); st3(A.S.jerk_s, idx, ld3(H.jerk_s, g));
         st3(A.S.acc_d, idx, ld3(H.acc_d, g)); st3(A.S.jerk_d, idx, ld3(H.jerk_d, g));
@@ -740,6 +835,8 @@ __device__ void bundle_retire(const HardArgs &A, BundleSmem &B) {
     double t_ref0 = 0., t_ref1 = 0., t_ref2 = 0., t_ed = 0., t_edd = 0.;
     long long t_work = 0, t_t0 = 0;
     float t_thrf = 0.f, t_thrc = 0.f, t_E = 0.f;
+    long long t_label = 0, t_fragn = 0;
+    int t_n0 = 0;
     if (tid < B.ncl) {
         keep = !(B.c_flags[tid] & CF_FIN);
         t_idx = B.c_idx[tid]; t_n = B.c_n[tid]; t_goff = B.c_goff[tid];
@@ -747,6 +844,7 @@ __device__ void bundle_retire(const HardArgs &A, BundleSmem &B) {
         t_ref0 = B.c_ref[3 * tid]; t_ref1 = B.c_ref[3 * tid + 1]; t_ref2 = B.c_ref[3 * tid + 2];
         t_ed = B.c_ed[tid]; t_edd = B.c_edd[tid]; t_work = B.c_work[tid]; t_t0 = B.c_t0[tid];
         t_thrf = B.c_thrf[tid]; t_thrc = B.c_thrc[tid]; t_E = B.c_E32[tid];
+        t_label = B.c_label[tid]; t_fragn = B.c_fragn[tid]; t_n0 = B.c_n0[tid];
     }
     static_assert(BMAXCL <= BT, "one thread per bundle cluster");
     nk = bscan(keep, B.ws, nkeep);
@@ -782,6 +880,7 @@ __device__ void bundle_retire(const HardArgs &A, BundleSmem &B) {
         B.c_ref[3 * nk] = t_ref0; B.c_ref[3 * nk + 1] = t_ref1; B.c_ref[3 * nk + 2] = t_ref2;
         B.c_ed[nk] = t_ed; B.c_edd[nk] = t_edd; B.c_work[nk] = t_work; B.c_t0[nk] = t_t0;
         B.c_thrf[nk] = t_thrf; B.c_thrc[nk] = t_thrc; B.c_E32[nk] = t_E;
+        B.c_label[nk] = t_label; B.c_fragn[nk] = t_fragn; B.c_n0[nk] = t_n0;
     }
     __syncthreads();
 #pragma unroll

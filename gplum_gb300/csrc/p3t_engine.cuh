@@ -17,8 +17,14 @@ struct Engine {
     DevBuf<double> epart, et;
     DevBuf<int> icnt;
     DevBuf<char> compact_tmp;
+    // KOMINAMI fragments appended by the last hard part: particles
+    // [frag_lo, frag_hi) with their clusters in frag_cl
+    DevBuf<int32_t> frag_cl;
+    int frag_lo = 0, frag_hi = 0;
+    long long id_next = 0;  // next particle id (src/main_p3t.cpp:233,295-305)
 
     int ensure(int n);
+    int grow(int n);  // capacity for n bodies, keeping the state
     Params params() const;
     int load(int n, const long long *id, const double *mass, const double *r_planet, const double *f,
              const double *pos, const double *vel);

@@ -120,6 +120,13 @@ class GpuSystem:
             raise RuntimeError(f"p3t_hard failed with status {nc}")
         return cols[:2 * min(nc, col_cap)].reshape(-1, 2), ed
 
+    def set_fragmentation(self, a_frag, n_frag=10, m_min=9.426627927538057e-12, seed=0):
+        """KOMINAMI fragmentation of the collision outcome (a_frag = 0: off)."""
+        self._chk(self.lib.p3t_set_fragmentation(a_frag, n_frag, m_min, seed), "p3t_set_fragmentation")
+
+    def id_next(self):
+        return int(self.lib.p3t_id_next())
+
     def tree_soft(self):
         """Device octree + interaction lists from the current state, then the
         soft force (replaces a host build_lists + soft_force pair)."""

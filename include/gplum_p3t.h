@@ -181,6 +181,20 @@ int p3t_set_hard_tiers(int warp_min, int cta_min);
  * (256 members) run one per CTA.  1: the size tiers of p3t_set_hard_tiers.
  * Both give identical results.  No counterpart in GPLUM's interface. */
 int p3t_set_hard_mode(int mode);
+/* KOMINAMI fragmentation of the collision outcome (src/collisionB.h:7-93;
+ * Collision::a_frag, N_frag, Collision0::m_min of parameter.dat).  a_frag = 0
+ * (the default) is perfect accretion.  A collision makes
+ * n = min(N_frag, floor(a_frag m_imp / m_min)) fragments (none if n < 2) of
+ * total mass a_frag m_imp on a circle around the merged pair; they join the
+ * particle system after the hard launch with new ids (id_next onwards) in
+ * the reference's order.  GPLUM draws the circle's phase from drand48 in
+ * OpenMP order; here it is a counter-based draw keyed by (tree step,
+ * impactor id, target id, seed).  Needs the bundle form of the hard launch
+ * (p3t_set_hard_mode(0)); clusters above its capacity cannot fragment (status
+ * bit 16). */
+int p3t_set_fragmentation(double a_frag, int n_frag, double m_min, unsigned long long seed);
+/* The next particle id the system will hand out (src/main_p3t.cpp:233). */
+long long p3t_id_next(void);
 
 /* ---- learned work-queue order (no counterpart in GPLUM) ------------------
  * A 4-32-32-1 FP32 MLP (tanh) predicts log2(1 + block steps) of each cluster

@@ -92,6 +92,17 @@ class CpuSystem:
     def f(self, name):
         return getattr(self.lib, f"{self.kind}_{name}")
 
+    def set_fragmentation(self, a_frag, n_frag=10, m_min=9.426627927538057e-12, seed=0):
+        """KOMINAMI fragmentation in the restatement, with the keyed phase
+        draw the device uses (a_frag = 0: off)."""
+        assert self.kind == "orc"
+        self.lib.orc_set_frag(ctypes.c_double(a_frag), ctypes.c_int(n_frag), ctypes.c_double(m_min), ctypes.c_int(0),
+                              ctypes.c_ulonglong(seed))
+
+    def id_next(self):
+        self.lib.orc_id_next.restype = ctypes.c_longlong
+        return int(self.lib.orc_id_next())
+
     def load(self, disk):
         n = len(disk["mass"])
         self._keep = [np.ascontiguousarray(disk[k]) for k in ("id", "mass", "r_planet", "f", "pos", "vel")]
