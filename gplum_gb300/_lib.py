@@ -72,6 +72,7 @@ SIGNATURES = {
     "p3t_hard_integrate": (I, [I]),
     "p3t_hard_fetch": (I, [I, VP, VP]),
     "p3t_correct_and_search": (I, [I]),
+    "p3t_remove_out_of_boundary": (I, [D, D, VP]),
     "p3t_state_tree_soft": (I, [D, I, I]),
     "p3t_tree_lists_counts": (I, [VP]),
     "p3t_tree_lists_get": (I, [VP] * 7),

@@ -790,7 +790,13 @@ int Engine::merge(double *edisp) {
     *edisp = e;
     frag_lo = frag_hi = n;
     if (nk == n) return 0;
-    // order-preserving compaction of every field through a scratch copy
+    return compact(n, nk);
+}
+
+// order-preserving compaction of every field to the bodies with keep = 1
+// (kpos: their new positions, nk: how many)
+int Engine::compact(int n, int nk) {
+    int r = 0;
     if ((r = compact_tmp.reserve((size_t)n * 3 * sizeof(double)))) return r;
     auto comp = [&](auto *fld, int w) -> int {
         using T2 = std::remove_pointer_t<decltype(fld)>;
@@ -812,6 +818,65 @@ int Engine::merge(double *edisp) {
     n_clusters = 0;
     frag_lo = frag_hi = nk;
     return cuda_status(cudaStreamSynchronize(c->stream));
+}
+
+// removeParticlesOutOfBoundary, src/func.h:209-355
+__global__ void k_remove_flag(State S, double rmax2, double rmin2, int32_t *keep, int32_t *gone) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.n) return;
+    const V3 x = ld3(S.pos, i);
+    const double pos2 = dot(x, x);
+    const int out = (pos2 > rmax2 || pos2 < rmin2) ? 1 : 0;
+    keep[i] = 1 - out;
+    gone[i] = out;
+}
+__global__ void k_remove_list(const int32_t *gone, const int32_t *gpos, int n, int32_t *list) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && gone[i]) list[gpos[i]] = i;
+}
+// the energy the removed bodies take with them, in list (index) order
+__global__ void k_remove_energy(State S, Params P, const int32_t *list, int nr, double *out) {
+    if (threadIdx.x || blockIdx.x) return;
+    double e = 0.;
+    for (int a = 0; a < nr; a++) {
+        const int i = list[a];
+        const double massi = S.mass[i];
+        const V3 veli = ld3(S.vel, i);
+        e -= dot(0.5 * massi * veli, veli);
+        e -= massi * S.phi_s[i];
+        e -= massi * S.phi_d[i];
+        e -= massi * S.phi[i];
+        for (int b = 0; b < a; b++) {
+            const int j = list[b];
+            if (S.id[i] != S.id[j]) {
+                const V3 dr = ld3(S.pos, i) - ld3(S.pos, j);
+                const double rinv = 1. / sqrt(dot(dr, dr) + P.eps2);
+                e += -massi * S.mass[j] * rinv;
+            }
+        }
+    }
+    *out = e;
+}
+
+int Engine::remove(double r_max, double r_min, double *edisp, int *n_removed) {
+    const int n = S.n;
+    int r = 0;
+    if ((r = keep.reserve(n)) || (r = kpos.reserve(n)) || (r = tflag.reserve(n)) || (r = tpos.reserve(n)) ||
+        (r = et.reserve(2)))
+        return r;
+    k_remove_flag<<<nb(n), 256, 0, c->stream>>>(S, r_max * r_max, r_min * r_min, keep.p, tflag.p);
+    int32_t nr = 0;
+    if ((r = scan(tflag.p, tpos.p, n, &nr))) return r;
+    *n_removed = nr;
+    *edisp = 0.;
+    if (nr == 0) return 0;
+    if ((r = members_tmp.reserve(std::max(n, nr)))) return r;
+    k_remove_list<<<nb(n), 256, 0, c->stream>>>(tflag.p, tpos.p, n, members_tmp.p);
+    k_remove_energy<<<1, 32, 0, c->stream>>>(S, params(), members_tmp.p, nr, et.p);
+    if ((r = d2h(c, edisp, et.p, sizeof(double)))) return r;
+    int32_t nk = 0;
+    if ((r = scan(keep.p, kpos.p, n, &nk))) return r;
+    return compact(n, nk);
 }
 
 }  // namespace p3t
@@ -975,6 +1040,13 @@ int p3t_correct(int initial) {
 }
 
 int p3t_correct_and_search(int initial) { return p3t_correct(initial); }
+
+int p3t_remove_out_of_boundary(double r_max, double r_min, double *edisp) {
+    if (!g_eng.c) return -(int)cudaErrorNoDevice;
+    int nr = 0;
+    int r = g_eng.remove(r_max, r_min, edisp, &nr);
+    return r ? r : nr;
+}
 
 int p3t_neighbor_counts(int *ngb_tot, int *with_ngb) {
     Context *c = ctx_get(0);

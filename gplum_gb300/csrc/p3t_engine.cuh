@@ -36,6 +36,8 @@ struct Engine {
     int energy(double *out5);
     int cutoff_radii();
     int merge(double *edisp);
+    int remove(double r_max, double r_min, double *edisp, int *n_removed);
+    int compact(int n, int nk);
     int scan(const int32_t *in, int32_t *out, int n, int32_t *total);
 };
 

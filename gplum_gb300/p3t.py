@@ -182,6 +182,14 @@ class GpuSystem:
         self._chk(self.lib.p3t_merge(ctypes.byref(e)), "p3t_merge")
         return e.value
 
+    def remove(self, r_max, r_min):
+        """removeParticlesOutOfBoundary: (bodies removed, energy they took)."""
+        e = ctypes.c_double(0.0)
+        n = self.lib.p3t_remove_out_of_boundary(r_max, r_min, ctypes.byref(e))
+        if n < 0:
+            raise RuntimeError(f"p3t_remove_out_of_boundary failed with status {n}")
+        return n, e.value
+
     def counts(self):
         a, b = ctypes.c_int(), ctypes.c_int()
         self._chk(self.lib.p3t_neighbor_counts(ctypes.byref(a), ctypes.byref(b)), "p3t_neighbor_counts")

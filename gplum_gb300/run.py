@@ -29,8 +29,9 @@ def startup(g, disk):
     return g.energy()
 
 
-def step(g, istep, reset_step=1024):
-    """One tree step (src/main_p3t.cpp:423-717).  Returns (collision pairs,
+def step(g, istep, reset_step=1024, r_max=40.0, r_min=0.1):
+    """One tree step (src/main_p3t.cpp:423-717; r_max and r_min as in
+    parameter.dat, defaults src/read.h:111-112).  Returns (collision pairs,
     energy after the step, energy dissipated in this step)."""
     g.kick()
     g.cluster()
@@ -42,7 +43,9 @@ def step(g, istep, reset_step=1024):
     e = g.energy()
     if len(cols):
         edisp += g.merge(len(cols))
-    if len(cols) or istep % reset_step == reset_step - 1:
+    n_rem, e_rem = g.remove(r_max, r_min)
+    edisp += e_rem
+    if len(cols) or n_rem or istep % reset_step == reset_step - 1:
         g.prepare()
         g.tree_soft()
         g.correct(True)

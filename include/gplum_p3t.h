@@ -243,6 +243,10 @@ int p3t_energy(double *out5);
 /* MergeParticle, src/func.h:160-207 (order-preserving removal of the merged
  * twins); adds the dissipated energy to *edisp. */
 int p3t_merge(double *edisp);
+/* removeParticlesOutOfBoundary, src/func.h:209-355: bodies with |x| above
+ * r_max or below r_min leave the system (order-preserving); *edisp receives
+ * the energy they take with them.  Returns how many left. */
+int p3t_remove_out_of_boundary(double r_max, double r_min, double *edisp);
 
 /* ---- soft force without allocation ---------------------------------------------
  * No counterpart in GPLUM.  For callers that cannot allocate device memory

@@ -99,6 +99,14 @@ class CpuSystem:
         self.lib.orc_set_frag(ctypes.c_double(a_frag), ctypes.c_int(n_frag), ctypes.c_double(m_min), ctypes.c_int(0),
                               ctypes.c_ulonglong(seed))
 
+    def remove(self, r_max, r_min):
+        """removeParticlesOutOfBoundary: (bodies removed, energy they took)."""
+        e = ctypes.c_double(0.0)
+        fn = self.f("remove")
+        fn.restype = ctypes.c_int
+        n = fn(ctypes.c_double(r_max), ctypes.c_double(r_min), ctypes.byref(e))
+        return n, e.value
+
     def id_next(self):
         self.lib.orc_id_next.restype = ctypes.c_longlong
         return int(self.lib.orc_id_next())

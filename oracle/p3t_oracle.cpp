@@ -1627,6 +1627,46 @@ void orc_energy(double *out) {  // Energy::calcEnergy, src/energy.h:29-63
     out[1] = ek; out[2] = es; out[3] = ep; out[4] = ed;
     out[0] = ek + es + (ep + ed);
 }
+// removeParticlesOutOfBoundary, src/func.h:209-355: bodies with |x|^2 above
+// r_max^2 or below r_min^2 leave; their kinetic and potential energies and
+// their mutual potential go to the dissipated energy (list in index order,
+// the single-thread order of the reference's critical section).
+int orc_remove(double r_max, double r_min, double *edisp) {
+    const double rmax2 = r_max * r_max, rmin2 = r_min * r_min;
+    std::vector<int> rl;
+    for (int i = 0; i < (int)S.size(); i++) {
+        const double pos2 = dot(S[i].pos, S[i].pos);
+        if (pos2 > rmax2 || pos2 < rmin2) rl.push_back(i);
+    }
+    double e = 0.;
+    for (size_t i = 0; i < rl.size(); i++) {
+        const Ptcl &a = S[rl[i]];
+        const double massi = a.mass;
+        const V3 veli = a.vel;
+        e -= dot(0.5 * massi * veli, veli);
+        e -= massi * a.phi_s;
+        e -= massi * a.phi_d;
+        e -= massi * a.phi;
+        for (size_t j = 0; j < i; j++) {
+            const Ptcl &b = S[rl[j]];
+            if (a.id != b.id) {
+                const V3 dr = a.pos - b.pos;
+                const double rinv = 1. / std::sqrt(dot(dr, dr) + P.eps2);
+                e += -massi * b.mass * rinv;
+            }
+        }
+    }
+    if (!rl.empty()) {
+        std::vector<char> gone(S.size(), 0);
+        for (int i : rl) gone[i] = 1;
+        size_t w = 0;
+        for (size_t r = 0; r < S.size(); r++)
+            if (!gone[r]) S[w++] = S[r];
+        S.resize(w);
+    }
+    *edisp += e;
+    return (int)rl.size();
+}
 // MergeParticle, src/func.h:160-207 (order-preserving removal)
 void orc_merge(int n_col, double *edisp) {
     (void)n_col;

@@ -426,6 +426,11 @@ void ref_energy(double *out) {
 
 // MergeParticle (src/func.h:160-207): folds dead twins into their targets.
 void ref_merge(int n_col, double *edisp) { MergeParticle(g_pp, n_col, *edisp); }
+// removeParticlesOutOfBoundary (src/func.h:209-355); its report goes nowhere
+int ref_remove(double r_max, double r_min, double *edisp) {
+    std::ofstream sink("/dev/null");
+    return removeParticlesOutOfBoundary(g_pp, *edisp, r_max, r_min, sink);
+}
 
 }  // extern "C"
 

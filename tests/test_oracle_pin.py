@@ -54,3 +54,22 @@ def test_steps_match_reference_with_collisions():
         for k in ("pos", "vel", "acc", "acc_d", "jerk_d", "dt", "mass", "id_cluster", "number"):
             np.testing.assert_array_equal(ref.get(k), orc.get(k), err_msg=f"step {st} {k}")
     assert ncol > 0
+
+
+def test_out_of_boundary_removal_matches_reference():
+    """removeParticlesOutOfBoundary (src/func.h:209-355): same bodies leave,
+    same energy bookkeeping, bit for bit."""
+    P = P3TParams()
+    d = make_disk(1500, 1e-9, 0.95, 1.05, ecc_hill=3.0, inc_hill=1.5, seed=41)
+    out = {}
+    for kind in ("ref", "orc"):
+        s = H.CpuSystem(kind, P)
+        H.p3t_init(s, d, H.tree_lists_fn(P))
+        r = np.sqrt((s.get("pos") ** 2).sum(1))
+        r_min, r_max = np.quantile(r, 0.02), np.quantile(r, 0.97)
+        n, e = s.remove(r_max, r_min)
+        out[kind] = (n, e, s.get("id"), s.get("pos"))
+    assert out["ref"][0] == out["orc"][0] > 50
+    assert out["ref"][1] == out["orc"][1]
+    np.testing.assert_array_equal(out["orc"][2], out["ref"][2])
+    np.testing.assert_array_equal(out["orc"][3], out["ref"][3])

@@ -181,3 +181,23 @@ def test_isolated_bodies_take_the_sun_hermite(gpu):
             s.correct(False)
             s.kick()
         sync_state(orc, g)
+
+
+def test_out_of_boundary_removal(gpu):
+    """removeParticlesOutOfBoundary on the device: the same bodies leave and
+    take the same energy (to 1e-12) as in the restatement."""
+    P = P3TParams()
+    d = make_disk(3000, 1e-9, 0.95, 1.05, ecc_hill=3.0, inc_hill=1.5, seed=42)
+    orc, g, lf = both(d, P)
+    H.p3t_init(orc, d, lf)
+    H.p3t_init(g, d, lf)
+    sync_state(orc, g)
+    r = np.sqrt((orc.get("pos") ** 2).sum(1))
+    r_min, r_max = np.quantile(r, 0.03), np.quantile(r, 0.96)
+    n1, e1 = orc.remove(r_max, r_min)
+    n2, e2 = g.remove(r_max, r_min)
+    assert n1 == n2 > 100
+    assert abs(e2 - e1) <= 1e-12 * abs(e1)
+    np.testing.assert_array_equal(g.get("id"), orc.get("id"))
+    np.testing.assert_array_equal(g.get("pos"), orc.get("pos"))
+    assert g.n == orc.n == 3000 - n1
