@@ -307,6 +307,9 @@ def gpu_arm(args, rank, world):
     flops = EPEP_FLOPS * n_epep + EPSP_FLOPS * n_epsp
     lib = _lib.host_lib()
 
+    from gplum_gb300 import autotune
+
+    tuning = autotune.load(lib)  # work split chosen by gplum_gb300/autotune.py on this workload
     sf = soft.SoftForce(P, precision=0)
     sf.upload_particles(epj)
     sf.upload_lists(L)
@@ -393,6 +396,7 @@ def gpu_arm(args, rank, world):
         "e2e": {"value": 1.0 / float(np.median(e2e)), "unit": "steps/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": args.steps,
+        "soft_tiles": tuning["soft_tiles"] if tuning else [128, 64, 32],
         "clocks": clocks,
     }
     if not args.skip_step:

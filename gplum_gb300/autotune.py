@@ -1,0 +1,139 @@
+"""Autotuner for the launch shapes of the hot path.
+
+Two choices are made by measurement on the live workload instead of fixed in
+code:
+
+* the soft kernel's work split by i-group size (p3t_set_soft_tiles: above
+  t_ipt2 members two i-particles per thread, above t_s1 one, above t_s2 the
+  j lists split two ways, else four) -- timed on the 1,048,576-body soft-force
+  disk (0.5-1.5 AU, m = 1e-10, theta = 0.5, n_group_limit = 256);
+* the one-cluster-per-team form's size cutoffs of the hard launch
+  (p3t_set_hard_tiers: clusters of >= cta_min members one per CTA, >= warp_min
+  one per warp, smaller one per thread) -- timed from one restored state of the
+  1,048,576-body hard-part disk.  (The default bundle form has no cutoffs; its
+  queue order comes from the learned cost model, gplum_gb300/scheduler.py.)
+
+    python -m gplum_gb300.autotune --out gplum_gb300/tuning.json
+
+Every candidate gives the same neighbour results and forces equal to
+rounding (soft) or bit-identical results (hard); only the time differs.
+"""
+import argparse
+import json
+import os
+import time
+
+import numpy as np
+
+from . import _lib
+
+TUNING = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning.json")
+SOFT_GRID = [(a, b, c) for a in (64, 96, 128) for b in (32, 48, 64) for c in (0, 16, 32) if c <= b <= a]
+TIER_GRID = [(w, t) for w in (2, 4, 8, 16) for t in (32, 64, 128, 256)]
+
+
+def _timed(lib, fn, reps):
+    ts = []
+    for _ in range(reps):
+        lib.p3t_synchronize()
+        t0 = time.perf_counter()
+        fn()
+        lib.p3t_synchronize()
+        ts.append(time.perf_counter() - t0)
+    return float(np.median(ts))
+
+
+def tune_soft(lib, run, grid=SOFT_GRID, reps=5):
+    """Times `run` (one soft-force launch on resident lists) for each work
+    split; installs the fastest.  Returns (best, {split: ms})."""
+    table = {}
+    for cfg in grid:
+        _lib.check(lib.p3t_set_soft_tiles(*cfg), "p3t_set_soft_tiles")
+        run()
+        table[cfg] = 1e3 * _timed(lib, run, reps)
+    best = min(table, key=table.get)
+    _lib.check(lib.p3t_set_soft_tiles(*best), "p3t_set_soft_tiles")
+    return best, table
+
+
+def tune_tiers(g, istep=1, grid=TIER_GRID):
+    """Times the one-cluster-per-team hard launch from one restored state for
+    each (warp_min, cta_min); leaves the fastest installed (and the bundle
+    form selected).  Returns (best, {cutoffs: ms})."""
+    lib = g.lib
+    _lib.check(lib.p3t_state_snapshot(0), "p3t_state_snapshot")
+    table = {}
+    lib.p3t_set_hard_mode(1)
+    try:
+        for wm, cm in grid:
+            _lib.check(lib.p3t_set_hard_tiers(wm, cm), "p3t_set_hard_tiers")
+            _lib.check(lib.p3t_state_snapshot(1), "p3t_state_snapshot")
+            table[(wm, cm)] = 1e3 * _timed(lib, lambda: g.hard(istep), 1)
+    finally:
+        lib.p3t_set_hard_mode(0)
+        lib.p3t_state_snapshot(1)
+    best = min(table, key=table.get)
+    _lib.check(lib.p3t_set_hard_tiers(*best), "p3t_set_hard_tiers")
+    return best, table
+
+
+def load(lib=None, path=TUNING):
+    """Installs a tuning file's choices; returns them (None without a file)."""
+    if not os.path.exists(path):
+        return None
+    lib = lib or _lib.host_lib()
+    t = json.load(open(path))
+    if "soft_tiles" in t:
+        _lib.check(lib.p3t_set_soft_tiles(*t["soft_tiles"]), "p3t_set_soft_tiles")
+    if "hard_tiers" in t:
+        _lib.check(lib.p3t_set_hard_tiers(*t["hard_tiers"]), "p3t_set_hard_tiers")
+    return t
+
+
+def main():
+    from .disk import P3TParams, disk_1m_hard, disk_1m_soft
+    from .p3t import GpuSystem
+    from .radii import cutoff_radii
+    from .soft import SoftForce, epj_records
+    from .tree import build_lists
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--out", default=TUNING)
+    args = ap.parse_args()
+    P = P3TParams(n_group_limit=256)
+    # soft: resident lists of the soft-force disk
+    d = disk_1m_soft()
+    r_out, r_search, _ = cutoff_radii(d["pos"], d["vel"], d["mass"], P)
+    epj = epj_records(d["pos"], d["vel"], d["mass"], r_out, r_search, ids=d["id"])
+    L = build_lists(d["pos"], d["mass"], r_search, P.theta, P.n_leaf_limit, P.n_group_limit)
+    sf = SoftForce(P, precision=0)
+    sf.upload_particles(epj)
+    sf.upload_lists(L)
+    lib = _lib.host_lib()
+    soft_best, soft_table = tune_soft(lib, lambda: sf.run(emit_candidates=True))
+    # hard: tier cutoffs of the per-team form on the hard-part disk
+    d = disk_1m_hard()
+    g = GpuSystem(P)
+    g.load(d)
+    g.set_r_planet()
+    g.prepare()
+    for _ in range(2):
+        g.tree_soft()
+        g.correct(True)
+    g.kick()
+    g.cluster()
+    hard_best, hard_table = tune_tiers(g)
+    out = {"soft_tiles": list(soft_best),
+           "soft_ms": {",".join(map(str, k)): v for k, v in soft_table.items()},
+           "hard_tiers": list(hard_best),
+           "hard_ms": {",".join(map(str, k)): v for k, v in hard_table.items()},
+           "workloads": {"soft": "1048576-body disk 0.5-1.5 AU, m=1e-10, theta=0.5, n_group_limit=256",
+                         "hard": "1048576-body hard-part disk 0.95-1.05 AU, m=7e-11, rms e=6h, rms i=3h"}}
+    json.dump(out, open(args.out, "w"), indent=1)
+    print(json.dumps({"soft_tiles": out["soft_tiles"], "soft_ms_best": soft_table[soft_best],
+                      "soft_ms_default": soft_table.get((128, 64, 32)), "hard_tiers": out["hard_tiers"],
+                      "hard_ms_best": hard_table[hard_best], "hard_ms_default": hard_table.get((8, 64))}))
+
+
+if __name__ == "__main__":
+    main()

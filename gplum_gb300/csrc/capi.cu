@@ -159,6 +159,9 @@ SoftArgs make_args(Context *c, DevSet &d, int n_group, int n_ptcl, int n_spj, bo
     A.cand = d.cand.p;
     A.cand_cap = c->cand_cap;
     A.status = c->status;
+    A.t_ipt2 = c->tiles[0];
+    A.t_s1 = c->tiles[1];
+    A.t_s2 = c->tiles[2];
     return A;
 }
 
@@ -215,6 +218,15 @@ int p3t_set_params(const double *params21) {
     CTX_OR_FAIL(c);
     std::memcpy(c->params, params21, 21 * sizeof(double));
     c->params_version++;
+    return 0;
+}
+
+int p3t_set_soft_tiles(int t_ipt2, int t_s1, int t_s2) {
+    CTX_OR_FAIL(c);
+    if (t_s2 < 0 || t_s2 > 32 || t_s1 < t_s2 || t_s1 > 64 || t_ipt2 < t_s1 || t_ipt2 > 128) return ST_BAD_INDEX;
+    c->tiles[0] = t_ipt2;
+    c->tiles[1] = t_s1;
+    c->tiles[2] = t_s2;
     return 0;
 }
 

@@ -30,6 +30,11 @@ struct SoftArgs {
     int *cand;        // optional [n_iptcl x cand_cap] table of j indices
     int cand_cap;
     int *status;
+    // work split of an i-group of ni members over the CTA's 128 threads:
+    // ni > t_ipt2: 2 i per thread; > t_s1: 1 i per thread; > t_s2: the j list
+    // split 2 ways; else 4 ways (0 <= t_s2 <= 32, t_s2 <= t_s1 <= 64,
+    // t_s1 <= t_ipt2 <= 128; 0 = the defaults 128, 64, 32)
+    int t_ipt2, t_s1, t_s2;
 };
 
 cudaError_t launch_pack_epj(const EPJRec *in, int n, SoftPtcl *out, double *mass, double *r_out, double *r_search,

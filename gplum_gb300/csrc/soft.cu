@@ -6,7 +6,8 @@
 // group origin once (FP64 subtraction, then the FP32 rounding the functor
 // applies) and then reused by every i of the group.
 //
-// Work split per CTA, by group size ni (uniform per CTA):
+// Work split per CTA, by group size ni (uniform per CTA; the thresholds are
+// SoftArgs::t_ipt2/t_s1/t_s2, set by the autotuner, defaults shown):
 //   ni > 128 : 2 i per thread           ni in (64,128] : 1 i per thread
 //   ni in (32,64] : two sub-blocks of 64 threads, each taking half of every
 //   j tile      ni <= 32 : four sub-blocks of 32 threads, a quarter each.
@@ -295,11 +296,11 @@ __global__ void __launch_bounds__(SB, 4) soft_mixed_kernel(SoftArgs A) {
     // n_group_limit <= 256) run as consecutive chunks over the same lists
     for (int ib = 0; ib < ni_all; ib += 2 * SB) {
         const int ni = min(2 * SB, ni_all - ib);
-        if (ni > 128)
+        if (ni > A.t_ipt2)
             group_mixed<1, 2, EMIT>(A, g, ib, ni, sa, sb, sc, sidx, scnt, redf, redi);
-        else if (ni > 64)
+        else if (ni > A.t_s1)
             group_mixed<1, 1, EMIT>(A, g, ib, ni, sa, sb, sc, sidx, scnt, redf, redi);
-        else if (ni > 32)
+        else if (ni > A.t_s2)
             group_mixed<2, 1, EMIT>(A, g, ib, ni, sa, sb, sc, sidx, scnt, redf, redi);
         else
             group_mixed<4, 1, EMIT>(A, g, ib, ni, sa, sb, sc, sidx, scnt, redf, redi);
@@ -481,11 +482,11 @@ __global__ void __launch_bounds__(SB, 2) soft_f64_kernel(SoftArgs A) {
     const int ni_all = A.i_off[g + 1] - A.i_off[g];
     for (int ib = 0; ib < ni_all; ib += 2 * SB) {
         const int ni = min(2 * SB, ni_all - ib);
-        if (ni > 128)
+        if (ni > A.t_ipt2)
             group_f64<1, 2, EMIT>(A, g, ib, ni, da, db, dc, dids, sidx, scnt, redd, redi);
-        else if (ni > 64)
+        else if (ni > A.t_s1)
             group_f64<1, 1, EMIT>(A, g, ib, ni, da, db, dc, dids, sidx, scnt, redd, redi);
-        else if (ni > 32)
+        else if (ni > A.t_s2)
             group_f64<2, 1, EMIT>(A, g, ib, ni, da, db, dc, dids, sidx, scnt, redd, redi);
         else
             group_f64<4, 1, EMIT>(A, g, ib, ni, da, db, dc, dids, sidx, scnt, redd, redi);
@@ -561,8 +562,14 @@ cudaError_t launch_pack_epj(const EPJRec *in, int n, SoftPtcl *out, double *mass
     return cudaGetLastError();
 }
 
-cudaError_t launch_soft(const SoftArgs &A, int precision, bool emit, cudaStream_t st) {
+cudaError_t launch_soft(const SoftArgs &Ain, int precision, bool emit, cudaStream_t st) {
+    SoftArgs A = Ain;
     if (A.n_group <= 0) return cudaSuccess;
+    if (A.t_ipt2 <= 0 && A.t_s1 <= 0 && A.t_s2 <= 0) {
+        A.t_ipt2 = 128;
+        A.t_s1 = 64;
+        A.t_s2 = 32;
+    }
     if (precision == 0) {
         if (emit)
             soft_mixed_kernel<true><<<A.n_group, SB, 0, st>>>(A);

@@ -42,6 +42,13 @@ int p3t_set_params(const double *params21);
  * cand_cap = neighbour-candidate slots per particle for the device-side
  * correction (default 64). */
 int p3t_set_options(int precision, int trace_mode, int cand_cap);
+/* Work split of the soft kernel by i-group size ni: ni > t_ipt2 two
+ * i-particles per thread, > t_s1 one per thread, > t_s2 the j lists split
+ * two ways, else four (0 <= t_s2 <= 32 <= ..., t_s2 <= t_s1 <= 64,
+ * t_s1 <= t_ipt2 <= 128; defaults 128, 64, 32).  Set by the autotuner
+ * (gplum_gb300/autotune.py); forces agree to rounding across settings, the
+ * neighbour fields bit for bit. */
+int p3t_set_soft_tiles(int t_ipt2, int t_s1, int t_s2);
 /* The library's CUDA stream (cudaStream_t) for callers that order their own
  * work or timing events after the library's launches. */
 void *p3t_stream(void);

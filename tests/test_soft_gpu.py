@@ -179,3 +179,30 @@ def test_host_one_call_equals_resident(gpu):
     sf.upload_lists(L)
     sf.run()
     assert a.tobytes() == sf.download().tobytes()
+
+
+@pytest.mark.parametrize("tiles", [(0, 0, 0), (64, 32, 16), (128, 64, 0)])
+def test_work_splits_agree(gpu, tiles):
+    """Every work split the autotuner may choose gives the same neighbour
+    fields and forces equal to rounding (sub-block partial sums combine in a
+    different grouping)."""
+    P, d, s = prepared_state(n=20000, seed=9, ecc_hill=3.0, inc_hill=1.5, params=P3TParams(n_group_limit=256))
+    epi, epj = records(s)
+    L = lists_for(s, P)
+    sf = soft.SoftForce(P, precision=0)
+    sf.upload_particles(epj)
+    sf.upload_lists(L)
+    lib = sf.lib
+    try:
+        lib.p3t_set_soft_tiles(128, 64, 32)
+        sf.run(emit_candidates=False)
+        ref = sf.download().copy()
+        assert lib.p3t_set_soft_tiles(*tiles) == 0
+        sf.run(emit_candidates=False)
+        got = sf.download()
+    finally:
+        lib.p3t_set_soft_tiles(128, 64, 32)
+    for k in ("number", "rank", "id_max", "id_min"):
+        np.testing.assert_array_equal(got[k], ref[k])
+    assert rel_err(got["acc"].astype(np.float64), ref["acc"].astype(np.float64)).max() < 1e-6
+    assert lib.p3t_set_soft_tiles(40, 64, 32) != 0  # invalid: t_ipt2 < t_s1
