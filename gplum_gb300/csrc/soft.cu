@@ -100,6 +100,23 @@ __device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, in
     if (EMIT) {
         for (int t = tid; t < ni; t += SB) scnt[t] = 0;
     }
+    // Screen prefilter.  The force's r^2 (residue-corrected displacement, FMA)
+    // differs from the screen's exact r^2 by FP32 rounding (< 6e-7 relative)
+    // and by the residues, |delta| <= 1.06e-7 (2 L + r_s) for a pair inside
+    // the search radius r_s, L the group's largest local coordinate.  With
+    // L <= 2e4 r_s,min the force's r^2 stays below 1.01 r_s^2 for every pair
+    // the exact screen accepts, so skipping pairs above that is exact.
+    bool pre_ok;
+    {
+        float L = 0.f, rmin2 = 3.0e38f;
+#pragma unroll
+        for (int k = 0; k < IPT; k++)
+            if (vi[k]) {
+                L = fmaxf(L, fmaxf(fabsf(xi[k]), fmaxf(fabsf(yi[k]), fabsf(zi[k]))));
+                rmin2 = fminf(rmin2, rs2i[k]);
+            }
+        pre_ok = __syncthreads_and(L * L <= 4.0e8f * rmin2) != 0;
+    }
 
     // ---- EP-EP ----
     for (int base = 0; base < nj; base += TJ) {
@@ -133,8 +150,6 @@ __device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, in
                 for (int k = 0; k < IPT; k++) {
                     // the functor's FP32 displacement (screen) ...
                     const float hx = xi[k] - a.x, hy = yi[k] - a.y, hz = zi[k] - a.z;
-                    const float r2r =
-                        __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(hx, hx), __fmul_rn(hy, hy)), __fmul_rn(hz, hz)), eps2);
                     // ... and the same displacement with the low parts restored (force)
                     const float rx = hx + (xl[k] - c.x), ry = hy + (yl[k] - c.y), rz = hz + (zl[k] - c.z);
                     const float r2f = fmaf(rx, rx, fmaf(ry, ry, fmaf(rz, rz, eps2)));
@@ -147,7 +162,13 @@ __device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, in
                     ty[k] = fmaf(mr3, ry, ty[k]);
                     tz[k] = fmaf(mr3, rz, tz[k]);
                     tp[k] += mr;
-                    if (r2r < fmaxf(rs2i[k], b.y)) {
+                    // the exact screen only where the force's r^2 is within 1 % of
+                    // the search radius (pre_ok: proven to miss no neighbour)
+                    const float rs2 = fmaxf(rs2i[k], b.y);
+                    if (pre_ok && !(r2f < 1.01f * rs2)) continue;
+                    const float r2r =
+                        __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(hx, hx), __fmul_rn(hy, hy)), __fmul_rn(hz, hz)), eps2);
+                    if (r2r < rs2) {
                         const int idj = __float_as_int(b.z), rkj = __float_as_int(b.w);
                         if ((idi[k] != idj || rki[k] != rkj) && vi[k]) {
                             ngb[k] += 1;
@@ -207,8 +228,9 @@ __device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, in
                 for (int k = 0; k < IPT; k++) {
                     const float rx = a.x - xi[k], ry = a.y - yi[k], rz = a.z - zi[k];
                     const float r2 = fmaf(rx, rx, fmaf(ry, ry, fmaf(rz, rz, eps2)));
-                    float ri = rsqrtf(r2);
-                    ri = ri * fmaf(-0.5f * r2, ri * ri, 1.5f);
+                    // rsqrt without the Newton step: its 2-ulp error is far below the
+                    // quadrupole truncation of a far cell
+                    const float ri = rsqrtf(r2);
                     const float r2i = ri * ri;
                     const float r3i = r2i * ri;
                     const float r4i = r2i * r2i;
