@@ -7,6 +7,9 @@ code:
   t_ipt2 members two i-particles per thread, above t_s1 one, above t_s2 the
   j lists split two ways, else four) -- timed on the 1,048,576-body soft-force
   disk (0.5-1.5 AU, m = 1e-10, theta = 0.5, n_group_limit = 256);
+* the bundle form's heavy-cluster threshold (p3t_set_hard_heavy: clusters
+  whose learned prediction of log2(1 + block steps) reaches it run alone in a
+  CTA first) -- timed from restored states of the hard-part disk;
 * the one-cluster-per-team form's size cutoffs of the hard launch
   (p3t_set_hard_tiers: clusters of >= cta_min members one per CTA, >= warp_min
   one per warp, smaller one per thread) -- timed from one restored state of the
@@ -77,6 +80,28 @@ def tune_tiers(g, istep=1, grid=TIER_GRID):
     return best, table
 
 
+HEAVY_GRID = (0.0, 5.5, 6.0, 6.5, 7.0, 7.5)
+
+
+def tune_heavy(g, istep=1, grid=HEAVY_GRID):
+    """Times the bundled hard launch with the learned order from one restored
+    state for each heavy-cluster threshold; installs the fastest.  Returns
+    (best, {threshold: ms})."""
+    import ctypes
+
+    lib = g.lib
+    _lib.check(lib.p3t_state_snapshot(0), "p3t_state_snapshot")
+    table = {}
+    for h in grid:
+        _lib.check(lib.p3t_set_hard_heavy(ctypes.c_float(h)), "p3t_set_hard_heavy")
+        _lib.check(lib.p3t_state_snapshot(1), "p3t_state_snapshot")
+        table[h] = 1e3 * _timed(lib, lambda: g.hard(istep), 1)
+    lib.p3t_state_snapshot(1)
+    best = min(table, key=table.get)
+    _lib.check(lib.p3t_set_hard_heavy(ctypes.c_float(best)), "p3t_set_hard_heavy")
+    return best, table
+
+
 def load(lib=None, path=TUNING):
     """Installs a tuning file's choices; returns them (None without a file)."""
     if not os.path.exists(path):
@@ -87,6 +112,10 @@ def load(lib=None, path=TUNING):
         _lib.check(lib.p3t_set_soft_tiles(*t["soft_tiles"]), "p3t_set_soft_tiles")
     if "hard_tiers" in t:
         _lib.check(lib.p3t_set_hard_tiers(*t["hard_tiers"]), "p3t_set_hard_tiers")
+    if "hard_heavy" in t:
+        import ctypes
+
+        _lib.check(lib.p3t_set_hard_heavy(ctypes.c_float(t["hard_heavy"])), "p3t_set_hard_heavy")
     return t
 
 
@@ -123,16 +152,34 @@ def main():
     g.kick()
     g.cluster()
     hard_best, hard_table = tune_tiers(g)
+    from . import scheduler
+
+    heavy_best, heavy_table = None, {}
+    if scheduler.load(lib=g.lib) is not None:
+        # two tree steps' states: the heavy threshold matters where predictions differ
+        for istep in (1, 2):
+            b, t = tune_heavy(g, istep)
+            for k, v in t.items():
+                heavy_table[k] = heavy_table.get(k, 0.0) + v
+            g.hard(istep)
+            g.tree_soft()
+            g.correct(False)
+            g.kick()
+            g.cluster()
+        heavy_best = min(heavy_table, key=heavy_table.get)
     out = {"soft_tiles": list(soft_best),
            "soft_ms": {",".join(map(str, k)): v for k, v in soft_table.items()},
            "hard_tiers": list(hard_best),
+           "hard_heavy": heavy_best if heavy_best is not None else 6.5,
+           "hard_heavy_ms": {str(k): v for k, v in heavy_table.items()},
            "hard_ms": {",".join(map(str, k)): v for k, v in hard_table.items()},
            "workloads": {"soft": "1048576-body disk 0.5-1.5 AU, m=1e-10, theta=0.5, n_group_limit=256",
                          "hard": "1048576-body hard-part disk 0.95-1.05 AU, m=7e-11, rms e=6h, rms i=3h"}}
     json.dump(out, open(args.out, "w"), indent=1)
     print(json.dumps({"soft_tiles": out["soft_tiles"], "soft_ms_best": soft_table[soft_best],
                       "soft_ms_default": soft_table.get((128, 64, 32)), "hard_tiers": out["hard_tiers"],
-                      "hard_ms_best": hard_table[hard_best], "hard_ms_default": hard_table.get((8, 64))}))
+                      "hard_ms_best": hard_table[hard_best], "hard_ms_default": hard_table.get((8, 64)),
+                      "hard_heavy": out["hard_heavy"], "hard_heavy_ms": out["hard_heavy_ms"]}))
 
 
 if __name__ == "__main__":

@@ -1071,7 +1071,7 @@ __global__ void k_isolated(IsoArgs A) {
 constexpr int ORDER_NB = 4096;
 
 __global__ void k_order_bins(const int32_t *cnt, const float *prio, int nc, int mode, int warp_min, int cta_min,
-                             float pmin, float pscale, int32_t *bin, int32_t *hist) {
+                             float pmin, float pscale, int heavy_key, int32_t *bin, int32_t *hist, int32_t *n_heavy) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nc) return;
     const int n = cnt[k];
@@ -1084,6 +1084,9 @@ __global__ void k_order_bins(const int32_t *cnt, const float *prio, int nc, int 
     const int b = tier * ORDER_NB + (ORDER_NB - 1 - key);
     bin[k] = b;
     atomicAdd(&hist[b], 1);
+    // bundle form: clusters predicted to take long chains of block steps run
+    // alone in a CTA first (they head tier 1, the order being by prediction)
+    if (mode == 0 && tier == 1 && key >= heavy_key) atomicAdd(n_heavy, 1);
 }
 
 // exclusive offsets of the 3 x ORDER_NB bins (one block of 1024) and the
@@ -1187,6 +1190,7 @@ static std::vector<ColRec> g_cols;
 static double g_edisp[2] = {0., 0.};
 static int g_warp_min = 8, g_cta_min = 64;
 static int g_hard_mode = 0;  // 0: bundles, 1: thread/warp/CTA tiers
+static float g_heavy = 6.5f;  // predicted log2(1 + block steps) from which a cluster runs alone (0: never)
 static FragParams g_frag = {0., 9.426627927538057e-12, 10, 0, 0ULL};  // off (a_frag = 0)
 static int g_frag_cap = 0;  // fragment slots of the current launch
 
@@ -1269,6 +1273,12 @@ int p3t_set_fragmentation(double a_frag, int n_frag, double m_min, unsigned long
 
 long long p3t_id_next(void) { return g_eng.id_next; }
 
+int p3t_set_hard_heavy(float log2_steps) {
+    if (!(log2_steps >= 0.f)) return ST_BAD_INDEX;
+    g_heavy = log2_steps;
+    return 0;
+}
+
 int p3t_set_hard_mode(int mode) {
     if (mode != 0 && mode != 1) return ST_BAD_INDEX;
     g_hard_mode = mode;
@@ -1317,8 +1327,9 @@ int p3t_hard_enqueue(void) {
     // the bundle capacity first; tier mode: CTA >= g_cta_min > warp >=
     // g_warp_min > thread), then by priority (the caller's, the learned cost
     // model's, else the size), highest first
-    if ((r = B.bin.reserve(nc + 1)) || (r = B.hist.reserve(3 * ORDER_NB)) || (r = B.ntier.reserve(3))) return r;
+    if ((r = B.bin.reserve(nc + 1)) || (r = B.hist.reserve(3 * ORDER_NB)) || (r = B.ntier.reserve(4))) return r;
     cudaMemsetAsync(B.hist.p, 0, 3 * ORDER_NB * sizeof(int32_t), c->stream);
+    cudaMemsetAsync(B.ntier.p, 0, 4 * sizeof(int32_t), c->stream);
     if (nc > 0) {
         const float *prio = nullptr;
         float pmin = 0.f, pscale = 1.f;
@@ -1331,8 +1342,13 @@ int p3t_hard_enqueue(void) {
         } else {
             prio = sched_priority(c, nc, &pmin, &pscale);
         }
+        // heavy clusters: learned prediction of log2(1 + block steps) >= g_heavy
+        int heavy_key = 2147483647;
+        if (prio && (int)g_prio.size() != nc && g_heavy > 0.f)
+            heavy_key = std::min(ORDER_NB - 1, (int)((g_heavy - pmin) * pscale));
         k_order_bins<<<(nc + 255) / 256, 256, 0, c->stream>>>(E.cl_cnt.p, prio, nc, g_hard_mode, g_warp_min, g_cta_min,
-                                                              pmin, pscale, B.bin.p, B.hist.p);
+                                                              pmin, pscale, heavy_key, B.bin.p, B.hist.p,
+                                                              B.ntier.p + 3);
         k_order_scan<<<1, 1024, 0, c->stream>>>(B.hist.p, B.ntier.p);
         k_order_scatter<<<(nc + 255) / 256, 256, 0, c->stream>>>(B.bin.p, nc, B.hist.p, B.order.p);
         if ((r = cuda_status(cudaGetLastError()))) return r;

@@ -84,7 +84,7 @@ struct BundleSmem {
     // claimed, not yet admitted clusters
     int pend_c[BCLAIM], pend_n[BCLAIM];
     int ws[BT / 32];
-    int used, ncl, fresh_k, fresh_p, n_sv, n_pend, i_pend, exhausted, any, grew;
+    int used, ncl, fresh_k, fresh_p, n_sv, n_pend, i_pend, exhausted, any, grew, phase;
 };
 
 __device__ __forceinline__ unsigned long long dbits(double x) {
@@ -386,11 +386,36 @@ __device__ void bundle_detect(const HardArgs &A, BundleSmem &B, bool second) {
 // ---- bundle lifecycle ---------------------------------------------------------------
 // warp 0: claim clusters from the queue and admit them while they fit (lane
 // 0 decides, the decisions are broadcast so the warp's control flow stays
-// uniform)
+// uniform).  Phase 0: the heavy clusters (the first n_tier[3] of tier 1:
+// predicted long chains of block steps), one at a time and alone in the
+// bundle, so their iterations stay short; phase 1: the rest, packed.
 __device__ void bundle_refill(const HardArgs &A, BundleSmem &B) {
     const int lane = threadIdx.x & 31;
+    const int n_heavy = A.n_tier[3];
     if (threadIdx.x < 32) {
-        for (int guard = 0; guard < (1 << 20); guard++) {
+        int lone = 0;
+        if (lane == 0 && B.phase == 0) {
+            if (B.ncl > 0) {
+                lone = 1;  // a heavy cluster is running: nothing joins it
+            } else {
+                const int q = atomicAdd(&A.queue[2], 1);
+                if (q < n_heavy) {
+                    const int c = A.order[A.n_tier[0] + q];
+                    const int k = B.ncl++;
+                    B.c_idx[k] = c;
+                    B.c_off[k] = 0;
+                    B.c_n[k] = A.cnt[c];
+                    B.c_flags[k] = CF_FRESH;
+                    B.used = B.c_n[k];
+                    lone = 1;
+                } else {
+                    B.phase = 1;
+                }
+            }
+        }
+        lone = __shfl_sync(0xffffffffu, lone, 0);
+        __syncwarp();
+        for (int guard = 0; !lone && guard < (1 << 20); guard++) {
             int stop = 0, claim = 0;
             if (lane == 0 && B.i_pend >= B.n_pend) {
                 if (B.exhausted) stop = 1;
@@ -404,10 +429,10 @@ __device__ void bundle_refill(const HardArgs &A, BundleSmem &B) {
                 if (lane == 0) q = atomicAdd(&A.queue[1], BCLAIM);
                 q = __shfl_sync(0xffffffffu, q, 0);
                 const int qi = q + lane;
-                const bool ok = lane < BCLAIM && qi < A.n_tier[1];
+                const bool ok = lane < BCLAIM && qi < A.n_tier[1] - n_heavy;
                 const unsigned m = __ballot_sync(0xffffffffu, ok);
                 if (ok) {
-                    const int c = A.order[A.n_tier[0] + qi];
+                    const int c = A.order[A.n_tier[0] + n_heavy + qi];
                     B.pend_c[lane] = c;
                     B.pend_n[lane] = A.cnt[c];
                 }
@@ -926,6 +951,7 @@ __global__ void __launch_bounds__(BT, 2) k_hard_bundles(HardArgs A) {
         B.n_pend = 0;
         B.i_pend = 0;
         B.exhausted = 0;
+        B.phase = 0;
     }
     __syncthreads();
     for (int guard = 0; guard < (1 << 30); guard++) {

@@ -188,6 +188,12 @@ int p3t_set_hard_tiers(int warp_min, int cta_min);
  * (256 members) run one per CTA.  1: the size tiers of p3t_set_hard_tiers.
  * Both give identical results.  No counterpart in GPLUM's interface. */
 int p3t_set_hard_mode(int mode);
+/* Bundle form with the learned order: clusters whose predicted
+ * log2(1 + block steps) is at least log2_steps run first, each alone in a
+ * CTA, so the longest chains of block steps do not wait on a full bundle
+ * (default 6.5, about 90 block steps; set by the autotuner; 0 turns it
+ * off).  Results do not depend on it. */
+int p3t_set_hard_heavy(float log2_steps);
 /* KOMINAMI fragmentation of the collision outcome (src/collisionB.h:7-93;
  * Collision::a_frag, N_frag, Collision0::m_min of parameter.dat).  a_frag = 0
  * (the default) is perfect accretion.  A collision makes
