@@ -7,8 +7,9 @@ phase of the step stay on the GPU.
 integrates the 3000-body disk (0.95-1.05 AU, m = 1e-9, rms e = 2 h,
 rms i = h, dt_tree = 2^-7) and prints the relative energy error
 (Energy::calcEnergyError, src/energy.h:65-67: (E - E_init - E_dissipated) /
-E_init, where the dissipated energy sums the hard part's collisions and the
-merges, src/main_p3t.cpp:539,641).
+E_init, where the dissipated energy sums the hard part's collisions, the
+merges and the bodies removed outside [r_min, r_max],
+src/main_p3t.cpp:539,641,645).
 """
 import argparse
 import json
