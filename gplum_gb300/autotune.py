@@ -4,8 +4,8 @@ Two choices are made by measurement on the live workload instead of fixed in
 code:
 
 * the soft kernel's work split by i-group size (p3t_set_soft_tiles: above
-  t_ipt2 members two i-particles per thread, above t_s1 one, above t_s2 the
-  j lists split two ways, else four) -- timed on the 1,048,576-body soft-force
+  t_ipt2 members two i-particles per thread (256: never), above t_s1 one,
+  above t_s2 the j lists split two ways, else four) -- timed on the 1,048,576-body soft-force
   disk (0.5-1.5 AU, m = 1e-10, theta = 0.5, n_group_limit = 256);
 * the bundle form's heavy-cluster threshold (p3t_set_hard_heavy: clusters
   whose learned prediction of log2(1 + block steps) reaches it run alone in a
@@ -31,7 +31,7 @@ import numpy as np
 from . import _lib
 
 TUNING = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning.json")
-SOFT_GRID = [(a, b, c) for a in (64, 96, 128) for b in (32, 48, 64) for c in (0, 16, 32) if c <= b <= a]
+SOFT_GRID = [(a, b, c) for a in (64, 96, 128, 256) for b in (32, 48, 64) for c in (0, 16, 32) if c <= b <= a]
 TIER_GRID = [(w, t) for w in (2, 4, 8, 16) for t in (32, 64, 128, 256)]
 
 
@@ -128,6 +128,8 @@ def main():
 
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=TUNING)
+    ap.add_argument("--soft-only", action="store_true",
+                    help="retune the soft work split only; keep the file's other entries")
     args = ap.parse_args()
     P = P3TParams(n_group_limit=256)
     # soft: resident lists of the soft-force disk
@@ -140,6 +142,13 @@ def main():
     sf.upload_lists(L)
     lib = _lib.host_lib()
     soft_best, soft_table = tune_soft(lib, lambda: sf.run(emit_candidates=True))
+    if args.soft_only:
+        out = json.load(open(args.out)) if os.path.exists(args.out) else {}
+        out["soft_tiles"] = list(soft_best)
+        out["soft_ms"] = {",".join(map(str, k)): v for k, v in soft_table.items()}
+        json.dump(out, open(args.out, "w"), indent=1)
+        print(json.dumps({"soft_tiles": out["soft_tiles"], "soft_ms_best": soft_table[soft_best]}))
+        return
     # hard: tier cutoffs of the per-team form on the hard-part disk
     d = disk_1m_hard()
     g = GpuSystem(P)

@@ -223,7 +223,8 @@ int p3t_set_params(const double *params21) {
 
 int p3t_set_soft_tiles(int t_ipt2, int t_s1, int t_s2) {
     CTX_OR_FAIL(c);
-    if (t_s2 < 0 || t_s2 > 32 || t_s1 < t_s2 || t_s1 > 64 || t_ipt2 < t_s1 || t_ipt2 > 128) return ST_BAD_INDEX;
+    if (t_s2 < 0 || t_s2 > 32 || t_s1 < t_s2 || t_s1 > 64 || t_ipt2 < t_s1 || (t_ipt2 > 128 && t_ipt2 != 256))
+        return ST_BAD_INDEX;
     c->tiles[0] = t_ipt2;
     c->tiles[1] = t_s1;
     c->tiles[2] = t_s2;

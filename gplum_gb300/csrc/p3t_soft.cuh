@@ -33,7 +33,8 @@ struct SoftArgs {
     // work split of an i-group of ni members over the CTA's 128 threads:
     // ni > t_ipt2: 2 i per thread; > t_s1: 1 i per thread; > t_s2: the j list
     // split 2 ways; else 4 ways (0 <= t_s2 <= 32, t_s2 <= t_s1 <= 64,
-    // t_s1 <= t_ipt2 <= 128; 0 = the defaults 128, 64, 32)
+    // t_s1 <= t_ipt2 <= 128 or t_ipt2 = 256: never 2 i per thread, groups
+    // above 128 in chunks of 128; 0 = the defaults 128, 64, 32)
     int t_ipt2, t_s1, t_s2;
 };
 

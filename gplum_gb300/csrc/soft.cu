@@ -8,11 +8,13 @@
 //
 // Work split per CTA, by group size ni (uniform per CTA; the thresholds are
 // SoftArgs::t_ipt2/t_s1/t_s2, set by the autotuner, defaults shown):
-//   ni > 128 : 2 i per thread           ni in (64,128] : 1 i per thread
+//   ni > 128 : 2 consecutive i per thread   ni in (64,128] : 1 i per thread
+//   (t_ipt2 = 256: one i per thread throughout, groups above 128 in chunks)
 //   ni in (32,64] : two sub-blocks of 64 threads, each taking half of every
 //   j tile      ni <= 32 : four sub-blocks of 32 threads, a quarter each.
 // Sub-block partial sums are combined in a fixed order, so results do not
-// depend on scheduling.
+// depend on scheduling.  Warps whose i-slots all lie past ni skip the pair
+// loops, so the issue slots spent follow ni in steps of 32 i-slots.
 //
 // Mixed kernel (reference functors src/gravity_kernel.hpp:25-121 and
 // 138-238 of GPLUM, PIKG specs src/gravity_kernel_epep.pikg and
@@ -53,9 +55,57 @@ __device__ __forceinline__ void fold(float &hi, float &lo, float v) {
 
 // --------------------------------------------------------------------------
 // mixed precision
+//
+// Packed pairs: every FP32 operation of the pair loops acts on two list
+// entries at once (float2 through fma.rn.f32x2 / add.rn.f32x2 /
+// mul.rn.f32x2, one issue slot for two lanes' worth of FP32 work).  A tile
+// is staged pair-interleaved -- entries 2q and 2q+1 side by side in each
+// float4 -- so one shared-memory load yields ready packed operands.  The
+// tile's j coordinates (and, for superparticles, the quadrupole terms) are
+// stored negated, so every difference is an addition and the superparticle
+// terms come out with the force's sign; each product and sum is the exact
+// negation of the unnegated one.  A tile is padded to a multiple of 32
+// entries with massless entries 1e18 away, which contribute exact zeros.
+//
+// Neighbour screen: inside the loop a pair only sets a bit when the force's
+// r^2 lies below 1.01 max(r_s,i^2, r_s,j^2) (precomputed per i and per j as
+// 1.01 r_s^2: x -> rn(1.01 x) is monotone, so the max commutes); after each
+// chunk of 32 entries the flagged pairs alone are re-screened exactly, in
+// list order, with the functor's FP32 arithmetic.
+constexpr int TP = TJ / 2;  // entry pairs per tile
+
+struct MixedTile {
+    // EP-EP: a = (-hx0,-hx1,-hy0,-hy1) b = (-hz0,-hz1,m0,m1)
+    //        c = (-xl0,-xl1,-yl0,-yl1) d = (-zl0,-zl1,ro2_0,ro2_1) e = (t0,t1) t = 1.01 rs2_j
+    // EP-SP: a = (-x0,-x1,-y0,-y1)     b = (-z0,-z1,m0,m1)
+    //        c = -(q'xx, q'yy)         d = -(q'zz, mtr)   f = -(3qxy, 3qyz)  e = -(3qzx)
+    float4 a[TP], b[TP], c[TP], d[TP], f[TP];
+    float2 e[TP];
+    float4 r[TJ];  // EP-EP exact screen: (rs2, id, rank, -)
+    int idx[TJ];   // EP-EP particle index of each entry (candidate emission)
+};
+
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+    // MUFU reciprocal square root; every argument here is a normal positive float
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float2 rsqrt2(float2 v) { return make_float2(rsqrt_ftz(v.x), rsqrt_ftz(v.y)); }
+__device__ __forceinline__ float2 lo2(float4 v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); }
+__device__ __forceinline__ float2 dup2(float v) { return make_float2(v, v); }
+__device__ __forceinline__ void put2(float4 *arr, int t, int comp, float v) {
+    // entry t's value of packed component comp (0: .x/.y, 1: .z/.w)
+    reinterpret_cast<float *>(arr)[4 * (t >> 1) + 2 * comp + (t & 1)] = v;
+}
+__device__ __forceinline__ float get2(const float4 *arr, int t, int comp) {
+    return reinterpret_cast<const float *>(arr)[4 * (t >> 1) + 2 * comp + (t & 1)];
+}
+
 template <int S, int IPT, bool EMIT>
-__device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, int ni, float4 *sa, float4 *sb,
-                                            float4 *sc, int *sidx, int *scnt, float *redf, int *redi) {
+__device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, int ni, MixedTile &T, int *scnt,
+                                            float *redf, int *redi) {
     // i-particles [ib, ib + ni) of group g (ni <= 2 * SB); the origin is the
     // group's first i-particle, as in the functor
     constexpr int W = SB / S;
@@ -65,19 +115,20 @@ __device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, in
     const int j0 = A.j_off[g], nj = A.j_off[g + 1] - j0;
     const int s0 = A.s_off[g], ns = A.s_off[g + 1] - s0;
     const float eps2 = A.eps2;
+    const float2 eps2_2 = dup2(eps2);
 
     int p_first = A.i_idx[i0];
     if ((unsigned)p_first >= (unsigned)A.n_iptcl) { atomicOr(A.status, ST_BAD_INDEX); p_first = 0; }
     const double ox = A.iptcl[p_first].x, oy = A.iptcl[p_first].y, oz = A.iptcl[p_first].z;
 
-    float xi[IPT], yi[IPT], zi[IPT], xl[IPT], yl[IPT], zl[IPT], ro2i[IPT], rs2i[IPT];
+    float xi[IPT], yi[IPT], zi[IPT], xl[IPT], yl[IPT], zl[IPT], ro2i[IPT], rs2i[IPT], thi[IPT];
     int idi[IPT], rki[IPT], pid[IPT], li[IPT];
     bool vi[IPT];
     float ahx[IPT], alx[IPT], ahy[IPT], aly[IPT], ahz[IPT], alz[IPT], ahp[IPT], alp[IPT];
     int ngb[IPT], rk[IPT], idmax[IPT], idmin[IPT];
 #pragma unroll
     for (int k = 0; k < IPT; k++) {
-        li[k] = lane + k * W;
+        li[k] = lane * IPT + k;
         vi[k] = li[k] < ni;
         int p = vi[k] ? A.i_idx[i0 + ib + li[k]] : p_first;
         if ((unsigned)p >= (unsigned)A.n_iptcl) { atomicOr(A.status, ST_BAD_INDEX); p = 0; vi[k] = false; }
@@ -97,6 +148,9 @@ __device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, in
         ahx[k] = alx[k] = ahy[k] = aly[k] = ahz[k] = alz[k] = ahp[k] = alp[k] = 0.f;
         ngb[k] = 0; rk[k] = 0; idmax[k] = -1; idmin[k] = INT32_MAX_;
     }
+    // a warp whose i-slots all lie past the group skips the pair loops (it
+    // still stages tiles and meets every barrier)
+    const bool wact = (lane & ~31) * IPT < ni;
     if (EMIT) {
         for (int t = tid; t < ni; t += SB) scnt[t] = 0;
     }
@@ -105,8 +159,8 @@ __device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, in
     // and by the residues, |delta| <= 1.06e-7 (2 L + r_s) for a pair inside
     // the search radius r_s, L the group's largest local coordinate.  With
     // L <= 2e4 r_s,min the force's r^2 stays below 1.01 r_s^2 for every pair
-    // the exact screen accepts, so skipping pairs above that is exact.
-    bool pre_ok;
+    // the exact screen accepts, so leaving pairs above that unflagged is
+    // exact; otherwise every pair is flagged.
     {
         float L = 0.f, rmin2 = 3.0e38f;
 #pragma unroll
@@ -115,62 +169,102 @@ __device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, in
                 L = fmaxf(L, fmaxf(fabsf(xi[k]), fmaxf(fabsf(yi[k]), fabsf(zi[k]))));
                 rmin2 = fminf(rmin2, rs2i[k]);
             }
-        pre_ok = __syncthreads_and(L * L <= 4.0e8f * rmin2) != 0;
+        const bool pre_ok = __syncthreads_and(L * L <= 4.0e8f * rmin2) != 0;
+#pragma unroll
+        for (int k = 0; k < IPT; k++) thi[k] = pre_ok ? 1.01f * rs2i[k] : 3.0e38f;
     }
+    const float2 c15 = dup2(1.5f), cm05 = dup2(-0.5f);
 
     // ---- EP-EP ----
     for (int base = 0; base < nj; base += TJ) {
         const int nt = min(TJ, nj - base);
         __syncthreads();
-        if (tid < nt) {
-            int p = A.j_idx[j0 + base + tid];
-            if ((unsigned)p >= (unsigned)A.n_ptcl) { atomicOr(A.status, ST_BAD_INDEX); p = 0; }
-            const SoftPtcl r = A.ptcl[p];
-            const double dx = r.x - ox, dy = r.y - oy, dz = r.z - oz;
-            const float hx = __double2float_rn(dx), hy = __double2float_rn(dy), hz = __double2float_rn(dz);
-            sa[tid] = make_float4(hx, hy, hz, r.m);
-            sb[tid] = make_float4(r.ro2, r.rs2, __int_as_float(r.id_local), __int_as_float(r.rank));
-            sc[tid] = make_float4(__double2float_rn(dx - (double)hx), __double2float_rn(dy - (double)hy),
-                                  __double2float_rn(dz - (double)hz), 0.f);
-            if (EMIT) sidx[tid] = p;
+        {
+            const int t = tid;
+            if (t < nt) {
+                int p = A.j_idx[j0 + base + t];
+                if ((unsigned)p >= (unsigned)A.n_ptcl) { atomicOr(A.status, ST_BAD_INDEX); p = 0; }
+                const SoftPtcl r = A.ptcl[p];
+                const double dx = r.x - ox, dy = r.y - oy, dz = r.z - oz;
+                const float hx = __double2float_rn(dx), hy = __double2float_rn(dy), hz = __double2float_rn(dz);
+                put2(T.a, t, 0, -hx); put2(T.a, t, 1, -hy);
+                put2(T.b, t, 0, -hz); put2(T.b, t, 1, r.m);
+                put2(T.c, t, 0, -__double2float_rn(dx - (double)hx));
+                put2(T.c, t, 1, -__double2float_rn(dy - (double)hy));
+                put2(T.d, t, 0, -__double2float_rn(dz - (double)hz));
+                put2(T.d, t, 1, r.ro2);
+                reinterpret_cast<float *>(T.e)[t] = 1.01f * r.rs2;
+                T.r[t] = make_float4(r.rs2, __int_as_float(r.id_local), __int_as_float(r.rank), 0.f);
+                if (EMIT) T.idx[t] = p;
+            } else {  // padding: massless, far away, never flagged
+                put2(T.a, t, 0, -1.0e18f); put2(T.a, t, 1, -1.0e18f);
+                put2(T.b, t, 0, -1.0e18f); put2(T.b, t, 1, 0.f);
+                put2(T.c, t, 0, 0.f); put2(T.c, t, 1, 0.f);
+                put2(T.d, t, 0, 0.f); put2(T.d, t, 1, 0.f);
+                reinterpret_cast<float *>(T.e)[t] = 0.f;
+                T.r[t] = make_float4(0.f, __int_as_float(-1), __int_as_float(-1), 0.f);
+            }
         }
         __syncthreads();
-        const int jb = sub * (TJ / S), je = min(jb + TJ / S, nt);
+        // this sub-block's share of the tile, in whole chunks of 32 entries
+        const int jb = sub * (TJ / S);
+        const int je = wact ? min(jb + TJ / S, (nt + CHUNK - 1) & ~(CHUNK - 1)) : jb;
         for (int c0 = jb; c0 < je; c0 += CHUNK) {
-            const int c1 = min(c0 + CHUNK, je);
-            float tx[IPT], ty[IPT], tz[IPT], tp[IPT];
+            float2 tx[IPT], ty[IPT], tz[IPT], tp[IPT];
+            unsigned nm[IPT];
 #pragma unroll
-            for (int k = 0; k < IPT; k++) tx[k] = ty[k] = tz[k] = tp[k] = 0.f;
-#pragma unroll 4
-            for (int jj = c0; jj < c1; jj++) {
-                const float4 a = sa[jj];
-                const float4 b = sb[jj];
-                const float4 c = sc[jj];
+            for (int k = 0; k < IPT; k++) {
+                tx[k] = ty[k] = tz[k] = tp[k] = dup2(0.f);
+                nm[k] = 0u;
+            }
+#pragma unroll 8
+            for (int q = 0; q < CHUNK / 2; q++) {
+                const int pq = (c0 >> 1) + q;
+                const float4 a = T.a[pq], b = T.b[pq], c = T.c[pq], d = T.d[pq];
+                const float2 e = T.e[pq];
 #pragma unroll
                 for (int k = 0; k < IPT; k++) {
-                    // the functor's FP32 displacement (screen) ...
-                    const float hx = xi[k] - a.x, hy = yi[k] - a.y, hz = zi[k] - a.z;
-                    // ... and the same displacement with the low parts restored (force)
-                    const float rx = hx + (xl[k] - c.x), ry = hy + (yl[k] - c.y), rz = hz + (zl[k] - c.z);
-                    const float r2f = fmaf(rx, rx, fmaf(ry, ry, fmaf(rz, rz, eps2)));
-                    const float r2 = fmaxf(r2f, fmaxf(ro2i[k], b.x));
-                    float ri = rsqrtf(r2);
-                    ri = ri * fmaf(-0.5f * r2, ri * ri, 1.5f);
-                    const float mr = a.w * ri;
-                    const float mr3 = mr * (ri * ri);
-                    tx[k] = fmaf(mr3, rx, tx[k]);
-                    ty[k] = fmaf(mr3, ry, ty[k]);
-                    tz[k] = fmaf(mr3, rz, tz[k]);
-                    tp[k] += mr;
-                    // the exact screen only where the force's r^2 is within 1 % of
-                    // the search radius (pre_ok: proven to miss no neighbour)
-                    const float rs2 = fmaxf(rs2i[k], b.y);
-                    if (pre_ok && !(r2f < 1.01f * rs2)) continue;
+                    // the functor's FP32 displacement, then the low parts restored
+                    const float2 hx = __fadd2_rn(dup2(xi[k]), lo2(a));
+                    const float2 hy = __fadd2_rn(dup2(yi[k]), hi2(a));
+                    const float2 hz = __fadd2_rn(dup2(zi[k]), lo2(b));
+                    const float2 rx = __fadd2_rn(hx, __fadd2_rn(dup2(xl[k]), lo2(c)));
+                    const float2 ry = __fadd2_rn(hy, __fadd2_rn(dup2(yl[k]), hi2(c)));
+                    const float2 rz = __fadd2_rn(hz, __fadd2_rn(dup2(zl[k]), lo2(d)));
+                    const float2 r2f = __ffma2_rn(rx, rx, __ffma2_rn(ry, ry, __ffma2_rn(rz, rz, eps2_2)));
+                    const float2 r2 = make_float2(fmaxf(r2f.x, fmaxf(ro2i[k], d.z)), fmaxf(r2f.y, fmaxf(ro2i[k], d.w)));
+                    float2 ri = rsqrt2(r2);
+                    ri = __fmul2_rn(ri, __ffma2_rn(__fmul2_rn(cm05, r2), __fmul2_rn(ri, ri), c15));
+                    const float2 mr = __fmul2_rn(hi2(b), ri);
+                    const float2 mr3 = __fmul2_rn(mr, __fmul2_rn(ri, ri));
+                    tx[k] = __ffma2_rn(mr3, rx, tx[k]);
+                    ty[k] = __ffma2_rn(mr3, ry, ty[k]);
+                    tz[k] = __ffma2_rn(mr3, rz, tz[k]);
+                    tp[k] = __fadd2_rn(tp[k], mr);
+                    if (r2f.x < fmaxf(thi[k], e.x)) nm[k] |= 1u << (2 * q);
+                    if (r2f.y < fmaxf(thi[k], e.y)) nm[k] |= 2u << (2 * q);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < IPT; k++) {
+                fold(ahx[k], alx[k], tx[k].x + tx[k].y);
+                fold(ahy[k], aly[k], ty[k].x + ty[k].y);
+                fold(ahz[k], alz[k], tz[k].x + tz[k].y);
+                fold(ahp[k], alp[k], tp[k].x + tp[k].y);
+                // exact screen of the flagged pairs, in list order
+                unsigned m = vi[k] ? nm[k] : 0u;
+                while (m) {
+                    const int jj = c0 + __ffs(m) - 1;
+                    m &= m - 1;
+                    const float hx = __fadd_rn(xi[k], get2(T.a, jj, 0));
+                    const float hy = __fadd_rn(yi[k], get2(T.a, jj, 1));
+                    const float hz = __fadd_rn(zi[k], get2(T.b, jj, 0));
+                    const float4 rr = T.r[jj];
                     const float r2r =
                         __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(hx, hx), __fmul_rn(hy, hy)), __fmul_rn(hz, hz)), eps2);
-                    if (r2r < rs2) {
-                        const int idj = __float_as_int(b.z), rkj = __float_as_int(b.w);
-                        if ((idi[k] != idj || rki[k] != rkj) && vi[k]) {
+                    if (r2r < fmaxf(rs2i[k], rr.x)) {
+                        const int idj = __float_as_int(rr.y), rkj = __float_as_int(rr.z);
+                        if (idi[k] != idj || rki[k] != rkj) {
                             ngb[k] += 1;
                             rk[k] += abs(rki[k] - rkj);
                             idmax[k] = max(idmax[k], idj);
@@ -178,7 +272,7 @@ __device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, in
                             if (EMIT) {
                                 const int slot = atomicAdd(&scnt[li[k]], 1);
                                 if (slot < A.cand_cap)
-                                    A.cand[(size_t)pid[k] * A.cand_cap + slot] = sidx[jj];
+                                    A.cand[(size_t)pid[k] * A.cand_cap + slot] = T.idx[jj];
                                 else
                                     atomicOr(A.status, ST_CAND_OVERFLOW);
                             }
@@ -186,74 +280,90 @@ __device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, in
                     }
                 }
             }
-#pragma unroll
-            for (int k = 0; k < IPT; k++) {
-                fold(ahx[k], alx[k], tx[k]);
-                fold(ahy[k], aly[k], ty[k]);
-                fold(ahz[k], alz[k], tz[k]);
-                fold(ahp[k], alp[k], tp[k]);
-            }
         }
     }
 
     // ---- EP-SP (quadrupole) ----
+    const float2 c05 = dup2(-0.5f), c25 = dup2(-2.5f);
     for (int base = 0; base < ns; base += TJ) {
         const int nt = min(TJ, ns - base);
         __syncthreads();
-        if (tid < nt) {
-            int q = A.s_idx[s0 + base + tid];
-            if ((unsigned)q >= (unsigned)A.n_spj) { atomicOr(A.status, ST_BAD_INDEX); q = 0; }
-            const SPJRec &r = A.spj[q];
-            const float qxx = (float)r.xx, qyy = (float)r.yy, qzz = (float)r.zz;
-            const float qxy = (float)r.xy, qyz = (float)r.yz, qzx = (float)r.xz;
-            const float tr = A.trace_mode ? (float)(r.xx + r.yy + r.zz) : (float)(r.xx + r.yy + r.xx);
-            sa[tid] = make_float4(__double2float_rn(r.pos[0] - ox), __double2float_rn(r.pos[1] - oy),
-                                  __double2float_rn(r.pos[2] - oz), (float)r.mass);
-            sb[tid] = make_float4(3.0f * qxx - tr, 3.0f * qyy - tr, 3.0f * qzz - tr, -(eps2 * tr));
-            sc[tid] = make_float4(3.0f * qxy, 3.0f * qyz, 3.0f * qzx, 0.f);
+        {
+            const int t = tid;
+            if (t < nt) {
+                int q = A.s_idx[s0 + base + t];
+                if ((unsigned)q >= (unsigned)A.n_spj) { atomicOr(A.status, ST_BAD_INDEX); q = 0; }
+                const SPJRec &r = A.spj[q];
+                const float qxx = (float)r.xx, qyy = (float)r.yy, qzz = (float)r.zz;
+                const float qxy = (float)r.xy, qyz = (float)r.yz, qzx = (float)r.xz;
+                const float tr = A.trace_mode ? (float)(r.xx + r.yy + r.zz) : (float)(r.xx + r.yy + r.xx);
+                put2(T.a, t, 0, -__double2float_rn(r.pos[0] - ox));
+                put2(T.a, t, 1, -__double2float_rn(r.pos[1] - oy));
+                put2(T.b, t, 0, -__double2float_rn(r.pos[2] - oz));
+                put2(T.b, t, 1, (float)r.mass);
+                put2(T.c, t, 0, -(3.0f * qxx - tr));
+                put2(T.c, t, 1, -(3.0f * qyy - tr));
+                put2(T.d, t, 0, -(3.0f * qzz - tr));
+                put2(T.d, t, 1, eps2 * tr);
+                put2(T.f, t, 0, -(3.0f * qxy));
+                put2(T.f, t, 1, -(3.0f * qyz));
+                reinterpret_cast<float *>(T.e)[t] = -(3.0f * qzx);
+            } else {  // padding: massless, far away
+                put2(T.a, t, 0, -1.0e18f); put2(T.a, t, 1, -1.0e18f);
+                put2(T.b, t, 0, -1.0e18f); put2(T.b, t, 1, 0.f);
+                put2(T.c, t, 0, 0.f); put2(T.c, t, 1, 0.f);
+                put2(T.d, t, 0, 0.f); put2(T.d, t, 1, 0.f);
+                put2(T.f, t, 0, 0.f); put2(T.f, t, 1, 0.f);
+                reinterpret_cast<float *>(T.e)[t] = 0.f;
+            }
         }
         __syncthreads();
-        const int jb = sub * (TJ / S), je = min(jb + TJ / S, nt);
+        const int jb = sub * (TJ / S);
+        const int je = wact ? min(jb + TJ / S, (nt + CHUNK - 1) & ~(CHUNK - 1)) : jb;
         for (int c0 = jb; c0 < je; c0 += CHUNK) {
-            const int c1 = min(c0 + CHUNK, je);
-            float tx[IPT], ty[IPT], tz[IPT], tp[IPT];
+            float2 tx[IPT], ty[IPT], tz[IPT], tp[IPT];
 #pragma unroll
-            for (int k = 0; k < IPT; k++) tx[k] = ty[k] = tz[k] = tp[k] = 0.f;
-#pragma unroll 2
-            for (int jj = c0; jj < c1; jj++) {
-                const float4 a = sa[jj];
-                const float4 q1 = sb[jj];
-                const float4 q2 = sc[jj];
+            for (int k = 0; k < IPT; k++) tx[k] = ty[k] = tz[k] = tp[k] = dup2(0.f);
+#pragma unroll 4
+            for (int q = 0; q < CHUNK / 2; q++) {
+                const int pq = (c0 >> 1) + q;
+                const float4 a = T.a[pq], b = T.b[pq], c = T.c[pq], d = T.d[pq], f = T.f[pq];
+                const float2 e = T.e[pq];
 #pragma unroll
                 for (int k = 0; k < IPT; k++) {
-                    const float rx = a.x - xi[k], ry = a.y - yi[k], rz = a.z - zi[k];
-                    const float r2 = fmaf(rx, rx, fmaf(ry, ry, fmaf(rz, rz, eps2)));
+                    // r' = x_i - x_j (the negated displacement); with the tile's
+                    // negated quadrupole, qr = -Q'r' and nrqr = -(mtr + r'Q'r')
+                    const float2 rx = __fadd2_rn(dup2(xi[k]), lo2(a));
+                    const float2 ry = __fadd2_rn(dup2(yi[k]), hi2(a));
+                    const float2 rz = __fadd2_rn(dup2(zi[k]), lo2(b));
+                    const float2 r2 = __ffma2_rn(rx, rx, __ffma2_rn(ry, ry, __ffma2_rn(rz, rz, eps2_2)));
                     // rsqrt without the Newton step: its 2-ulp error is far below the
                     // quadrupole truncation of a far cell
-                    const float ri = rsqrtf(r2);
-                    const float r2i = ri * ri;
-                    const float r3i = r2i * ri;
-                    const float r4i = r2i * r2i;
-                    const float r5i = r2i * r3i;
-                    const float qrx = fmaf(q1.x, rx, fmaf(q2.x, ry, q2.z * rz));
-                    const float qry = fmaf(q1.y, ry, fmaf(q2.y, rz, q2.x * rx));
-                    const float qrz = fmaf(q1.z, rz, fmaf(q2.z, rx, q2.y * ry));
-                    const float rqr = fmaf(qrx, rx, fmaf(qry, ry, fmaf(qrz, rz, q1.w)));
-                    const float rqr4 = rqr * r4i;
-                    const float meff = fmaf(0.5f, rqr4, a.w);
-                    const float meff3 = fmaf(2.5f, rqr4, a.w) * r3i;
-                    tx[k] = fmaf(r5i, qrx, fmaf(-meff3, rx, tx[k]));
-                    ty[k] = fmaf(r5i, qry, fmaf(-meff3, ry, ty[k]));
-                    tz[k] = fmaf(r5i, qrz, fmaf(-meff3, rz, tz[k]));
-                    tp[k] = fmaf(meff, ri, tp[k]);
+                    const float2 ri = rsqrt2(r2);
+                    const float2 r2i = __fmul2_rn(ri, ri);
+                    const float2 r3i = __fmul2_rn(r2i, ri);
+                    const float2 r4i = __fmul2_rn(r2i, r2i);
+                    const float2 r5i = __fmul2_rn(r2i, r3i);
+                    const float2 qrx = __ffma2_rn(lo2(c), rx, __ffma2_rn(lo2(f), ry, __fmul2_rn(e, rz)));
+                    const float2 qry = __ffma2_rn(hi2(c), ry, __ffma2_rn(hi2(f), rz, __fmul2_rn(lo2(f), rx)));
+                    const float2 qrz = __ffma2_rn(lo2(d), rz, __ffma2_rn(e, rx, __fmul2_rn(hi2(f), ry)));
+                    const float2 nrqr = __ffma2_rn(qrx, rx, __ffma2_rn(qry, ry, __ffma2_rn(qrz, rz, hi2(d))));
+                    const float2 nrqr4 = __fmul2_rn(nrqr, r4i);
+                    const float2 meff = __ffma2_rn(c05, nrqr4, hi2(b));
+                    const float2 meff3 = __fmul2_rn(__ffma2_rn(c25, nrqr4, hi2(b)), r3i);
+                    // acc_i += r5i Q'r - meff3 r  with r = -r'
+                    tx[k] = __ffma2_rn(r5i, qrx, __ffma2_rn(meff3, rx, tx[k]));
+                    ty[k] = __ffma2_rn(r5i, qry, __ffma2_rn(meff3, ry, ty[k]));
+                    tz[k] = __ffma2_rn(r5i, qrz, __ffma2_rn(meff3, rz, tz[k]));
+                    tp[k] = __ffma2_rn(meff, ri, tp[k]);
                 }
             }
 #pragma unroll
             for (int k = 0; k < IPT; k++) {
-                fold(ahx[k], alx[k], tx[k]);
-                fold(ahy[k], aly[k], ty[k]);
-                fold(ahz[k], alz[k], tz[k]);
-                fold(ahp[k], alp[k], tp[k]);
+                fold(ahx[k], alx[k], tx[k].x + tx[k].y);
+                fold(ahy[k], aly[k], ty[k].x + ty[k].y);
+                fold(ahz[k], alz[k], tz[k].x + tz[k].y);
+                fold(ahp[k], alp[k], tp[k].x + tp[k].y);
             }
         }
     }
@@ -307,25 +417,26 @@ __device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, in
 
 template <bool EMIT>
 __global__ void __launch_bounds__(SB, 4) soft_mixed_kernel(SoftArgs A) {
-    __shared__ float4 sa[TJ], sb[TJ], sc[TJ];
-    __shared__ int sidx[EMIT ? TJ : 1];
+    __shared__ MixedTile T;
     __shared__ int scnt[EMIT ? 2 * SB : 1];
     __shared__ float redf[SB * 8];
     __shared__ int redi[SB * 4];
     const int g = A.group_order ? A.group_order[blockIdx.x] : blockIdx.x;
     const int ni_all = A.i_off[g + 1] - A.i_off[g];
     // groups above 2 * SB members (not produced by a tree with
-    // n_group_limit <= 256) run as consecutive chunks over the same lists
-    for (int ib = 0; ib < ni_all; ib += 2 * SB) {
-        const int ni = min(2 * SB, ni_all - ib);
+    // n_group_limit <= 256) run as consecutive chunks over the same lists;
+    // t_ipt2 >= 2 * SB (one i per thread throughout) chunks by SB
+    const int span = A.t_ipt2 >= 2 * SB ? SB : 2 * SB;
+    for (int ib = 0; ib < ni_all; ib += span) {
+        const int ni = min(span, ni_all - ib);
         if (ni > A.t_ipt2)
-            group_mixed<1, 2, EMIT>(A, g, ib, ni, sa, sb, sc, sidx, scnt, redf, redi);
+            group_mixed<1, 2, EMIT>(A, g, ib, ni, T, scnt, redf, redi);
         else if (ni > A.t_s1)
-            group_mixed<1, 1, EMIT>(A, g, ib, ni, sa, sb, sc, sidx, scnt, redf, redi);
+            group_mixed<1, 1, EMIT>(A, g, ib, ni, T, scnt, redf, redi);
         else if (ni > A.t_s2)
-            group_mixed<2, 1, EMIT>(A, g, ib, ni, sa, sb, sc, sidx, scnt, redf, redi);
+            group_mixed<2, 1, EMIT>(A, g, ib, ni, T, scnt, redf, redi);
         else
-            group_mixed<4, 1, EMIT>(A, g, ib, ni, sa, sb, sc, sidx, scnt, redf, redi);
+            group_mixed<4, 1, EMIT>(A, g, ib, ni, T, scnt, redf, redi);
         __syncthreads();
     }
 }
@@ -351,7 +462,7 @@ __device__ __forceinline__ void group_f64(const SoftArgs &A, int g, int ib, int 
     const int p_first = A.i_idx[i0];
 #pragma unroll
     for (int k = 0; k < IPT; k++) {
-        li[k] = lane + k * W;
+        li[k] = lane * IPT + k;
         vi[k] = li[k] < ni;
         int p = vi[k] ? A.i_idx[i0 + ib + li[k]] : p_first;
         if ((unsigned)p >= (unsigned)A.n_iptcl) { atomicOr(A.status, ST_BAD_INDEX); p = 0; vi[k] = false; }
@@ -362,6 +473,7 @@ __device__ __forceinline__ void group_f64(const SoftArgs &A, int g, int ib, int 
         ax[k] = ay[k] = az[k] = ap[k] = 0.;
         ngb[k] = 0; rk[k] = 0; idmax[k] = -1; idmin[k] = INT32_MAX_;
     }
+    const bool wact = (lane & ~31) * IPT < ni;
     if (EMIT)
         for (int t = tid; t < ni; t += SB) scnt[t] = 0;
 
@@ -378,7 +490,7 @@ __device__ __forceinline__ void group_f64(const SoftArgs &A, int g, int ib, int 
             if (EMIT) sidx[tid] = p;
         }
         __syncthreads();
-        const int jb = sub * (TJ / S), je = min(jb + TJ / S, nt);
+        const int jb = sub * (TJ / S), je = wact ? min(jb + TJ / S, nt) : jb;
         for (int jj = jb; jj < je; jj++) {
             const D4 a = da[jj];
             const D4 b = db[jj];
@@ -427,7 +539,7 @@ __device__ __forceinline__ void group_f64(const SoftArgs &A, int g, int ib, int 
             dc[tid] = D4c(3. * r.xy, 3. * r.yz, 3. * r.xz, 0.);
         }
         __syncthreads();
-        const int jb = sub * (TJ / S), je = min(jb + TJ / S, nt);
+        const int jb = sub * (TJ / S), je = wact ? min(jb + TJ / S, nt) : jb;
         for (int jj = jb; jj < je; jj++) {
             const D4 a = da[jj], q1 = db[jj], q2 = dc[jj];
 #pragma unroll
@@ -502,8 +614,9 @@ __global__ void __launch_bounds__(SB, 2) soft_f64_kernel(SoftArgs A) {
     __shared__ int redi[SB * 4];
     const int g = A.group_order ? A.group_order[blockIdx.x] : blockIdx.x;
     const int ni_all = A.i_off[g + 1] - A.i_off[g];
-    for (int ib = 0; ib < ni_all; ib += 2 * SB) {
-        const int ni = min(2 * SB, ni_all - ib);
+    const int span = A.t_ipt2 >= 2 * SB ? SB : 2 * SB;
+    for (int ib = 0; ib < ni_all; ib += span) {
+        const int ni = min(span, ni_all - ib);
         if (ni > A.t_ipt2)
             group_f64<1, 2, EMIT>(A, g, ib, ni, da, db, dc, dids, sidx, scnt, redd, redi);
         else if (ni > A.t_s1)

@@ -45,7 +45,8 @@ int p3t_set_options(int precision, int trace_mode, int cand_cap);
 /* Work split of the soft kernel by i-group size ni: ni > t_ipt2 two
  * i-particles per thread, > t_s1 one per thread, > t_s2 the j lists split
  * two ways, else four (0 <= t_s2 <= 32 <= ..., t_s2 <= t_s1 <= 64,
- * t_s1 <= t_ipt2 <= 128; defaults 128, 64, 32).  Set by the autotuner
+ * t_s1 <= t_ipt2 <= 128, or t_ipt2 = 256: one i-particle per thread
+ * throughout, groups above 128 in chunks; defaults 128, 64, 32).  Set by the autotuner
  * (gplum_gb300/autotune.py); forces agree to rounding across settings, the
  * neighbour fields bit for bit. */
 int p3t_set_soft_tiles(int t_ipt2, int t_s1, int t_s2);
@@ -286,8 +287,8 @@ int p3t_soft_force_noalloc(int n, const void *epj, int n_group, const int *i_off
                            void *stream);
 
 /* ---- measurement -------------------------------------------------------------
- * FMA throughput of this GPU (TFLOP/s, FMA = 2 flops), FP32 (fp64 = 0) or
- * FP64 (fp64 = 1): the roofline denominators of the soft (FP32-pipe) and
+ * FMA throughput of this GPU (TFLOP/s, FMA = 2 flops), FP32 (fp64 = 0),
+ * FP64 (fp64 = 1) or packed FP32 pairs (fp64 = 2, fma.rn.f32x2): the roofline denominators of the soft (FP32-pipe) and
  * hard (FP64-pipe) kernels.  No counterpart in GPLUM. */
 int p3t_probe_fma_peak(int fp64, double *tflops);
 

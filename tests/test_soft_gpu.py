@@ -181,7 +181,7 @@ def test_host_one_call_equals_resident(gpu):
     assert a.tobytes() == sf.download().tobytes()
 
 
-@pytest.mark.parametrize("tiles", [(0, 0, 0), (64, 32, 16), (128, 64, 0)])
+@pytest.mark.parametrize("tiles", [(0, 0, 0), (64, 32, 16), (128, 64, 0), (256, 64, 32)])
 def test_work_splits_agree(gpu, tiles):
     """Every work split the autotuner may choose gives the same neighbour
     fields and forces equal to rounding (sub-block partial sums combine in a
@@ -206,3 +206,4 @@ def test_work_splits_agree(gpu, tiles):
         np.testing.assert_array_equal(got[k], ref[k])
     assert rel_err(got["acc"].astype(np.float64), ref["acc"].astype(np.float64)).max() < 1e-6
     assert lib.p3t_set_soft_tiles(40, 64, 32) != 0  # invalid: t_ipt2 < t_s1
+    assert lib.p3t_set_soft_tiles(200, 64, 32) != 0  # invalid: neither <= 128 nor 256
