@@ -397,6 +397,7 @@ def gpu_arm(args, rank, world):
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": args.steps,
         "soft_tiles": tuning["soft_tiles"] if tuning else [128, 64, 32],
+        "soft_ctas_per_sm": tuning.get("soft_occ", 5) if tuning else 5,
         "clocks": clocks,
     }
     if not args.skip_step:

@@ -4,8 +4,9 @@ Two choices are made by measurement on the live workload instead of fixed in
 code:
 
 * the soft kernel's work split by i-group size (p3t_set_soft_tiles: above
-  t_ipt2 members two i-particles per thread (256: never), above t_s1 one,
-  above t_s2 the j lists split two ways, else four) -- timed on the 1,048,576-body soft-force
+  t_s1 members one i-particle per thread, above t_s2 the j lists split two
+  ways, else four) and its register budget (p3t_set_soft_occupancy: 4, 5 or
+  6 resident CTAs per SM) -- timed on the 1,048,576-body soft-force
   disk (0.5-1.5 AU, m = 1e-10, theta = 0.5, n_group_limit = 256);
 * the bundle form's heavy-cluster threshold (p3t_set_hard_heavy: clusters
   whose learned prediction of log2(1 + block steps) reaches it run alone in a
@@ -31,7 +32,8 @@ import numpy as np
 from . import _lib
 
 TUNING = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning.json")
-SOFT_GRID = [(a, b, c) for a in (64, 96, 128, 256) for b in (32, 48, 64) for c in (0, 16, 32) if c <= b <= a]
+# (t_ipt2, t_s1, t_s2, CTAs per SM); the mixed form always runs one i per thread
+SOFT_GRID = [(128, b, c, o) for b in (32, 48, 64) for c in (0, 16, 32) for o in (4, 5, 6) if c <= b]
 TIER_GRID = [(w, t) for w in (2, 4, 8, 16) for t in (32, 64, 128, 256)]
 
 
@@ -51,11 +53,13 @@ def tune_soft(lib, run, grid=SOFT_GRID, reps=5):
     split; installs the fastest.  Returns (best, {split: ms})."""
     table = {}
     for cfg in grid:
-        _lib.check(lib.p3t_set_soft_tiles(*cfg), "p3t_set_soft_tiles")
+        _lib.check(lib.p3t_set_soft_tiles(*cfg[:3]), "p3t_set_soft_tiles")
+        _lib.check(lib.p3t_set_soft_occupancy(cfg[3]), "p3t_set_soft_occupancy")
         run()
         table[cfg] = 1e3 * _timed(lib, run, reps)
     best = min(table, key=table.get)
-    _lib.check(lib.p3t_set_soft_tiles(*best), "p3t_set_soft_tiles")
+    _lib.check(lib.p3t_set_soft_tiles(*best[:3]), "p3t_set_soft_tiles")
+    _lib.check(lib.p3t_set_soft_occupancy(best[3]), "p3t_set_soft_occupancy")
     return best, table
 
 
@@ -110,6 +114,8 @@ def load(lib=None, path=TUNING):
     t = json.load(open(path))
     if "soft_tiles" in t:
         _lib.check(lib.p3t_set_soft_tiles(*t["soft_tiles"]), "p3t_set_soft_tiles")
+    if "soft_occ" in t:
+        _lib.check(lib.p3t_set_soft_occupancy(t["soft_occ"]), "p3t_set_soft_occupancy")
     if "hard_tiers" in t:
         _lib.check(lib.p3t_set_hard_tiers(*t["hard_tiers"]), "p3t_set_hard_tiers")
     if "hard_heavy" in t:
@@ -144,10 +150,12 @@ def main():
     soft_best, soft_table = tune_soft(lib, lambda: sf.run(emit_candidates=True))
     if args.soft_only:
         out = json.load(open(args.out)) if os.path.exists(args.out) else {}
-        out["soft_tiles"] = list(soft_best)
+        out["soft_tiles"] = list(soft_best[:3])
+        out["soft_occ"] = soft_best[3]
         out["soft_ms"] = {",".join(map(str, k)): v for k, v in soft_table.items()}
         json.dump(out, open(args.out, "w"), indent=1)
-        print(json.dumps({"soft_tiles": out["soft_tiles"], "soft_ms_best": soft_table[soft_best]}))
+        print(json.dumps({"soft_tiles": out["soft_tiles"], "soft_occ": out["soft_occ"],
+                          "soft_ms_best": soft_table[soft_best]}))
         return
     # hard: tier cutoffs of the per-team form on the hard-part disk
     d = disk_1m_hard()
@@ -176,7 +184,8 @@ def main():
             g.kick()
             g.cluster()
         heavy_best = min(heavy_table, key=heavy_table.get)
-    out = {"soft_tiles": list(soft_best),
+    out = {"soft_tiles": list(soft_best[:3]),
+           "soft_occ": soft_best[3],
            "soft_ms": {",".join(map(str, k)): v for k, v in soft_table.items()},
            "hard_tiers": list(hard_best),
            "hard_heavy": heavy_best if heavy_best is not None else 6.5,
@@ -186,7 +195,7 @@ def main():
                          "hard": "1048576-body hard-part disk 0.95-1.05 AU, m=7e-11, rms e=6h, rms i=3h"}}
     json.dump(out, open(args.out, "w"), indent=1)
     print(json.dumps({"soft_tiles": out["soft_tiles"], "soft_ms_best": soft_table[soft_best],
-                      "soft_ms_default": soft_table.get((128, 64, 32)), "hard_tiers": out["hard_tiers"],
+                      "soft_ms_default": soft_table.get((128, 64, 32, 5)), "hard_tiers": out["hard_tiers"],
                       "hard_ms_best": hard_table[hard_best], "hard_ms_default": hard_table.get((8, 64)),
                       "hard_heavy": out["hard_heavy"], "hard_heavy_ms": out["hard_heavy_ms"]}))
 

@@ -162,6 +162,7 @@ SoftArgs make_args(Context *c, DevSet &d, int n_group, int n_ptcl, int n_spj, bo
     A.t_ipt2 = c->tiles[0];
     A.t_s1 = c->tiles[1];
     A.t_s2 = c->tiles[2];
+    A.occ = c->soft_occ;
     return A;
 }
 
@@ -228,6 +229,13 @@ int p3t_set_soft_tiles(int t_ipt2, int t_s1, int t_s2) {
     c->tiles[0] = t_ipt2;
     c->tiles[1] = t_s1;
     c->tiles[2] = t_s2;
+    return 0;
+}
+
+int p3t_set_soft_occupancy(int ctas_per_sm) {
+    CTX_OR_FAIL(c);
+    if (ctas_per_sm < 4 || ctas_per_sm > 6) return ST_BAD_INDEX;
+    c->soft_occ = ctas_per_sm;
     return 0;
 }
 

@@ -7,12 +7,13 @@
 // cudaMalloc/cudaFree.  p3t_soft_force_noalloc serves them: the caller passes
 // the body records, the interaction lists, the superparticles and the output
 // buffer (all device-accessible), and the only scratch the computation needs
-// -- the packed body records the soft kernel gathers, and one status word --
-// lives in file-scope static device arrays.
+// -- the packed body records the soft kernel gathers, their FP32 splits, the
+// packed superparticles, and one status word -- lives in file-scope static
+// device arrays.
 //
 // Those arrays exist once per GPU that loads this library and stay allocated
-// until the process exits (P3T_NOALLOC_MAX_BODIES x 48 B = 3 MiB, plus one
-// status word).  Their device addresses are looked up once per device, on
+// until the process exits (P3T_NOALLOC_MAX_BODIES x 80 B = 5 MiB,
+// P3T_NOALLOC_MAX_SPJ x 64 B = 4 MiB, plus one status word).  Their device addresses are looked up once per device, on
 // that device's first call (cudaGetSymbolAddress with the device current), so
 // the first call on a device should happen before any stream capture.  Every
 // call shares the arrays: calls that overlap on the GPU (different streams,
@@ -28,11 +29,15 @@
 namespace {
 
 static __device__ __align__(256) p3t::SoftPtcl g_noalloc_bodies[P3T_NOALLOC_MAX_BODIES];
+static __device__ __align__(256) p3t::SoftSplit g_noalloc_split[P3T_NOALLOC_MAX_BODIES];
+static __device__ __align__(256) p3t::SpjPack g_noalloc_spj[P3T_NOALLOC_MAX_SPJ];
 static __device__ __align__(256) int g_noalloc_status[1];
 
 struct DeviceScratch {
     bool ready = false;
     p3t::SoftPtcl *bodies = nullptr;
+    p3t::SoftSplit *split = nullptr;
+    p3t::SpjPack *spj = nullptr;
     int *status = nullptr;
 };
 constexpr int MAX_DEVICES = 64;
@@ -51,6 +56,10 @@ int scratch_for_current_device(DeviceScratch **out) {
     DeviceScratch &s = g_scratch[dev];
     if (!s.ready) {
         e = cudaGetSymbolAddress((void **)&s.bodies, g_noalloc_bodies);
+        if (e != cudaSuccess) return -(int)e;
+        e = cudaGetSymbolAddress((void **)&s.split, g_noalloc_split);
+        if (e != cudaSuccess) return -(int)e;
+        e = cudaGetSymbolAddress((void **)&s.spj, g_noalloc_spj);
         if (e != cudaSuccess) return -(int)e;
         e = cudaGetSymbolAddress((void **)&s.status, g_noalloc_status);
         if (e != cudaSuccess) return -(int)e;
@@ -94,6 +103,13 @@ extern "C" int p3t_soft_force_noalloc(int n, const void *epj, int n_group, const
                      n, P3T_NOALLOC_MAX_BODIES);
         return -(int)cudaErrorInvalidValue;
     }
+    if (n_spj > P3T_NOALLOC_MAX_SPJ) {
+        std::fprintf(stderr,
+                     "[gplum_p3t] p3t_soft_force_noalloc: %d superparticles exceed the static scratch of %d; "
+                     "use p3t_soft_force_host or the resident path for larger systems\n",
+                     n_spj, P3T_NOALLOC_MAX_SPJ);
+        return -(int)cudaErrorInvalidValue;
+    }
     if (n_group < 0 || n_spj < 0 || (trace_mode != 0 && trace_mode != 1)) return -(int)cudaErrorInvalidValue;
     if (n == 0 || n_group == 0) return 0;
     DeviceScratch *s = nullptr;
@@ -129,6 +145,9 @@ extern "C" int p3t_soft_force_noalloc(int n, const void *epj, int n_group, const
     A.cand = nullptr;
     A.cand_cap = 0;
     A.status = s->status;
+    A.jsplit = s->split;
+    A.isplit = s->split;
+    A.spjp = s->spj;
     if ((e = launch_soft(A, 0, false, st)) != cudaSuccess) return -(int)e;
     int h = 0;
     if ((e = cudaMemcpyAsync(&h, s->status, sizeof(int), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return -(int)e;

@@ -71,6 +71,7 @@ struct Context {
     int trace_mode = 0;
     int cand_cap = 64;
     int tiles[3] = {128, 64, 32};  // soft-kernel work split (SoftArgs::t_ipt2, t_s1, t_s2)
+    int soft_occ = 5;              // mixed soft kernel: resident CTAs per SM (SoftArgs::occ)
     // resident problem
     DevSet res;
     int res_n = 0, res_groups = 0, res_spj = 0;

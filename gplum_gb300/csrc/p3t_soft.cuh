@@ -4,6 +4,23 @@
 
 namespace p3t {
 
+// Mixed form, per particle: the FP32 two-float split of the FP64 position
+// (xh = rn(x), xl = rn(x - xh); xh + xl carries x to ~2^-48 relative) with
+// the mass and squared r_out, so the pair loops form displacements from FP32
+// data alone.
+struct __align__(16) SoftSplit {
+    float xh, yh, zh, m, xl, yl, zl, ro2;
+};
+static_assert(sizeof(SoftSplit) == 32, "SoftSplit");
+// Mixed form, per superparticle: the split position, the mass, and the
+// quadrupole terms the pair loop uses, negated: -(3Q - tr I) and
+// eps^2 tr (= -mtr), tr as trace_mode selects.
+struct __align__(16) SpjPack {
+    float xh, yh, zh, m, xl, yl, zl, nmtr;
+    float nqxx, nqyy, nqzz, nqxy, nqyz, nqzx, pad0, pad1;
+};
+static_assert(sizeof(SpjPack) == 64, "SpjPack");
+
 struct SoftArgs {
     // CSR lists (see include/p3t_tree.h)
     const int *i_off, *i_idx, *j_off, *j_idx, *s_off, *s_idx;
@@ -31,11 +48,19 @@ struct SoftArgs {
     int cand_cap;
     int *status;
     // work split of an i-group of ni members over the CTA's 128 threads:
-    // ni > t_ipt2: 2 i per thread; > t_s1: 1 i per thread; > t_s2: the j list
+    // ni > t_ipt2: 2 i per thread (FP64 form only); > t_s1: 1 i per thread; > t_s2: the j list
     // split 2 ways; else 4 ways (0 <= t_s2 <= 32, t_s2 <= t_s1 <= 64,
     // t_s1 <= t_ipt2 <= 128 or t_ipt2 = 256: never 2 i per thread, groups
     // above 128 in chunks of 128; 0 = the defaults 128, 64, 32)
     int t_ipt2, t_s1, t_s2;
+    // mixed form: resident CTAs per SM the kernel is compiled for (4, 5 or 6;
+    // 0 = 5), i.e. its register budget
+    int occ;
+    // mixed form scratch, filled by launch_soft before the pair kernel:
+    // [n_iptcl], [n_ptcl] and [n_spj] records.  nullptr = launch_soft's own
+    // per-device buffers (stream-ordered, grown on demand).
+    SoftSplit *isplit, *jsplit;
+    SpjPack *spjp;
 };
 
 cudaError_t launch_pack_epj(const EPJRec *in, int n, SoftPtcl *out, double *mass, double *r_out, double *r_search,

@@ -36,6 +36,8 @@
 // Optional candidate emission: every screen hit (j != i) appends j's particle
 // index to the i's row of a [n x cap] candidate table; the device-side
 // cutoff correction and neighbour search read it instead of a tree query.
+#include <mutex>
+
 #include "p3t_common.cuh"
 #include "p3t_soft.cuh"
 
@@ -67,22 +69,34 @@ __device__ __forceinline__ void fold(float &hi, float &lo, float v) {
 // negation of the unnegated one.  A tile is padded to a multiple of 32
 // entries with massless entries 1e18 away, which contribute exact zeros.
 //
+// Displacements.  EP-EP: from the two-float splits (SoftSplit),
+// r = (xh_i - xh_j) + (xl_i - xl_j) in FP32: the first difference rounds
+// relative to r itself and the split carries x to ~2^-48, so r keeps ~1e-7
+// relative precision however far the pair sits from the group origin.
+// EP-SP: relative to the group origin (the functor's epi[0]), each side's
+// local coordinate rounded from its split, rn((xh - oxh) + (xl - oxl)).
+// No FP64 arithmetic in the staging except the functor's own local
+// coordinates of the j-particles, which the exact neighbour screen needs.
+//
 // Neighbour screen: inside the loop a pair only sets a bit when the force's
 // r^2 lies below 1.01 max(r_s,i^2, r_s,j^2) (precomputed per i and per j as
 // 1.01 r_s^2: x -> rn(1.01 x) is monotone, so the max commutes); after each
 // chunk of 32 entries the flagged pairs alone are re-screened exactly, in
-// list order, with the functor's FP32 arithmetic.
-constexpr int TP = TJ / 2;  // entry pairs per tile
+// list order, with the functor's FP32 arithmetic on its own rounded local
+// coordinates rn(x - x_epi[0]).
+constexpr int TM = 128;     // list entries per mixed-form tile
+constexpr int TP = TM / 2;  // entry pairs per tile
 
 struct MixedTile {
-    // EP-EP: a = (-hx0,-hx1,-hy0,-hy1) b = (-hz0,-hz1,m0,m1)
-    //        c = (-xl0,-xl1,-yl0,-yl1) d = (-zl0,-zl1,ro2_0,ro2_1) e = (t0,t1) t = 1.01 rs2_j
-    // EP-SP: a = (-x0,-x1,-y0,-y1)     b = (-z0,-z1,m0,m1)
-    //        c = -(q'xx, q'yy)         d = -(q'zz, mtr)   f = -(3qxy, 3qyz)  e = -(3qzx)
+    // EP-EP: a = -(xh0,xh1,yh0,yh1) b = (-zh0,-zh1,m0,m1)
+    //        c = -(xl0,xl1,yl0,yl1) d = (-zl0,-zl1,ro2_0,ro2_1) e = (t0,t1) t = 1.01 rs2_j
+    // EP-SP: a = -(x0,x1,y0,y1) local  b = (-z0,-z1,m0,m1)
+    //        c = -(q'xx, q'yy)         d = (-q'zz, -mtr)   f = -(3qxy, 3qyz)  e = -(3qzx)
     float4 a[TP], b[TP], c[TP], d[TP], f[TP];
     float2 e[TP];
-    float4 r[TJ];  // EP-EP exact screen: (rs2, id, rank, -)
-    int idx[TJ];   // EP-EP particle index of each entry (candidate emission)
+    float4 r[TM];  // EP-EP exact screen: the functor's local (x, y, z) and rs2
+    int2 q[TM];    // EP-EP (id_local, rank)
+    int idx[TM];   // EP-EP particle index of each entry (candidate emission)
 };
 
 __device__ __forceinline__ float rsqrt_ftz(float x) {
@@ -99,13 +113,10 @@ __device__ __forceinline__ void put2(float4 *arr, int t, int comp, float v) {
     // entry t's value of packed component comp (0: .x/.y, 1: .z/.w)
     reinterpret_cast<float *>(arr)[4 * (t >> 1) + 2 * comp + (t & 1)] = v;
 }
-__device__ __forceinline__ float get2(const float4 *arr, int t, int comp) {
-    return reinterpret_cast<const float *>(arr)[4 * (t >> 1) + 2 * comp + (t & 1)];
-}
 
-template <int S, int IPT, bool EMIT>
-__device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, int ni, MixedTile &T, int *scnt,
-                                            float *redf, int *redi) {
+template <int S, int IPT, bool EMIT, int UNR>
+__device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, int ni, MixedTile &T, float4 *sI,
+                                            int4 *sQ, int *scnt, float *redf, int *redi) {
     // i-particles [ib, ib + ni) of group g (ni <= 2 * SB); the origin is the
     // group's first i-particle, as in the functor
     constexpr int W = SB / S;
@@ -120,9 +131,15 @@ __device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, in
     int p_first = A.i_idx[i0];
     if ((unsigned)p_first >= (unsigned)A.n_iptcl) { atomicOr(A.status, ST_BAD_INDEX); p_first = 0; }
     const double ox = A.iptcl[p_first].x, oy = A.iptcl[p_first].y, oz = A.iptcl[p_first].z;
+    const SoftSplit o = A.isplit[p_first];
 
-    float xi[IPT], yi[IPT], zi[IPT], xl[IPT], yl[IPT], zl[IPT], ro2i[IPT], rs2i[IPT], thi[IPT];
-    int idi[IPT], rki[IPT], pid[IPT], li[IPT];
+    // per i, in registers: split position (EP-EP force), r_out^2 and the
+    // flag threshold; in shared memory (sI, sQ, one slot per thread and i;
+    // read only by the exact screen and the final write): the functor's local
+    // coordinates, rs2, id_local, rank, the particle index
+    float xh[IPT], yh[IPT], zh[IPT], xl[IPT], yl[IPT], zl[IPT], xf[IPT], yf[IPT], zf[IPT];
+    float ro2i[IPT], thi[IPT];
+    int li[IPT];
     bool vi[IPT];
     float ahx[IPT], alx[IPT], ahy[IPT], aly[IPT], ahz[IPT], alz[IPT], ahp[IPT], alp[IPT];
     int ngb[IPT], rk[IPT], idmax[IPT], idmin[IPT];
@@ -132,19 +149,16 @@ __device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, in
         vi[k] = li[k] < ni;
         int p = vi[k] ? A.i_idx[i0 + ib + li[k]] : p_first;
         if ((unsigned)p >= (unsigned)A.n_iptcl) { atomicOr(A.status, ST_BAD_INDEX); p = 0; vi[k] = false; }
-        pid[k] = p;
         const SoftPtcl r = A.iptcl[p];
-        const double dx = r.x - ox, dy = r.y - oy, dz = r.z - oz;
-        xi[k] = __double2float_rn(dx);
-        yi[k] = __double2float_rn(dy);
-        zi[k] = __double2float_rn(dz);
-        xl[k] = __double2float_rn(dx - (double)xi[k]);
-        yl[k] = __double2float_rn(dy - (double)yi[k]);
-        zl[k] = __double2float_rn(dz - (double)zi[k]);
+        const SoftSplit sp = A.isplit[p];
+        xf[k] = __double2float_rn(r.x - ox);
+        yf[k] = __double2float_rn(r.y - oy);
+        zf[k] = __double2float_rn(r.z - oz);
+        sI[tid * IPT + k] = make_float4(xf[k], yf[k], zf[k], r.rs2);
+        sQ[tid * IPT + k] = make_int4(r.id_local, r.rank, p, 0);
+        xh[k] = sp.xh; yh[k] = sp.yh; zh[k] = sp.zh;
+        xl[k] = sp.xl; yl[k] = sp.yl; zl[k] = sp.zl;
         ro2i[k] = r.ro2;
-        rs2i[k] = r.rs2;
-        idi[k] = r.id_local;
-        rki[k] = r.rank;
         ahx[k] = alx[k] = ahy[k] = aly[k] = ahz[k] = alz[k] = ahp[k] = alp[k] = 0.f;
         ngb[k] = 0; rk[k] = 0; idmax[k] = -1; idmin[k] = INT32_MAX_;
     }
@@ -154,47 +168,48 @@ __device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, in
     if (EMIT) {
         for (int t = tid; t < ni; t += SB) scnt[t] = 0;
     }
-    // Screen prefilter.  The force's r^2 (residue-corrected displacement, FMA)
-    // differs from the screen's exact r^2 by FP32 rounding (< 6e-7 relative)
-    // and by the residues, |delta| <= 1.06e-7 (2 L + r_s) for a pair inside
-    // the search radius r_s, L the group's largest local coordinate.  With
-    // L <= 2e4 r_s,min the force's r^2 stays below 1.01 r_s^2 for every pair
-    // the exact screen accepts, so leaving pairs above that unflagged is
-    // exact; otherwise every pair is flagged.
+    // Screen prefilter.  The force's r^2 (split displacement, FMA) is within
+    // 5e-7 relative of the exact r^2; the functor's differs from the exact one
+    // by its rounding of the local coordinates, |delta| <= 1.06e-7 (2 L + r_s)
+    // per component for a pair inside the search radius r_s, L the group's
+    // largest local coordinate.  With L <= 2e4 r_s,min the force's r^2 stays
+    // below 1.01 r_s^2 for every pair the exact screen accepts, so leaving
+    // pairs above that unflagged is exact; otherwise every pair is flagged.
     {
         float L = 0.f, rmin2 = 3.0e38f;
 #pragma unroll
         for (int k = 0; k < IPT; k++)
             if (vi[k]) {
-                L = fmaxf(L, fmaxf(fabsf(xi[k]), fmaxf(fabsf(yi[k]), fabsf(zi[k]))));
-                rmin2 = fminf(rmin2, rs2i[k]);
+                L = fmaxf(L, fmaxf(fabsf(xf[k]), fmaxf(fabsf(yf[k]), fabsf(zf[k]))));
+                rmin2 = fminf(rmin2, sI[tid * IPT + k].w);
             }
         const bool pre_ok = __syncthreads_and(L * L <= 4.0e8f * rmin2) != 0;
 #pragma unroll
-        for (int k = 0; k < IPT; k++) thi[k] = pre_ok ? 1.01f * rs2i[k] : 3.0e38f;
+        for (int k = 0; k < IPT; k++) thi[k] = pre_ok ? 1.01f * sI[tid * IPT + k].w : 3.0e38f;
     }
     const float2 c15 = dup2(1.5f), cm05 = dup2(-0.5f);
 
     // ---- EP-EP ----
-    for (int base = 0; base < nj; base += TJ) {
-        const int nt = min(TJ, nj - base);
+    for (int base = 0; base < nj; base += TM) {
+        const int nt = min(TM, nj - base);
         __syncthreads();
-        {
-            const int t = tid;
+        for (int t = tid; t < TM; t += SB) {
             if (t < nt) {
                 int p = A.j_idx[j0 + base + t];
                 if ((unsigned)p >= (unsigned)A.n_ptcl) { atomicOr(A.status, ST_BAD_INDEX); p = 0; }
-                const SoftPtcl r = A.ptcl[p];
-                const double dx = r.x - ox, dy = r.y - oy, dz = r.z - oz;
-                const float hx = __double2float_rn(dx), hy = __double2float_rn(dy), hz = __double2float_rn(dz);
-                put2(T.a, t, 0, -hx); put2(T.a, t, 1, -hy);
-                put2(T.b, t, 0, -hz); put2(T.b, t, 1, r.m);
-                put2(T.c, t, 0, -__double2float_rn(dx - (double)hx));
-                put2(T.c, t, 1, -__double2float_rn(dy - (double)hy));
-                put2(T.d, t, 0, -__double2float_rn(dz - (double)hz));
-                put2(T.d, t, 1, r.ro2);
-                reinterpret_cast<float *>(T.e)[t] = 1.01f * r.rs2;
-                T.r[t] = make_float4(r.rs2, __int_as_float(r.id_local), __int_as_float(r.rank), 0.f);
+                const SoftSplit sp = A.jsplit[p];
+                const SoftPtcl &r = A.ptcl[p];
+                const double x = r.x, y = r.y, z = r.z;
+                const float rs2 = r.rs2;
+                const int id = r.id_local, rank = r.rank;
+                put2(T.a, t, 0, -sp.xh); put2(T.a, t, 1, -sp.yh);
+                put2(T.b, t, 0, -sp.zh); put2(T.b, t, 1, sp.m);
+                put2(T.c, t, 0, -sp.xl); put2(T.c, t, 1, -sp.yl);
+                put2(T.d, t, 0, -sp.zl); put2(T.d, t, 1, sp.ro2);
+                reinterpret_cast<float *>(T.e)[t] = 1.01f * rs2;
+                T.r[t] = make_float4(__double2float_rn(x - ox), __double2float_rn(y - oy), __double2float_rn(z - oz),
+                                     rs2);
+                T.q[t] = make_int2(id, rank);
                 if (EMIT) T.idx[t] = p;
             } else {  // padding: massless, far away, never flagged
                 put2(T.a, t, 0, -1.0e18f); put2(T.a, t, 1, -1.0e18f);
@@ -202,13 +217,14 @@ __device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, in
                 put2(T.c, t, 0, 0.f); put2(T.c, t, 1, 0.f);
                 put2(T.d, t, 0, 0.f); put2(T.d, t, 1, 0.f);
                 reinterpret_cast<float *>(T.e)[t] = 0.f;
-                T.r[t] = make_float4(0.f, __int_as_float(-1), __int_as_float(-1), 0.f);
+                T.r[t] = make_float4(1.0e18f, 1.0e18f, 1.0e18f, 0.f);
+                T.q[t] = make_int2(-1, -1);
             }
         }
         __syncthreads();
         // this sub-block's share of the tile, in whole chunks of 32 entries
-        const int jb = sub * (TJ / S);
-        const int je = wact ? min(jb + TJ / S, (nt + CHUNK - 1) & ~(CHUNK - 1)) : jb;
+        const int jb = sub * (TM / S);
+        const int je = wact ? min(jb + TM / S, (nt + CHUNK - 1) & ~(CHUNK - 1)) : jb;
         for (int c0 = jb; c0 < je; c0 += CHUNK) {
             float2 tx[IPT], ty[IPT], tz[IPT], tp[IPT];
             unsigned nm[IPT];
@@ -217,20 +233,16 @@ __device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, in
                 tx[k] = ty[k] = tz[k] = tp[k] = dup2(0.f);
                 nm[k] = 0u;
             }
-#pragma unroll 8
+#pragma unroll UNR
             for (int q = 0; q < CHUNK / 2; q++) {
                 const int pq = (c0 >> 1) + q;
                 const float4 a = T.a[pq], b = T.b[pq], c = T.c[pq], d = T.d[pq];
                 const float2 e = T.e[pq];
 #pragma unroll
                 for (int k = 0; k < IPT; k++) {
-                    // the functor's FP32 displacement, then the low parts restored
-                    const float2 hx = __fadd2_rn(dup2(xi[k]), lo2(a));
-                    const float2 hy = __fadd2_rn(dup2(yi[k]), hi2(a));
-                    const float2 hz = __fadd2_rn(dup2(zi[k]), lo2(b));
-                    const float2 rx = __fadd2_rn(hx, __fadd2_rn(dup2(xl[k]), lo2(c)));
-                    const float2 ry = __fadd2_rn(hy, __fadd2_rn(dup2(yl[k]), hi2(c)));
-                    const float2 rz = __fadd2_rn(hz, __fadd2_rn(dup2(zl[k]), lo2(d)));
+                    const float2 rx = __fadd2_rn(__fadd2_rn(dup2(xh[k]), lo2(a)), __fadd2_rn(dup2(xl[k]), lo2(c)));
+                    const float2 ry = __fadd2_rn(__fadd2_rn(dup2(yh[k]), hi2(a)), __fadd2_rn(dup2(yl[k]), hi2(c)));
+                    const float2 rz = __fadd2_rn(__fadd2_rn(dup2(zh[k]), lo2(b)), __fadd2_rn(dup2(zl[k]), lo2(d)));
                     const float2 r2f = __ffma2_rn(rx, rx, __ffma2_rn(ry, ry, __ffma2_rn(rz, rz, eps2_2)));
                     const float2 r2 = make_float2(fmaxf(r2f.x, fmaxf(ro2i[k], d.z)), fmaxf(r2f.y, fmaxf(ro2i[k], d.w)));
                     float2 ri = rsqrt2(r2);
@@ -253,61 +265,71 @@ __device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, in
                 fold(ahp[k], alp[k], tp[k].x + tp[k].y);
                 // exact screen of the flagged pairs, in list order
                 unsigned m = vi[k] ? nm[k] : 0u;
-                while (m) {
+                if (m) {
+                    const float4 me = sI[tid * IPT + k];
+                    const int4 mq = sQ[tid * IPT + k];
+                    do {
                     const int jj = c0 + __ffs(m) - 1;
                     m &= m - 1;
-                    const float hx = __fadd_rn(xi[k], get2(T.a, jj, 0));
-                    const float hy = __fadd_rn(yi[k], get2(T.a, jj, 1));
-                    const float hz = __fadd_rn(zi[k], get2(T.b, jj, 0));
                     const float4 rr = T.r[jj];
+                    const float hx = __fsub_rn(me.x, rr.x);
+                    const float hy = __fsub_rn(me.y, rr.y);
+                    const float hz = __fsub_rn(me.z, rr.z);
                     const float r2r =
                         __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(hx, hx), __fmul_rn(hy, hy)), __fmul_rn(hz, hz)), eps2);
-                    if (r2r < fmaxf(rs2i[k], rr.x)) {
-                        const int idj = __float_as_int(rr.y), rkj = __float_as_int(rr.z);
-                        if (idi[k] != idj || rki[k] != rkj) {
+                    if (r2r < fmaxf(me.w, rr.w)) {
+                        const int2 qq = T.q[jj];
+                        const int idj = qq.x, rkj = qq.y;
+                        if (mq.x != idj || mq.y != rkj) {
                             ngb[k] += 1;
-                            rk[k] += abs(rki[k] - rkj);
+                            rk[k] += abs(mq.y - rkj);
                             idmax[k] = max(idmax[k], idj);
                             idmin[k] = min(idmin[k], idj);
                             if (EMIT) {
                                 const int slot = atomicAdd(&scnt[li[k]], 1);
                                 if (slot < A.cand_cap)
-                                    A.cand[(size_t)pid[k] * A.cand_cap + slot] = T.idx[jj];
+                                    A.cand[(size_t)mq.z * A.cand_cap + slot] = T.idx[jj];
                                 else
                                     atomicOr(A.status, ST_CAND_OVERFLOW);
                             }
                         }
                     }
+                    } while (m);
                 }
             }
         }
     }
 
     // ---- EP-SP (quadrupole) ----
+    // origin-relative FP32 coordinates of the i-particles
+#pragma unroll
+    for (int k = 0; k < IPT; k++) {
+        xf[k] = __fadd_rn(__fsub_rn(xh[k], o.xh), __fsub_rn(xl[k], o.xl));
+        yf[k] = __fadd_rn(__fsub_rn(yh[k], o.yh), __fsub_rn(yl[k], o.yl));
+        zf[k] = __fadd_rn(__fsub_rn(zh[k], o.zh), __fsub_rn(zl[k], o.zl));
+    }
     const float2 c05 = dup2(-0.5f), c25 = dup2(-2.5f);
-    for (int base = 0; base < ns; base += TJ) {
-        const int nt = min(TJ, ns - base);
+    for (int base = 0; base < ns; base += TM) {
+        const int nt = min(TM, ns - base);
         __syncthreads();
-        {
-            const int t = tid;
+        for (int t = tid; t < TM; t += SB) {
             if (t < nt) {
                 int q = A.s_idx[s0 + base + t];
                 if ((unsigned)q >= (unsigned)A.n_spj) { atomicOr(A.status, ST_BAD_INDEX); q = 0; }
-                const SPJRec &r = A.spj[q];
-                const float qxx = (float)r.xx, qyy = (float)r.yy, qzz = (float)r.zz;
-                const float qxy = (float)r.xy, qyz = (float)r.yz, qzx = (float)r.xz;
-                const float tr = A.trace_mode ? (float)(r.xx + r.yy + r.zz) : (float)(r.xx + r.yy + r.xx);
-                put2(T.a, t, 0, -__double2float_rn(r.pos[0] - ox));
-                put2(T.a, t, 1, -__double2float_rn(r.pos[1] - oy));
-                put2(T.b, t, 0, -__double2float_rn(r.pos[2] - oz));
-                put2(T.b, t, 1, (float)r.mass);
-                put2(T.c, t, 0, -(3.0f * qxx - tr));
-                put2(T.c, t, 1, -(3.0f * qyy - tr));
-                put2(T.d, t, 0, -(3.0f * qzz - tr));
-                put2(T.d, t, 1, eps2 * tr);
-                put2(T.f, t, 0, -(3.0f * qxy));
-                put2(T.f, t, 1, -(3.0f * qyz));
-                reinterpret_cast<float *>(T.e)[t] = -(3.0f * qzx);
+                const float4 *rp = reinterpret_cast<const float4 *>(A.spjp + q);
+                const float4 p0 = rp[0], p1 = rp[1], p2 = rp[2], p3 = rp[3];
+                // -(local coordinate) = (oxh - xh) + (oxl - xl)
+                put2(T.a, t, 0, __fadd_rn(__fsub_rn(o.xh, p0.x), __fsub_rn(o.xl, p1.x)));
+                put2(T.a, t, 1, __fadd_rn(__fsub_rn(o.yh, p0.y), __fsub_rn(o.yl, p1.y)));
+                put2(T.b, t, 0, __fadd_rn(__fsub_rn(o.zh, p0.z), __fsub_rn(o.zl, p1.z)));
+                put2(T.b, t, 1, p0.w);
+                put2(T.c, t, 0, p2.x);
+                put2(T.c, t, 1, p2.y);
+                put2(T.d, t, 0, p2.z);
+                put2(T.d, t, 1, p1.w);
+                put2(T.f, t, 0, p2.w);
+                put2(T.f, t, 1, p3.x);
+                reinterpret_cast<float *>(T.e)[t] = p3.y;
             } else {  // padding: massless, far away
                 put2(T.a, t, 0, -1.0e18f); put2(T.a, t, 1, -1.0e18f);
                 put2(T.b, t, 0, -1.0e18f); put2(T.b, t, 1, 0.f);
@@ -318,8 +340,8 @@ __device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, in
             }
         }
         __syncthreads();
-        const int jb = sub * (TJ / S);
-        const int je = wact ? min(jb + TJ / S, (nt + CHUNK - 1) & ~(CHUNK - 1)) : jb;
+        const int jb = sub * (TM / S);
+        const int je = wact ? min(jb + TM / S, (nt + CHUNK - 1) & ~(CHUNK - 1)) : jb;
         for (int c0 = jb; c0 < je; c0 += CHUNK) {
             float2 tx[IPT], ty[IPT], tz[IPT], tp[IPT];
 #pragma unroll
@@ -333,9 +355,9 @@ __device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, in
                 for (int k = 0; k < IPT; k++) {
                     // r' = x_i - x_j (the negated displacement); with the tile's
                     // negated quadrupole, qr = -Q'r' and nrqr = -(mtr + r'Q'r')
-                    const float2 rx = __fadd2_rn(dup2(xi[k]), lo2(a));
-                    const float2 ry = __fadd2_rn(dup2(yi[k]), hi2(a));
-                    const float2 rz = __fadd2_rn(dup2(zi[k]), lo2(b));
+                    const float2 rx = __fadd2_rn(dup2(xf[k]), lo2(a));
+                    const float2 ry = __fadd2_rn(dup2(yf[k]), hi2(a));
+                    const float2 rz = __fadd2_rn(dup2(zf[k]), lo2(b));
                     const float2 r2 = __ffma2_rn(rx, rx, __ffma2_rn(ry, ry, __ffma2_rn(rz, rz, eps2_2)));
                     // rsqrt without the Newton step: its 2-ulp error is far below the
                     // quadrupole truncation of a far cell
@@ -394,7 +416,7 @@ __device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, in
 #pragma unroll
         for (int k = 0; k < IPT; k++) {
             if (!vi[k]) continue;
-            ForceRec &o = A.force[pid[k]];
+            ForceRec &o = A.force[sQ[tid * IPT + k].z];
             ForceRec r;
             if (A.accumulate) {
                 r = o;
@@ -415,28 +437,30 @@ __device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, in
     }
 }
 
-template <bool EMIT>
-__global__ void __launch_bounds__(SB, 4) soft_mixed_kernel(SoftArgs A) {
+// One i-particle per thread throughout (groups above SB members run as
+// chunks of SB over the same lists): the packed pair loops keep two list
+// entries in flight per thread, and the register budget this leaves allows
+// OCC resident CTAs per SM (the autotuner picks 4, 5 or 6).
+template <bool EMIT, int OCC>
+__global__ void __launch_bounds__(SB, OCC) soft_mixed_kernel(SoftArgs A) {
     __shared__ MixedTile T;
-    __shared__ int scnt[EMIT ? 2 * SB : 1];
+    __shared__ float4 sI[SB];
+    __shared__ int4 sQ[SB];
+    __shared__ int scnt[EMIT ? SB : 1];
     __shared__ float redf[SB * 8];
     __shared__ int redi[SB * 4];
     const int g = A.group_order ? A.group_order[blockIdx.x] : blockIdx.x;
     const int ni_all = A.i_off[g + 1] - A.i_off[g];
-    // groups above 2 * SB members (not produced by a tree with
-    // n_group_limit <= 256) run as consecutive chunks over the same lists;
-    // t_ipt2 >= 2 * SB (one i per thread throughout) chunks by SB
-    const int span = A.t_ipt2 >= 2 * SB ? SB : 2 * SB;
-    for (int ib = 0; ib < ni_all; ib += span) {
-        const int ni = min(span, ni_all - ib);
-        if (ni > A.t_ipt2)
-            group_mixed<1, 2, EMIT>(A, g, ib, ni, T, scnt, redf, redi);
-        else if (ni > A.t_s1)
-            group_mixed<1, 1, EMIT>(A, g, ib, ni, T, scnt, redf, redi);
+    // EP-EP unroll depth: as deep as the register budget holds without spills
+    constexpr int UNR = OCC <= 4 ? 8 : 2;
+    for (int ib = 0; ib < ni_all; ib += SB) {
+        const int ni = min(SB, ni_all - ib);
+        if (ni > A.t_s1)
+            group_mixed<1, 1, EMIT, UNR>(A, g, ib, ni, T, sI, sQ, scnt, redf, redi);
         else if (ni > A.t_s2)
-            group_mixed<2, 1, EMIT>(A, g, ib, ni, T, scnt, redf, redi);
+            group_mixed<2, 1, EMIT, UNR>(A, g, ib, ni, T, sI, sQ, scnt, redf, redi);
         else
-            group_mixed<4, 1, EMIT>(A, g, ib, ni, T, scnt, redf, redi);
+            group_mixed<4, 1, EMIT, UNR>(A, g, ib, ni, T, sI, sQ, scnt, redf, redi);
         __syncthreads();
     }
 }
@@ -697,6 +721,80 @@ cudaError_t launch_pack_epj(const EPJRec *in, int n, SoftPtcl *out, double *mass
     return cudaGetLastError();
 }
 
+// Mixed-form preprocessing: per-particle splits and packed superparticles.
+__global__ void split_kernel(const SoftPtcl *__restrict__ p, int n, SoftSplit *out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const SoftPtcl r = p[i];
+    SoftSplit s;
+    s.xh = __double2float_rn(r.x);
+    s.yh = __double2float_rn(r.y);
+    s.zh = __double2float_rn(r.z);
+    s.xl = __double2float_rn(r.x - (double)s.xh);
+    s.yl = __double2float_rn(r.y - (double)s.yh);
+    s.zl = __double2float_rn(r.z - (double)s.zh);
+    s.m = r.m;
+    s.ro2 = r.ro2;
+    out[i] = s;
+}
+
+__global__ void spj_pack_kernel(const SPJRec *__restrict__ in, int n, float eps2, int trace_mode, SpjPack *out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const SPJRec &r = in[i];
+    SpjPack s;
+    s.xh = __double2float_rn(r.pos[0]);
+    s.yh = __double2float_rn(r.pos[1]);
+    s.zh = __double2float_rn(r.pos[2]);
+    s.xl = __double2float_rn(r.pos[0] - (double)s.xh);
+    s.yl = __double2float_rn(r.pos[1] - (double)s.yh);
+    s.zl = __double2float_rn(r.pos[2] - (double)s.zh);
+    s.m = (float)r.mass;
+    const float qxx = (float)r.xx, qyy = (float)r.yy, qzz = (float)r.zz;
+    const float tr = trace_mode ? (float)(r.xx + r.yy + r.zz) : (float)(r.xx + r.yy + r.xx);
+    s.nmtr = eps2 * tr;
+    s.nqxx = -(3.0f * qxx - tr);
+    s.nqyy = -(3.0f * qyy - tr);
+    s.nqzz = -(3.0f * qzz - tr);
+    s.nqxy = -(3.0f * (float)r.xy);
+    s.nqyz = -(3.0f * (float)r.yz);
+    s.nqzx = -(3.0f * (float)r.xz);
+    s.pad0 = s.pad1 = 0.f;
+    out[i] = s;
+}
+
+namespace {
+
+// launch_soft's own scratch for callers that pass none: per device, grown
+// stream-ordered on the launching stream
+struct MixedScratch {
+    SoftSplit *isplit = nullptr, *jsplit = nullptr;
+    size_t icap = 0, jcap = 0;
+    SpjPack *spj = nullptr;
+    size_t scap = 0;
+};
+constexpr int MAX_DEV = 64;
+MixedScratch g_mixed[MAX_DEV];
+std::mutex g_mixed_mu;
+
+template <class T>
+cudaError_t grow(T **p, size_t *cap, size_t n, cudaStream_t st) {
+    if (n <= *cap) return cudaSuccess;
+    if (*p) {
+        cudaError_t e = cudaFreeAsync(*p, st);
+        if (e != cudaSuccess) return e;
+        *p = nullptr;
+        *cap = 0;
+    }
+    const size_t want = n + n / 4 + 1024;
+    cudaError_t e = cudaMallocAsync((void **)p, want * sizeof(T), st);
+    if (e != cudaSuccess) return e;
+    *cap = want;
+    return cudaSuccess;
+}
+
+}  // namespace
+
 cudaError_t launch_soft(const SoftArgs &Ain, int precision, bool emit, cudaStream_t st) {
     SoftArgs A = Ain;
     if (A.n_group <= 0) return cudaSuccess;
@@ -706,10 +804,42 @@ cudaError_t launch_soft(const SoftArgs &Ain, int precision, bool emit, cudaStrea
         A.t_s2 = 32;
     }
     if (precision == 0) {
-        if (emit)
-            soft_mixed_kernel<true><<<A.n_group, SB, 0, st>>>(A);
+        const bool same = A.iptcl == A.ptcl;
+        if (!A.jsplit || !A.spjp || (!same && !A.isplit)) {
+            int dev = 0;
+            cudaError_t e = cudaGetDevice(&dev);
+            if (e != cudaSuccess) return e;
+            if (dev < 0 || dev >= MAX_DEV) return cudaErrorInvalidDevice;
+            std::lock_guard<std::mutex> lk(g_mixed_mu);
+            MixedScratch &m = g_mixed[dev];
+            if ((e = grow(&m.jsplit, &m.jcap, (size_t)A.n_ptcl, st)) != cudaSuccess) return e;
+            if ((e = grow(&m.spj, &m.scap, (size_t)(A.n_spj > 0 ? A.n_spj : 1), st)) != cudaSuccess) return e;
+            if (!same && (e = grow(&m.isplit, &m.icap, (size_t)A.n_iptcl, st)) != cudaSuccess) return e;
+            A.jsplit = m.jsplit;
+            A.spjp = m.spj;
+            A.isplit = m.isplit;
+        }
+        if (same) A.isplit = A.jsplit;
+        if (A.n_ptcl > 0) split_kernel<<<(A.n_ptcl + 255) / 256, 256, 0, st>>>(A.ptcl, A.n_ptcl, A.jsplit);
+        if (!same && A.n_iptcl > 0)
+            split_kernel<<<(A.n_iptcl + 255) / 256, 256, 0, st>>>(A.iptcl, A.n_iptcl, A.isplit);
+        if (A.n_spj > 0)
+            spj_pack_kernel<<<(A.n_spj + 255) / 256, 256, 0, st>>>(A.spj, A.n_spj, A.eps2, A.trace_mode, A.spjp);
+        const int occ = A.occ ? A.occ : 5;
+#define P3T_SOFT_MIXED(OCC)                                                  \
+    do {                                                                     \
+        if (emit)                                                            \
+            soft_mixed_kernel<true, OCC><<<A.n_group, SB, 0, st>>>(A);       \
+        else                                                                 \
+            soft_mixed_kernel<false, OCC><<<A.n_group, SB, 0, st>>>(A);      \
+    } while (0)
+        if (occ == 4)
+            P3T_SOFT_MIXED(4);
+        else if (occ == 6)
+            P3T_SOFT_MIXED(6);
         else
-            soft_mixed_kernel<false><<<A.n_group, SB, 0, st>>>(A);
+            P3T_SOFT_MIXED(5);
+#undef P3T_SOFT_MIXED
     } else {
         if (emit)
             soft_f64_kernel<true><<<A.n_group, SB, 0, st>>>(A);

@@ -43,13 +43,18 @@ int p3t_set_params(const double *params21);
  * correction (default 64). */
 int p3t_set_options(int precision, int trace_mode, int cand_cap);
 /* Work split of the soft kernel by i-group size ni: ni > t_ipt2 two
- * i-particles per thread, > t_s1 one per thread, > t_s2 the j lists split
+ * i-particles per thread (FP64 form; the mixed form runs groups above 128
+ * members as chunks of 128), > t_s1 one per thread, > t_s2 the j lists split
  * two ways, else four (0 <= t_s2 <= 32 <= ..., t_s2 <= t_s1 <= 64,
  * t_s1 <= t_ipt2 <= 128, or t_ipt2 = 256: one i-particle per thread
  * throughout, groups above 128 in chunks; defaults 128, 64, 32).  Set by the autotuner
  * (gplum_gb300/autotune.py); forces agree to rounding across settings, the
  * neighbour fields bit for bit. */
 int p3t_set_soft_tiles(int t_ipt2, int t_s1, int t_s2);
+/* Register budget of the mixed soft kernel, as resident CTAs of 128 threads
+ * per SM it is compiled for: 4, 5 (default) or 6.  Set by the autotuner;
+ * results do not depend on it. */
+int p3t_set_soft_occupancy(int ctas_per_sm);
 /* The library's CUDA stream (cudaStream_t) for callers that order their own
  * work or timing events after the library's launches. */
 void *p3t_stream(void);
@@ -272,15 +277,17 @@ int p3t_remove_out_of_boundary(double r_max, double r_min, double *edisp);
  * ForceGrav::clear followed by both functors) are device-accessible
  * pointers; stream is a cudaStream_t (0 for the default stream); the call
  * returns after the stream has finished its work.  The library allocates
- * nothing for it: its only scratch is a static per-device array of
- * P3T_NOALLOC_MAX_BODIES packed bodies (3 MiB, held by every GPU that loads
- * the library until the process exits) and a status word.  n above
- * P3T_NOALLOC_MAX_BODIES is rejected with -cudaErrorInvalidValue and a
- * message on stderr.  The first call on a device looks up the static
+ * nothing for it: its only scratch is static per-device arrays of
+ * P3T_NOALLOC_MAX_BODIES packed bodies and their FP32 position splits
+ * (5 MiB), P3T_NOALLOC_MAX_SPJ packed superparticles (4 MiB), held by every
+ * GPU that loads the library until the process exits, and a status word.
+ * n above P3T_NOALLOC_MAX_BODIES or n_spj above P3T_NOALLOC_MAX_SPJ is
+ * rejected with -cudaErrorInvalidValue and a message on stderr.  The first call on a device looks up the static
  * array's device address, so make it before any stream capture.  All calls
  * share the scratch: calls that overlap on the GPU race and must be
  * serialised by the caller. */
 #define P3T_NOALLOC_MAX_BODIES 65536
+#define P3T_NOALLOC_MAX_SPJ 65536
 int p3t_soft_force_noalloc(int n, const void *epj, int n_group, const int *i_off, const int *i_idx,
                            const int *j_off, const int *j_idx, const int *s_off, const int *s_idx,
                            const void *spj, int n_spj, double eps2, int trace_mode, void *force,

@@ -181,7 +181,7 @@ def test_host_one_call_equals_resident(gpu):
     assert a.tobytes() == sf.download().tobytes()
 
 
-@pytest.mark.parametrize("tiles", [(0, 0, 0), (64, 32, 16), (128, 64, 0), (256, 64, 32)])
+@pytest.mark.parametrize("tiles", [(0, 0, 0), (64, 32, 16), (128, 64, 0), (256, 64, 32), (128, 64, 32, 4), (128, 48, 16, 6)])
 def test_work_splits_agree(gpu, tiles):
     """Every work split the autotuner may choose gives the same neighbour
     fields and forces equal to rounding (sub-block partial sums combine in a
@@ -197,13 +197,17 @@ def test_work_splits_agree(gpu, tiles):
         lib.p3t_set_soft_tiles(128, 64, 32)
         sf.run(emit_candidates=False)
         ref = sf.download().copy()
-        assert lib.p3t_set_soft_tiles(*tiles) == 0
+        assert lib.p3t_set_soft_tiles(*tiles[:3]) == 0
+        if len(tiles) > 3:
+            assert lib.p3t_set_soft_occupancy(tiles[3]) == 0
         sf.run(emit_candidates=False)
         got = sf.download()
     finally:
         lib.p3t_set_soft_tiles(128, 64, 32)
+        lib.p3t_set_soft_occupancy(5)
     for k in ("number", "rank", "id_max", "id_min"):
         np.testing.assert_array_equal(got[k], ref[k])
     assert rel_err(got["acc"].astype(np.float64), ref["acc"].astype(np.float64)).max() < 1e-6
     assert lib.p3t_set_soft_tiles(40, 64, 32) != 0  # invalid: t_ipt2 < t_s1
     assert lib.p3t_set_soft_tiles(200, 64, 32) != 0  # invalid: neither <= 128 nor 256
+    assert lib.p3t_set_soft_occupancy(3) != 0
