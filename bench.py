@@ -29,6 +29,10 @@ N_BODIES = 1048576
 METRIC = "P3T steps/s, N=1M: mixed+batched vs plain FP64 on GB300 @ rel force err\u22641e-6"
 EPEP_FLOPS = 32  # per pair, FMA = 2, rsqrt/min/max/compare = 1
 EPSP_FLOPS = 70
+# DRAM bytes (read + write) of one pair-kernel launch on this workload, from the
+# ncu capture in profiles/soft_mixed_kernel_1m_disk.md (the bench itself cannot
+# read DRAM counters); refreshed with each capture
+SOFT_TRAFFIC_BYTES = 510.4e6
 
 
 def workload(seed=2):
@@ -391,11 +395,15 @@ def gpu_arm(args, rank, world):
                       "achieved_tflops": achieved64, "fp64_peak_tflops": peak64.value},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
                      "frac": achieved / peak.value, "peak_source": "measured (FP32 FMA microbenchmark)",
-                     "flops_per_step": flops, "traffic": None},
+                     "flops_per_step": flops,
+                     # DRAM bytes read + written by one launch of the pair kernel, from the
+                     # ncu capture summarised in profiles/soft_mixed_kernel_1m_disk.md
+                     "traffic": SOFT_TRAFFIC_BYTES, "traffic_source": "ncu, profiles/soft_mixed_kernel_1m_disk.md"},
         "interactions_per_s": (n_epep + n_epsp) / (ms_step * 1e-3),
         "e2e": {"value": 1.0 / float(np.median(e2e)), "unit": "steps/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
-        "gpu_launches": args.steps,
+        # per step: position splits, superparticle pack, pair kernel
+        "gpu_launches": 3 * args.steps,
         "soft_tiles": tuning["soft_tiles"] if tuning else [128, 64, 32],
         "soft_ctas_per_sm": tuning.get("soft_occ", 5) if tuning else 5,
         "clocks": clocks,
