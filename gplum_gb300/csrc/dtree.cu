@@ -5,7 +5,8 @@
 // TreeForForce with LONG_SYMMETRY search and quadrupole moments, called at
 // src/main_p3t.cpp:344-355,581-587,672-676):
 //   * 63-bit Morton keys on the root cube (side = 1.0001 x the largest
-//     extent), bodies in key order (ties by index);
+//     extent, anchored at the bodies' lower corner with margin
+//     (side - extent)/2 on every axis), bodies in key order (ties by index);
 //   * a node splits into one child per occupied octant while it holds more
 //     than min(n_leaf_limit, n_group_limit) bodies (21 levels at most);
 //   * i-groups are the highest nodes with at most n_group_limit bodies (or
@@ -78,7 +79,8 @@ __global__ void k_bbox_partial(const double *pos, int n, double *part) {
     if (threadIdx.x < 6) part[6 * blockIdx.x + threadIdx.x] = s[threadIdx.x][0];
 }
 
-// root cube as the host builder: out = {base.xyz, size, scale} (one block of 256)
+// root cube as the host builder: out = {base.xyz, size, scale} (one block of
+// 256); anchored at the lower corner, so a thin axis is not cut at coarse levels
 __global__ void k_bbox_root(const double *part, int nblk, double *out) {
     __shared__ double s[6][256];
     double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
@@ -101,13 +103,10 @@ __global__ void k_bbox_root(const double *part, int nblk, double *out) {
         __syncthreads();
     }
     if (threadIdx.x) return;
-    double size = 0.;
-    for (int d = 0; d < 3; d++) size = fmax(size, s[3 + d][0] - s[d][0]);
-    size = size * 1.0001 + 1e-300;
-    for (int d = 0; d < 3; d++) {
-        const double cen = 0.5 * (s[d][0] + s[3 + d][0]);
-        out[d] = cen - 0.5 * size;
-    }
+    double ext = 0.;
+    for (int d = 0; d < 3; d++) ext = fmax(ext, s[3 + d][0] - s[d][0]);
+    const double size = ext * 1.0001 + 1e-300;
+    for (int d = 0; d < 3; d++) out[d] = s[d][0] - 0.5 * (size - ext);
     out[3] = size;
     out[4] = double(1 << 21) / size;
 }
@@ -838,7 +837,7 @@ int p3t_state_tree(double theta, int n_leaf_limit, int n_group_limit) {
 int p3t_state_tree_soft(double theta, int n_leaf_limit, int n_group_limit) {
     int r = p3t_state_tree(theta, n_leaf_limit, n_group_limit);
     if (r) return r;
-    return p3t_soft_run(1);
+    return soft_run_state();
 }
 
 int p3t_tree_lists_counts(long long *counts) {

@@ -587,6 +587,38 @@ int Engine::ensure(int n) {
     return 0;
 }
 
+__global__ void k_max_number(const ForceRec *__restrict__ F, int n, int *out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int v = i < n ? F[i].number : 0;
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0 && v > 0) atomicMax(out, v);
+}
+
+int soft_run_state() {
+    Context *c = g_eng.c ? g_eng.c : ctx_get(0);
+    if (!c) return -(int)cudaErrorNoDevice;
+    for (int attempt = 0;; attempt++) {
+        int r = p3t_soft_run(1);
+        if (r) return r;
+        const int st = read_status(c);
+        if (st == 0) return 0;
+        if (st != ST_CAND_OVERFLOW || attempt >= 3) return st;
+        // widest row needed: the largest screen-hit count of this pass
+        if ((r = g_eng.counters.reserve(4))) return r;
+        int32_t *mx = g_eng.counters.p + 2;
+        cudaMemsetAsync(mx, 0, sizeof(int32_t), c->stream);
+        const int n = c->res_n;
+        k_max_number<<<(n + 255) / 256, 256, 0, c->stream>>>(c->res.force.p, n, mx);
+        int h = 0;
+        if ((r = d2h(c, &h, mx, sizeof(int)))) return r;
+        int cap = c->cand_cap;
+        while (cap < h) cap *= 2;
+        if (cap == c->cand_cap || cap > (1 << 16)) return st;
+        c->cand_cap = cap;
+        if (g_eng.S.cap > 0 && (r = g_eng.ensure(g_eng.S.n))) return r;
+    }
+}
+
 // Capacity for n bodies keeping the first S.n of every field (new
 // particles from fragmentation).
 int Engine::grow(int n) {
@@ -1029,7 +1061,7 @@ int p3t_state_soft(int n_group, const int *i_off, const int *i_idx, const int *j
     int r = g_eng.pack_soft();
     if (r) return r;
     if ((r = p3t_upload_lists(n_group, i_off, i_idx, j_off, j_idx, s_off, s_idx, spj, n_spj))) return r;
-    return p3t_soft_run(1);
+    return soft_run_state();
 }
 
 int p3t_correct(int initial) {

@@ -43,6 +43,13 @@ struct Engine {
 
 extern Engine g_eng;
 
+// Soft pass with candidate emission over the engine's resident state and
+// lists.  When a particle had more screen hits than the candidate table's
+// width, the width grows to the next power of two above the largest count
+// and the pass runs again (a few embryos among planetesimals have hundreds
+// of candidates; the table starts at 64).
+int soft_run_state();
+
 // Device priorities (higher first) of the current clusters from the learned
 // cost model, with the scale that maps them to the order's bins, or nullptr
 // when the size order applies (sched.cu).

@@ -176,13 +176,16 @@ P3TTree *p3t_tree_build(int n, const double *pos, const double *mass, const doub
             lo[d] = std::min(lo[d], pos[3 * i + d]);
             hi[d] = std::max(hi[d], pos[3 * i + d]);
         }
-    double size = 0.;
-    for (int d = 0; d < 3; d++) size = std::max(size, hi[d] - lo[d]);
-    size = size * 1.0001 + 1e-300;
-    double cen[3];
-    for (int d = 0; d < 3; d++) cen[d] = 0.5 * (lo[d] + hi[d]);
+    double ext = 0.;
+    for (int d = 0; d < 3; d++) ext = std::max(ext, hi[d] - lo[d]);
+    const double size = ext * 1.0001 + 1e-300;
+    // the cube is anchored at the bodies' lower corner (margin (size - ext)/2
+    // on every axis): along the widest axis this centres the bodies, and a
+    // thin axis (a disk's normal) is not cut through the bodies until the
+    // cells are thinner than the bodies' extent along it -- a cut near the
+    // mid-plane at a coarse level would leave sparse, wide groups on one side
     double base[3];
-    for (int d = 0; d < 3; d++) base[d] = cen[d] - 0.5 * size;
+    for (int d = 0; d < 3; d++) base[d] = lo[d] - 0.5 * (size - ext);
     // Morton keys and sort
     std::vector<std::pair<uint64_t, int>> kv(n);
     const double scale = double(1 << 21) / size;

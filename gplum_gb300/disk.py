@@ -73,14 +73,17 @@ def _solve_kepler(l, e):
 
 
 def make_disk(n, m, a_in, a_out, p=1.5, ecc_hill=2.0, inc_hill=1.0, seed=0, m_sun=1.0,
-              dens=density_code_units(2.0), f=1.0):
-    """Returns dict(id, mass, r_planet, f, pos, vel) for n equal-mass bodies."""
+              dens=density_code_units(2.0), f=1.0, a=None):
+    """Returns dict(id, mass, r_planet, f, pos, vel) for n equal-mass bodies
+    (semimajor axes drawn from the annulus, or the given array `a`)."""
     rng = np.random.Generator(np.random.PCG64(seed))
     h = (m / (3.0 * m_sun)) ** (1.0 / 3.0)
     # dN/da ~ a Sigma ~ a^(1-p): inverse CDF in a^(2-p)
     q = 2.0 - p
     u = rng.random(n)
-    if abs(q) < 1e-12:
+    if a is not None:
+        a = np.asarray(a, np.float64)
+    elif abs(q) < 1e-12:
         a = a_in * (a_out / a_in) ** u
     else:
         a = (a_in**q + u * (a_out**q - a_in**q)) ** (1.0 / q)
@@ -129,3 +132,18 @@ def disk_1m_hard(n=1048576, seed=3, m_at_1m=7e-11):
     cluster at this n.)"""
     m = m_at_1m * (1048576.0 / n) ** 1.5
     return make_disk(n, m, 0.95, 1.05, ecc_hill=6.0, inc_hill=3.0, seed=seed)
+
+
+def disk_1m_embryos(n=1048576, seed=4, m=1e-10, m_embryo=3.0e-7, a_embryo=(0.7, 0.9, 1.1, 1.3)):
+    """Embryo workload: n planetesimals of m = 1e-10 in 0.5-1.5 AU with the
+    hard-part disk's random velocities (rms e = 6 h, rms i = 3 h), plus four
+    embryos of 0.1 Earth mass (3e-7 M_sun) at 0.7, 0.9, 1.1 and 1.3 AU (rms
+    e = 2 h, rms i = h of their own mass).  The embryos carry the last ids."""
+    d = make_disk(n, m, 0.5, 1.5, ecc_hill=6.0, inc_hill=3.0, seed=seed)
+    e = make_disk(len(a_embryo), m_embryo, 0.5, 1.5, ecc_hill=2.0, inc_hill=1.0, seed=seed + 1000,
+                  a=np.array(a_embryo))
+    out = {k: np.concatenate([d[k], e[k]]) for k in ("mass", "r_planet", "f", "pos", "vel")}
+    out["id"] = np.arange(n + len(a_embryo), dtype=np.int64)
+    out["pos"] = np.ascontiguousarray(out["pos"])
+    out["vel"] = np.ascontiguousarray(out["vel"])
+    return out

@@ -83,8 +83,10 @@ class GpuSystem:
         self._chk(self.lib.p3t_correct(1 if initial else 0), "p3t_correct")
 
     def neighbor_ids_local(self, i):
-        out = np.zeros(self.cand_cap, np.int32)
-        m = self.lib.p3t_neighbor_list(i, out.ctypes.data_as(VP), self.cand_cap)
+        # the library widens its neighbour table past cand_cap when a body needs it
+        cap = max(self.cand_cap, 1 << 14)
+        out = np.zeros(cap, np.int32)
+        m = self.lib.p3t_neighbor_list(i, out.ctypes.data_as(VP), cap)
         return out[:max(m, 0)]
 
     def pairs(self):

@@ -3,9 +3,13 @@
 phase of the step stay on the GPU.
 
     python -m gplum_gb300.run --steps 1000
+    python -m gplum_gb300.run --workload embryos --a-frag 0.5 --schedule size --timing --steps 100
 
 integrates the 3000-body disk (0.95-1.05 AU, m = 1e-9, rms e = 2 h,
-rms i = h, dt_tree = 2^-7) and prints the relative energy error
+rms i = h, dt_tree = 2^-7), or the embryo disk (1,048,576 planetesimals
+plus four 0.1 Earth-mass embryos, KOMINAMI fragments with --a-frag), with
+the hard queue in the learned or the size order, and prints the relative
+energy error
 (Energy::calcEnergyError, src/energy.h:65-67: (E - E_init - E_dissipated) /
 E_init, where the dissipated energy sums the hard part's collisions, the
 merges and the bodies removed outside [r_min, r_max],
@@ -30,59 +34,102 @@ def startup(g, disk):
     return g.energy()
 
 
-def step(g, istep, reset_step=1024, r_max=40.0, r_min=0.1):
+def step(g, istep, reset_step=1024, r_max=40.0, r_min=0.1, clock=None):
     """One tree step (src/main_p3t.cpp:423-717; r_max and r_min as in
     parameter.dat, defaults src/read.h:111-112).  Returns (collision pairs,
-    energy after the step, energy dissipated in this step)."""
-    g.kick()
-    g.cluster()
-    cols, ed = g.hard(istep)
+    energy after the step, energy dissipated in this step).  With `clock` a
+    dict, adds the synchronised wall time of each phase to it."""
+
+    def timed(name, fn):
+        if clock is None:
+            return fn()
+        g.lib.p3t_synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        g.lib.p3t_synchronize()
+        clock[name] = clock.get(name, 0.0) + time.perf_counter() - t0
+        return r
+
+    timed("kick", g.kick)
+    timed("cluster", g.cluster)
+    cols, ed = timed("hard", lambda: g.hard(istep))
     edisp = float(ed[0])
-    g.tree_soft()
-    g.correct(False)
-    g.kick()
-    e = g.energy()
+    timed("tree_soft", g.tree_soft)
+    timed("correct", lambda: g.correct(False))
+    timed("kick", g.kick)
+    e = timed("energy", g.energy)
     if len(cols):
-        edisp += g.merge(len(cols))
-    n_rem, e_rem = g.remove(r_max, r_min)
+        edisp += timed("merge", lambda: g.merge(len(cols)))
+    n_rem, e_rem = timed("remove", lambda: g.remove(r_max, r_min))
     edisp += e_rem
     if len(cols) or n_rem or istep % reset_step == reset_step - 1:
-        g.prepare()
-        g.tree_soft()
-        g.correct(True)
-        e = g.energy()
+        timed("radii", g.prepare)
+        timed("tree_soft", g.tree_soft)
+        timed("correct", lambda: g.correct(True))
+        e = timed("energy", g.energy)
     return cols, e, edisp
 
 
-def run(g, disk, steps, reset_step=1024):
+def run(g, disk, steps, reset_step=1024, clock=None):
     """Start-up and `steps` tree steps; returns the energy-error trace and
     the collision count."""
     e0 = startup(g, disk)
     edisp = 0.0
     de, ncol = [], 0
     for istep in range(1, steps + 1):
-        cols, e, ed = step(g, istep, reset_step)
+        cols, e, ed = step(g, istep, reset_step, clock=clock)
         edisp += ed
         ncol += len(cols)
         de.append((e[0] - e0[0] - edisp) / e0[0])
     return np.array(de), ncol
 
 
+WORKLOADS = {
+    "disk3000": "3000-body disk, 0.95-1.05 AU, m=1e-9, rms e=2h, rms i=h, dt_tree=2^-7",
+    "embryos": "1048576 planetesimals m=1e-10 in 0.5-1.5 AU (rms e=6h, rms i=3h) + 4 embryos of 3e-7 "
+               "at 0.7/0.9/1.1/1.3 AU, theta=0.5, n_group_limit=256",
+}
+
+
 def main():
-    from .disk import P3TParams, disk_3000
+    from . import autotune, scheduler
+    from .disk import P3TParams, disk_1m_embryos, disk_3000
     from .p3t import GpuSystem
 
     ap = argparse.ArgumentParser()
     ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--workload", default="disk3000", choices=sorted(WORKLOADS))
+    ap.add_argument("--n", type=int, default=1048576, help="planetesimals of the embryo workload")
+    ap.add_argument("--schedule", default="learned", choices=["learned", "size"],
+                    help="hard work-queue order: the learned cost model or cluster size")
+    ap.add_argument("--a-frag", type=float, default=0.0,
+                    help="KOMINAMI fragmentation a_frag (0: perfect accretion)")
+    ap.add_argument("--timing", action="store_true", help="synchronised per-phase wall times")
     args = ap.parse_args()
-    P = P3TParams()
+    if args.workload == "disk3000":
+        P, disk = P3TParams(), disk_3000()
+    else:
+        P, disk = P3TParams(n_group_limit=256), disk_1m_embryos(args.n)
     g = GpuSystem(P)
+    autotune.load(g.lib)
+    model = scheduler.load(lib=g.lib) if args.schedule == "learned" else None
+    g.lib.p3t_set_schedule(1 if model is not None else 0)
+    if args.a_frag > 0:
+        g.set_fragmentation(args.a_frag)
+    clock = {} if args.timing else None
     t0 = time.perf_counter()
-    de, ncol = run(g, disk_3000(), args.steps)
+    de, ncol = run(g, disk, args.steps, clock=clock)
     t = time.perf_counter() - t0
-    print(json.dumps({"workload": "3000-body disk, 0.95-1.05 AU, m=1e-9, dt_tree=2^-7", "steps": args.steps,
-                      "max_abs_dE_over_E": float(np.abs(de).max()), "final_dE_over_E": float(de[-1]),
-                      "collisions": ncol, "n_final": g.n, "wall_s": t}))
+    pos = g.get("pos")
+    out = {"workload": WORKLOADS[args.workload], "steps": args.steps,
+           "schedule": "learned cost model" if model is not None else "size",
+           "a_frag": args.a_frag, "max_abs_dE_over_E": float(np.abs(de).max()), "final_dE_over_E": float(de[-1]),
+           "collisions": ncol, "n_initial": len(disk["mass"]), "n_final": g.n, "wall_s": t,
+           # identical for every schedule: the queue order never changes the arithmetic
+           "final_state_checksum": float(np.sum(pos * np.arange(1, 4))) + float(np.sum(g.get("id")))}
+    if clock is not None:
+        out["phases_s"] = clock
+    print(json.dumps(out))
 
 
 if __name__ == "__main__":

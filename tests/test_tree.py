@@ -34,3 +34,27 @@ def test_single_particle_and_tiny_groups():
     L = lists_for(s, P, n_group_limit=1)
     assert L["n_group"] == 5
     assert np.array_equal(np.sort(L["i_idx"]), np.arange(5))
+
+
+def test_thin_disk_with_off_centre_bodies_keeps_groups_compact():
+    """Embryos on inclined orbits move the bodies' bounding box off the disk's
+    mid-plane.  The root cube is anchored at the bodies' lower corner, so the
+    thin axis is not cut through the disk at coarse levels: no group spreads
+    over a wide patch of the disk (a cut near the mid-plane would leave sparse
+    groups of the few bodies above it, each as wide as a coarse cell, with
+    EPJ lists of tens of thousands)."""
+    from gplum_gb300.disk import P3TParams, disk_1m_embryos
+    from gplum_gb300.radii import cutoff_radii
+    from gplum_gb300.tree import build_lists
+
+    P = P3TParams(n_group_limit=256)
+    d = disk_1m_embryos()  # 1,048,576 planetesimals + 4 embryos (a few seconds on the host)
+    ro, rs, _ = cutoff_radii(d["pos"], d["vel"], d["mass"], P)
+    L = build_lists(d["pos"], d["mass"], rs, P.theta, P.n_leaf_limit, P.n_group_limit)
+    pos = d["pos"]
+    assert 0.5 * (pos[:, 2].max() + pos[:, 2].min()) > 1e-3  # the box is off the mid-plane
+    box = np.array([np.ptp(pos[L["i_idx"][L["i_off"][g]:L["i_off"][g + 1]], :2], axis=0).max()
+                    for g in range(L["n_group"])])
+    assert box.max() < 0.15  # groups of <= 256 of a million bodies; a coarse-level cut gave 0.37 AU
+    nj = np.diff(L["j_off"])
+    assert nj.max() < 5 * np.median(nj)  # a coarse-level cut gave 38,049 against a median of 417
