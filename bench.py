@@ -32,7 +32,7 @@ EPSP_FLOPS = 70
 # DRAM bytes (read + write) of one pair-kernel launch on this workload, from the
 # ncu capture in profiles/soft_mixed_kernel_1m_disk.md (the bench itself cannot
 # read DRAM counters); refreshed with each capture
-SOFT_TRAFFIC_BYTES = 510.4e6
+SOFT_TRAFFIC_BYTES = 344.1e6
 
 
 def workload(seed=2):

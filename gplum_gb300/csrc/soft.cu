@@ -66,8 +66,9 @@ __device__ __forceinline__ void fold(float &hi, float &lo, float v) {
 // tile's j coordinates (and, for superparticles, the quadrupole terms) are
 // stored negated, so every difference is an addition and the superparticle
 // terms come out with the force's sign; each product and sum is the exact
-// negation of the unnegated one.  A tile is padded to a multiple of 32
-// entries with massless entries 1e18 away, which contribute exact zeros.
+// negation of the unnegated one.  A tile is padded with massless entries
+// 1e18 away, which contribute exact zeros; the pair loops run over the
+// entries rounded up to a multiple of 16.
 //
 // Displacements.  EP-EP: from the two-float splits (SoftSplit),
 // r = (xh_i - xh_j) + (xl_i - xl_j) in FP32: the first difference rounds
@@ -222,10 +223,12 @@ __device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, in
             }
         }
         __syncthreads();
-        // this sub-block's share of the tile, in whole chunks of 32 entries
+        // this sub-block's share of the tile, in chunks of 32 entries (the last
+        // one of a list may be 16)
         const int jb = sub * (TM / S);
-        const int je = wact ? min(jb + TM / S, (nt + CHUNK - 1) & ~(CHUNK - 1)) : jb;
+        const int je = wact ? min(jb + TM / S, (nt + 15) & ~15) : jb;
         for (int c0 = jb; c0 < je; c0 += CHUNK) {
+            const int nq = min(CHUNK, je - c0) >> 1;  // entry pairs in this chunk: 16, or 8 at a list's end
             float2 tx[IPT], ty[IPT], tz[IPT], tp[IPT];
             unsigned nm[IPT];
 #pragma unroll
@@ -234,7 +237,7 @@ __device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, in
                 nm[k] = 0u;
             }
 #pragma unroll UNR
-            for (int q = 0; q < CHUNK / 2; q++) {
+            for (int q = 0; q < nq; q++) {
                 const int pq = (c0 >> 1) + q;
                 const float4 a = T.a[pq], b = T.b[pq], c = T.c[pq], d = T.d[pq];
                 const float2 e = T.e[pq];
@@ -341,13 +344,14 @@ __device__ __forceinline__ void group_mixed(const SoftArgs &A, int g, int ib, in
         }
         __syncthreads();
         const int jb = sub * (TM / S);
-        const int je = wact ? min(jb + TM / S, (nt + CHUNK - 1) & ~(CHUNK - 1)) : jb;
+        const int je = wact ? min(jb + TM / S, (nt + 15) & ~15) : jb;
         for (int c0 = jb; c0 < je; c0 += CHUNK) {
+            const int nq = min(CHUNK, je - c0) >> 1;  // entry pairs in this chunk: 16, or 8 at a list's end
             float2 tx[IPT], ty[IPT], tz[IPT], tp[IPT];
 #pragma unroll
             for (int k = 0; k < IPT; k++) tx[k] = ty[k] = tz[k] = tp[k] = dup2(0.f);
 #pragma unroll 4
-            for (int q = 0; q < CHUNK / 2; q++) {
+            for (int q = 0; q < nq; q++) {
                 const int pq = (c0 >> 1) + q;
                 const float4 a = T.a[pq], b = T.b[pq], c = T.c[pq], d = T.d[pq], f = T.f[pq];
                 const float2 e = T.e[pq];
