@@ -38,6 +38,11 @@ SIGNATURES = {
     "p3t_status": (I, []),
     "p3t_soft_force_host": (I, [I, VP, I, VP, VP, VP, VP, VP, VP, VP, I, VP]),
     "p3t_probe_fma_peak": (I, [I, VP]),
+    "p3t_snapshot_write_host": (I, [ctypes.c_char_p, I, VP, I, VP]),
+    "p3t_snapshot_read_host": (I, [ctypes.c_char_p, I, VP, I, VP]),
+    "p3t_snapshot_write": (I, [ctypes.c_char_p, I, VP, I]),
+    "p3t_snapshot_wait": (I, []),
+    "p3t_snapshot_read": (I, [ctypes.c_char_p, I, VP]),
     "p3t_state_load": (I, [I, VP, VP, VP, VP, VP, VP]),
     "p3t_state_n": (I, []),
     "p3t_state_get": (I, [I, VP]),

@@ -1002,6 +1002,7 @@ static void *field_ptr(int field, int *width, int *kind) {
         case 19: return S.r_planet;
         case 20: return S.v_disp;
         case 21: return S.r_out_inv;
+        case 22: return S.f;
         case 100: *kind = 1; return S.id;
         case 101: *kind = 1; return S.id_cluster;
         case 102: *kind = 2; return S.number;

@@ -16,7 +16,7 @@ from .soft import configure
 VP = ctypes.c_void_p
 VEC_FIELDS = {"pos": 0, "vel": 1, "acc": 2, "acc_d": 3, "jerk_d": 4, "acc_s": 5, "jerk_s": 6}
 SCALAR_FIELDS = {"phi": 10, "phi_d": 11, "phi_s": 12, "mass": 13, "r_out": 14, "r_search": 15, "dt": 16,
-                 "acc0": 17, "time": 18, "r_planet": 19, "v_disp": 20, "r_out_inv": 21}
+                 "acc0": 17, "time": 18, "r_planet": 19, "v_disp": 20, "r_out_inv": 21, "f": 22}
 I64_FIELDS = {"id": 100, "id_cluster": 101}
 I32_FIELDS = {"number": 102, "n_cluster": 103, "dead": 104, "merged": 105, "rank": 106, "id_min": 107,
               "id_max": 108}
@@ -128,6 +128,27 @@ class GpuSystem:
 
     def id_next(self):
         return int(self.lib.p3t_id_next())
+
+    def write_snapshot(self, path, binary, header, async_write=False):
+        """The state to a GPLUM snapshot file (snapNNNNNN.dat ASCII or the
+        snap_tmp.dat binary restart); with async_write the file is written by
+        a host thread while later phases run (wait_snapshot joins it)."""
+        h = header._c()
+        self._chk(self.lib.p3t_snapshot_write(str(path).encode(), int(binary), ctypes.byref(h),
+                                              1 if async_write else 0), "p3t_snapshot_write")
+
+    def wait_snapshot(self):
+        self._chk(self.lib.p3t_snapshot_wait(), "p3t_snapshot_wait")
+
+    def read_snapshot(self, path, binary):
+        """Loads a GPLUM snapshot file into the state (GPLUM's start-up read);
+        returns its header."""
+        from .snapshot import Header, _Header
+        h = _Header()
+        n = self.lib.p3t_snapshot_read(str(path).encode(), int(binary), ctypes.byref(h))
+        if n < 0:
+            raise RuntimeError(f"p3t_snapshot_read failed with status {n}")
+        return Header._from(h)
 
     def tree_soft(self):
         """Device octree + interaction lists from the current state, then the

@@ -4,6 +4,8 @@ phase of the step stay on the GPU.
 
     python -m gplum_gb300.run --steps 1000
     python -m gplum_gb300.run --workload embryos --a-frag 0.5 --schedule size --timing --steps 100
+    python -m gplum_gb300.run --steps 1000 --output-dir out --snap-every 100 --snap-tmp-every 100
+    python -m gplum_gb300.run --steps 2000 --output-dir out --restart
 
 integrates the 3000-body disk (0.95-1.05 AU, m = 1e-9, rms e = 2 h,
 rms i = h, dt_tree = 2^-7), or the embryo disk (1,048,576 planetesimals
@@ -70,17 +72,48 @@ def step(g, istep, reset_step=1024, r_max=40.0, r_min=0.1, clock=None):
     return cols, e, edisp
 
 
-def run(g, disk, steps, reset_step=1024, clock=None):
-    """Start-up and `steps` tree steps; returns the energy-error trace and
-    the collision count."""
-    e0 = startup(g, disk)
-    edisp = 0.0
+def run(g, disk, steps, reset_step=1024, clock=None, out_dir=None, snap_every=0, snap_tmp_every=0,
+        restart=False):
+    """Start-up (or a restart from out_dir/snap_tmp.dat) and tree steps up to
+    `steps`; returns the energy-error trace and the collision count.  With
+    out_dir: snapNNNNNN.dat (ASCII) every snap_every steps and the binary
+    restart file snap_tmp.dat every snap_tmp_every steps, as GPLUM's
+    outputStep / makeSnapTmp (src/main_p3t.cpp:738-764); the ASCII files
+    are written by a host thread while the next steps run."""
+    import os
+
+    from .snapshot import Header, energy7
+
+    P = g.params
+    if restart:
+        h = g.read_snapshot(os.path.join(out_dir, "snap_tmp.dat"), 1)
+        istep0 = int(round(h.time / P.dt_tree))
+        g.prepare()
+        g.tree_soft()
+        g.correct(False)  # correctForceLong: the restart keeps the hard-part state (src/main_p3t.cpp:357-359)
+        e_init, edisp = h.e_init, float(h.e_now[6])
+        e0 = np.array([e_init[0]])
+    else:
+        istep0 = 0
+        e0 = startup(g, disk)
+        e_init, edisp = energy7(e0), 0.0
     de, ncol = [], 0
-    for istep in range(1, steps + 1):
+
+    def header(istep, e):
+        return Header(time=istep * P.dt_tree, id_next=g.id_next(), e_init=e_init, e_now=energy7(e, edisp))
+
+    for istep in range(istep0 + 1, steps + 1):
         cols, e, ed = step(g, istep, reset_step, clock=clock)
         edisp += ed
         ncol += len(cols)
         de.append((e[0] - e0[0] - edisp) / e0[0])
+        if out_dir and snap_every and istep % snap_every == 0:
+            g.write_snapshot(os.path.join(out_dir, "snap%06d.dat" % (istep // snap_every)), 0, header(istep, e),
+                             async_write=True)
+        if out_dir and snap_tmp_every and istep % snap_tmp_every == 0:
+            g.write_snapshot(os.path.join(out_dir, "snap_tmp.dat"), 1, header(istep, e))
+    if out_dir:
+        g.wait_snapshot()
     return np.array(de), ncol
 
 
@@ -105,6 +138,10 @@ def main():
     ap.add_argument("--a-frag", type=float, default=0.0,
                     help="KOMINAMI fragmentation a_frag (0: perfect accretion)")
     ap.add_argument("--timing", action="store_true", help="synchronised per-phase wall times")
+    ap.add_argument("--output-dir", default=None, help="directory of the snapshot files")
+    ap.add_argument("--snap-every", type=int, default=0, help="snapNNNNNN.dat (ASCII) every this many steps")
+    ap.add_argument("--snap-tmp-every", type=int, default=0, help="snap_tmp.dat (binary) every this many steps")
+    ap.add_argument("--restart", action="store_true", help="continue from OUTPUT_DIR/snap_tmp.dat (GPLUM -r)")
     args = ap.parse_args()
     if args.workload == "disk3000":
         P, disk = P3TParams(), disk_3000()
@@ -118,12 +155,18 @@ def main():
         g.set_fragmentation(args.a_frag)
     clock = {} if args.timing else None
     t0 = time.perf_counter()
-    de, ncol = run(g, disk, args.steps, clock=clock)
+    if args.output_dir:
+        import os
+
+        os.makedirs(args.output_dir, exist_ok=True)
+    de, ncol = run(g, disk, args.steps, clock=clock, out_dir=args.output_dir, snap_every=args.snap_every,
+                   snap_tmp_every=args.snap_tmp_every, restart=args.restart)
     t = time.perf_counter() - t0
     pos = g.get("pos")
     out = {"workload": WORKLOADS[args.workload], "steps": args.steps,
            "schedule": "learned cost model" if model is not None else "size",
-           "a_frag": args.a_frag, "max_abs_dE_over_E": float(np.abs(de).max()), "final_dE_over_E": float(de[-1]),
+           "a_frag": args.a_frag, "max_abs_dE_over_E": float(np.abs(de).max()) if len(de) else 0.0,
+           "final_dE_over_E": float(de[-1]) if len(de) else 0.0,
            "collisions": ncol, "n_initial": len(disk["mass"]), "n_final": g.n, "wall_s": t,
            # identical for every schedule: the queue order never changes the arithmetic
            "final_state_checksum": float(np.sum(pos * np.arange(1, 4))) + float(np.sum(g.get("id")))}

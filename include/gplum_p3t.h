@@ -115,7 +115,7 @@ int p3t_soft_force_host(int n, const void *epj, int n_group, const int *i_off, c
  * on that state.  Field codes of p3t_state_get / p3t_state_set:
  *   double[n][3]: 0 pos, 1 vel, 2 acc (soft), 3 acc_d, 4 jerk_d, 5 acc_s, 6 jerk_s
  *   double[n]:   10 phi, 11 phi_d, 12 phi_s, 13 mass, 14 r_out, 15 r_search,
- *                16 dt, 17 acc0, 18 time, 19 r_planet, 20 v_disp, 21 r_out_inv
+ *                16 dt, 17 acc0, 18 time, 19 r_planet, 20 v_disp, 21 r_out_inv, 22 f
  *   int64[n]:   100 id, 101 id_cluster
  *   int32[n]:   102 neighbor.number, 103 n_cluster, 104 isDead, 105 isMerged,
  *               106 neighbor.rank, 107 neighbor.id_min, 108 neighbor.id_max */
@@ -292,6 +292,59 @@ int p3t_soft_force_noalloc(int n, const void *epj, int n_group, const int *i_off
                            const int *j_off, const int *j_idx, const int *s_off, const int *s_idx,
                            const void *spj, int n_spj, double eps2, int trace_mode, void *force,
                            void *stream);
+
+/* ---- snapshots (GPLUM's output and restart files) --------------------------------
+ * snapNNNNNN.dat (ASCII, makeSnap src/func.h:53-66) and snap_tmp.dat
+ * (binary, makeSnapTmp src/func.h:68-80): a FileHeader (src/energy.h:65-127)
+ * then every body -- FPGrav::writeAscii / writeBinary, src/particle.h:829-876
+ * -- in order, byte for byte as GPLUM writes them (the binary body record is
+ * GPLUM's 344-byte FPGrav of the build with individual cutoffs, quadrupole
+ * moments and collisions).  Energies are GPLUM's Energy fields in order:
+ * etot, ekin, ephi_sun, ephi_planet, ephi, ephi_d, edisp (the ASCII header
+ * carries etot, ekin, ephi_sun, ephi_planet and edisp). */
+typedef struct {
+    int n_body;
+    int id_next;
+    double time;
+    double e_init[7];
+    double e_now[7];
+} p3t_file_header_t;
+/* Host arrays of n bodies (pos, vel and the *_d / *_s vectors: 3 per body).
+ * Writing needs id, mass, pos, vel (and r_planet, f for ASCII); other null
+ * pointers write GPLUM's defaults.  Reading fills the non-null arrays. */
+typedef struct {
+    long long *id;
+    double *mass, *r_planet, *f;
+    double *pos, *vel;
+    double *acc, *acc_d, *jerk_d, *acc_s, *jerk_s;
+    double *phi, *phi_d, *phi_s, *r_out, *r_search, *r_out_inv, *v_disp, *time, *dt, *acc0;
+    long long *id_cluster;
+    int *number, *rank, *id_max, *id_min, *n_cluster, *dead, *merged;
+} p3t_bodies_t;
+#define P3T_IO_ERROR (-1001)        /* the file could not be opened, written or closed */
+#define P3T_IO_FORMAT (-1002)       /* the file is not in the expected format */
+#define P3T_IO_BAD_ARGUMENT (-1003) /* a null pointer or too small capacity */
+/* The file from host arrays (n bodies; header->n_body is set to n).  No GPU. */
+int p3t_snapshot_write_host(const char *path, int binary, const p3t_file_header_t *header, int n,
+                            const p3t_bodies_t *bodies);
+/* Reads a file's header and, with cap >= its body count, its bodies; returns
+ * the body count.  An ASCII file may lack the header line (GPLUM's initial
+ * conditions).  No GPU. */
+int p3t_snapshot_read_host(const char *path, int binary, p3t_file_header_t *header, int cap,
+                           const p3t_bodies_t *bodies);
+/* The device state's bodies to a file.  async = 1: the device-to-host copies
+ * are queued on the library stream (ordered before later phases) and the file
+ * is formatted and written by a host thread while the next phases run;
+ * p3t_snapshot_wait() joins it and returns its status.  A new write first
+ * waits for the previous one. */
+int p3t_snapshot_write(const char *path, int binary, const p3t_file_header_t *header, int async);
+int p3t_snapshot_wait(void);
+/* Loads a file into the device state (GPLUM's start-up read,
+ * src/main_p3t.cpp:238-305): every body's time set to header time, neighbour
+ * counts, cluster sizes and merge/dead flags cleared; a binary file restores
+ * every FPGrav field the step carries.  The next id continues from
+ * max(header id_next - 1, largest id) + 1.  Returns the body count. */
+int p3t_snapshot_read(const char *path, int binary, p3t_file_header_t *header);
 
 /* ---- measurement -------------------------------------------------------------
  * FMA throughput of this GPU (TFLOP/s, FMA = 2 flops), FP32 (fp64 = 0),

@@ -29,7 +29,7 @@ VP = ctypes.c_void_p
 # field codes of *_get_f64 / *_get_i64
 VEC_FIELDS = {"pos": 0, "vel": 1, "acc": 2, "acc_d": 3, "jerk_d": 4, "acc_s": 5, "jerk_s": 6}
 SCALAR_FIELDS = {"phi": 10, "phi_d": 11, "phi_s": 12, "mass": 13, "r_out": 14, "r_search": 15,
-                 "dt": 16, "acc0": 17, "time": 18, "r_planet": 19, "v_disp": 20, "r_out_inv": 21}
+                 "dt": 16, "acc0": 17, "time": 18, "r_planet": 19, "v_disp": 20, "r_out_inv": 21, "f": 22}
 INT_FIELDS = {"id": 0, "id_cluster": 1, "number": 2, "n_cluster": 3, "dead": 4, "merged": 5,
               "rank": 6, "id_min": 7, "id_max": 8}
 

@@ -1441,6 +1441,7 @@ void orc_get_f64(int field, double *out) {
             case 19: out[i] = p.r_planet; break;
             case 20: out[i] = p.v_disp; break;
             case 21: out[i] = p.r_out_inv; break;
+            case 22: out[i] = p.f; break;
             default: break;
         }
         if (v) { out[3 * i] = v->x; out[3 * i + 1] = v->y; out[3 * i + 2] = v->z; }

@@ -273,6 +273,7 @@ void ref_get_f64(int field, double *out) {
             case 19: out[i] = p.r_planet; break;
             case 20: out[i] = p.v_disp; break;
             case 21: out[i] = p.r_out_inv; break;
+            case 22: out[i] = p.f; break;
             default: break;
         }
     }
@@ -309,6 +310,59 @@ void ref_set_f64(int field, const double *in) {
             default: break;
         }
     }
+}
+
+// GPLUM's snapshot writers on the reference system's bodies: FileHeader
+// (src/energy.h:65-127) then FPGrav::writeAscii / writeBinary
+// (src/particle.h:845-876) of every body in order -- the single-process
+// behaviour of FDPS's writeParticleAscii / writeParticleBinary, which
+// makeSnap / makeSnapTmp call (src/func.h:53-80).  e_init / e_now: the seven
+// Energy fields in declaration order.
+int ref_write_snapshot(const char *path, int binary, double time, int id_next, const double *e_init,
+                       const double *e_now) {
+    Energy a, b;
+    double *fa[7] = {&a.etot, &a.ekin, &a.ephi_sun, &a.ephi_planet, &a.ephi, &a.ephi_d, &a.edisp};
+    double *fb[7] = {&b.etot, &b.ekin, &b.ephi_sun, &b.ephi_planet, &b.ephi, &b.ephi_d, &b.edisp};
+    for (int k = 0; k < 7; k++) {
+        *fa[k] = e_init[k];
+        *fb[k] = e_now[k];
+    }
+    FileHeader h(ref_n(), id_next, time, a, b);
+    FILE *fp = std::fopen(path, binary ? "wb" : "w");
+    if (!fp) return -1;
+    if (binary) {
+        h.writeBinary(fp);
+        for (int i = 0; i < ref_n(); i++) g_pp[i].writeBinary(fp);
+    } else {
+        h.writeAscii(fp);
+        for (int i = 0; i < ref_n(); i++) g_pp[i].writeAscii(fp);
+    }
+    std::fclose(fp);
+    return 0;
+}
+// sizeof(FPGrav), sizeof(FileHeader) and the byte offsets of FPGrav's members
+// in GPLUM's compiled class
+void ref_fpgrav_layout(long long *out) {
+    FP_t p;
+    const char *b = (const char *)&p;
+    long long v[] = {(long long)sizeof(FP_t), (long long)sizeof(FileHeader),
+                     (long long)((const char *)&p.id_local - b), (long long)((const char *)&p.myrank - b),
+                     (long long)((const char *)&p.pos - b), (long long)((const char *)&p.r_out - b),
+                     (long long)((const char *)&p.r_search - b), (long long)((const char *)&p.id - b),
+                     (long long)((const char *)&p.mass - b), (long long)((const char *)&p.vel - b),
+                     (long long)((const char *)&p.acc_d - b), (long long)((const char *)&p.acc - b),
+                     (long long)((const char *)&p.acc_s - b), (long long)((const char *)&p.jerk_d - b),
+                     (long long)((const char *)&p.jerk_s - b), (long long)((const char *)&p.acc_gd - b),
+                     (long long)((const char *)&p.phi - b), (long long)((const char *)&p.phi_d - b),
+                     (long long)((const char *)&p.phi_s - b), (long long)((const char *)&p.v_disp - b),
+                     (long long)((const char *)&p.r_out_inv - b), (long long)((const char *)&p.time - b),
+                     (long long)((const char *)&p.dt - b), (long long)((const char *)&p.acc0 - b),
+                     (long long)((const char *)&p.r_planet - b), (long long)((const char *)&p.f - b),
+                     (long long)((const char *)&p.neighbor - b), (long long)((const char *)&p.id_cluster - b),
+                     (long long)((const char *)&p.n_cluster - b), (long long)((const char *)&p.inDomain - b),
+                     (long long)((const char *)&p.isSent - b), (long long)((const char *)&p.isDead - b),
+                     (long long)((const char *)&p.isMerged - b)};
+    for (size_t k = 0; k < sizeof v / sizeof v[0]; k++) out[k] = v[k];
 }
 
 // setIDLocalAndMyrank (src/func.h:135-149) followed by setCutoffRadii
