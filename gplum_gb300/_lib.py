@@ -43,6 +43,9 @@ SIGNATURES = {
     "p3t_snapshot_write": (I, [ctypes.c_char_p, I, VP, I]),
     "p3t_snapshot_wait": (I, []),
     "p3t_snapshot_read": (I, [ctypes.c_char_p, I, VP]),
+    "p3t_collisions_write_host": (I, [ctypes.c_char_p, I, I, VP]),
+    "p3t_collision_records": (I, [I, VP]),
+    "p3t_collisions_write": (I, [ctypes.c_char_p, I]),
     "p3t_state_load": (I, [I, VP, VP, VP, VP, VP, VP]),
     "p3t_state_n": (I, []),
     "p3t_state_get": (I, [I, VP]),

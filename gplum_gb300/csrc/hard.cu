@@ -53,6 +53,12 @@ struct ColRec {
     int32_t cluster, seq, n;  // cluster index, collision number within it, cluster size
     int32_t n_frag, frag0;    // fragments made (KOMINAMI) and the first one's fragment index
     int64_t id_frag;          // temporary id of the first fragment (the others count down)
+    // the collision-file record (Collision0::write2File, src/collisionA.h:122-148):
+    // masses (twins included) and states before the collision, and the
+    // relative shifts of the centre of mass, |pos_g_new - pos_g| / |pos_g| etc.
+    double mass_imp, mass_tar, mass_frag;
+    double pos_imp[3], pos_tar[3], vel_imp[3], vel_tar[3];
+    double dpos_g_rel, dvel_g_rel;
 };
 
 // One fragment (KOMINAMI), in creation order within its cluster: the FPGrav
@@ -345,6 +351,26 @@ __device__ int collide(const Params &P, const Hard &H, int imp, int tar, double 
     }
     const V3 pos_new = (m_imp * pos_imp + m_tar * pos_tar - masspos) / mass_rem_k;
     const V3 vel_new = (m_imp * vel_imp + m_tar * vel_tar - massvel) / mass_rem_k;
+    {
+        // the record: Collision0::setParticle's centre of mass after the
+        // collision -- fragments (in creation order), then the remnant and the
+        // target (src/collisionA.h:232-234,288-291,344-348)
+        double mass_tot = 0.;
+        for (int i = 0; i < n_frag; i++) mass_tot += mass_frag / n_frag;
+        const V3 mp = masspos + ((m_imp - mass_frag_k) * pos_new + m_tar * pos_new);
+        const V3 mv = massvel + ((m_imp - mass_frag_k) * vel_new + m_tar * vel_new);
+        mass_tot += m_imp - mass_frag_k + m_tar;
+        const V3 dpos_g = mp / mass_tot - pos_g, dvel_g = mv / mass_tot - vel_g;
+        rec.mass_imp = m_imp;
+        rec.mass_tar = m_tar;
+        rec.mass_frag = mass_frag_k;
+        rec.pos_imp[0] = pos_imp.x; rec.pos_imp[1] = pos_imp.y; rec.pos_imp[2] = pos_imp.z;
+        rec.pos_tar[0] = pos_tar.x; rec.pos_tar[1] = pos_tar.y; rec.pos_tar[2] = pos_tar.z;
+        rec.vel_imp[0] = vel_imp.x; rec.vel_imp[1] = vel_imp.y; rec.vel_imp[2] = vel_imp.z;
+        rec.vel_tar[0] = vel_tar.x; rec.vel_tar[1] = vel_tar.y; rec.vel_tar[2] = vel_tar.z;
+        rec.dpos_g_rel = sqrt(dot(dpos_g, dpos_g) / dot(pos_g, pos_g));
+        rec.dvel_g_rel = sqrt(dot(dvel_g, dvel_g) / dot(vel_g, vel_g));
+    }
     // setParticle (flag_merge)
     H.r_planet[imp] = 0.;
     H.r_planet[tar] *= pow(mass_rem_k / m_tar, 1. / 3.);
@@ -1489,6 +1515,19 @@ int p3t_hard_fetch(int col_cap, long long *col_pairs, double *edisp) {
                 map.push_back(cr.id_frag - j);
                 map.push_back(E.id_next++);
             }
+        // the collision records carry the final ids (Collision0::setNewFragmentID,
+        // src/collisionA.h:116-120, applied before the records are written)
+        auto remap = [&](long long v) {
+            if (v >= 0) return v;
+            for (size_t k = 0; k + 1 < map.size(); k += 2)
+                if (map[k] == v) return map[k + 1];
+            return v;
+        };
+        for (ColRec &cr : g_cols) {
+            cr.id_imp = remap(cr.id_imp);
+            cr.id_tar = remap(cr.id_tar);
+            if (cr.n_frag) cr.id_frag = remap(cr.id_frag);
+        }
         std::vector<int> ord(nfr);
         for (int k = 0; k < nfr; k++) ord[k] = k;
         std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
@@ -1518,6 +1557,41 @@ int p3t_hard_fetch(int col_cap, long long *col_pairs, double *edisp) {
     int st = read_status(c);
     if (st) return st;
     return ncol;
+}
+
+int p3t_collision_records(int cap, p3t_collision_t *out) {
+    const int n = (int)g_cols.size();
+    if (cap < 0 || (cap > 0 && !out)) return P3T_IO_BAD_ARGUMENT;
+    for (int k = 0; k < n && k < cap; k++) {
+        const ColRec &c = g_cols[k];
+        p3t_collision_t &o = out[k];
+        o.time = c.time;
+        o.id_imp = c.id_imp;
+        o.id_tar = c.id_tar;
+        o.n_frag = c.n_frag;
+        o.id_frag = c.n_frag ? c.id_frag : 0;
+        o.mass_imp = c.mass_imp;
+        o.mass_tar = c.mass_tar;
+        o.mass_frag = c.mass_frag;
+        for (int d = 0; d < 3; d++) {
+            o.pos_imp[d] = c.pos_imp[d];
+            o.pos_tar[d] = c.pos_tar[d];
+            o.vel_imp[d] = c.vel_imp[d];
+            o.vel_tar[d] = c.vel_tar[d];
+        }
+        o.flag = 1;  // flag_merge: both outcomes of this build merge (src/collisionA.h:101, collisionB.h:90)
+        o.dpos_g_rel = c.dpos_g_rel;
+        o.dvel_g_rel = c.dvel_g_rel;
+    }
+    return n;
+}
+
+int p3t_collisions_write(const char *path, int append) {
+    const int n = (int)g_cols.size();
+    std::vector<p3t_collision_t> v(n);
+    const int r = p3t_collision_records(n, v.data());
+    if (r < 0) return r;
+    return p3t_collisions_write_host(path, append, n, v.data());
 }
 
 int p3t_hard(int istep, int col_cap, long long *col_pairs, double *edisp) {

@@ -311,6 +311,29 @@ int p3t_snapshot_write_host(const char *path, int binary, const p3t_file_header_
     return r;
 }
 
+int p3t_collisions_write_host(const char *path, int append, int n, const p3t_collision_t *records) {
+    if (!path || n < 0 || (n > 0 && !records)) return P3T_IO_BAD_ARGUMENT;
+    FILE *fp = std::fopen(path, append ? "a" : "w");
+    if (!fp) return P3T_IO_ERROR;
+    int r = 0;
+    char buf[1024];
+    for (int k = 0; k < n && !r; k++) {
+        const p3t_collision_t &c = records[k];
+        // std::fixed, setprecision(8) for the time; std::scientific,
+        // setprecision(15) for the doubles; tab-separated
+        const int m = std::snprintf(
+            buf, sizeof buf,
+            "%.8f\t%lld\t%lld\t%d\t%lld\t%.15e\t%.15e\t%.15e\t%.15e\t%.15e\t%.15e\t%.15e\t%.15e\t%.15e\t"
+            "%.15e\t%.15e\t%.15e\t%.15e\t%.15e\t%.15e\t%d\t%.15e\t%.15e\n",
+            c.time, c.id_imp, c.id_tar, c.n_frag, c.id_frag, c.mass_imp, c.mass_tar, c.mass_frag, c.pos_imp[0],
+            c.pos_imp[1], c.pos_imp[2], c.pos_tar[0], c.pos_tar[1], c.pos_tar[2], c.vel_imp[0], c.vel_imp[1],
+            c.vel_imp[2], c.vel_tar[0], c.vel_tar[1], c.vel_tar[2], c.flag, c.dpos_g_rel, c.dvel_g_rel);
+        r = write_all(fp, buf, (size_t)m);
+    }
+    if (std::fclose(fp) != 0 && !r) r = P3T_IO_ERROR;
+    return r;
+}
+
 int p3t_snapshot_read_host(const char *path, int binary, p3t_file_header_t *header, int cap,
                            const p3t_bodies_t *bodies) {
     if (!path || !header || cap < 0 || (cap > 0 && !bodies)) return P3T_IO_BAD_ARGUMENT;

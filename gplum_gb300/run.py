@@ -78,10 +78,13 @@ def run(g, disk, steps, reset_step=1024, clock=None, out_dir=None, snap_every=0,
     `steps`; returns the energy-error trace and the collision count.  With
     out_dir: snapNNNNNN.dat (ASCII) every snap_every steps and the binary
     restart file snap_tmp.dat every snap_tmp_every steps, as GPLUM's
-    outputStep / makeSnapTmp (src/main_p3t.cpp:738-764); the ASCII files
-    are written by a host thread while the next steps run."""
+    outputStep / makeSnapTmp (src/main_p3t.cpp:738-764), and each step's
+    collisions appended to collisionNNNNNN.dat (src/main_p3t.cpp:390-396,
+    751-758); the ASCII files are written by a host thread while the next
+    steps run."""
     import os
 
+    from . import _lib
     from .snapshot import Header, energy7
 
     P = g.params
@@ -102,10 +105,16 @@ def run(g, disk, steps, reset_step=1024, clock=None, out_dir=None, snap_every=0,
     def header(istep, e):
         return Header(time=istep * P.dt_tree, id_next=g.id_next(), e_init=e_init, e_now=energy7(e, edisp))
 
+    if out_dir and snap_every and not restart:
+        g.write_snapshot(os.path.join(out_dir, "snap%06d.dat" % 0), 0, header(0, e0), async_write=True)
     for istep in range(istep0 + 1, steps + 1):
         cols, e, ed = step(g, istep, reset_step, clock=clock)
         edisp += ed
         ncol += len(cols)
+        if out_dir and snap_every and len(cols):
+            # collisionNNNNNN.dat holds the collisions since snapshot NNNNNN-1
+            path = os.path.join(out_dir, "collision%06d.dat" % ((istep - 1) // snap_every + 1))
+            _lib.check(g.lib.p3t_collisions_write(path.encode(), 1), "p3t_collisions_write")
         de.append((e[0] - e0[0] - edisp) / e0[0])
         if out_dir and snap_every and istep % snap_every == 0:
             g.write_snapshot(os.path.join(out_dir, "snap%06d.dat" % (istep // snap_every)), 0, header(istep, e),

@@ -346,6 +346,31 @@ int p3t_snapshot_wait(void);
  * max(header id_next - 1, largest id) + 1.  Returns the body count. */
 int p3t_snapshot_read(const char *path, int binary, p3t_file_header_t *header);
 
+/* ---- collision records (collisionNNNNNN.dat) ---------------------------------------
+ * One line per collision of a tree step, Collision0::write2File
+ * (src/collisionA.h:122-148): time, impactor and target ids, fragment count
+ * and first fragment id (final ids, src/hard.h:838-855), masses (twins
+ * included) and states before the collision, the flag word, and the
+ * relative shifts of the centre of mass |pos_g_new - pos_g| / |pos_g| and
+ * |vel_g_new - vel_g| / |vel_g|. */
+typedef struct {
+    double time;
+    long long id_imp, id_tar;
+    int n_frag;
+    long long id_frag;
+    double mass_imp, mass_tar, mass_frag;
+    double pos_imp[3], pos_tar[3], vel_imp[3], vel_tar[3];
+    int flag;
+    double dpos_g_rel, dvel_g_rel;
+} p3t_collision_t;
+/* Appends (append = 1) or writes n records in GPLUM's format.  No GPU. */
+int p3t_collisions_write_host(const char *path, int append, int n, const p3t_collision_t *records);
+/* The records of the last p3t_hard / p3t_hard_fetch, in collision-list
+ * order: copies up to cap of them, returns how many there are. */
+int p3t_collision_records(int cap, p3t_collision_t *out);
+/* The last hard call's records to a collision file (append = 1: add to it). */
+int p3t_collisions_write(const char *path, int append);
+
 /* ---- measurement -------------------------------------------------------------
  * FMA throughput of this GPU (TFLOP/s, FMA = 2 flops), FP32 (fp64 = 0),
  * FP64 (fp64 = 1) or packed FP32 pairs (fp64 = 2, fma.rn.f32x2): the roofline denominators of the soft (FP32-pipe) and

@@ -497,8 +497,13 @@ struct ColRec {
     double edisp, edisp_d;
     int n_frag;       // fragments made by this collision
     int64_t id_frag;  // temporary id of its first fragment (the others count down)
+    // the collision-file record (Collision0::write2File, src/collisionA.h:122-148)
+    double mass_imp, mass_tar, mass_frag;
+    V3 pos_imp, pos_tar, vel_imp, vel_tar;
+    double dpos_g_rel, dvel_g_rel;
 };
 std::vector<ColRec> COLS;
+ColRec LAST_UNIT;  // the record of the last orc_collide_unit
 double EDISP = 0., EDISP_D = 0.;
 
 // KOMINAMI fragmentation (src/collisionB.h:7-93; m_min src/collisionA.h:57,152).
@@ -593,6 +598,27 @@ int collide(std::vector<HPtcl> &c, std::map<int, std::vector<int>> &twins, int i
     }
     const V3 pos_new = (m_imp * pos_imp + m_tar * pos_tar - masspos) / mass_rem;
     const V3 vel_new = (m_imp * vel_imp + m_tar * vel_tar - massvel) / mass_rem;
+    {
+        // the record: masses and states before the collision, and
+        // Collision0::setParticle's centre of mass after it -- fragments in
+        // creation order, then remnant and target (src/collisionA.h:232-234,
+        // 288-291,344-348) -- against pos_g / vel_g (src/collisionA.h:205-206)
+        double mass_tot = 0.;
+        for (int i = 0; i < n_frag; i++) mass_tot += F[i].mass;
+        const V3 mp = masspos + ((m_imp - mass_frag) * pos_new + m_tar * pos_new);
+        const V3 mv = massvel + ((m_imp - mass_frag) * vel_new + m_tar * vel_new);
+        mass_tot += m_imp - mass_frag + m_tar;
+        const V3 dpos_g = mp / mass_tot - pos_g, dvel_g = mv / mass_tot - vel_g;
+        rec.mass_imp = m_imp;
+        rec.mass_tar = m_tar;
+        rec.mass_frag = mass_frag;
+        rec.pos_imp = pos_imp;
+        rec.pos_tar = pos_tar;
+        rec.vel_imp = vel_imp;
+        rec.vel_tar = vel_tar;
+        rec.dpos_g_rel = std::sqrt(dot(dpos_g, dpos_g) / dot(pos_g, pos_g));
+        rec.dvel_g_rel = std::sqrt(dot(dvel_g, dvel_g) / dot(vel_g, vel_g));
+    }
     // setParticle (flag_merge)
     c[imp].r_planet = 0.;
     c[tar].r_planet *= std::pow(mass_rem / m_tar, 1. / 3.);
@@ -1225,6 +1251,12 @@ int hard_all(int istep) {
         std::map<int64_t, int64_t> o2n;
         for (const ColRec &r : COLS)
             for (int j = 0; j < r.n_frag; j++) o2n[r.id_frag - j] = ID_NEXT++;
+        // the records carry the final ids (Collision0::setNewFragmentID)
+        for (ColRec &r : COLS) {
+            if (r.id_imp < 0) r.id_imp = o2n.at(r.id_imp);
+            if (r.id_tar < 0) r.id_tar = o2n.at(r.id_tar);
+            if (r.n_frag) r.id_frag = o2n.at(r.id_frag);
+        }
         for (int q = 0; q < ncl; q++) {
             const auto &cl = clusters[order[q]];
             for (Ptcl h : cfrag[q]) {
@@ -1584,6 +1616,7 @@ int orc_collide_unit(int n, const double *in, int n_tw, const int *tw, int imp, 
     double e1 = 0., e2 = 0.;
     int64_t idn = *id_next;
     const int nf = collide(c, twins, imp, tar, e1, e2, rec, idn);
+    LAST_UNIT = rec;
     *id_next = idn;
     edisp[0] = e1;
     edisp[1] = e2;
@@ -1609,6 +1642,20 @@ int orc_hard(int istep, long long *col_out, int col_cap, double *edisp_out) {
     edisp_out[1] = EDISP_D;
     return nc;
 }
+// record k of the last hard part: time id_imp id_tar n_frag id_frag mass_imp
+// mass_tar mass_frag pos_imp(3) pos_tar(3) vel_imp(3) vel_tar(3) flag
+// dpos_g_rel dvel_g_rel (25 doubles)
+static void put_record(const ColRec &r, double *o) {
+    o[0] = r.time; o[1] = (double)r.id_imp; o[2] = (double)r.id_tar; o[3] = r.n_frag;
+    o[4] = r.n_frag ? (double)r.id_frag : 0.;
+    o[5] = r.mass_imp; o[6] = r.mass_tar; o[7] = r.mass_frag;
+    const V3 v[4] = {r.pos_imp, r.pos_tar, r.vel_imp, r.vel_tar};
+    for (int q = 0; q < 4; q++) { o[8 + 3 * q] = v[q].x; o[9 + 3 * q] = v[q].y; o[10 + 3 * q] = v[q].z; }
+    o[20] = 1.;  // flag_merge
+    o[21] = r.dpos_g_rel; o[22] = r.dvel_g_rel; o[23] = o[24] = 0.;
+}
+void orc_col_record(int k, double *out) { put_record(COLS[k], out); }
+void orc_last_unit_record(double *out) { put_record(LAST_UNIT, out); }
 void orc_col_edisp(int k, double *out) {
     out[0] = COLS[k].edisp;
     out[1] = COLS[k].edisp_d;

@@ -508,6 +508,10 @@ extern "C" void ref_set_frag(double a_frag, int n_frag, double m_min) {
 #endif
     Collision0::m_min = m_min;
 }
+// Collision0::write2File of each unit collision, appended to this file when set
+static std::string g_col_file;
+extern "C" void ref_set_collision_file(const char *path) { g_col_file = path ? path : ""; }
+
 extern "C" int ref_collide_unit(int n, const double *in, int n_tw, const int *tw, int imp, int tar,
                                 long long *id_next, double *out, int cap, double *edisp) {
     std::vector<FPHard> pp(n);
@@ -533,6 +537,10 @@ extern "C" int ref_collide_unit(int n, const double *in, int n_tw, const int *tw
     edisp[0] = col.calcEnergyDissipation(pp, merge_list);
     edisp[1] = col.getHardEnergyDissipation();
     col.setNeighbors(pp);
+    if (!g_col_file.empty()) {
+        std::ofstream f(g_col_file, std::ios::app);
+        col.write2File(f);
+    }
     // the merge-list bookkeeping that follows in src/hermite.h:413-423
     if (col.flag_merge && pp[imp].isMerged) pp[imp].isMerged = false;
     *id_next = idn;

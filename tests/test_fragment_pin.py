@@ -96,3 +96,48 @@ def test_without_fragmentation_the_reference_is_perfect_accretion():
     b = H.collide_unit("ref", P, (0.0, 10, 1e-11), rec, [], 0, 1)
     np.testing.assert_array_equal(a[0], b[0])
     np.testing.assert_array_equal(a[2], b[2])
+
+
+def _record_struct(o):
+    """p3t_collision_t from the restatement's 25-double record."""
+    import ctypes
+
+    from gplum_gb300.collisions import Record
+
+    r = Record()
+    r.time = o[0]
+    r.id_imp, r.id_tar, r.n_frag, r.id_frag = int(o[1]), int(o[2]), int(o[3]), int(o[4])
+    r.mass_imp, r.mass_tar, r.mass_frag = o[5], o[6], o[7]
+    for d in range(3):
+        r.pos_imp[d], r.pos_tar[d], r.vel_imp[d], r.vel_tar[d] = o[8 + d], o[11 + d], o[14 + d], o[17 + d]
+    r.flag = int(o[20])
+    r.dpos_g_rel, r.dvel_g_rel = o[21], o[22]
+    return r
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_collision_record_line_matches_the_reference(name, tmp_path):
+    """collisionNNNNNN.dat: GPLUM's Collision0::write2File line for the
+    collision against the restatement's record written by the library's
+    formatter (p3t_collisions_write_host), byte for byte."""
+    import ctypes
+
+    from gplum_gb300 import collisions
+
+    case = CASES[name]
+    P, rec = cluster()
+    for tar, twin in case["twins"]:
+        merge(rec, tar, twin)
+    want, got = tmp_path / "ref.dat", tmp_path / "ours.dat"
+    ref = H.load("ref_kominami")
+    ref.ref_set_collision_file(str(want).encode())
+    try:
+        H.collide_unit("ref_kominami", P, case["frag"], rec, case["twins"], 0, 1, id_next=7, seed=2024)
+    finally:
+        ref.ref_set_collision_file(None)
+    H.collide_unit("orc", P, case["frag"], rec, case["twins"], 0, 1, id_next=7, seed=2024)
+    # the restatement's phase comes from drand48 seeded like the reference (mode 1 in collide_unit)
+    o = np.zeros(25)
+    H.load("orc").orc_last_unit_record(o.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    collisions.write_host(got, [_record_struct(o)])
+    assert got.read_bytes() == want.read_bytes()

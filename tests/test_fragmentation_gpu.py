@@ -7,9 +7,12 @@ bodies in the same order with the same new ids, and the same state to
 1e-12 relative (positions and velocities go through the CUDA and host
 libm's pow/sin/cos); the merge that follows must leave the same bodies.
 """
+import ctypes
+
 import numpy as np
 import pytest
 
+from gplum_gb300 import collisions
 from gplum_gb300.disk import P3TParams, make_disk
 from gplum_gb300.p3t import GpuSystem
 from oracle import harness as H
@@ -51,6 +54,19 @@ def test_fragmenting_collisions_match_the_oracle(gpu):
             c2, e2 = g.hard(istep)
             np.testing.assert_array_equal(c2, c1)
             np.testing.assert_allclose(e2, e1, rtol=1e-9, atol=1e-30)
+            # the collision-file records (final ids; masses, states before the
+            # collision, centre-of-mass shifts)
+            recs = collisions.records(g.lib)
+            assert len(recs) == len(c1)
+            for k, r in enumerate(recs):
+                o = np.zeros(25)
+                orc.lib.orc_col_record(k, o.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+                assert (r.id_imp, r.id_tar, r.n_frag, r.id_frag, r.flag) == tuple(int(x) for x in o[[1, 2, 3, 4, 20]])
+                assert r.time == o[0]
+                got = np.array([r.mass_imp, r.mass_tar, r.mass_frag, *r.pos_imp, *r.pos_tar, *r.vel_imp, *r.vel_tar])
+                np.testing.assert_allclose(got, o[5:20], rtol=1e-12, atol=0)
+                # the shifts are rounding-level differences of O(1) values
+                assert abs(r.dpos_g_rel - o[21]) <= 1e-13 and abs(r.dvel_g_rel - o[22]) <= 1e-13
             assert g.n == orc.n
             n_frag_total += g.n - 3000 if istep == 1 else 0
             assert g.id_next() == orc.id_next()
