@@ -11,6 +11,9 @@ code:
 * the bundle form's heavy-cluster threshold (p3t_set_hard_heavy: clusters
   whose learned prediction of log2(1 + block steps) reaches it run alone in a
   CTA first) -- timed from restored states of the hard-part disk;
+* whether the bundle form's clusters above 256 bodies run in a concurrent
+  wide launch (lone bundles of up to 512 slots) or one per CTA in the main
+  launch (p3t_set_hard_wide) -- timed from one restored state;
 * the one-cluster-per-team form's size cutoffs of the hard launch
   (p3t_set_hard_tiers: clusters of >= cta_min members one per CTA, >= warp_min
   one per warp, smaller one per thread) -- timed from one restored state of the
@@ -106,6 +109,26 @@ def tune_heavy(g, istep=1, grid=HEAVY_GRID):
     return best, table
 
 
+def tune_wide(g, istep=1, reps=2):
+    """Times the bundled hard launch from one restored state with the clusters
+    above 256 bodies in the concurrent wide launch (1) or one per CTA in the
+    main launch (0); installs the faster.  Returns (best, {choice: ms})."""
+    lib = g.lib
+    _lib.check(lib.p3t_state_snapshot(0), "p3t_state_snapshot")
+    table = {}
+    for w in (1, 0):
+        _lib.check(lib.p3t_set_hard_wide(w), "p3t_set_hard_wide")
+        ts = []
+        for _ in range(reps):
+            _lib.check(lib.p3t_state_snapshot(1), "p3t_state_snapshot")
+            ts.append(1e3 * _timed(lib, lambda: g.hard(istep), 1))
+        table[w] = float(min(ts))
+    lib.p3t_state_snapshot(1)
+    best = min(table, key=table.get)
+    _lib.check(lib.p3t_set_hard_wide(best), "p3t_set_hard_wide")
+    return best, table
+
+
 def load(lib=None, path=TUNING):
     """Installs a tuning file's choices; returns them (None without a file)."""
     if not os.path.exists(path):
@@ -118,6 +141,8 @@ def load(lib=None, path=TUNING):
         _lib.check(lib.p3t_set_soft_occupancy(t["soft_occ"]), "p3t_set_soft_occupancy")
     if "hard_tiers" in t:
         _lib.check(lib.p3t_set_hard_tiers(*t["hard_tiers"]), "p3t_set_hard_tiers")
+    if "hard_wide" in t:
+        _lib.check(lib.p3t_set_hard_wide(int(t["hard_wide"])), "p3t_set_hard_wide")
     if "hard_heavy" in t:
         import ctypes
 
@@ -172,6 +197,7 @@ def main():
     from . import scheduler
 
     heavy_best, heavy_table = None, {}
+    wide_best, wide_table = tune_wide(g)
     if scheduler.load(lib=g.lib) is not None:
         # two tree steps' states: the heavy threshold matters where predictions differ
         for istep in (1, 2):
@@ -189,6 +215,8 @@ def main():
            "soft_ms": {",".join(map(str, k)): v for k, v in soft_table.items()},
            "hard_tiers": list(hard_best),
            "hard_heavy": heavy_best if heavy_best is not None else 6.5,
+           "hard_wide": wide_best,
+           "hard_wide_ms": {str(k): v for k, v in wide_table.items()},
            "hard_heavy_ms": {str(k): v for k, v in heavy_table.items()},
            "hard_ms": {",".join(map(str, k)): v for k, v in hard_table.items()},
            "workloads": {"soft": "1048576-body disk 0.5-1.5 AU, m=1e-10, theta=0.5, n_group_limit=256",

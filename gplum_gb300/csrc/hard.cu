@@ -98,6 +98,7 @@ struct HardArgs {
     FragRec *frags;      // [frag_cap] fragments of this launch
     int32_t *n_frags;    // fragments made so far
     int frag_base, frag_cap;  // hard slots frag_base + k hold fragment k
+    int wide;                 // bundle form: clusters above BCAP_MAIN in k_hard_wide (1) or run_cluster (0)
 };
 
 // ---- FPHard::predict / correct / calcDeltat, src/particle.h:1183-1314 ----
@@ -1101,7 +1102,7 @@ __global__ void k_order_bins(const int32_t *cnt, const float *prio, int nc, int 
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nc) return;
     const int n = cnt[k];
-    const int tier = (mode == 0) ? (n > BCAP ? 0 : 1) : (n >= cta_min ? 0 : (n >= warp_min ? 1 : 2));
+    const int tier = (mode == 0) ? (n > BCAP_MAIN ? 0 : 1) : (n >= cta_min ? 0 : (n >= warp_min ? 1 : 2));
     int key = n < ORDER_NB - 1 ? n : ORDER_NB - 1;
     if (prio) {
         const float v = (prio[k] - pmin) * pscale;
@@ -1217,6 +1218,7 @@ static double g_edisp[2] = {0., 0.};
 static int g_warp_min = 8, g_cta_min = 64;
 static int g_hard_mode = 0;  // 0: bundles, 1: thread/warp/CTA tiers
 static float g_heavy = 6.5f;  // predicted log2(1 + block steps) from which a cluster runs alone (0: never)
+static int g_wide = 1;        // clusters above BCAP_MAIN bodies: wide lone bundles (1) or one per CTA (0)
 static FragParams g_frag = {0., 9.426627927538057e-12, 10, 0, 0ULL};  // off (a_frag = 0)
 static int g_frag_cap = 0;  // fragment slots of the current launch
 
@@ -1302,6 +1304,12 @@ long long p3t_id_next(void) { return g_eng.id_next; }
 int p3t_set_hard_heavy(float log2_steps) {
     if (!(log2_steps >= 0.f)) return ST_BAD_INDEX;
     g_heavy = log2_steps;
+    return 0;
+}
+
+int p3t_set_hard_wide(int on) {
+    if (on != 0 && on != 1) return ST_BAD_INDEX;
+    g_wide = on;
     return 0;
 }
 
@@ -1426,20 +1434,42 @@ int p3t_hard_integrate(int istep) {
         A.n_frags = B.n_frags.p;
         A.frag_base = E.n_members;
         A.frag_cap = g_frag_cap;
+        A.wide = g_wide;
         int sms = 152;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
         if (g_hard_mode == 0) {
             static bool attr = false;
-            const int smem = (int)sizeof(BundleSmem);
+            static cudaStream_t s_wide = nullptr;
+            static cudaEvent_t ev_ready = nullptr, ev_done = nullptr;
+            const int smem = (int)sizeof(BundleSmem<BCAP_MAIN>), smem_w = (int)sizeof(BundleSmem<BCAP_WIDE>);
             if (!attr) {
                 if ((r = cuda_status(cudaFuncSetAttribute(k_hard_bundles, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                          smem))))
+                                                          smem))) ||
+                    (r = cuda_status(cudaFuncSetAttribute(k_hard_wide, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                          smem_w))) ||
+                    (r = cuda_status(cudaStreamCreateWithFlags(&s_wide, cudaStreamNonBlocking))) ||
+                    (r = cuda_status(cudaEventCreateWithFlags(&ev_ready, cudaEventDisableTiming))) ||
+                    (r = cuda_status(cudaEventCreateWithFlags(&ev_done, cudaEventDisableTiming))))
                     return r;
                 attr = true;
+            }
+            // the clusters above BCAP_MAIN bodies on a second stream, started
+            // first so that they hold SMs from the beginning (a handful of CTAs;
+            // they leave at once when there are none)
+            if (A.wide) {
+                if ((r = cuda_status(cudaEventRecord(ev_ready, c->stream))) ||
+                    (r = cuda_status(cudaStreamWaitEvent(s_wide, ev_ready, 0))))
+                    return r;
+                k_hard_wide<<<std::max(1, sms / 16), BT, smem_w, s_wide>>>(A);
+                if ((r = cuda_status(cudaGetLastError()))) return r;
             }
             // persistent: 2 CTAs per SM (fewer when there are few clusters)
             const int blocks = std::max(1, std::min(sms * 2, (nc + 3) / 4));
             k_hard_bundles<<<blocks, BT, smem, c->stream>>>(A);
+            if ((r = cuda_status(cudaGetLastError()))) return r;
+            if (A.wide && ((r = cuda_status(cudaEventRecord(ev_done, s_wide))) ||
+                           (r = cuda_status(cudaStreamWaitEvent(c->stream, ev_done, 0)))))
+                return r;
         } else {
             const int blocks = std::max(1, std::min(sms * 2, (nc + 3) / 4));
             k_hard_clusters<<<blocks, 128, 0, c->stream>>>(A);

@@ -20,8 +20,9 @@
 //   - collision detection over unordered member pairs, FP32 prefilter, FP64
 //     R for the survivors and a per-cluster lexicographic (R, pair) minimum.
 // Finished clusters leave the bundle and the queue refills it, so the CTA
-// stays full until the queue is empty.  Clusters larger than BCAP take the
-// one-cluster-per-CTA form (run_cluster<128>) first.
+// stays full until the queue is empty.  Clusters larger than BCAP_MAIN run
+// concurrently in k_hard_wide: alone in a wide bundle of BCAP_WIDE slots, or
+// beyond that in the one-cluster-per-CTA form (run_cluster<128>).
 //
 // The global per-slot arrays (struct Hard) stay the state of record; shared
 // memory mirrors the fields that other members read (positions, velocities,
@@ -46,7 +47,8 @@
 namespace p3t {
 
 constexpr int BT = 128;      // threads of a bundle (one CTA)
-constexpr int BCAP = 256;    // member slots of a bundle
+constexpr int BCAP_MAIN = 256;  // member slots of a bundle
+constexpr int BCAP_WIDE = 512;  // member slots of the wide form (clusters of 257..512 bodies, one at a time)
 constexpr int BMAXCL = 128;  // clusters in a bundle at once
 constexpr int BSURV = 64;    // colliding-pair candidates kept per block step
 constexpr int BCLAIM = 8;    // clusters claimed from the queue at a time
@@ -54,6 +56,7 @@ constexpr int BCLAIM = 8;    // clusters claimed from the queue at a time
 enum : int { CF_COL = 1, CF_FIN = 2, CF_FRESH = 4, CF_EXACT = 8 };
 enum : unsigned char { MF_ACT = 1, MF_TGT = 2 };
 
+template <int BCAP>
 struct BundleSmem {
     // member mirror (pool slot p)
     double pos[3 * BCAP], vel[3 * BCAP], xp[3 * BCAP], vp[3 * BCAP];
@@ -116,7 +119,8 @@ __device__ __forceinline__ int bscan(int v, int *ws, int &total) {
 }
 
 // FP32 copy of a position relative to the cluster origin, with the bound check
-__device__ __forceinline__ void st32b(BundleSmem &B, float *dst, int p, V3 x, int k) {
+template <int BCAP>
+__device__ __forceinline__ void st32b(BundleSmem<BCAP> &B, float *dst, int p, V3 x, int k) {
     const float u0 = (float)(x.x - B.c_ref[3 * k]), u1 = (float)(x.y - B.c_ref[3 * k + 1]),
                 u2 = (float)(x.z - B.c_ref[3 * k + 2]);
     dst[3 * p] = u0;
@@ -127,7 +131,8 @@ __device__ __forceinline__ void st32b(BundleSmem &B, float *dst, int p, V3 x, in
 }
 
 // mirror every field of slot p from the state of record (global slot g)
-__device__ __forceinline__ void mirror_all(BundleSmem &B, const Hard &H, int p, int g, int k, bool with32) {
+template <int BCAP>
+__device__ __forceinline__ void mirror_all(BundleSmem<BCAP> &B, const Hard &H, int p, int g, int k, bool with32) {
     const V3 x = ld3(H.pos, g);
     st3(B.pos, p, x);
     st3(B.vel, p, ld3(H.vel, g));
@@ -152,7 +157,8 @@ __device__ __forceinline__ void mirror_all(BundleSmem &B, const Hard &H, int p, 
 
 // ---- pair phases ------------------------------------------------------------
 // ordered list of the occupied slots whose flag has `bit`
-__device__ int bundle_list(BundleSmem &B, unsigned char bit) {
+template <int BCAP>
+__device__ int bundle_list(BundleSmem<BCAP> &B, unsigned char bit) {
     constexpr int PER = BCAP / BT;
     const int base = threadIdx.x * PER;
     int c = 0;
@@ -174,7 +180,8 @@ __device__ int bundle_list(BundleSmem &B, unsigned char bit) {
 
 // the seven terms (acc_d xyz, jerk_d xyz, -phi_d) of target s from partner t,
 // the arithmetic of hard_force for one pair
-__device__ __forceinline__ void pair_terms(const Params &P, const BundleSmem &B, int mode, int s, int t, double *o) {
+template <int BCAP>
+__device__ __forceinline__ void pair_terms(const Params &P, const BundleSmem<BCAP> &B, int mode, int s, int t, double *o) {
     V3 xi, vi, xj, vj;
     if (mode == 1) { xi = ld3(B.xp, s); vi = ld3(B.vp, s); }
     else { xi = ld3(B.pos, s); vi = ld3(B.vel, s); }
@@ -205,7 +212,8 @@ __device__ __forceinline__ void pair_terms(const Params &P, const BundleSmem &B,
 }
 
 // terms of ring[0..m), then in-order addition into the targets' accumulators
-__device__ void bundle_drain(const Params &P, BundleSmem &B, int mode, int m) {
+template <int BCAP>
+__device__ void bundle_drain(const Params &P, BundleSmem<BCAP> &B, int mode, int m) {
     const int q = threadIdx.x;
     int sq = -1;
     if (q < m) {
@@ -236,7 +244,8 @@ __device__ void bundle_drain(const Params &P, BundleSmem &B, int mode, int m) {
 
 // mode 0: full (pos/vel, with phi); 1: predicted i and j; 2: corrected i,
 // predicted j -- for the nt targets in B.tgt
-__device__ void bundle_pairs(const HardArgs &A, BundleSmem &B, int mode, int nt) {
+template <int BCAP>
+__device__ void bundle_pairs(const HardArgs &A, BundleSmem<BCAP> &B, int mode, int nt) {
     const int tid = threadIdx.x;
     constexpr int PER = BCAP / BT;
     for (int i = tid; i < nt; i += BT) {
@@ -311,7 +320,8 @@ __device__ void bundle_pairs(const HardArgs &A, BundleSmem &B, int mode, int nt)
 // sun force and the accumulated pair sums of the targets to the state of
 // record, then mergeAccJerk for the merged targets (merge_sel 1: active
 // phase, merged alive targets; 2: all merged targets with twins)
-__device__ void bundle_finalize(const HardArgs &A, BundleSmem &B, int mode, int nt, int merge_sel) {
+template <int BCAP>
+__device__ void bundle_finalize(const HardArgs &A, BundleSmem<BCAP> &B, int mode, int nt, int merge_sel) {
     const Hard &H = A.H;
     for (int i = threadIdx.x; i < nt; i += BT) {
         const int s = B.tgt[i], g = B.gslot[s];
@@ -343,7 +353,8 @@ __device__ void bundle_finalize(const HardArgs &A, BundleSmem &B, int mode, int 
 // ---- collision detection ------------------------------------------------------
 // unordered pairs {a, b} of each cluster, balanced over members: member a
 // takes b = a + d (mod n) for d = 1..n/2 (the pair at distance n/2 once)
-__device__ void bundle_detect(const HardArgs &A, BundleSmem &B, bool second) {
+template <int BCAP>
+__device__ void bundle_detect(const HardArgs &A, BundleSmem<BCAP> &B, bool second) {
     for (int p = threadIdx.x; p < B.used; p += BT) {
         if (B.dead[p]) continue;
         const int k = B.cl[p];
@@ -389,7 +400,8 @@ __device__ void bundle_detect(const HardArgs &A, BundleSmem &B, bool second) {
 // uniform).  Phase 0: the heavy clusters (the first n_tier[3] of tier 1:
 // predicted long chains of block steps), one at a time and alone in the
 // bundle, so their iterations stay short; phase 1: the rest, packed.
-__device__ void bundle_refill(const HardArgs &A, BundleSmem &B) {
+template <int BCAP>
+__device__ void bundle_refill(const HardArgs &A, BundleSmem<BCAP> &B) {
     const int lane = threadIdx.x & 31;
     const int n_heavy = A.n_tier[3];
     if (threadIdx.x < 32) {
@@ -472,7 +484,8 @@ __device__ void bundle_refill(const HardArgs &A, BundleSmem &B) {
 }
 
 // load the fresh clusters (bundle indices fresh_k..ncl-1, slots fresh_p..used-1)
-__device__ void bundle_load(const HardArgs &A, BundleSmem &B) {
+template <int BCAP>
+__device__ void bundle_load(const HardArgs &A, BundleSmem<BCAP> &B) {
     const Hard &H = A.H;
     const int tid = threadIdx.x;
     const int k0 = B.fresh_k, k1 = B.ncl, p0 = B.fresh_p, p1 = B.used;
@@ -561,7 +574,8 @@ __device__ void bundle_load(const HardArgs &A, BundleSmem &B) {
 // A cluster made fragments (KOMINAMI): its member range grows by them, the
 // clusters after it move up, and every slot is mirrored again from the
 // state of record (fragments are rare; owners are remapped).
-__device__ void bundle_grow(const HardArgs &A, BundleSmem &B) {
+template <int BCAP>
+__device__ void bundle_grow(const HardArgs &A, BundleSmem<BCAP> &B) {
     const Hard &H = A.H;
     const int tid = threadIdx.x;
     static_assert(BMAXCL <= BT, "one thread per bundle cluster");
@@ -623,7 +637,8 @@ __device__ void bundle_grow(const HardArgs &A, BundleSmem &B) {
 
 // one block step of every cluster in the bundle (timeIntegrate_multi body,
 // src/hermite.h:224-479)
-__device__ void bundle_step(const HardArgs &A, BundleSmem &B) {
+template <int BCAP>
+__device__ void bundle_step(const HardArgs &A, BundleSmem<BCAP> &B) {
     const Params &P = A.P;
     const Hard &H = A.H;
     // makeActiveList: ts = min over alive members of th + dt
@@ -813,7 +828,8 @@ __device__ void bundle_step(const HardArgs &A, BundleSmem &B) {
 }
 
 // final forces, write-back and removal of the finished clusters
-__device__ void bundle_retire(const HardArgs &A, BundleSmem &B) {
+template <int BCAP>
+__device__ void bundle_retire(const HardArgs &A, BundleSmem<BCAP> &B) {
     const Hard &H = A.H;
     const int tid = threadIdx.x;
     FOR_SLOTS(p) B.flag[p] = (B.c_flags[B.cl[p]] & CF_FIN) ? MF_TGT : 0;
@@ -926,15 +942,72 @@ __device__ void bundle_retire(const HardArgs &A, BundleSmem &B) {
     __syncthreads();
 }
 
-// one CTA: the huge clusters one at a time, then bundles until the queue is empty
-__global__ void __launch_bounds__(BT, 2) k_hard_bundles(HardArgs A) {
+// The clusters above BCAP_MAIN bodies (the queue's tier 0), concurrently
+// with k_hard_bundles: one CTA takes one at a time -- up to BCAP_WIDE bodies
+// (fragment room included) as a lone wide bundle, the lane-dense form, larger
+// ones in the one-cluster-per-CTA form.  Same arithmetic, bit for bit, as
+// every other form.
+__global__ void __launch_bounds__(BT, 1) k_hard_wide(HardArgs A) {
     extern __shared__ __align__(16) unsigned char bundle_smem[];
-    BundleSmem &B = *reinterpret_cast<BundleSmem *>(bundle_smem);
+    BundleSmem<BCAP_WIDE> &B = *reinterpret_cast<BundleSmem<BCAP_WIDE> *>(bundle_smem);
     __shared__ double red_d[4];
     __shared__ long long red_l[4];
     __shared__ int q_sh;
     const int tid = threadIdx.x;
-    {
+    Team<128> tm{tid, red_d, red_l};
+    const int room = (A.frag.a_frag > 0.) ? 2 * A.frag.n_frag_max : 0;
+    for (int guard = 0; guard < (1 << 30); guard++) {
+        if (tid == 0) q_sh = atomicAdd(&A.queue[0], 1);
+        __syncthreads();
+        const int q = q_sh;
+        __syncthreads();
+        if (q >= A.n_tier[0]) break;
+        const int c = A.order[q];
+        const int n = A.cnt[c];
+        if (n + room > BCAP_WIDE) {
+            run_cluster<128>(A, c, tm);
+            continue;
+        }
+        if (tid == 0) {
+            B.ncl = 1;
+            B.c_idx[0] = c;
+            B.c_off[0] = 0;
+            B.c_n[0] = n;
+            B.c_flags[0] = CF_FRESH;
+            B.used = n;
+            B.fresh_k = 0;
+            B.fresh_p = 0;
+            B.n_pend = B.i_pend = 0;
+            B.exhausted = 1;
+            B.phase = 1;
+        }
+        __syncthreads();
+        bundle_load(A, B);
+        {
+            const int nt = bundle_list(B, MF_TGT);
+            bundle_pairs(A, B, 0, nt);
+            bundle_finalize(A, B, 0, nt, 2);
+        }
+        // bundle_step advances the cluster by one block step; it retires when done
+        for (int it = 0; it < MAX_BLOCK_STEPS + 8; it++) {
+            bundle_step(A, B);
+            if (B.any) bundle_retire(A, B);
+            if (B.ncl == 0) break;
+        }
+        __syncthreads();
+    }
+}
+
+// one CTA: (without k_hard_wide) the clusters above BCAP_MAIN one at a time,
+// then bundles until the queue is empty
+__global__ void __launch_bounds__(BT, 2) k_hard_bundles(HardArgs A) {
+    extern __shared__ __align__(16) unsigned char bundle_smem[];
+    BundleSmem<BCAP_MAIN> &B = *reinterpret_cast<BundleSmem<BCAP_MAIN> *>(bundle_smem);
+    __shared__ double red_d[4];
+    __shared__ long long red_l[4];
+    __shared__ int q_sh;
+    const int tid = threadIdx.x;
+    if (!A.wide) {
         Team<128> tm{tid, red_d, red_l};
         for (int guard = 0; guard < (1 << 30); guard++) {
             if (tid == 0) q_sh = atomicAdd(&A.queue[0], 1);

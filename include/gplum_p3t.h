@@ -200,6 +200,11 @@ int p3t_set_hard_mode(int mode);
  * (default 6.5, about 90 block steps; set by the autotuner; 0 turns it
  * off).  Results do not depend on it. */
 int p3t_set_hard_heavy(float log2_steps);
+/* Bundle form: the clusters above 256 bodies run in a second, concurrent
+ * launch as lone bundles of up to 512 slots (1, default) or one cluster per
+ * CTA inside the main launch (0).  Results are bit-identical; set by the
+ * autotuner. */
+int p3t_set_hard_wide(int on);
 /* KOMINAMI fragmentation of the collision outcome (src/collisionB.h:7-93;
  * Collision::a_frag, N_frag, Collision0::m_min of parameter.dat).  a_frag = 0
  * (the default) is perfect accretion.  A collision makes

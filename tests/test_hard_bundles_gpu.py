@@ -23,12 +23,12 @@ FIELDS = ("pos", "vel", "acc_d", "jerk_d", "acc_s", "jerk_s", "phi_s", "phi_d", 
           "id", "dead", "merged", "n_cluster")
 
 
-def prepared(n, f, seed):
+def prepared(n, f, seed, mfac=1.0):
     """The 0.95-1.05 AU disk with rms e = 6 h, rms i = 3 h and the body mass of
-    the hard-part workload at this n (7e-11 at 1,048,576 bodies, scaled n^-1.5);
-    f inflates the collision radii to force collisions."""
+    the hard-part workload at this n (7e-11 at 1,048,576 bodies, scaled n^-1.5,
+    times mfac); f inflates the collision radii to force collisions."""
     P = P3TParams(n_group_limit=256)
-    m = 7e-11 * (1048576.0 / n) ** 1.5
+    m = 7e-11 * (1048576.0 / n) ** 1.5 * mfac
     d = make_disk(n, m, 0.95, 1.05, ecc_hill=6.0, inc_hill=3.0, seed=seed, f=f)
     g = GpuSystem(P)
     g.load(d)
@@ -52,22 +52,34 @@ def run(g, mode, nc):
     return cols, ed, {k: g.get(k) for k in FIELDS}, cost
 
 
-@pytest.mark.parametrize("n,f,seed", [(65536, 1.0, 5), (65536, 40.0, 6), (8192, 200.0, 7)])
-def test_bundles_match_tiers_bitwise(gpu, n, f, seed):
-    g = prepared(n, f, seed)
+# the last two: heavier bodies near percolation give clusters of 257-512 bodies
+# (the wide lone bundles) and, with mfac 2, of more than 512 (the
+# one-cluster-per-CTA form inside the wide launch)
+@pytest.mark.parametrize("n,f,seed,mfac", [(65536, 1.0, 5, 1.0), (65536, 40.0, 6, 1.0), (8192, 200.0, 7, 1.0),
+                                           (16384, 30.0, 8, 1.5), (16384, 1.0, 8, 2.0)])
+def test_bundles_match_tiers_bitwise(gpu, n, f, seed, mfac):
+    g = prepared(n, f, seed, mfac)
     off, _ = g.cluster_lists()
     nc = len(off) - 1
     assert nc > 100
+    if mfac > 1.0:
+        assert np.diff(off).max() > (512 if mfac >= 2.0 else 256)
     assert g.lib.p3t_state_snapshot(0) == 0
     try:
-        b = run(g, 0, nc)
         t = run(g, 1, nc)
+        forms = []
+        for wide in (1, 0):  # clusters above 256 bodies: concurrent wide launch / one per CTA
+            assert g.lib.p3t_set_hard_wide(wide) == 0
+            forms.append(run(g, 0, nc))
     finally:
         g.lib.p3t_set_hard_mode(0)
-    np.testing.assert_array_equal(b[0], t[0])
-    assert b[1].tobytes() == t[1].tobytes()
-    for k in FIELDS:
-        assert b[2][k].tobytes() == t[2][k].tobytes(), k
-    np.testing.assert_array_equal(b[3], t[3])
+        g.lib.p3t_set_hard_wide(1)
+    for b in forms:
+        np.testing.assert_array_equal(b[0], t[0])
+        assert b[1].tobytes() == t[1].tobytes()
+        for k in FIELDS:
+            assert b[2][k].tobytes() == t[2][k].tobytes(), k
+        np.testing.assert_array_equal(b[3], t[3])
+    b = forms[0]
     if f > 1.0:
         assert len(b[0]) > 0
