@@ -102,6 +102,29 @@ struct Uploader {
     void add(void *dst, const void *src, size_t bytes) {
         if (bytes) items.push_back({dst, src, bytes, is_pinned(src)});
     }
+    // queues the copies; returns once they are on the stream (the caller's
+    // pinned sources and the staging buffer must stay untouched until the
+    // stream has run them)
+    int issue() {
+        size_t stage = 0;
+        for (auto &it : items)
+            if (!it.pinned) stage += (it.bytes + 255) / 256 * 256;
+        int r = grow_host(&c->h_stage, &c->h_stage_cap, stage);
+        if (r) return r;
+        char *h = (char *)c->h_stage;
+        for (auto &it : items) {
+            const void *src = it.src;
+            if (!it.pinned) {
+                std::memcpy(h, it.src, it.bytes);
+                src = h;
+                h += (it.bytes + 255) / 256 * 256;
+            }
+            r = cuda_status(cudaMemcpyAsync(it.dst, src, it.bytes, cudaMemcpyHostToDevice, c->stream));
+            if (r) return r;
+        }
+        items.clear();
+        return 0;
+    }
     int flush() {
         size_t stage = 0;
         for (auto &it : items)
@@ -167,8 +190,9 @@ SoftArgs make_args(Context *c, DevSet &d, int n_group, int n_ptcl, int n_spj, bo
 }
 
 // Launch order: largest groups first (less tail imbalance).
-int set_group_order(Context *c, DevSet &d, int n_group, const int *i_off_h, const int *j_off_h,
-                           const int *s_off_h) {
+// launch order of the groups: most pair work first (i-slots in whole warps x
+// list entries, a superparticle counted twice)
+static void group_order_host(int n_group, const int *i_off_h, const int *j_off_h, const int *s_off_h, int *ord) {
     std::vector<std::pair<long long, int>> w(n_group);
     for (int g = 0; g < n_group; g++) {
         const long long ni = i_off_h[g + 1] - i_off_h[g];
@@ -176,8 +200,13 @@ int set_group_order(Context *c, DevSet &d, int n_group, const int *i_off_h, cons
         w[g] = {-(((ni + 31) / 32) * 32 * nj), g};
     }
     std::sort(w.begin(), w.end());
-    std::vector<int> ord(n_group);
     for (int g = 0; g < n_group; g++) ord[g] = w[g].second;
+}
+
+int set_group_order(Context *c, DevSet &d, int n_group, const int *i_off_h, const int *j_off_h,
+                           const int *s_off_h) {
+    std::vector<int> ord(n_group);
+    group_order_host(n_group, i_off_h, j_off_h, s_off_h, ord.data());
     int r = d.order.reserve((size_t)n_group);
     if (r) return r;
     r = cuda_status(cudaMemcpyAsync(d.order.p, ord.data(), n_group * sizeof(int), cudaMemcpyHostToDevice, c->stream));
@@ -339,15 +368,58 @@ int p3t_download_forces(void *force, int n) {
     return read_status(c);
 }
 
+// One call, host buffers in and out, with a single wait: every upload is
+// queued at once (pinned sources go straight to the copy engine), the group
+// launch order is computed on the host while they run, then the kernels and
+// the force download follow on the stream.
 int p3t_soft_force_host(int n, const void *epj, int n_group, const int *i_off, const int *i_idx, const int *j_off,
                         const int *j_idx, const int *s_off, const int *s_idx, const void *spj, int n_spj,
                         void *force) {
-    int r = p3t_upload_particles(n, epj);
-    if (r) return r;
-    r = p3t_upload_lists(n_group, i_off, i_idx, j_off, j_idx, s_off, s_idx, spj, n_spj);
-    if (r) return r;
-    r = p3t_soft_run(0);
-    if (r) return r;
+    CTX_OR_FAIL(c);
+    if (n < 0 || n_group < 0 || n_spj < 0 || (n > 0 && (!epj || !force)) ||
+        (n_group > 0 && (!i_off || !j_off || !s_off)))
+        return ST_BAD_INDEX;
+    DevSet &d = c->res;
+    const long long ni = n_group ? i_off[n_group] : 0, nj = n_group ? j_off[n_group] : 0,
+                    ns = n_group ? s_off[n_group] : 0;
+    int r = 0;
+    if ((r = d.epj_stage.reserve(n)) || (r = d.ptcl.reserve(n)) || (r = d.mass.reserve(n)) ||
+        (r = d.r_out.reserve(n)) || (r = d.r_search.reserve(n)) || (r = d.force.reserve(n)) ||
+        (r = d.acc64.reserve(n)) || (r = d.i_off.reserve(n_group + 1)) || (r = d.j_off.reserve(n_group + 1)) ||
+        (r = d.s_off.reserve(n_group + 1)) || (r = d.i_idx.reserve(ni)) || (r = d.j_idx.reserve(nj)) ||
+        (r = d.s_idx.reserve(ns)) || (r = d.spj.reserve(n_spj)) || (r = d.order.reserve((size_t)n_group)) ||
+        (r = grow_host(&c->h_order, &c->h_order_cap, (size_t)n_group * sizeof(int) + 4)))
+        return r;
+    Uploader u(c);
+    u.add(d.epj_stage.p, epj, (size_t)n * sizeof(EPJRec));
+    u.add(d.i_off.p, i_off, (n_group + 1) * sizeof(int));
+    u.add(d.j_off.p, j_off, (n_group + 1) * sizeof(int));
+    u.add(d.s_off.p, s_off, (n_group + 1) * sizeof(int));
+    u.add(d.i_idx.p, i_idx, ni * sizeof(int));
+    u.add(d.j_idx.p, j_idx, nj * sizeof(int));
+    u.add(d.s_idx.p, s_idx, ns * sizeof(int));
+    u.add(d.spj.p, spj, (size_t)n_spj * sizeof(SPJRec));
+    // an early return leaves no copy of this call running (the caller's
+    // buffers and the staging and order buffers are reused afterwards)
+    auto fail = [&](int e) {
+        cudaStreamSynchronize(c->stream);
+        return e;
+    };
+    if ((r = u.issue())) return fail(r);
+    if ((r = cuda_status(launch_pack_epj(d.epj_stage.p, n, d.ptcl.p, d.mass.p, d.r_out.p, d.r_search.p, c->stream))))
+        return fail(r);
+    c->res_n = n;
+    c->res_groups = n_group;
+    c->res_spj = n_spj;
+    if (n_group > 0) {
+        // h_order is free: every call ends with a wait on the stream
+        group_order_host(n_group, i_off, j_off, s_off, (int *)c->h_order);
+        if ((r = cuda_status(cudaMemcpyAsync(d.order.p, c->h_order, n_group * sizeof(int), cudaMemcpyHostToDevice,
+                                             c->stream))))
+            return fail(r);
+    }
+    d.order_valid = true;
+    if ((r = p3t_soft_run(0))) return fail(r);
     return p3t_download_forces(force, n);
 }
 

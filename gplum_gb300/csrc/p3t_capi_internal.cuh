@@ -83,6 +83,8 @@ struct Context {
     size_t h_stage_cap = 0;
     void *h_out = nullptr;
     size_t h_out_cap = 0;
+    void *h_order = nullptr;  // group launch order on its way to the device
+    size_t h_order_cap = 0;
     WalkSlot walk[MAX_TAGS];
 
     void release() {
@@ -90,8 +92,9 @@ struct Context {
         idx.release();
         if (h_stage) cudaFreeHost(h_stage);
         if (h_out) cudaFreeHost(h_out);
-        h_stage = h_out = nullptr;
-        h_stage_cap = h_out_cap = 0;
+        if (h_order) cudaFreeHost(h_order);
+        h_stage = h_out = h_order = nullptr;
+        h_stage_cap = h_out_cap = h_order_cap = 0;
         for (auto &w : walk) {
             w.d.release();
             if (w.h_in) cudaFreeHost(w.h_in);
