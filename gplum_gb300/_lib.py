@@ -69,6 +69,7 @@ SIGNATURES = {
     "p3t_set_soft_tiles": (I, [I, I, I]),
     "p3t_set_soft_occupancy": (I, [I]),
     "p3t_set_hard_wide": (I, [I]),
+    "p3t_set_hard_bundle": (I, [I, I]),
     "p3t_set_hard_heavy": (I, [ctypes.c_float]),
     "p3t_id_next": (ctypes.c_longlong, []),
     "p3t_mlp_set": (I, [VP, VP]),

@@ -109,23 +109,30 @@ def tune_heavy(g, istep=1, grid=HEAVY_GRID):
     return best, table
 
 
-def tune_wide(g, istep=1, reps=2):
-    """Times the bundled hard launch from one restored state with the clusters
-    above 256 bodies in the concurrent wide launch (1) or one per CTA in the
-    main launch (0); installs the faster.  Returns (best, {choice: ms})."""
+# (member slots, CTAs per SM, clusters above the slots in the wide launch)
+BUNDLE_GRID = ((256, 2, 0), (256, 2, 1), (128, 3, 1), (128, 4, 1))
+
+
+def tune_wide(g, istep=1, reps=2, grid=BUNDLE_GRID):
+    """Times the bundled hard launch from one restored state for each bundle
+    shape (p3t_set_hard_bundle) and placement of the clusters above it
+    (p3t_set_hard_wide: concurrent wide launch or one per CTA in the main
+    launch); installs the fastest.  Returns (best, {choice: ms})."""
     lib = g.lib
     _lib.check(lib.p3t_state_snapshot(0), "p3t_state_snapshot")
     table = {}
-    for w in (1, 0):
+    for cap, occ, w in grid:
+        _lib.check(lib.p3t_set_hard_bundle(cap, occ), "p3t_set_hard_bundle")
         _lib.check(lib.p3t_set_hard_wide(w), "p3t_set_hard_wide")
         ts = []
         for _ in range(reps):
             _lib.check(lib.p3t_state_snapshot(1), "p3t_state_snapshot")
             ts.append(1e3 * _timed(lib, lambda: g.hard(istep), 1))
-        table[w] = float(min(ts))
+        table[(cap, occ, w)] = float(min(ts))
     lib.p3t_state_snapshot(1)
     best = min(table, key=table.get)
-    _lib.check(lib.p3t_set_hard_wide(best), "p3t_set_hard_wide")
+    _lib.check(lib.p3t_set_hard_bundle(best[0], best[1]), "p3t_set_hard_bundle")
+    _lib.check(lib.p3t_set_hard_wide(best[2]), "p3t_set_hard_wide")
     return best, table
 
 
@@ -143,6 +150,8 @@ def load(lib=None, path=TUNING):
         _lib.check(lib.p3t_set_hard_tiers(*t["hard_tiers"]), "p3t_set_hard_tiers")
     if "hard_wide" in t:
         _lib.check(lib.p3t_set_hard_wide(int(t["hard_wide"])), "p3t_set_hard_wide")
+    if "hard_bundle" in t:
+        _lib.check(lib.p3t_set_hard_bundle(*t["hard_bundle"]), "p3t_set_hard_bundle")
     if "hard_heavy" in t:
         import ctypes
 
@@ -215,8 +224,9 @@ def main():
            "soft_ms": {",".join(map(str, k)): v for k, v in soft_table.items()},
            "hard_tiers": list(hard_best),
            "hard_heavy": heavy_best if heavy_best is not None else 6.5,
-           "hard_wide": wide_best,
-           "hard_wide_ms": {str(k): v for k, v in wide_table.items()},
+           "hard_bundle": list(wide_best[:2]),
+           "hard_wide": wide_best[2],
+           "hard_bundle_ms": {",".join(map(str, k)): v for k, v in wide_table.items()},
            "hard_heavy_ms": {str(k): v for k, v in heavy_table.items()},
            "hard_ms": {",".join(map(str, k)): v for k, v in hard_table.items()},
            "workloads": {"soft": "1048576-body disk 0.5-1.5 AU, m=1e-10, theta=0.5, n_group_limit=256",

@@ -1097,12 +1097,12 @@ __global__ void k_isolated(IsoArgs A) {
 // arbitrary; no result depends on the order, only the makespan does.
 constexpr int ORDER_NB = 4096;
 
-__global__ void k_order_bins(const int32_t *cnt, const float *prio, int nc, int mode, int warp_min, int cta_min,
+__global__ void k_order_bins(const int32_t *cnt, const float *prio, int nc, int mode, int main_cap, int warp_min, int cta_min,
                              float pmin, float pscale, int heavy_key, int32_t *bin, int32_t *hist, int32_t *n_heavy) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nc) return;
     const int n = cnt[k];
-    const int tier = (mode == 0) ? (n > BCAP_MAIN ? 0 : 1) : (n >= cta_min ? 0 : (n >= warp_min ? 1 : 2));
+    const int tier = (mode == 0) ? (n > main_cap ? 0 : 1) : (n >= cta_min ? 0 : (n >= warp_min ? 1 : 2));
     int key = n < ORDER_NB - 1 ? n : ORDER_NB - 1;
     if (prio) {
         const float v = (prio[k] - pmin) * pscale;
@@ -1218,7 +1218,8 @@ static double g_edisp[2] = {0., 0.};
 static int g_warp_min = 8, g_cta_min = 64;
 static int g_hard_mode = 0;  // 0: bundles, 1: thread/warp/CTA tiers
 static float g_heavy = 6.5f;  // predicted log2(1 + block steps) from which a cluster runs alone (0: never)
-static int g_wide = 1;        // clusters above BCAP_MAIN bodies: wide lone bundles (1) or one per CTA (0)
+static int g_wide = 1;        // clusters above the bundle capacity: wide lone bundles (1) or one per CTA (0)
+static int g_bcap = 256, g_bocc = 2;  // bundle member slots and CTAs per SM (256/2, 128/3, 128/4)
 static FragParams g_frag = {0., 9.426627927538057e-12, 10, 0, 0ULL};  // off (a_frag = 0)
 static int g_frag_cap = 0;  // fragment slots of the current launch
 
@@ -1307,6 +1308,14 @@ int p3t_set_hard_heavy(float log2_steps) {
     return 0;
 }
 
+int p3t_set_hard_bundle(int member_slots, int ctas_per_sm) {
+    const bool ok = (member_slots == 256 && ctas_per_sm == 2) || (member_slots == 128 && (ctas_per_sm == 3 || ctas_per_sm == 4));
+    if (!ok) return ST_BAD_INDEX;
+    g_bcap = member_slots;
+    g_bocc = ctas_per_sm;
+    return 0;
+}
+
 int p3t_set_hard_wide(int on) {
     if (on != 0 && on != 1) return ST_BAD_INDEX;
     g_wide = on;
@@ -1380,7 +1389,7 @@ int p3t_hard_enqueue(void) {
         int heavy_key = 2147483647;
         if (prio && (int)g_prio.size() != nc && g_heavy > 0.f)
             heavy_key = std::min(ORDER_NB - 1, (int)((g_heavy - pmin) * pscale));
-        k_order_bins<<<(nc + 255) / 256, 256, 0, c->stream>>>(E.cl_cnt.p, prio, nc, g_hard_mode, g_warp_min, g_cta_min,
+        k_order_bins<<<(nc + 255) / 256, 256, 0, c->stream>>>(E.cl_cnt.p, prio, nc, g_hard_mode, g_bcap, g_warp_min, g_cta_min,
                                                               pmin, pscale, heavy_key, B.bin.p, B.hist.p,
                                                               B.ntier.p + 3);
         k_order_scan<<<1, 1024, 0, c->stream>>>(B.hist.p, B.ntier.p);
@@ -1441,10 +1450,18 @@ int p3t_hard_integrate(int istep) {
             static bool attr = false;
             static cudaStream_t s_wide = nullptr;
             static cudaEvent_t ev_ready = nullptr, ev_done = nullptr;
-            const int smem = (int)sizeof(BundleSmem<BCAP_MAIN>), smem_w = (int)sizeof(BundleSmem<BCAP_WIDE>);
+            const int smem_w = (int)sizeof(BundleSmem<BCAP_WIDE>);
+            const int smem = g_bcap == 128 ? (int)sizeof(BundleSmem<128>) : (int)sizeof(BundleSmem<256>);
             if (!attr) {
-                if ((r = cuda_status(cudaFuncSetAttribute(k_hard_bundles, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                          smem))) ||
+                if ((r = cuda_status(cudaFuncSetAttribute(k_hard_bundles<256, 2>,
+                                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                          (int)sizeof(BundleSmem<256>)))) ||
+                    (r = cuda_status(cudaFuncSetAttribute(k_hard_bundles<128, 3>,
+                                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                          (int)sizeof(BundleSmem<128>)))) ||
+                    (r = cuda_status(cudaFuncSetAttribute(k_hard_bundles<128, 4>,
+                                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                          (int)sizeof(BundleSmem<128>)))) ||
                     (r = cuda_status(cudaFuncSetAttribute(k_hard_wide, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                           smem_w))) ||
                     (r = cuda_status(cudaStreamCreateWithFlags(&s_wide, cudaStreamNonBlocking))) ||
@@ -1463,9 +1480,14 @@ int p3t_hard_integrate(int istep) {
                 k_hard_wide<<<std::max(1, sms / 16), BT, smem_w, s_wide>>>(A);
                 if ((r = cuda_status(cudaGetLastError()))) return r;
             }
-            // persistent: 2 CTAs per SM (fewer when there are few clusters)
-            const int blocks = std::max(1, std::min(sms * 2, (nc + 3) / 4));
-            k_hard_bundles<<<blocks, BT, smem, c->stream>>>(A);
+            // persistent: g_bocc CTAs per SM (fewer when there are few clusters)
+            const int blocks = std::max(1, std::min(sms * g_bocc, (nc + 3) / 4));
+            if (g_bcap == 256)
+                k_hard_bundles<256, 2><<<blocks, BT, smem, c->stream>>>(A);
+            else if (g_bocc == 3)
+                k_hard_bundles<128, 3><<<blocks, BT, smem, c->stream>>>(A);
+            else
+                k_hard_bundles<128, 4><<<blocks, BT, smem, c->stream>>>(A);
             if ((r = cuda_status(cudaGetLastError()))) return r;
             if (A.wide && ((r = cuda_status(cudaEventRecord(ev_done, s_wide))) ||
                            (r = cuda_status(cudaStreamWaitEvent(c->stream, ev_done, 0)))))

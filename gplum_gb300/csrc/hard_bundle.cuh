@@ -6,7 +6,7 @@
 // warp (or thread) per cluster leaves most lanes idle: a cluster has a few
 // active members per block step, and a serial pair loop per member has one
 // live partner in several.  Here the CTA keeps up to BCAP members of up to
-// BMAXCL clusters in shared memory and advances every cluster by one block
+// bmaxcl(BCAP) clusters in shared memory and advances every cluster by one block
 // step per iteration, so each phase runs over the union of the bundle's
 // work items:
 //   - member phases (predict, correct, time steps) over all members or all
@@ -49,7 +49,8 @@ namespace p3t {
 constexpr int BT = 128;      // threads of a bundle (one CTA)
 constexpr int BCAP_MAIN = 256;  // member slots of a bundle
 constexpr int BCAP_WIDE = 512;  // member slots of the wide form (clusters of 257..512 bodies, one at a time)
-constexpr int BMAXCL = 128;  // clusters in a bundle at once
+// clusters in a bundle at once: half its member slots, at most one per thread
+__host__ __device__ constexpr int bmaxcl(int cap) { return cap / 2 < 128 ? cap / 2 : 128; }
 constexpr int BSURV = 64;    // colliding-pair candidates kept per block step
 constexpr int BCLAIM = 8;    // clusters claimed from the queue at a time
 
@@ -72,14 +73,14 @@ struct BundleSmem {
     short tgt[BCAP], cl[BCAP], owner[BCAP];
     unsigned char dead[BCAP], merged[BCAP], flag[BCAP];
     // clusters (bundle index k)
-    double c_ts[BMAXCL], c_ref[3 * BMAXCL], c_ed[BMAXCL], c_edd[BMAXCL];
-    unsigned long long c_key[BMAXCL], c_red[4 * BMAXCL];
-    long long c_pb[BMAXCL], c_work[BMAXCL], c_t0[BMAXCL];
-    long long c_label[BMAXCL], c_fragn[BMAXCL];  // id_cluster, fragments made (KOMINAMI)
-    int c_n0[BMAXCL], c_addn[BMAXCL], c_addg[BMAXCL];  // members at admission; new fragments (count, first slot)
-    float c_thrf[BMAXCL], c_thrc[BMAXCL], c_E32[BMAXCL];
-    int c_idx[BMAXCL], c_off[BMAXCL], c_n[BMAXCL], c_goff[BMAXCL], c_steps[BMAXCL], c_ncol[BMAXCL];
-    int c_flags[BMAXCL], c_imp[BMAXCL], c_tar[BMAXCL];
+    double c_ts[bmaxcl(BCAP)], c_ref[3 * bmaxcl(BCAP)], c_ed[bmaxcl(BCAP)], c_edd[bmaxcl(BCAP)];
+    unsigned long long c_key[bmaxcl(BCAP)], c_red[4 * bmaxcl(BCAP)];
+    long long c_pb[bmaxcl(BCAP)], c_work[bmaxcl(BCAP)], c_t0[bmaxcl(BCAP)];
+    long long c_label[bmaxcl(BCAP)], c_fragn[bmaxcl(BCAP)];  // id_cluster, fragments made (KOMINAMI)
+    int c_n0[bmaxcl(BCAP)], c_addn[bmaxcl(BCAP)], c_addg[bmaxcl(BCAP)];  // members at admission; new fragments (count, first slot)
+    float c_thrf[bmaxcl(BCAP)], c_thrc[bmaxcl(BCAP)], c_E32[bmaxcl(BCAP)];
+    int c_idx[bmaxcl(BCAP)], c_off[bmaxcl(BCAP)], c_n[bmaxcl(BCAP)], c_goff[bmaxcl(BCAP)], c_steps[bmaxcl(BCAP)], c_ncol[bmaxcl(BCAP)];
+    int c_flags[bmaxcl(BCAP)], c_imp[bmaxcl(BCAP)], c_tar[bmaxcl(BCAP)];
     // colliding-pair candidates
     double sv_R[BSURV];
     long long sv_p[BSURV];
@@ -464,7 +465,7 @@ __device__ void bundle_refill(const HardArgs &A, BundleSmem<BCAP> &B) {
                     const int c = B.pend_c[B.i_pend], n = B.pend_n[B.i_pend];
                     // with fragmentation, keep room for the fragments of a collision
                     const int room = (A.frag.a_frag > 0.) ? 2 * A.frag.n_frag_max : 0;
-                    if (B.used + n + room > BCAP || B.ncl >= BMAXCL) break;
+                    if (B.used + n + room > BCAP || B.ncl >= bmaxcl(BCAP)) break;
                     const int k = B.ncl++;
                     B.c_idx[k] = c;
                     B.c_off[k] = B.used;
@@ -578,7 +579,7 @@ template <int BCAP>
 __device__ void bundle_grow(const HardArgs &A, BundleSmem<BCAP> &B) {
     const Hard &H = A.H;
     const int tid = threadIdx.x;
-    static_assert(BMAXCL <= BT, "one thread per bundle cluster");
+    static_assert(bmaxcl(BCAP) <= BT, "one thread per bundle cluster");
     const int add = (tid < B.ncl) ? B.c_addn[tid] : 0;
     const int nn = (tid < B.ncl) ? B.c_n[tid] + add : 0;
     int tot;
@@ -887,7 +888,7 @@ __device__ void bundle_retire(const HardArgs &A, BundleSmem<BCAP> &B) {
         t_thrf = B.c_thrf[tid]; t_thrc = B.c_thrc[tid]; t_E = B.c_E32[tid];
         t_label = B.c_label[tid]; t_fragn = B.c_fragn[tid]; t_n0 = B.c_n0[tid];
     }
-    static_assert(BMAXCL <= BT, "one thread per bundle cluster");
+    static_assert(bmaxcl(BCAP) <= BT, "one thread per bundle cluster");
     nk = bscan(keep, B.ws, nkeep);
     noff = bscan(keep ? t_n : 0, B.ws, tot);
     // slots: read the old placement before anything moves
@@ -998,11 +999,12 @@ __global__ void __launch_bounds__(BT, 1) k_hard_wide(HardArgs A) {
     }
 }
 
-// one CTA: (without k_hard_wide) the clusters above BCAP_MAIN one at a time,
-// then bundles until the queue is empty
-__global__ void __launch_bounds__(BT, 2) k_hard_bundles(HardArgs A) {
+// one CTA: (without k_hard_wide) the clusters above BCAP one at a time, then
+// bundles of BCAP member slots until the queue is empty; OCC CTAs per SM
+template <int BCAP, int OCC>
+__global__ void __launch_bounds__(BT, OCC) k_hard_bundles(HardArgs A) {
     extern __shared__ __align__(16) unsigned char bundle_smem[];
-    BundleSmem<BCAP_MAIN> &B = *reinterpret_cast<BundleSmem<BCAP_MAIN> *>(bundle_smem);
+    BundleSmem<BCAP> &B = *reinterpret_cast<BundleSmem<BCAP> *>(bundle_smem);
     __shared__ double red_d[4];
     __shared__ long long red_l[4];
     __shared__ int q_sh;

@@ -200,11 +200,15 @@ int p3t_set_hard_mode(int mode);
  * (default 6.5, about 90 block steps; set by the autotuner; 0 turns it
  * off).  Results do not depend on it. */
 int p3t_set_hard_heavy(float log2_steps);
-/* Bundle form: the clusters above 256 bodies run in a second, concurrent
+/* Bundle form: the clusters above the bundle's member slots run in a second, concurrent
  * launch as lone bundles of up to 512 slots (1, default) or one cluster per
  * CTA inside the main launch (0).  Results are bit-identical; set by the
  * autotuner. */
 int p3t_set_hard_wide(int on);
+/* Bundle form: member slots per bundle and resident CTAs per SM -- 256/2
+ * (default), 128/3 or 128/4 (clusters above the slot count go to the wide
+ * or one-per-CTA form).  Results are bit-identical; set by the autotuner. */
+int p3t_set_hard_bundle(int member_slots, int ctas_per_sm);
 /* KOMINAMI fragmentation of the collision outcome (src/collisionB.h:7-93;
  * Collision::a_frag, N_frag, Collision0::m_min of parameter.dat).  a_frag = 0
  * (the default) is perfect accretion.  A collision makes

@@ -68,12 +68,15 @@ def test_bundles_match_tiers_bitwise(gpu, n, f, seed, mfac):
     try:
         t = run(g, 1, nc)
         forms = []
-        for wide in (1, 0):  # clusters above 256 bodies: concurrent wide launch / one per CTA
+        # bundle shapes and placements of the clusters above the slots
+        for cap, occ, wide in ((256, 2, 1), (256, 2, 0), (128, 3, 1)):
+            assert g.lib.p3t_set_hard_bundle(cap, occ) == 0
             assert g.lib.p3t_set_hard_wide(wide) == 0
             forms.append(run(g, 0, nc))
     finally:
         g.lib.p3t_set_hard_mode(0)
         g.lib.p3t_set_hard_wide(1)
+        g.lib.p3t_set_hard_bundle(256, 2)
     for b in forms:
         np.testing.assert_array_equal(b[0], t[0])
         assert b[1].tobytes() == t[1].tobytes()
