@@ -124,9 +124,12 @@ def p3t_step_measure(precision, steps=2, n=N_BODIES, hard_mode=0, learned=True, 
     from gplum_gb300.p3t import GpuSystem
     from gplum_gb300.tree import build_lists
 
+    from gplum_gb300 import autotune
+
     P = P3TParams(n_group_limit=256)
     d = disk_1m_hard(n)
     g = GpuSystem(P, precision=precision)
+    autotune.load(g.lib)  # launch shapes chosen by gplum_gb300/autotune.py
     g.lib.p3t_set_hard_mode(hard_mode)
     model = scheduler.load(lib=g.lib) if learned else None
     g.lib.p3t_set_schedule(1 if model is not None else 0)

@@ -187,8 +187,14 @@ __device__ __forceinline__ void corr_pair(const State &S, const Params &P, int i
     }
 }
 
-__global__ void k_correct(State S, Params P, const ForceRec *__restrict__ F, const int32_t *__restrict__ cand, int cap,
-                          int initial, int32_t *counters, int *status) {
+// INITIAL: correctForceLongInitial (hard-part terms, sun force, first time
+// step) or correctForceLong; compiled separately so that the plain pass
+// carries none of the initial pass's registers
+template <bool INITIAL>
+__global__ void __launch_bounds__(128, 4) k_correct(State S, Params P, const ForceRec *__restrict__ F,
+                                                    const int32_t *__restrict__ cand, int cap, int32_t *counters,
+                                                    int *status) {
+    constexpr bool initial = INITIAL;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= S.n) return;
     const ForceRec fr = F[i];
@@ -721,8 +727,12 @@ int Engine::correct(int initial) {
     if (!c->res.cand.p || !c->res.force.p || c->res_n != S.n) return ST_BAD_INDEX;
     if ((r = counters.reserve(4))) return r;
     cudaMemsetAsync(counters.p, 0, 4 * sizeof(int32_t), c->stream);
-    k_correct<<<nb(S.n, 128), 128, 0, c->stream>>>(S, P, c->res.force.p, c->res.cand.p, c->cand_cap, initial,
-                                                     counters.p, c->status);
+    if (initial)
+        k_correct<true><<<nb(S.n, 128), 128, 0, c->stream>>>(S, P, c->res.force.p, c->res.cand.p, c->cand_cap,
+                                                             counters.p, c->status);
+    else
+        k_correct<false><<<nb(S.n, 128), 128, 0, c->stream>>>(S, P, c->res.force.p, c->res.cand.p, c->cand_cap,
+                                                              counters.p, c->status);
     if (initial) k_copy3<<<nb(3 * S.n), 256, 0, c->stream>>>(S.acc_d, S.acc_d_new, S.n);
     return cuda_status(cudaGetLastError());
 }

@@ -197,12 +197,12 @@ int p3t_set_hard_mode(int mode);
 /* Bundle form with the learned order: clusters whose predicted
  * log2(1 + block steps) is at least log2_steps run first, each alone in a
  * CTA, so the longest chains of block steps do not wait on a full bundle
- * (default 6.5, about 90 block steps; set by the autotuner; 0 turns it
+ * (default 5.5, about 45 block steps; set by the autotuner; 0 turns it
  * off).  Results do not depend on it. */
 int p3t_set_hard_heavy(float log2_steps);
 /* Bundle form: the clusters above the bundle's member slots run in a second, concurrent
- * launch as lone bundles of up to 512 slots (1, default) or one cluster per
- * CTA inside the main launch (0).  Results are bit-identical; set by the
+ * launch as lone bundles of up to 512 slots (1) or one cluster per CTA
+ * inside the main launch (0, default).  Results are bit-identical; set by the
  * autotuner. */
 int p3t_set_hard_wide(int on);
 /* Bundle form: member slots per bundle and resident CTAs per SM -- 256/2

@@ -75,7 +75,7 @@ def test_bundles_match_tiers_bitwise(gpu, n, f, seed, mfac):
             forms.append(run(g, 0, nc))
     finally:
         g.lib.p3t_set_hard_mode(0)
-        g.lib.p3t_set_hard_wide(1)
+        g.lib.p3t_set_hard_wide(0)
         g.lib.p3t_set_hard_bundle(256, 2)
     for b in forms:
         np.testing.assert_array_equal(b[0], t[0])
