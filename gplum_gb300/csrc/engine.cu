@@ -138,71 +138,137 @@ struct CorrOut {
     int64_t idc;
 };
 
-__device__ __forceinline__ void corr_pair(const State &S, const Params &P, int i, int j, bool initial, V3 pos_i,
-                                          V3 vel_i, V3 accd_i, double ro_i, double roi_i, double rs_i, int cap,
-                                          CorrOut &o) {
-    const double mj = S.mass[j];
-    const double r_out = dmax(ro_i, S.r_out[j]);
-    const double r_out_inv = dmin(roi_i, S.r_out_inv[j]);
-    const double r_search = dmax(rs_i, S.r_search[j]);
-    const V3 dr = ld3(S.pos, j) - pos_i;
-    double dr2 = dot(dr, dr);
-    dr2 += P.eps2;
-    const double rij = sqrt(dr2);
-    const V3 dv = ld3(S.vel, j) - vel_i;
-    const V3 da = ld3(S.acc_d, j) - accd_i;
-    const double drdv = dot(dr, dv);
-    const double dv2 = dot(dv, dv);
-    const double da2 = dot(da, da);
-    const double t_min = dmin(dmax(-drdv / sqrt(dv2), 0.), P.dt_tree);
-    const double dr2_min = dmin(dr2, dr2 + 2. * drdv * t_min + dv2 * t_min * t_min);
-    const double r_crit = P.R_search2 * r_out;
-    const double v_crit_a = P.R_search3 * 0.5 * P.dt_tree;
-    if (dr2_min < r_crit * r_crit || dv2 < v_crit_a * v_crit_a * da2 || (initial && da2 == 0.)) {
-        if (rij < r_search) {
-            // NeighborList::addNeighbor, src/neighbor.h:635-670
-            if (o.number < cap) S.nbr[(size_t)i * cap + o.number] = j;
-            o.number++;
-            o.idc = (S.id[j] < o.idc) ? S.id[j] : o.idc;
-            o.acc0 += r_out * r_out / mj;
-        }
+// correctForceLong / correctForceLongInitial (src/gravity_soft.h:245-528) in
+// three passes, so that the FP64 pair arithmetic runs lane-dense: a warp
+// instruction of the FP64 pipe costs the pipe all 32 lanes whatever the
+// mask, and bodies have from 0 to dozens of candidates.
+//   1. per body: its candidates (the soft kernel's screen hits) in ascending
+//      index order, invalid and same-id entries dropped, appended to a pair
+//      list (a block of consecutive slots per body);
+//   2. per pair: the pair's terms (corr_pair's arithmetic, unchanged);
+//   3. per body: the terms folded in candidate order -- the order of
+//      GPLUM's loop -- then the write-back (and, initially, the sun force
+//      and the first time step).
+// Results are bit-identical to one thread walking its candidates.
+struct PairTerms {
+    V3 acc, acc_d, jerk;
+    double phi, phi_d, acc0;
+    int flags;  // 1: neighbour, 2: inside r_out
+};
+
+// the next smallest candidate of body i above `last` (lists are short; -1: none)
+__device__ __forceinline__ int next_cand(const int32_t *__restrict__ cand, int i, int cap, int kc, int last) {
+    int best = 0x7fffffff;
+    for (int u = 0; u < kc; u++) {
+        const int c = cand[(size_t)i * cap + u];
+        if (c > last && c < best) best = c;
     }
-    if (rij < r_out) {
-        const double rinv = 1. / rij;
-        const double r2inv = rinv * rinv;
-        const double r3inv = rinv * r2inv;
-        const double W = cut_W(P, rij, r_out_inv);
-        const double K = cut_K(P, rij, r_out_inv);
-        const double r_min = dmin(rinv, r_out_inv);
-        o.phi -= mj * (rinv * W - r_min);
-        addto(o.acc, mj * (r3inv * K - r_min * r_min * r_min) * dr);
-        if (initial) {
-            const double alpha = drdv * r2inv;
-            const double dKdt = cut_dKdt(P, rij, r_out_inv, alpha);
-            const double alpha_c = alpha * (1. - K);
-            o.phi_d -= mj * rinv * (1. - W);
-            addto(o.acc_d, mj * r3inv * (1. - K) * dr);
-            addto(o.jerk, mj * r3inv * ((1. - K) * dv - (3. * alpha_c + dKdt) * dr));
+    return best == 0x7fffffff ? -1 : best;
+}
+
+// pass 1: per body, the usable candidates in ascending index order -- counted
+// (fill = false) or written to the body's slots of the pair list (fill = true)
+template <bool FILL>
+__global__ void k_corr_list(State S, const ForceRec *__restrict__ F, const int32_t *__restrict__ cand, int cap,
+                            int32_t *pair_n, const int32_t *__restrict__ pair_base, int32_t *pair_i, int32_t *pair_j,
+                            int *status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.n) return;
+    const int k = F[i].number;
+    const int64_t id_i = S.id[i];
+    const int kc = min(k, cap);
+    if (!FILL && k > cap) atomicOr(status, ST_CAND_OVERFLOW);
+    const int base = FILL ? pair_base[i] : 0;
+    int m = 0, last = -1;
+    for (int t = 0; t < kc; t++) {
+        const int j = next_cand(cand, i, cap, kc, last);
+        if (j < 0) break;
+        last = j;
+        if ((unsigned)j >= (unsigned)S.n) {
+            if (!FILL) atomicOr(status, ST_BAD_INDEX);
+            continue;
         }
+        if (S.id[j] == id_i) continue;
+        if (FILL) {
+            pair_i[base + m] = i;
+            pair_j[base + m] = j;
+        }
+        m++;
+    }
+    if (!FILL) pair_n[i] = m;
+}
+
+// corr_pair's arithmetic for one pair (src/gravity_soft.h:75-242), terms out
+template <bool INITIAL>
+__global__ void __launch_bounds__(128) k_corr_pairs(State S, Params P, int np, const int32_t *__restrict__ pair_i,
+                                                    const int32_t *__restrict__ pair_j, PairTerms *out) {
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < np; q += gridDim.x * blockDim.x) {
+        const int i = pair_i[q], j = pair_j[q];
+        PairTerms o;
+        o.flags = 0;
+        const V3 pos_i = ld3(S.pos, i), vel_i = ld3(S.vel, i), accd_i = ld3(S.acc_d, i);
+        const double mj = S.mass[j];
+        const double r_out = dmax(S.r_out[i], S.r_out[j]);
+        const double r_out_inv = dmin(S.r_out_inv[i], S.r_out_inv[j]);
+        const double r_search = dmax(S.r_search[i], S.r_search[j]);
+        const V3 dr = ld3(S.pos, j) - pos_i;
+        double dr2 = dot(dr, dr);
+        dr2 += P.eps2;
+        const double rij = sqrt(dr2);
+        const V3 dv = ld3(S.vel, j) - vel_i;
+        const V3 da = ld3(S.acc_d, j) - accd_i;
+        const double drdv = dot(dr, dv);
+        const double dv2 = dot(dv, dv);
+        const double da2 = dot(da, da);
+        const double t_min = dmin(dmax(-drdv / sqrt(dv2), 0.), P.dt_tree);
+        const double dr2_min = dmin(dr2, dr2 + 2. * drdv * t_min + dv2 * t_min * t_min);
+        const double r_crit = P.R_search2 * r_out;
+        const double v_crit_a = P.R_search3 * 0.5 * P.dt_tree;
+        if (dr2_min < r_crit * r_crit || dv2 < v_crit_a * v_crit_a * da2 || (INITIAL && da2 == 0.)) {
+            if (rij < r_search) {
+                // NeighborList::addNeighbor, src/neighbor.h:635-670
+                o.flags |= 1;
+                o.acc0 = r_out * r_out / mj;
+            }
+        }
+        if (rij < r_out) {
+            o.flags |= 2;
+            const double rinv = 1. / rij;
+            const double r2inv = rinv * rinv;
+            const double r3inv = rinv * r2inv;
+            const double W = cut_W(P, rij, r_out_inv);
+            const double K = cut_K(P, rij, r_out_inv);
+            const double r_min = dmin(rinv, r_out_inv);
+            o.phi = mj * (rinv * W - r_min);
+            o.acc = mj * (r3inv * K - r_min * r_min * r_min) * dr;
+            if (INITIAL) {
+                const double alpha = drdv * r2inv;
+                const double dKdt = cut_dKdt(P, rij, r_out_inv, alpha);
+                const double alpha_c = alpha * (1. - K);
+                o.phi_d = mj * rinv * (1. - W);
+                o.acc_d = mj * r3inv * (1. - K) * dr;
+                o.jerk = mj * r3inv * ((1. - K) * dv - (3. * alpha_c + dKdt) * dr);
+            }
+        }
+        out[q] = o;
     }
 }
 
-// INITIAL: correctForceLongInitial (hard-part terms, sun force, first time
-// step) or correctForceLong; compiled separately so that the plain pass
-// carries none of the initial pass's registers
 template <bool INITIAL>
-__global__ void __launch_bounds__(128, 4) k_correct(State S, Params P, const ForceRec *__restrict__ F,
-                                                    const int32_t *__restrict__ cand, int cap, int32_t *counters,
+__global__ void __launch_bounds__(128, 4) k_correct(State S, Params P, const ForceRec *__restrict__ F, int cap,
+                                                    const int32_t *__restrict__ pair_base,
+                                                    const int32_t *__restrict__ pair_n,
+                                                    const int32_t *__restrict__ pair_j,
+                                                    const PairTerms *__restrict__ terms, int32_t *counters,
                                                     int *status) {
-    constexpr bool initial = INITIAL;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= S.n) return;
     const ForceRec fr = F[i];
     const V3 pos_i = ld3(S.pos, i), vel_i = ld3(S.vel, i), accd_i = ld3(S.acc_d, i);
-    const double m_i = S.mass[i], ro_i = S.r_out[i], roi_i = S.r_out_inv[i], rs_i = S.r_search[i];
+    const double m_i = S.mass[i], roi_i = S.r_out_inv[i];
     const int64_t id_i = S.id[i];
     V3 acc_s = ld3(S.acc_s, i), jerk_s = ld3(S.jerk_s, i);
-    if (initial) {
+    if (INITIAL) {
         double phs;
         sun_force(P, pos_i, vel_i, acc_s, jerk_s, &phs);
         st3(S.acc_s, i, acc_s);
@@ -215,31 +281,27 @@ __global__ void __launch_bounds__(128, 4) k_correct(State S, Params P, const For
     o.number = 0;
     o.idc = id_i;
     o.phi += m_i * roi_i;
-    const int k = fr.number;
-    if (k > 0) {
-        // candidates: the soft kernel's screen hits (for k <= 2 exactly the
-        // functor's id_min, id_max), taken in ascending index order
-        const int kc = min(k, cap);
-        if (k > cap) atomicOr(status, ST_CAND_OVERFLOW);
-        int last = -1;
-        for (int t = 0; t < kc; t++) {
-            // next smallest candidate above `last` (lists are short)
-            int best = 0x7fffffff;
-            for (int u = 0; u < kc; u++) {
-                const int c = cand[(size_t)i * cap + u];
-                if (c > last && c < best) best = c;
-            }
-            if (best == 0x7fffffff) break;
-            last = best;
-            if ((unsigned)best >= (unsigned)S.n) {
-                atomicOr(status, ST_BAD_INDEX);
-                continue;
-            }
-            if (S.id[best] == id_i) continue;
-            corr_pair(S, P, i, best, initial != 0, pos_i, vel_i, accd_i, ro_i, roi_i, rs_i, cap, o);
+    const int base = pair_base[i], m = pair_n[i];
+    for (int t = 0; t < m; t++) {
+        const PairTerms &q = terms[base + t];
+        if (q.flags & 1) {
+            const int j = pair_j[base + t];
+            if (o.number < cap) S.nbr[(size_t)i * cap + o.number] = j;
+            o.number++;
+            o.idc = (S.id[j] < o.idc) ? S.id[j] : o.idc;
+            o.acc0 += q.acc0;
         }
-        if (o.number > cap) atomicOr(status, ST_CAND_OVERFLOW);
+        if (q.flags & 2) {
+            o.phi -= q.phi;
+            addto(o.acc, q.acc);
+            if (INITIAL) {
+                o.phi_d -= q.phi_d;
+                addto(o.acc_d, q.acc_d);
+                addto(o.jerk, q.jerk);
+            }
+        }
     }
+    if (o.number > cap) atomicOr(status, ST_CAND_OVERFLOW);
     // write back (FPGrav::copyFromForce then the corrections)
     st3(S.acc, i, v3((double)fr.acc[0], (double)fr.acc[1], (double)fr.acc[2]) + o.acc);
     S.phi[i] = (double)fr.phi + o.phi;
@@ -254,7 +316,7 @@ __global__ void __launch_bounds__(128, 4) k_correct(State S, Params P, const For
         atomicAdd(&counters[0], o.number);
         atomicAdd(&counters[1], 1);
     }
-    if (initial) {
+    if (INITIAL) {
         st3(S.acc_d_new, i, o.acc_d);
         S.phi_d[i] = o.phi_d;
         st3(S.jerk_d, i, o.jerk);
@@ -725,14 +787,30 @@ int Engine::correct(int initial) {
     if (r) return r;
     // the candidate table of a soft pass over this state must exist
     if (!c->res.cand.p || !c->res.force.p || c->res_n != S.n) return ST_BAD_INDEX;
-    if ((r = counters.reserve(4))) return r;
+    if ((r = counters.reserve(4)) || (r = pair_n.reserve(S.n)) || (r = pair_base.reserve(S.n))) return r;
     cudaMemsetAsync(counters.p, 0, 4 * sizeof(int32_t), c->stream);
+    const int cap = c->cand_cap;
+    const ForceRec *F = c->res.force.p;
+    const int32_t *cand = c->res.cand.p;
+    k_corr_list<false><<<nb(S.n, 128), 128, 0, c->stream>>>(S, F, cand, cap, pair_n.p, nullptr, nullptr, nullptr,
+                                                            c->status);
+    int32_t np = 0;
+    if ((r = scan(pair_n.p, pair_base.p, S.n, &np))) return r;
+    if ((r = pair_i.reserve(np)) || (r = pair_j.reserve(np)) || (r = pair_terms.reserve(np))) return r;
+    k_corr_list<true><<<nb(S.n, 128), 128, 0, c->stream>>>(S, F, cand, cap, nullptr, pair_base.p, pair_i.p,
+                                                           pair_j.p, c->status);
+    if (np > 0) {
+        if (initial)
+            k_corr_pairs<true><<<nb(np, 128), 128, 0, c->stream>>>(S, P, np, pair_i.p, pair_j.p, pair_terms.p);
+        else
+            k_corr_pairs<false><<<nb(np, 128), 128, 0, c->stream>>>(S, P, np, pair_i.p, pair_j.p, pair_terms.p);
+    }
     if (initial)
-        k_correct<true><<<nb(S.n, 128), 128, 0, c->stream>>>(S, P, c->res.force.p, c->res.cand.p, c->cand_cap,
-                                                             counters.p, c->status);
+        k_correct<true><<<nb(S.n, 128), 128, 0, c->stream>>>(S, P, F, cap, pair_base.p, pair_n.p, pair_j.p,
+                                                             pair_terms.p, counters.p, c->status);
     else
-        k_correct<false><<<nb(S.n, 128), 128, 0, c->stream>>>(S, P, c->res.force.p, c->res.cand.p, c->cand_cap,
-                                                              counters.p, c->status);
+        k_correct<false><<<nb(S.n, 128), 128, 0, c->stream>>>(S, P, F, cap, pair_base.p, pair_n.p, pair_j.p,
+                                                              pair_terms.p, counters.p, c->status);
     if (initial) k_copy3<<<nb(3 * S.n), 256, 0, c->stream>>>(S.acc_d, S.acc_d_new, S.n);
     return cuda_status(cudaGetLastError());
 }

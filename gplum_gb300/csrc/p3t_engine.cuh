@@ -16,6 +16,9 @@ struct Engine {
     DevBuf<int64_t> cmin;
     DevBuf<double> epart, et;
     DevBuf<int> icnt;
+    // correction pair list: per body its count and first slot; per pair (i, j) and terms
+    DevBuf<int32_t> pair_n, pair_base, pair_i, pair_j;
+    DevBuf<struct PairTerms> pair_terms;
     DevBuf<char> compact_tmp;
     // KOMINAMI fragments appended by the last hard part: particles
     // [frag_lo, frag_hi) with their clusters in frag_cl
