@@ -147,3 +147,9 @@ def disk_1m_embryos(n=1048576, seed=4, m=1e-10, m_embryo=3.0e-7, a_embryo=(0.7, 
     out["pos"] = np.ascontiguousarray(out["pos"])
     out["vel"] = np.ascontiguousarray(out["vel"])
     return out
+
+
+def disk_8m(n=8388608, seed=5):
+    """Large disk: n planetesimals of m = 1.25e-11 in 0.3-3 AU, rms e = 4 h,
+    rms i = 2 h."""
+    return make_disk(n, 1.25e-11, 0.3, 3.0, ecc_hill=4.0, inc_hill=2.0, seed=seed)

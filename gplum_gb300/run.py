@@ -128,6 +128,7 @@ def run(g, disk, steps, reset_step=1024, clock=None, out_dir=None, snap_every=0,
 
 WORKLOADS = {
     "disk3000": "3000-body disk, 0.95-1.05 AU, m=1e-9, rms e=2h, rms i=h, dt_tree=2^-7",
+    "disk8m": "8388608 planetesimals m=1.25e-11 in 0.3-3 AU, rms e=4h, rms i=2h, theta=0.5, n_group_limit=256",
     "embryos": "1048576 planetesimals m=1e-10 in 0.5-1.5 AU (rms e=6h, rms i=3h) + 4 embryos of 3e-7 "
                "at 0.7/0.9/1.1/1.3 AU, theta=0.5, n_group_limit=256",
 }
@@ -135,7 +136,7 @@ WORKLOADS = {
 
 def main():
     from . import autotune, scheduler
-    from .disk import P3TParams, disk_1m_embryos, disk_3000
+    from .disk import P3TParams, disk_1m_embryos, disk_3000, disk_8m
     from .p3t import GpuSystem
 
     ap = argparse.ArgumentParser()
@@ -147,6 +148,8 @@ def main():
     ap.add_argument("--a-frag", type=float, default=0.0,
                     help="KOMINAMI fragmentation a_frag (0: perfect accretion)")
     ap.add_argument("--timing", action="store_true", help="synchronised per-phase wall times")
+    ap.add_argument("--plain-fp64", action="store_true",
+                    help="the plain FP64 form: FP64 soft kernel, one cluster per thread/warp/CTA, size order")
     ap.add_argument("--output-dir", default=None, help="directory of the snapshot files")
     ap.add_argument("--snap-every", type=int, default=0, help="snapNNNNNN.dat (ASCII) every this many steps")
     ap.add_argument("--snap-tmp-every", type=int, default=0, help="snap_tmp.dat (binary) every this many steps")
@@ -154,12 +157,16 @@ def main():
     args = ap.parse_args()
     if args.workload == "disk3000":
         P, disk = P3TParams(), disk_3000()
+    elif args.workload == "disk8m":
+        P, disk = P3TParams(n_group_limit=256), disk_8m()
     else:
         P, disk = P3TParams(n_group_limit=256), disk_1m_embryos(args.n)
-    g = GpuSystem(P)
+    g = GpuSystem(P, precision=1 if args.plain_fp64 else 0)
     autotune.load(g.lib)
-    model = scheduler.load(lib=g.lib) if args.schedule == "learned" else None
+    model = scheduler.load(lib=g.lib) if args.schedule == "learned" and not args.plain_fp64 else None
     g.lib.p3t_set_schedule(1 if model is not None else 0)
+    if args.plain_fp64:
+        g.lib.p3t_set_hard_mode(1)
     if args.a_frag > 0:
         g.set_fragmentation(args.a_frag)
     clock = {} if args.timing else None
@@ -172,8 +179,13 @@ def main():
                    snap_tmp_every=args.snap_tmp_every, restart=args.restart)
     t = time.perf_counter() - t0
     pos = g.get("pos")
+    import torch
+
+    free, total = torch.cuda.mem_get_info()
     out = {"workload": WORKLOADS[args.workload], "steps": args.steps,
+           "form": "plain FP64" if args.plain_fp64 else "mixed + batched",
            "schedule": "learned cost model" if model is not None else "size",
+           "device_memory_gb": (total - free) / 1e9, "ms_per_step": 1e3 * t / max(1, args.steps),
            "a_frag": args.a_frag, "max_abs_dE_over_E": float(np.abs(de).max()) if len(de) else 0.0,
            "final_dE_over_E": float(de[-1]) if len(de) else 0.0,
            "collisions": ncol, "n_initial": len(disk["mass"]), "n_final": g.n, "wall_s": t,
