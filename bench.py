@@ -157,6 +157,13 @@ def p3t_step_measure(precision, steps=2, n=N_BODIES, hard_mode=0, learned=True, 
         tree_soft()
         g.correct(True)
     e0 = g.energy()
+    # warm-up of the hard path (first-use allocations, kernel loading: ~11 ms
+    # once) on a copy of the state, which is then restored
+    assert g.lib.p3t_state_snapshot(0) == 0
+    g.kick()
+    g.cluster()
+    g.hard(1)
+    assert g.lib.p3t_state_snapshot(1) == 0
     ph.clear()
     clusters = []
     ncol = 0
