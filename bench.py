@@ -32,7 +32,7 @@ EPSP_FLOPS = 70
 # DRAM bytes (read + write) of one pair-kernel launch on this workload, from the
 # ncu capture in profiles/soft_mixed_kernel_1m_disk.md (the bench itself cannot
 # read DRAM counters); refreshed with each capture
-SOFT_TRAFFIC_BYTES = 344.1e6
+SOFT_TRAFFIC_BYTES = 195.0e6
 
 
 def workload(seed=2):
@@ -44,8 +44,12 @@ def workload(seed=2):
     P = P3TParams(n_group_limit=256)
     d = disk_1m_soft(N_BODIES, seed=seed)
     r_out, r_search, _ = cutoff_radii(d["pos"], d["vel"], d["mass"], P)
-    epj = epj_records(d["pos"], d["vel"], d["mass"], r_out, r_search, ids=d["id"])
-    L = build_lists(d["pos"], d["mass"], r_search, P.theta, P.n_leaf_limit, P.n_group_limit)
+    # particles in the tree's (Morton) order, the order of the EPJ array FDPS
+    # hands to the force kernels
+    perm = build_lists(d["pos"], d["mass"], r_search, P.theta, P.n_leaf_limit, P.n_group_limit)["i_idx"]
+    pos, vel, mass, r_out, r_search = d["pos"][perm], d["vel"][perm], d["mass"][perm], r_out[perm], r_search[perm]
+    epj = epj_records(pos, vel, mass, r_out, r_search, ids=d["id"][perm])
+    L = build_lists(pos, mass, r_search, P.theta, P.n_leaf_limit, P.n_group_limit)
     return P, epj, L
 
 
@@ -58,6 +62,7 @@ def config(L, extra=None):
     c = {"workload": "P3T soft force, 1048576-body disk 0.5-1.5 AU, m=1e-10, theta=0.5, "
                      "n_group_limit=256, quadrupole SPJ",
          "n_bodies": N_BODIES, "n_groups": int(L["n_group"]), "theta": 0.5, "n_group_limit": 256,
+         "particle_order": "tree (Morton) order, as FDPS passes its EPJ array",
          "l2": "flushed between timed steps (256 MiB write)", "parallelism": "replicas"}
     if extra:
         c.update(extra)
