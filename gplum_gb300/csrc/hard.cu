@@ -1483,7 +1483,7 @@ int p3t_hard_integrate(int istep) {
             // persistent: g_bocc CTAs per SM (fewer when there are few clusters)
             const int blocks = std::max(1, std::min(sms * g_bocc, (nc + 3) / 4));
             if (g_bcap == 256)
-                k_hard_bundles<256, 2><<<blocks, BT, smem, c->stream>>>(A);
+                k_hard_bundles<256, 2><<<blocks, bundle_threads(256), smem, c->stream>>>(A);
             else if (g_bocc == 3)
                 k_hard_bundles<128, 3><<<blocks, BT, smem, c->stream>>>(A);
             else

@@ -20,7 +20,11 @@
 //   - collision detection over unordered member pairs, FP32 prefilter, FP64
 //     R for the survivors and a per-cluster lexicographic (R, pair) minimum.
 // Finished clusters leave the bundle and the queue refills it, so the CTA
-// stays full until the queue is empty.  Clusters larger than BCAP_MAIN run
+// stays full until the queue is empty.  The main 256-slot bundle runs one
+// thread per slot (bundle_threads: 8 warps, 2 CTAs per SM at 128 registers):
+// the member phases are long dependent FP64 chains, and twice the warps of a
+// 128-thread bundle keep the FP64 pipe busier (55 % vs 47 % of cycles,
+// 10-11 % less time at 1M bodies).  Clusters larger than BCAP_MAIN run
 // concurrently in k_hard_wide: alone in a wide bundle of BCAP_WIDE slots, or
 // beyond that in the one-cluster-per-CTA form (run_cluster<128>).
 //
@@ -46,11 +50,15 @@
 
 namespace p3t {
 
-constexpr int BT = 128;      // threads of a bundle (one CTA)
+constexpr int BT = 128;      // threads of a bundle (one CTA) unless bundle_threads says otherwise
 constexpr int BCAP_MAIN = 256;  // member slots of a bundle
 constexpr int BCAP_WIDE = 512;  // member slots of the wide form (clusters of 257..512 bodies, one at a time)
 // clusters in a bundle at once: half its member slots, at most one per thread
 __host__ __device__ constexpr int bmaxcl(int cap) { return cap / 2 < 128 ? cap / 2 : 128; }
+// threads of a bundle of `cap` member slots: one per slot for the main
+// 256-slot form (8 warps; twice the warps per SM of 128 at 2 CTAs per SM,
+// for the FP64 dependency chains), 128 for the others
+__host__ __device__ constexpr int bundle_threads(int cap) { return cap == 256 ? 256 : 128; }
 constexpr int BSURV = 64;    // colliding-pair candidates kept per block step
 constexpr int BCLAIM = 8;    // clusters claimed from the queue at a time
 
@@ -59,17 +67,18 @@ enum : unsigned char { MF_ACT = 1, MF_TGT = 2 };
 
 template <int BCAP>
 struct BundleSmem {
+    static constexpr int NT = bundle_threads(BCAP);  // threads of the bundle
     // member mirror (pool slot p)
     double pos[3 * BCAP], vel[3 * BCAP], xp[3 * BCAP], vp[3 * BCAP];
     double mass[BCAP], roi[BCAP], fr[BCAP];
     double acc[7 * BCAP];  // force accumulators of the running pair phase
-    double term[7 * BT];   // FP64 pair terms of one drain
+    double term[7 * NT];   // FP64 pair terms of one drain
     long long id[BCAP];
     float pos32[3 * BCAP], xp32[3 * BCAP], roi32[BCAP], fr32[BCAP];
     int gslot[BCAP];
     int pfx[BCAP + 1];
-    int ring[2 * BT];
-    int seg[BT + 1];
+    int ring[2 * NT];
+    int seg[NT + 1];
     short tgt[BCAP], cl[BCAP], owner[BCAP];
     unsigned char dead[BCAP], merged[BCAP], flag[BCAP];
     // clusters (bundle index k)
@@ -87,7 +96,7 @@ struct BundleSmem {
     int sv_k[BSURV];
     // claimed, not yet admitted clusters
     int pend_c[BCLAIM], pend_n[BCLAIM];
-    int ws[BT / 32];
+    int ws[NT / 32];
     int used, ncl, fresh_k, fresh_p, n_sv, n_pend, i_pend, exhausted, any, grew, phase;
 };
 
@@ -96,7 +105,8 @@ __device__ __forceinline__ unsigned long long dbits(double x) {
 }
 __device__ __forceinline__ double bitsd(unsigned long long b) { return __longlong_as_double((long long)b); }
 
-// exclusive block-wide prefix sum of v; all threads must call
+// exclusive block-wide prefix sum of v over NT threads; all threads must call
+template <int NT>
 __device__ __forceinline__ int bscan(int v, int *ws, int &total) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     int x = v;
@@ -109,7 +119,7 @@ __device__ __forceinline__ int bscan(int v, int *ws, int &total) {
     __syncthreads();
     int off = 0, tot = 0;
 #pragma unroll
-    for (int k = 0; k < BT / 32; k++) {
+    for (int k = 0; k < NT / 32; k++) {
         const int c = ws[k];
         off += (k < w) ? c : 0;
         tot += c;
@@ -160,6 +170,7 @@ __device__ __forceinline__ void mirror_all(BundleSmem<BCAP> &B, const Hard &H, i
 // ordered list of the occupied slots whose flag has `bit`
 template <int BCAP>
 __device__ int bundle_list(BundleSmem<BCAP> &B, unsigned char bit) {
+    constexpr int BT = BundleSmem<BCAP>::NT;
     constexpr int PER = BCAP / BT;
     const int base = threadIdx.x * PER;
     int c = 0;
@@ -169,7 +180,7 @@ __device__ int bundle_list(BundleSmem<BCAP> &B, unsigned char bit) {
         if (p < B.used && (B.flag[p] & bit)) c++;
     }
     int tot;
-    int off = bscan(c, B.ws, tot);
+    int off = bscan<BT>(c, B.ws, tot);
 #pragma unroll
     for (int j = 0; j < PER; j++) {
         const int p = base + j;
@@ -215,6 +226,7 @@ __device__ __forceinline__ void pair_terms(const Params &P, const BundleSmem<BCA
 // terms of ring[0..m), then in-order addition into the targets' accumulators
 template <int BCAP>
 __device__ void bundle_drain(const Params &P, BundleSmem<BCAP> &B, int mode, int m) {
+    constexpr int BT = BundleSmem<BCAP>::NT;
     const int q = threadIdx.x;
     int sq = -1;
     if (q < m) {
@@ -227,7 +239,7 @@ __device__ void bundle_drain(const Params &P, BundleSmem<BCAP> &B, int mode, int
     }
     const int head = (q < m) && (q == 0 || (B.ring[q - 1] >> 16) != sq);
     int nseg;
-    const int off = bscan(head, B.ws, nseg);
+    const int off = bscan<BT>(head, B.ws, nseg);
     if (head) B.seg[off] = q;
     if (q == 0) B.seg[nseg] = m;
     __syncthreads();
@@ -247,6 +259,7 @@ __device__ void bundle_drain(const Params &P, BundleSmem<BCAP> &B, int mode, int
 // predicted j -- for the nt targets in B.tgt
 template <int BCAP>
 __device__ void bundle_pairs(const HardArgs &A, BundleSmem<BCAP> &B, int mode, int nt) {
+    constexpr int BT = BundleSmem<BCAP>::NT;
     const int tid = threadIdx.x;
     constexpr int PER = BCAP / BT;
     for (int i = tid; i < nt; i += BT) {
@@ -262,7 +275,7 @@ __device__ void bundle_pairs(const HardArgs &A, BundleSmem<BCAP> &B, int mode, i
 #pragma unroll
         for (int j = 0; j < PER; j++)
             if (base + j < nt) c += B.c_n[B.cl[B.tgt[base + j]]];
-        int off = bscan(c, B.ws, total);
+        int off = bscan<BT>(c, B.ws, total);
 #pragma unroll
         for (int j = 0; j < PER; j++)
             if (base + j < nt) {
@@ -303,7 +316,7 @@ __device__ void bundle_pairs(const HardArgs &A, BundleSmem<BCAP> &B, int mode, i
             e = (s << 16) | t;
         }
         int cnt;
-        const int off = bscan(live, B.ws, cnt);
+        const int off = bscan<BT>(live, B.ws, cnt);
         if (live) B.ring[ring_n + off] = e;
         ring_n += cnt;
         __syncthreads();
@@ -323,6 +336,7 @@ __device__ void bundle_pairs(const HardArgs &A, BundleSmem<BCAP> &B, int mode, i
 // phase, merged alive targets; 2: all merged targets with twins)
 template <int BCAP>
 __device__ void bundle_finalize(const HardArgs &A, BundleSmem<BCAP> &B, int mode, int nt, int merge_sel) {
+    constexpr int BT = BundleSmem<BCAP>::NT;
     const Hard &H = A.H;
     for (int i = threadIdx.x; i < nt; i += BT) {
         const int s = B.tgt[i], g = B.gslot[s];
@@ -356,6 +370,7 @@ __device__ void bundle_finalize(const HardArgs &A, BundleSmem<BCAP> &B, int mode
 // takes b = a + d (mod n) for d = 1..n/2 (the pair at distance n/2 once)
 template <int BCAP>
 __device__ void bundle_detect(const HardArgs &A, BundleSmem<BCAP> &B, bool second) {
+    constexpr int BT = BundleSmem<BCAP>::NT;
     for (int p = threadIdx.x; p < B.used; p += BT) {
         if (B.dead[p]) continue;
         const int k = B.cl[p];
@@ -487,6 +502,7 @@ __device__ void bundle_refill(const HardArgs &A, BundleSmem<BCAP> &B) {
 // load the fresh clusters (bundle indices fresh_k..ncl-1, slots fresh_p..used-1)
 template <int BCAP>
 __device__ void bundle_load(const HardArgs &A, BundleSmem<BCAP> &B) {
+    constexpr int BT = BundleSmem<BCAP>::NT;
     const Hard &H = A.H;
     const int tid = threadIdx.x;
     const int k0 = B.fresh_k, k1 = B.ncl, p0 = B.fresh_p, p1 = B.used;
@@ -577,13 +593,14 @@ __device__ void bundle_load(const HardArgs &A, BundleSmem<BCAP> &B) {
 // state of record (fragments are rare; owners are remapped).
 template <int BCAP>
 __device__ void bundle_grow(const HardArgs &A, BundleSmem<BCAP> &B) {
+    constexpr int BT = BundleSmem<BCAP>::NT;
     const Hard &H = A.H;
     const int tid = threadIdx.x;
     static_assert(bmaxcl(BCAP) <= BT, "one thread per bundle cluster");
     const int add = (tid < B.ncl) ? B.c_addn[tid] : 0;
     const int nn = (tid < B.ncl) ? B.c_n[tid] + add : 0;
     int tot;
-    const int noff = bscan(nn, B.ws, tot);
+    const int noff = bscan<BT>(nn, B.ws, tot);
     constexpr int PER = BCAP / BT;
     int mv_new[PER], mv_g[PER], mv_k[PER], mv_own[PER];
     int my_old_n = 0, my_addg = 0;
@@ -640,6 +657,7 @@ __device__ void bundle_grow(const HardArgs &A, BundleSmem<BCAP> &B) {
 // src/hermite.h:224-479)
 template <int BCAP>
 __device__ void bundle_step(const HardArgs &A, BundleSmem<BCAP> &B) {
+    constexpr int BT = BundleSmem<BCAP>::NT;
     const Params &P = A.P;
     const Hard &H = A.H;
     // makeActiveList: ts = min over alive members of th + dt
@@ -831,6 +849,7 @@ __device__ void bundle_step(const HardArgs &A, BundleSmem<BCAP> &B) {
 // final forces, write-back and removal of the finished clusters
 template <int BCAP>
 __device__ void bundle_retire(const HardArgs &A, BundleSmem<BCAP> &B) {
+    constexpr int BT = BundleSmem<BCAP>::NT;
     const Hard &H = A.H;
     const int tid = threadIdx.x;
     FOR_SLOTS(p) B.flag[p] = (B.c_flags[B.cl[p]] & CF_FIN) ? MF_TGT : 0;
@@ -889,8 +908,8 @@ __device__ void bundle_retire(const HardArgs &A, BundleSmem<BCAP> &B) {
         t_label = B.c_label[tid]; t_fragn = B.c_fragn[tid]; t_n0 = B.c_n0[tid];
     }
     static_assert(bmaxcl(BCAP) <= BT, "one thread per bundle cluster");
-    nk = bscan(keep, B.ws, nkeep);
-    noff = bscan(keep ? t_n : 0, B.ws, tot);
+    nk = bscan<BT>(keep, B.ws, nkeep);
+    noff = bscan<BT>(keep ? t_n : 0, B.ws, tot);
     // slots: read the old placement before anything moves
     constexpr int PER = BCAP / BT;
     int mv_new[PER], mv_g[PER], mv_k[PER], mv_own[PER];
@@ -1002,22 +1021,23 @@ __global__ void __launch_bounds__(BT, 1) k_hard_wide(HardArgs A) {
 // one CTA: (without k_hard_wide) the clusters above BCAP one at a time, then
 // bundles of BCAP member slots until the queue is empty; OCC CTAs per SM
 template <int BCAP, int OCC>
-__global__ void __launch_bounds__(BT, OCC) k_hard_bundles(HardArgs A) {
+__global__ void __launch_bounds__(bundle_threads(BCAP), OCC) k_hard_bundles(HardArgs A) {
+    constexpr int BT = BundleSmem<BCAP>::NT;
     extern __shared__ __align__(16) unsigned char bundle_smem[];
     BundleSmem<BCAP> &B = *reinterpret_cast<BundleSmem<BCAP> *>(bundle_smem);
-    __shared__ double red_d[4];
-    __shared__ long long red_l[4];
+    __shared__ double red_d[BT / 32];
+    __shared__ long long red_l[BT / 32];
     __shared__ int q_sh;
     const int tid = threadIdx.x;
     if (!A.wide) {
-        Team<128> tm{tid, red_d, red_l};
+        Team<BT> tm{tid, red_d, red_l};
         for (int guard = 0; guard < (1 << 30); guard++) {
             if (tid == 0) q_sh = atomicAdd(&A.queue[0], 1);
             __syncthreads();
             const int q = q_sh;
             __syncthreads();
             if (q >= A.n_tier[0]) break;
-            run_cluster<128>(A, A.order[q], tm);
+            run_cluster<BT>(A, A.order[q], tm);
         }
     }
     if (tid == 0) {
