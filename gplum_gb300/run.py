@@ -36,11 +36,12 @@ def startup(g, disk):
     return g.energy()
 
 
-def step(g, istep, reset_step=1024, r_max=40.0, r_min=0.1, clock=None):
+def step(g, istep, reset_step=1024, r_max=40.0, r_min=0.1, clock=None, stats=None):
     """One tree step (src/main_p3t.cpp:423-717; r_max and r_min as in
     parameter.dat, defaults src/read.h:111-112).  Returns (collision pairs,
     energy after the step, energy dissipated in this step).  With `clock` a
-    dict, adds the synchronised wall time of each phase to it."""
+    dict, adds the synchronised wall time of each phase to it; with `stats` a
+    list, appends the step's cluster counts after the hard part."""
 
     def timed(name, fn):
         if clock is None:
@@ -55,6 +56,8 @@ def step(g, istep, reset_step=1024, r_max=40.0, r_min=0.1, clock=None):
     timed("kick", g.kick)
     timed("cluster", g.cluster)
     cols, ed = timed("hard", lambda: g.hard(istep))
+    if stats is not None:
+        stats.append(dict(step=istep, **cluster_stats(g)))
     edisp = float(ed[0])
     timed("tree_soft", g.tree_soft)
     timed("correct", lambda: g.correct(False))
@@ -72,8 +75,32 @@ def step(g, istep, reset_step=1024, r_max=40.0, r_min=0.1, clock=None):
     return cols, e, edisp
 
 
+def cluster_stats(g):
+    """The hard system's counts as GPLUM logs them at snapshot steps
+    (src/main_p3t.cpp:543-547): clusters, isolated bodies, the largest
+    cluster -- and, beside it, the value GPLUM's
+    getNumberOfParticleInLargestClusterLocal returns (src/hard.h:143-149): its
+    test compares with the cluster count instead of the running maximum, so
+    it reports the size of the last cluster of its list, the one with the
+    largest id_cluster (makeList orders clusters by id_cluster,
+    src/hard.h:321-438)."""
+    off, mem = g.cluster_lists()
+    return cluster_counts(g.n, np.diff(off), g.get("id_cluster")[mem[off[:-1]]])
+
+
+def cluster_counts(n, sizes, cids):
+    """cluster_stats from the bodies' count n and each cluster's size and
+    id_cluster."""
+    sizes = np.asarray(sizes)
+    out = {"n_cluster": int(len(sizes)), "n_isolated": int(n - sizes.sum()),
+           "largest_cluster": int(sizes.max()) if len(sizes) else 0, "largest_cluster_as_gplum_logs": 0}
+    if len(sizes):
+        out["largest_cluster_as_gplum_logs"] = int(sizes[int(np.argmax(cids))])
+    return out
+
+
 def run(g, disk, steps, reset_step=1024, clock=None, out_dir=None, snap_every=0, snap_tmp_every=0,
-        restart=False):
+        restart=False, stats=None):
     """Start-up (or a restart from out_dir/snap_tmp.dat) and tree steps up to
     `steps`; returns the energy-error trace and the collision count.  With
     out_dir: snapNNNNNN.dat (ASCII) every snap_every steps and the binary
@@ -81,7 +108,8 @@ def run(g, disk, steps, reset_step=1024, clock=None, out_dir=None, snap_every=0,
     outputStep / makeSnapTmp (src/main_p3t.cpp:738-764), and each step's
     collisions appended to collisionNNNNNN.dat (src/main_p3t.cpp:390-396,
     751-758); the ASCII files are written by a host thread while the next
-    steps run."""
+    steps run.  With `stats` a list, the cluster counts of every snapshot
+    step (cluster_stats) are appended to it."""
     import os
 
     from . import _lib
@@ -108,7 +136,8 @@ def run(g, disk, steps, reset_step=1024, clock=None, out_dir=None, snap_every=0,
     if out_dir and snap_every and not restart:
         g.write_snapshot(os.path.join(out_dir, "snap%06d.dat" % 0), 0, header(0, e0), async_write=True)
     for istep in range(istep0 + 1, steps + 1):
-        cols, e, ed = step(g, istep, reset_step, clock=clock)
+        at_snap = snap_every and istep % snap_every == 0
+        cols, e, ed = step(g, istep, reset_step, clock=clock, stats=stats if at_snap else None)
         edisp += ed
         ncol += len(cols)
         if out_dir and snap_every and len(cols):
@@ -175,8 +204,9 @@ def main():
         import os
 
         os.makedirs(args.output_dir, exist_ok=True)
+    stats = []
     de, ncol = run(g, disk, args.steps, clock=clock, out_dir=args.output_dir, snap_every=args.snap_every,
-                   snap_tmp_every=args.snap_tmp_every, restart=args.restart)
+                   snap_tmp_every=args.snap_tmp_every, restart=args.restart, stats=stats)
     t = time.perf_counter() - t0
     pos = g.get("pos")
     import torch
@@ -191,6 +221,8 @@ def main():
            "collisions": ncol, "n_initial": len(disk["mass"]), "n_final": g.n, "wall_s": t,
            # identical for every schedule: the queue order never changes the arithmetic
            "final_state_checksum": float(np.sum(pos * np.arange(1, 4))) + float(np.sum(g.get("id")))}
+    if stats:
+        out["clusters_at_snapshots"] = stats
     if clock is not None:
         out["phases_s"] = clock
     print(json.dumps(out))

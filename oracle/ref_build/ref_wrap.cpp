@@ -466,6 +466,8 @@ void ref_col_edisp(int k, double *out) {
 }
 int ref_n_cluster() { return g_hard.getNumberOfClusterLocal(); }
 int ref_n_isolated() { return g_hard.getNumberOfIsolatedParticleLocal(); }
+// the figure GPLUM logs as the largest cluster (src/hard.h:143-149, as written)
+int ref_largest_cluster() { return g_hard.getNumberOfParticleInLargestClusterLocal(); }
 
 // energy (src/energy.h:29-63): out = {etot, ekin, ephi_sun, ephi, ephi_d}
 void ref_energy(double *out) {

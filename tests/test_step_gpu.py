@@ -77,6 +77,11 @@ def test_correction_neighbours_and_clusters(gpu, seed, ecc):
     assert sorted(got) == sorted(want.values())
     assert all(c == sorted(c) for c in got)
     assert [c[0] for c in got] == sorted(c[0] for c in got)
+    # the counts GPLUM logs at snapshot steps, from the device lists
+    from gplum_gb300.run import cluster_counts, cluster_stats
+
+    ids, sizes = np.unique(cid[num > 0], return_counts=True)
+    assert cluster_stats(g) == cluster_counts(g.n, sizes, ids)
 
 
 def test_hard_step_from_identical_states(gpu):
