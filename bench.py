@@ -217,7 +217,8 @@ def p3t_step_measure(precision, steps=2, n=N_BODIES, hard_mode=0, learned=True, 
 def cpu_step_baseline(n=N_BODIES, steps=1):
     """The same whole tree step run by GPLUM's arithmetic on the host cores
     (the oracle port, OpenMP over clusters and bodies as GPLUM's loops are),
-    with the same host tree; start-up not timed."""
+    with the same host tree; start-up not timed.  Returns (seconds per step,
+    ms per step by GPLUM's CALC_WTIME phase)."""
     from gplum_gb300.disk import P3TParams, disk_1m_hard
     from oracle import harness as H
 
@@ -225,10 +226,11 @@ def cpu_step_baseline(n=N_BODIES, steps=1):
     s = H.CpuSystem("orc", P)
     lf = H.tree_lists_fn(P)
     H.p3t_init(s, disk_1m_hard(n), lf)
+    clock = {}
     t0 = time.perf_counter()
     for istep in range(1, steps + 1):
-        H.p3t_step(s, istep, lf)
-    return (time.perf_counter() - t0) / steps
+        H.p3t_step(s, istep, lf, clock=clock)
+    return (time.perf_counter() - t0) / steps, {k: 1e3 * v / steps for k, v in clock.items()}
 
 
 def cpu_reference(L, epj, P, budget_s=20.0, threads=None):
@@ -432,9 +434,10 @@ def gpu_arm(args, rank, world):
                                "mixed_batched": mixed, "plain_fp64": plain,
                                "device_speedup": plain["device_ms_per_step"] / mixed["device_ms_per_step"],
                                "hard_speedup": plain["phases_ms"]["hard"] / mixed["phases_ms"]["hard"]}
-            cpu_s = cpu_step_baseline()
+            cpu_s, cpu_phases = cpu_step_baseline()
             out["p3t_step"]["cpu_baseline"] = {"value": 1.0 / cpu_s, "unit": "steps/s", "cores": os.cpu_count(),
-                                               "kind": "port", "sample": "1 tree step, same disk and host tree"}
+                                               "kind": "port", "sample": "1 tree step, same disk and host tree",
+                                               "phases_ms": cpu_phases}
         except Exception as e:
             out["p3t_step"] = {"error": repr(e)}
     try:

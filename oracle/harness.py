@@ -203,30 +203,42 @@ def p3t_init(sysm, disk, lists_fn):
     return sysm.energy()
 
 
-def p3t_step(sysm, istep, lists_fn, reset_step=1024):
+def p3t_step(sysm, istep, lists_fn, reset_step=1024, clock=None):
     """One tree step (src/main_p3t.cpp:423-717) on a single rank: kick,
     clusters, hard part, soft force + correction, kick, energy, merge,
-    re-force after collisions.  Returns a dict of what the step produced."""
-    sysm.kick()
-    sysm.cluster()
-    n_cluster = sysm.f("n_cluster")
-    cols, edisp = sysm.hard(istep)
+    re-force after collisions.  Returns a dict of what the step produced.
+    With `clock` a dict, adds each phase's wall time (seconds) under GPLUM's
+    CALC_WTIME names (src/time.h, src/main_p3t.cpp:437-710): calc_soft_force
+    (kicks, tree + lists, soft force, energy, merge, radii),
+    create_cluster, calc_hard_force, neighbor_search (correction)."""
+    import time
+
+    def timed(name, fn, *a):
+        t0 = time.perf_counter()
+        r = fn(*a)
+        if clock is not None:
+            clock[name] = clock.get(name, 0.0) + time.perf_counter() - t0
+        return r
+
+    timed("calc_soft_force", sysm.kick)
+    timed("create_cluster", sysm.cluster)
+    cols, edisp = timed("calc_hard_force", sysm.hard, istep)
     n_clusters = sysm.f("n_cluster")()
     n_iso = sysm.f("n_isolated")()
     sysm.f("set_id_local")()
-    sysm.soft_force(lists_fn(sysm))
-    sysm.correct(False)
-    sysm.kick()
-    e = sysm.energy()
+    timed("calc_soft_force", lambda: sysm.soft_force(lists_fn(sysm)))
+    timed("neighbor_search", sysm.correct, False)
+    timed("calc_soft_force", sysm.kick)
+    e = timed("calc_soft_force", sysm.energy)
     out = dict(cols=cols, edisp=edisp, n_clusters=n_clusters, n_iso=n_iso, energy=e)
     n_col = len(cols)
     if n_col:
-        out["edisp_merge"] = sysm.merge(n_col)
+        out["edisp_merge"] = timed("calc_soft_force", sysm.merge, n_col)
     if n_col or istep % reset_step == reset_step - 1:
-        sysm.prepare()
-        sysm.soft_force(lists_fn(sysm))
-        sysm.correct(True)
-        out["energy"] = sysm.energy()
+        timed("calc_soft_force", sysm.prepare)
+        timed("calc_soft_force", lambda: sysm.soft_force(lists_fn(sysm)))
+        timed("neighbor_search", sysm.correct, True)
+        out["energy"] = timed("calc_soft_force", sysm.energy)
     return out
 
 
