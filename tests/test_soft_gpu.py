@@ -138,6 +138,58 @@ def test_functor_calls_accumulate_into_records(gpu):
         np.testing.assert_allclose(a["acc"], b["acc"], rtol=0, atol=1e-5 * np.abs(b["acc"]).max())
 
 
+def _ragged(L, drop_j, drop_s):
+    """L with the EPJ lists of the groups in drop_j and the SPJ lists of those
+    in drop_s emptied."""
+    out = {"n_group": L["n_group"], "spj": L["spj"], "i_off": L["i_off"], "i_idx": L["i_idx"]}
+    for k, idx, drop in (("j", "j_idx", drop_j), ("s", "s_idx", drop_s)):
+        off = L[k + "_off"]
+        parts = [L[idx][off[g]:off[g + 1]] if g not in drop else L[idx][:0] for g in range(L["n_group"])]
+        out[k + "_off"] = np.concatenate([[0], np.cumsum([len(x) for x in parts])]).astype(np.int32)
+        out[idx] = np.concatenate(parts).astype(np.int32)
+    return out
+
+
+def test_empty_and_ragged_inputs(gpu):
+    """Zero-length inputs through every entry point: functor calls with no
+    j-particles or no superparticles leave the records as they were; an empty
+    system through the host call; groups whose EPJ or SPJ lists are empty
+    (resident run and host call) against the oracle on the same lists."""
+    P, d, s = prepared_state(n=2000, seed=13, ecc_hill=4.0, inc_hill=2.0)
+    soft.configure(P)
+    epi, epj = records(s)
+    L = lists_for(s, P)
+    ii = L["i_idx"][L["i_off"][0]:L["i_off"][1]]
+    ei = np.ascontiguousarray(epi[ii])
+    start = cleared_forces(len(ii))
+    start["acc"] = np.random.default_rng(1).normal(0, 1e-4, (len(ii), 3))
+    start["number"] = 2
+    start["id_min"] = 7
+    a = start.copy()
+    soft.calc_force_epep(ei, epj[:0], a)
+    soft.calc_force_epsp(ei, L["spj"][:0], a)
+    assert a.tobytes() == start.tobytes()
+    empty = {"n_group": 0, "spj": L["spj"][:0]}
+    for k in ("i", "j", "s"):
+        empty[k + "_off"] = np.zeros(1, np.int32)
+        empty[k + "_idx"] = np.zeros(0, np.int32)
+    assert len(soft.soft_force_host(P, epj[:0], empty)) == 0
+    ng = L["n_group"]
+    # disjoint: every group keeps one of its lists (a body with neither has phi = 0)
+    R = _ragged(L, {g for g in range(ng) if g % 5 == 1}, {g for g in range(ng) if g % 3 == 0 and g % 5 != 1})
+    assert (np.diff(R["j_off"]) == 0).any() and (np.diff(R["s_off"]) == 0).any()
+    sf = soft.SoftForce(P, precision=0)
+    sf.upload_particles(epj)
+    sf.upload_lists(R)
+    sf.run()
+    got = sf.download()
+    assert soft.soft_force_host(P, epj, R).tobytes() == got.tobytes()
+    ref32 = oracle_lists(0, R, epi, epj)
+    a64, _ = oracle_lists(1, R, epi, epj)
+    check_neighbours(got, ref32)
+    check_mixed_accuracy(got, ref32, a64)
+
+
 def test_multiwalk_forms_equal_resident(gpu):
     P, d, s = prepared_state(n=5000, seed=9, ecc_hill=4.0, inc_hill=2.0, params=P3TParams(n_group_limit=128))
     soft.configure(P)

@@ -206,3 +206,24 @@ def test_out_of_boundary_removal(gpu):
     np.testing.assert_array_equal(g.get("id"), orc.get("id"))
     np.testing.assert_array_equal(g.get("pos"), orc.get("pos"))
     assert g.n == orc.n == 3000 - n1
+
+
+def test_no_clusters(gpu):
+    """A sparse system in which no body has a neighbour: no clusters, an empty
+    hard queue, every body on the Kepler drift; three steps against the
+    oracle."""
+    P = P3TParams()
+    d = make_disk(200, 1e-12, 0.5, 1.5, ecc_hill=2.0, inc_hill=1.0, seed=27)
+    orc, g, lf = both(d, P)
+    H.p3t_init(orc, d, lf)
+    H.p3t_init(g, d, lf)
+    assert orc.get("number").max() == 0
+    for istep in (1, 2, 3):
+        a = H.p3t_step(orc, istep, lf)
+        b = H.p3t_step(g, istep, lf)
+        assert a["n_clusters"] == b["n_clusters"] == 0
+        assert len(a["cols"]) == len(b["cols"]) == 0
+        assert rel_err(g.get("pos"), orc.get("pos")).max() < 1e-12
+        np.testing.assert_array_equal(g.get("number"), orc.get("number"))
+    off, _ = g.cluster_lists()
+    assert len(off) == 1
