@@ -19,7 +19,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libp3t_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libgplum_ref.so")
 REF_KOM_SO = os.path.join(HERE, "_ref", "libgplum_ref_kominami.so")
-REF_SRC = "/root/reference/src"
+# GPLUM's src/ directory, for the reference build (from the environment; the
+# build recipe in __graft_entry__.py sets it where the reference tree exists)
+REF_SRC = os.environ.get("GPLUM_REF_SRC", "")
 
 F64P = ctypes.POINTER(ctypes.c_double)
 I32P = ctypes.POINTER(ctypes.c_int)
@@ -38,10 +40,11 @@ def build_oracle(with_ref=None):
     """Compiles the restatement (always) and the reference build (when the
     reference tree exists).  Quick: two translation units."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+    ref_src = os.environ.get("GPLUM_REF_SRC", REF_SRC)
     if with_ref is None:
-        with_ref = os.path.isdir(REF_SRC)
+        with_ref = bool(ref_src) and os.path.isdir(ref_src)
     if with_ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_SRC={REF_SRC}"], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_SRC={ref_src}"], check=True)
 
 
 def ref_available():

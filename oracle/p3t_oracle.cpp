@@ -19,6 +19,7 @@
 #include <numeric>
 #include <vector>
 
+#include "ngb_grid.h"
 #include "p3t_oracle.h"
 
 namespace {
@@ -991,49 +992,22 @@ double eccentricity(const Ptcl &p) {  // FPGrav::getEccentricity, src/particle.h
 }
 
 // --- correction + neighbour search, src/gravity_soft.h:75-528 -------------
+// Candidates of the correction: every j with |x_j - x_i| < max(1.1 r_search_i,
+// 1.1 r_search_j) (getRSearch, src/particle.h:119-125), ascending index.
 struct Grid {
-    double h = 1., x0[3] = {0, 0, 0};
-    int nc[3] = {1, 1, 1};
-    double rs_max = 0.;
-    std::vector<std::vector<int>> cells;
-    int coord(double x, int d) const {
-        int c = (int)((x - x0[d]) / h);
-        return std::max(0, std::min(nc[d] - 1, c));
-    }
+    NgbGrid g;
     void build() {
-        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-        rs_max = 0.;
-        for (const Ptcl &p : S) {
-            rs_max = std::max(rs_max, 1.1 * p.r_search);
-            const double x[3] = {p.pos.x, p.pos.y, p.pos.z};
-            for (int d = 0; d < 3; d++) { lo[d] = std::min(lo[d], x[d]); hi[d] = std::max(hi[d], x[d]); }
-        }
-        h = std::max(rs_max, 1e-12);
-        for (int d = 0; d < 3; d++) {
-            x0[d] = lo[d];
-            nc[d] = std::max(1, std::min(1024, (int)((hi[d] - lo[d]) / h) + 1));
-        }
-        cells.assign((size_t)nc[0] * nc[1] * nc[2], {});
-        for (int i = 0; i < (int)S.size(); i++) {
-            const Ptcl &p = S[i];
-            cells[((size_t)coord(p.pos.z, 2) * nc[1] + coord(p.pos.y, 1)) * nc[0] + coord(p.pos.x, 0)].push_back(i);
-        }
+        g.build((int)S.size(), [](int i, double &x, double &y, double &z) {
+            x = S[i].pos.x; y = S[i].pos.y; z = S[i].pos.z;
+        }, [](int i) { return 1.1 * S[i].r_search; });
     }
     void query(int i, std::vector<int> &out) const {
-        out.clear();
         const Ptcl &p = S[i];
-        const double x[3] = {p.pos.x, p.pos.y, p.pos.z};
-        const double rq = std::max(1.1 * p.r_search, rs_max);
-        int lo[3], hi[3];
-        for (int d = 0; d < 3; d++) { lo[d] = coord(x[d] - rq, d); hi[d] = coord(x[d] + rq, d); }
-        for (int cz = lo[2]; cz <= hi[2]; cz++)
-            for (int cy = lo[1]; cy <= hi[1]; cy++)
-                for (int cx = lo[0]; cx <= hi[0]; cx++)
-                    for (int j : cells[((size_t)cz * nc[1] + cy) * nc[0] + cx]) {
-                        const V3 d = S[j].pos - p.pos;
-                        const double r = std::max(1.1 * p.r_search, 1.1 * S[j].r_search);
-                        if (dot(d, d) < r * r) out.push_back(j);
-                    }
+        g.query(i, out, [&](int j) {
+            const V3 d = S[j].pos - p.pos;
+            const double r = std::max(1.1 * p.r_search, 1.1 * S[j].r_search);
+            return dot(d, d) < r * r;
+        });
     }
 };
 

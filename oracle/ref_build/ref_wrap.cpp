@@ -25,6 +25,7 @@
 #define PIKG_USE_FDPS_VECTOR
 
 #include <particle_simulator.hpp>
+#include "../ngb_grid.h"
 
 constexpr PS::F64 MY_PI = 3.14159265358979323846L;
 constexpr PS::F64 L_MKS = 149597870700;
@@ -89,63 +90,42 @@ struct RefSystem {
 
 // Neighbour query over the current particle set: every EPJ whose distance to
 // the query particle is below max(getRSearch_i, getRSearch_j) (the symmetric
-// LONG_SYMMETRY rule).  A uniform grid keeps it near O(1) per query.
+// LONG_SYMMETRY rule), in ascending particle index (oracle/ngb_grid.h).
 struct RefNgbTree {
     std::vector<EPJ_t> epj;
-    std::vector<std::vector<PS::S32>> cells;
-    PS::F64 h = 1., xmin[3] = {0, 0, 0};
-    PS::S32 nc[3] = {1, 1, 1};
-    PS::F64 rs_max = 0.;
+    NgbGrid grid;
+    std::vector<int> cand;
     std::vector<std::vector<EPJ_t>> out;
 
     void build(RefSystem<FP_t> &pp) {
         const PS::S32 n = pp.getNumberOfParticleLocal();
         epj.resize(n);
-        rs_max = 0.;
-        PS::F64 lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-        for (PS::S32 i = 0; i < n; i++) {
-            epj[i].copyFromFP(pp[i]);
-            rs_max = std::max(rs_max, epj[i].getRSearch());
-            for (int d = 0; d < 3; d++) {
-                lo[d] = std::min(lo[d], epj[i].pos[d]);
-                hi[d] = std::max(hi[d], epj[i].pos[d]);
-            }
-        }
-        h = std::max(rs_max, 1e-12);
-        for (int d = 0; d < 3; d++) {
-            xmin[d] = lo[d];
-            nc[d] = std::max(1, std::min(1024, (PS::S32)((hi[d] - lo[d]) / h) + 1));
-        }
-        cells.assign((size_t)nc[0] * nc[1] * nc[2], {});
-        for (PS::S32 i = 0; i < n; i++) cells[cellOf(epj[i].pos)].push_back(i);
+        for (PS::S32 i = 0; i < n; i++) epj[i].copyFromFP(pp[i]);
+        grid.build(n, [&](int i, double &x, double &y, double &z) {
+            x = epj[i].pos.x; y = epj[i].pos.y; z = epj[i].pos.z;
+        }, [&](int i) { return (double)epj[i].getRSearch(); });
         out.assign(1, {});
-    }
-    PS::S32 coord(PS::F64 x, int d) const {
-        PS::S32 c = (PS::S32)((x - xmin[d]) / h);
-        return std::max(0, std::min(nc[d] - 1, c));
-    }
-    size_t cellOf(const PS::F64vec &p) const {
-        return ((size_t)coord(p.z, 2) * nc[1] + coord(p.y, 1)) * nc[0] + coord(p.x, 0);
     }
     template <class Tp>
     PS::S32 getNeighborListOneParticle(const Tp &p, EPJ_t *&next) {
         std::vector<EPJ_t> &o = out[0];
         o.clear();
-        PS::F64 rq = std::max(p.getRSearch(), rs_max);
-        PS::S32 lo[3], hi[3];
-        for (int d = 0; d < 3; d++) {
-            lo[d] = coord(p.pos[d] - rq, d);
-            hi[d] = coord(p.pos[d] + rq, d);
+        // the query particle is one of the particles the tree was built on
+        // (setIDLocalAndMyrank ran before the correction); found by position
+        // otherwise
+        int i = (int)p.id_local;
+        if (i < 0 || i >= (int)epj.size() || !(epj[i].pos == p.pos)) {
+            i = -1;
+            for (int k = 0; k < (int)epj.size() && i < 0; k++)
+                if (epj[k].pos == p.pos && epj[k].id == p.id) i = k;
+            if (i < 0) PS::Abort(-1);
         }
-        for (PS::S32 cz = lo[2]; cz <= hi[2]; cz++)
-            for (PS::S32 cy = lo[1]; cy <= hi[1]; cy++)
-                for (PS::S32 cx = lo[0]; cx <= hi[0]; cx++) {
-                    for (PS::S32 j : cells[((size_t)cz * nc[1] + cy) * nc[0] + cx]) {
-                        PS::F64vec d = epj[j].pos - p.pos;
-                        PS::F64 r = std::max(p.getRSearch(), epj[j].getRSearch());
-                        if (d * d < r * r) o.push_back(epj[j]);
-                    }
-                }
+        grid.query(i, cand, [&](int j) {
+            PS::F64vec d = epj[j].pos - p.pos;
+            PS::F64 r = std::max(p.getRSearch(), epj[j].getRSearch());
+            return d * d < r * r;
+        });
+        for (int j : cand) o.push_back(epj[j]);
         next = o.data();
         return (PS::S32)o.size();
     }
