@@ -1,15 +1,36 @@
-"""P3T soft-force step on one GB300: GPLUM's EP-EP + EP-SP interaction pass
-over a 1,048,576-body disk (0.5-1.5 AU, m = 1e-10, theta = 0.5,
-n_group_limit = 256, quadrupole superparticles).
+"""Whole P3T tree steps per second on one GB300: GPLUM's main loop
+(src/main_p3t.cpp:423-717) on a 1,048,576-body disk, the mixed-precision
+batched form against the plain-FP64 form, in one run.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--no-extras]
 
-One step = the fused EP-EP + EP-SP kernel over every i-group of the tree's
-interaction lists (forces, potentials, neighbour counts and the neighbour
-candidates the correction pass reads), inputs resident in HBM.  Prints one
-JSON line.  `--impl reference` times GPLUM's functor arithmetic on the host
-cores instead (the CPU restatement in oracle/, pinned bit-for-bit to GPLUM's
-own code) on a bounded sample of the same groups.
+Workload: the batched-hard-part disk (1,048,576 bodies, 0.95-1.05 AU,
+m = 7e-11, rms e = 6 h, rms i = 3 h, theta 0.5, n_group_limit 256,
+dt_tree 2^-7, perfect accretion): ~115,700 neighbour clusters of 2 to ~260
+bodies per step.  One step = one p3t_tree_step call: kick, cluster labels
+and lists, the hard part (every cluster in one persistent launch, learned
+queue order, Kepler drift of the isolated bodies), device octree +
+interaction lists + soft force, FP64 cutoff correction and neighbour search,
+kick, energy, merge, out-of-boundary removal and the re-force pass after
+collisions.  State resident in HBM (0.34 GB, larger than L2); each step is
+timed by CUDA events on the library stream.
+
+Printed JSON line: `value` = mixed + batched steps/s; `fp64_form` = the
+plain-FP64 form (FP64 soft kernel, one cluster per thread/warp/CTA, size
+order) over the same number of steps from the same initial state;
+`roofline` = the hard launch (the dominant kernel) against the FP64 FMA peak
+of this GPU; `accuracy` = per-body relative soft-force error against the
+FP64 restatement on the step's own interaction lists, GPLUM's FP32 functor
+beside it, and |dE/E| over the timed steps; `e2e` = the same steps through
+the C ABI with GPLUM's FPGrav records in pinned host memory (copied in and
+out every step); `cpu_baseline` = the CPU restatement of GPLUM's step (the
+oracle) on the host cores.  Extras (one GPU only, skipped by --no-extras):
+the soft pass alone on the 1M soft-force disk, the 1000-step embryo run with
+fragmentation (learned vs size queue order) and the 8M-body large disk.
+
+`--impl reference` times GPLUM's step arithmetic on the host cores (the CPU
+restatement in oracle/, pinned bit for bit to GPLUM's own headers) on the
+same disk.
 """
 import argparse
 import ctypes
@@ -26,47 +47,21 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 N_BODIES = 1048576
-METRIC = "P3T steps/s, N=1M: mixed+batched vs plain FP64 on GB300 @ rel force err\u22641e-6"
-EPEP_FLOPS = 32  # per pair, FMA = 2, rsqrt/min/max/compare = 1
-EPSP_FLOPS = 70
-# DRAM bytes (read + write) of one pair-kernel launch on this workload, from the
-# ncu capture in profiles/soft_mixed_kernel_1m_disk.md (the bench itself cannot
-# read DRAM counters); refreshed with each capture
+METRIC = "P3T steps/s, N=1M: mixed+batched vs plain FP64 on GB300 @ rel force err≤1e-6"
+WORKLOAD = ("P3T tree step, 1048576-body disk 0.95-1.05 AU, m=7e-11, rms e=6h, rms i=3h, theta=0.5, "
+            "n_group_limit=256, dt_tree=2^-7, perfect accretion")
+# FP64 flops per evaluated hard pair term (predicted/corrected pass; full pass
+# with the potential and the W cutoff), per active member and block step
+# (two corrector passes, the sun force three times, the time step) and per
+# member prediction (every member, every block step), FMA = 2, sqrt/div = 1
+HARD_FLOPS_PC, HARD_FLOPS_FULL, HARD_FLOPS_MEMBER, HARD_FLOPS_PREDICT = 77, 120, 145, 30
+EPEP_FLOPS, EPSP_FLOPS = 32, 70  # per soft pair
+# DRAM bytes (read + write) per launch from the ncu captures summarised in
+# profiles/ (the bench cannot read DRAM counters itself)
+HARD_TRAFFIC_BYTES = 6.63e9
+HARD_TRAFFIC_SOURCE = "ncu, profiles/k_hard_bundles_1m_hard_disk.md"
 SOFT_TRAFFIC_BYTES = 195.0e6
-
-
-def workload(seed=2):
-    from gplum_gb300.disk import P3TParams, disk_1m_soft
-    from gplum_gb300.radii import cutoff_radii
-    from gplum_gb300.soft import epj_records
-    from gplum_gb300.tree import build_lists
-
-    P = P3TParams(n_group_limit=256)
-    d = disk_1m_soft(N_BODIES, seed=seed)
-    r_out, r_search, _ = cutoff_radii(d["pos"], d["vel"], d["mass"], P)
-    # particles in the tree's (Morton) order, the order of the EPJ array FDPS
-    # hands to the force kernels
-    perm = build_lists(d["pos"], d["mass"], r_search, P.theta, P.n_leaf_limit, P.n_group_limit)["i_idx"]
-    pos, vel, mass, r_out, r_search = d["pos"][perm], d["vel"][perm], d["mass"][perm], r_out[perm], r_search[perm]
-    epj = epj_records(pos, vel, mass, r_out, r_search, ids=d["id"][perm])
-    L = build_lists(pos, mass, r_search, P.theta, P.n_leaf_limit, P.n_group_limit)
-    return P, epj, L
-
-
-def pair_counts(L):
-    ni = np.diff(L["i_off"]).astype(np.int64)
-    return int((ni * np.diff(L["j_off"])).sum()), int((ni * np.diff(L["s_off"])).sum())
-
-
-def config(L, extra=None):
-    c = {"workload": "P3T soft force, 1048576-body disk 0.5-1.5 AU, m=1e-10, theta=0.5, "
-                     "n_group_limit=256, quadrupole SPJ",
-         "n_bodies": N_BODIES, "n_groups": int(L["n_group"]), "theta": 0.5, "n_group_limit": 256,
-         "particle_order": "tree (Morton) order, as FDPS passes its EPJ array",
-         "l2": "flushed between timed steps (256 MiB write)", "parallelism": "replicas"}
-    if extra:
-        c.update(extra)
-    return c
+SOFT_TRAFFIC_SOURCE = "ncu, profiles/soft_mixed_kernel_1m_disk.md"
 
 
 class ClockSampler:
@@ -112,139 +107,317 @@ class ClockSampler:
                 "reasons": sorted(reasons)}
 
 
-def p3t_step_measure(precision, steps=2, n=N_BODIES, hard_mode=0, learned=True, device_tree=True):
-    """The whole device P3T tree step (src/main_p3t.cpp:423-717) on the
-    hard-part disk (n bodies, 0.95-1.05 AU, rms e = 6 h): kick, cluster
-    labels + lists, hard part (one persistent launch), tree + interaction
-    lists + soft force, correction + neighbour search, kick, energy.  Wall-clock per phase
-    with the device synchronised at each phase boundary.  The octree and
-    interaction lists are built on the device (tree_soft: tree + lists + soft
-    force); device_tree=False builds them on the host instead.
-
-    precision 0/1: mixed / FP64 soft force; hard_mode 0/1: bundles / one
-    cluster per thread, warp or CTA; learned: queue in the order of the
-    committed cost model (else size order)."""
-    from gplum_gb300 import scheduler
-    from gplum_gb300.disk import P3TParams, disk_1m_hard
+# ---------------------------------------------------------------------------
+# the device step
+def new_system(form, P):
+    """A GpuSystem in one of the two forms: "mixed" (mixed soft kernel,
+    bundled hard launch, learned queue order, autotuned launch shapes) or
+    "plain" (FP64 soft kernel, one cluster per thread/warp/CTA, size order)."""
+    from gplum_gb300 import autotune, scheduler
     from gplum_gb300.p3t import GpuSystem
-    from gplum_gb300.tree import build_lists
 
-    from gplum_gb300 import autotune
-
-    P = P3TParams(n_group_limit=256)
-    d = disk_1m_hard(n)
-    g = GpuSystem(P, precision=precision)
-    autotune.load(g.lib)  # launch shapes chosen by gplum_gb300/autotune.py
-    g.lib.p3t_set_hard_mode(hard_mode)
-    model = scheduler.load(lib=g.lib) if learned else None
+    g = GpuSystem(P, precision=0 if form == "mixed" else 1)
+    autotune.load(g.lib)
+    g.lib.p3t_set_hard_mode(0 if form == "mixed" else 1)
+    model = scheduler.load(lib=g.lib) if form == "mixed" else None
     g.lib.p3t_set_schedule(1 if model is not None else 0)
-    ph = {}
+    g.lib.p3t_set_fragmentation(0.0, 10, 9.426627927538057e-12, 0)
+    return g
 
-    def lists():
-        t0 = time.perf_counter()
-        L = build_lists(g.get("pos"), d["mass"] if g.n == len(d["mass"]) else g.get("mass"), g.get("r_search"),
-                        P.theta, P.n_leaf_limit, P.n_group_limit)
-        ph["tree_host"] = ph.get("tree_host", 0.0) + time.perf_counter() - t0
-        return L
 
-    g.load(d)
+def hard_flops(g):
+    """The last hard launch: (ms, executed FP64 flops or None, algorithmic
+    FP64 flops, pair terms evaluated, longest block-step chain).  Executed:
+    the pair terms the launch evaluated (after its exact distance prefilter)
+    plus the member phases; algorithmic: GPLUM's loop, every (active, member)
+    pair three times per block step and all member pairs in the collision
+    test (src/hermite.h:98-479)."""
+    h = g.hard_launch_stats()
+    members = HARD_FLOPS_MEMBER * h["active"] + HARD_FLOPS_PREDICT * h["predictions"]
+    algorithmic = 231.0 * h["sweeps"] + 14.0 * h["coll_pairs"] + members
+    executed = HARD_FLOPS_PC * h["live_pc"] + HARD_FLOPS_FULL * h["live_full"] + members
+    return (h["ms"], (executed if h["counted"] else None), algorithmic, h["live_pc"] + h["live_full"],
+            h["max_block_steps"])
+
+
+def run_form(form, P, disk, warmup, steps, world, clocks=False, roofline=False):
+    """Start-up, `warmup` untimed steps, then `steps` steps timed by the
+    library's CUDA events; returns the system and a summary."""
+    import torch
+
+    g = new_system(form, P)
+    g.load(disk)
     g.set_r_planet()
-    g.prepare()
-
-    def tree_soft():
-        if device_tree:
-            g.tree_soft()
-        else:
-            L = lists()
-            g.soft_force(L)
-
-    for _ in range(2):
-        tree_soft()
-        g.correct(True)
-    e0 = g.energy()
-    # warm-up of the hard path (first-use allocations, kernel loading: ~11 ms
-    # once) on a copy of the state, which is then restored
-    assert g.lib.p3t_state_snapshot(0) == 0
-    g.kick()
-    g.cluster()
-    g.hard(1)
-    assert g.lib.p3t_state_snapshot(1) == 0
-    ph.clear()
-    clusters = []
-    ncol = 0
-
-    def timed(name, fn):
-        g.lib.p3t_synchronize()
-        t0 = time.perf_counter()
-        r = fn()
-        g.lib.p3t_synchronize()
-        ph[name] = ph.get(name, 0.0) + time.perf_counter() - t0
-        return r
-
-    t_all = time.perf_counter()
-    for istep in range(1, steps + 1):
-        timed("kick", g.kick)
-        timed("cluster", g.cluster)
-        cols, _ = timed("hard", lambda: g.hard(istep))
-        ncol += len(cols)
-        off, _m = g.cluster_lists()
-        clusters.append((len(off) - 1, int(np.diff(off).max()) if len(off) > 1 else 0))
-        timed("tree_soft", tree_soft)
-        timed("correct", lambda: g.correct(False))
-        timed("kick", g.kick)
-        e = timed("energy", g.energy)
-        if len(cols):
-            timed("merge", lambda: g.merge(len(cols)))
-            timed("radii", g.prepare)
-            timed("tree_soft", tree_soft)
-            timed("correct", lambda: g.correct(True))
-    total = (time.perf_counter() - t_all) / steps
-    g.lib.p3t_set_hard_mode(0)
-    g.lib.p3t_set_schedule(0)
-    ms = {k: 1e3 * v / steps for k, v in ph.items()}
-    # tree_host (host list build) is nested inside tree_soft when the tree is on the host
-    dev = sum(ms.values()) - 2.0 * ms.get("tree_host", 0.0)
-    return {"n_bodies": n, "steps": steps, "soft": "mixed" if precision == 0 else "fp64",
-            "hard": "bundles" if hard_mode == 0 else "cluster per thread/warp/CTA",
-            "queue": "learned cost model" if model is not None else "size",
-            "tree": "device" if device_tree else "host",
-            "ms_per_step": 1e3 * total, "device_ms_per_step": dev,
-            "phases_ms": ms, "clusters_per_step": [c[0] for c in clusters],
-            "largest_cluster": max(c[1] for c in clusters), "collisions": ncol,
-            "dE_over_E": float((e[0] - e0[0]) / e0[0])}
+    e0 = g.startup()
+    edisp = 0.0
+    istep = 0
+    for _ in range(warmup):
+        istep += 1
+        r = g.tree_step(istep)
+        edisp += r["edisp"]
+    lib = g.lib
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    _lib_sync(lib)
+    launches0 = lib.p3t_launch_count()
+    ms, phases, hard = [], [], []
+    ncol, de_max = 0, 0.0
+    t_wall = time.perf_counter()
+    sampler = ClockSampler() if clocks else None
+    if sampler:
+        sampler.__enter__()
+    try:
+        for _ in range(steps):
+            istep += 1
+            r = g.tree_step(istep)
+            ph = g.step_phases_ms()
+            ms.append(sum(ph.values()))
+            phases.append(ph)
+            ncol += r["n_col"]
+            edisp += r["edisp"]
+            de_max = max(de_max, abs((r["energy"][0] - e0[0] - edisp) / e0[0]))
+            if roofline:
+                hard.append(hard_flops(g) + (r["n_clusters"],))
+    finally:
+        _lib_sync(lib)
+        torch.cuda.synchronize()
+        if sampler:
+            sampler.__exit__()
+    wall = time.perf_counter() - t_wall
+    launches = lib.p3t_launch_count() - launches0
+    if world > 1:
+        torch.distributed.barrier()
+    out = {"form": form, "steps": steps, "warmup": warmup, "ms_per_step": float(np.mean(ms)),
+           "ms_per_step_min": float(np.min(ms)), "ms_per_step_max": float(np.max(ms)),
+           "wall_ms_per_step": 1e3 * wall / steps,
+           "phases_ms": {k: float(np.mean([p[k] for p in phases])) for k in phases[0]},
+           "collisions": ncol, "n_body_end": g.n, "dE_over_E_max": de_max,
+           "launches": int(launches), "istep": istep}
+    if sampler:
+        out["clocks"] = sampler.summary()
+    if hard:
+        out["hard"] = hard
+    return g, out
 
 
-def cpu_step_baseline(n=N_BODIES, steps=1):
-    """The same whole tree step run by GPLUM's arithmetic on the host cores
-    (the oracle port, OpenMP over clusters and bodies as GPLUM's loops are),
-    with the same host tree; start-up not timed.  Returns (seconds per step,
-    ms per step by GPLUM's CALC_WTIME phase)."""
-    from gplum_gb300.disk import P3TParams, disk_1m_hard
+def _lib_sync(lib):
+    from gplum_gb300 import _lib
+    _lib.check(lib.p3t_synchronize(), "p3t_synchronize")
+
+
+def soft_accuracy(g, P):
+    """Per-body relative error of the mixed soft force (the kernel's
+    ForceGrav records) against the FP64 restatement of GPLUM's functors on the
+    same interaction lists (the step's own device-built lists), and the same
+    figures for GPLUM's FP32 functor (src/gravity_kernel.hpp:25-238)."""
+    from gplum_gb300.layout import EPJ_DTYPE, FORCE_DTYPE, cleared_forces
+    from gplum_gb300.soft import epi_records
     from oracle import harness as H
 
-    P = P3TParams(n_group_limit=256)
-    s = H.CpuSystem("orc", P)
-    lf = H.tree_lists_fn(P)
-    H.p3t_init(s, disk_1m_hard(n), lf)
-    clock = {}
+    g.tree_soft()
+    n = g.n
+    f_gpu = np.zeros(n, FORCE_DTYPE)
+    from gplum_gb300 import _lib
+    _lib.check(g.lib.p3t_download_forces(f_gpu.ctypes.data_as(ctypes.c_void_p), n), "p3t_download_forces")
+    L = g.tree_lists(build=False)
+    epj = np.zeros(n, EPJ_DTYPE)
+    epj["id_local"] = np.arange(n)
+    for k in ("pos", "r_out", "r_search", "id", "mass", "vel", "acc_d"):
+        epj[k] = g.get(k)
+    epi = epi_records(epj)
+    H.CpuSystem("orc", P)  # the oracle's parameters
+    lib = H.load("orc")
+    vp = ctypes.c_void_p
+    args = [L["n_group"]] + [L[k].ctypes.data_as(vp) for k in ("i_off", "i_idx", "j_off", "j_idx", "s_off", "s_idx")]
+    acc4 = np.zeros(4 * n)
+    ngb4 = np.zeros(4 * n, np.int32)
+    dummy = cleared_forces(1)
     t0 = time.perf_counter()
-    for istep in range(1, steps + 1):
-        H.p3t_step(s, istep, lf, clock=clock)
-    return (time.perf_counter() - t0) / steps, {k: 1e3 * v / steps for k, v in clock.items()}
+    lib.orc_soft_lists(1, 0, *args, epi.ctypes.data_as(vp), epj.ctypes.data_as(vp), L["spj"].ctypes.data_as(vp),
+                       dummy.ctypes.data_as(vp), acc4.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                       ngb4.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), os.cpu_count())
+    t64 = time.perf_counter() - t0
+    f32 = cleared_forces(n)
+    lib.orc_soft_lists(0, 0, *args, epi.ctypes.data_as(vp), epj.ctypes.data_as(vp), L["spj"].ctypes.data_as(vp),
+                       f32.ctypes.data_as(vp), None, None, os.cpu_count())
+    a64 = acc4.reshape(n, 4)[:, :3]
+
+    def stats(a):
+        e = np.sqrt(((a.astype(np.float64) - a64) ** 2).sum(1)) / np.maximum(np.sqrt((a64 ** 2).sum(1)), 1e-300)
+        return {"median": float(np.median(e)), "p99": float(np.quantile(e, 0.99)),
+                "p999": float(np.quantile(e, 0.999)), "max": float(e.max()),
+                "frac_le_1e-6": float((e <= 1e-6).mean())}
+
+    same = all(np.array_equal(f_gpu[k], f32[k]) for k in ("number", "rank", "id_max", "id_min"))
+    return {"bodies": n, "groups": int(L["n_group"]),
+            "statistic": "per body |a - a_fp64| / |a_fp64| of the soft force, same lists",
+            "mixed_kernel": stats(f_gpu["acc"]), "gplum_fp32_functor": stats(f32["acc"]),
+            "neighbour_fields_equal_to_gplum_functor": bool(same), "fp64_oracle_s": t64}
 
 
-def cpu_reference(L, epj, P, budget_s=20.0, threads=None):
-    """GPLUM's functor arithmetic (oracle restatement, FP32 functors) on the
-    host cores over a sample of the groups; returns (steps/s, sample text, cores)."""
-    import ctypes
+def e2e_steps(g, istep0, steps):
+    """Steps through the C ABI with the state in GPLUM FPGrav records in
+    pinned host memory: records in, p3t_tree_step, records and collision
+    records out, every step."""
+    import torch
 
+    from gplum_gb300.collisions import Record, records
+    from gplum_gb300.layout import FPGRAV_DTYPE
+
+    n = g.n
+    cap = n + 65536
+    host = torch.empty(cap * FPGRAV_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True).numpy().view(FPGRAV_DTYPE)
+    g.get_fpgrav(host)
+    id_next = g.id_next()
+    t, h2d, d2h = [], 0, 0
+    istep = istep0
+    for _ in range(steps):
+        istep += 1
+        t0 = time.perf_counter()
+        m = g.n
+        g.put_fpgrav(host[:m], id_next)
+        r = g.tree_step(istep)
+        out = g.get_fpgrav(host)
+        cols = records(g.lib)
+        t.append(time.perf_counter() - t0)
+        id_next = g.id_next()
+        h2d += m * FPGRAV_DTYPE.itemsize
+        d2h += len(out) * FPGRAV_DTYPE.itemsize + len(cols) * ctypes.sizeof(Record)
+        del r
+    ms = float(np.median(t)) * 1e3
+    return {"value": 1e3 / ms, "unit": "steps/s", "h2d_bytes_per_step": int(h2d // steps),
+            "d2h_bytes_per_step": int(d2h // steps), "ms_per_step": ms, "steps": steps,
+            "path": "p3t_state_put_fpgrav + p3t_tree_step + p3t_state_get_fpgrav + p3t_collision_records, "
+                    "pinned FPGrav records"}
+
+
+def hard_roofline(hard, peak64):
+    """The hard launch over the timed steps: executed FP64 flops / launch
+    time against the FP64 FMA peak."""
+    ms = sum(h[0] for h in hard)
+    ex = [h[1] for h in hard]
+    alg = sum(h[2] for h in hard)
+    out = {"kernel": "k_hard_bundles<256,2> (one launch per tree step)", "bound": "fp64",
+           "launch_ms": ms / len(hard), "unit": "TFLOP/s", "peak": peak64,
+           "peak_source": "measured (FP64 FMA microbenchmark p3t_probe_fma_peak)",
+           "algorithmic_tflops": alg / (ms * 1e-3) / 1e12,
+           "pair_terms_per_launch": float(np.mean([h[3] for h in hard])),
+           "longest_cluster_block_steps": int(max(h[4] for h in hard)),
+           "clusters_per_launch": float(np.mean([h[5] for h in hard])),
+           "traffic": HARD_TRAFFIC_BYTES, "traffic_source": HARD_TRAFFIC_SOURCE,
+           "flops_note": "achieved counts executed pair terms (77 flop predicted/corrected, 120 full), 145 flop "
+                         "per active member and block step and 30 per member prediction; algorithmic counts "
+                         "GPLUM's loop (3 n_act n pair terms and n(n-1) collision tests per block step) and the "
+                         "same member work"}
+    if all(x is not None for x in ex):
+        out["achieved"] = sum(ex) / (ms * 1e-3) / 1e12
+        out["frac"] = out["achieved"] / peak64
+        out["flops_per_launch"] = sum(ex) / len(hard)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# extras
+def soft_pass(P_unused=None, cpu_budget_s=5.0):
+    """The soft pass alone on the 1M soft-force disk (0.5-1.5 AU, m = 1e-10):
+    the fused EP-EP + EP-SP kernel over every group of the host tree's lists,
+    inputs in HBM, L2 flushed between launches; its FP32 roofline and the
+    functor-level e2e through p3t_soft_force_host."""
+    import torch
+
+    from gplum_gb300 import _lib, soft
+    from gplum_gb300.disk import P3TParams, disk_1m_soft
+    from gplum_gb300.layout import FORCE_DTYPE
+    from gplum_gb300.radii import cutoff_radii
+    from gplum_gb300.soft import epj_records
+    from gplum_gb300.tree import build_lists
+
+    P = P3TParams(n_group_limit=256)
+    d = disk_1m_soft(N_BODIES, seed=2)
+    r_out, r_search, _ = cutoff_radii(d["pos"], d["vel"], d["mass"], P)
+    perm = build_lists(d["pos"], d["mass"], r_search, P.theta, P.n_leaf_limit, P.n_group_limit)["i_idx"]
+    pos, vel, mass, r_out, r_search = d["pos"][perm], d["vel"][perm], d["mass"][perm], r_out[perm], r_search[perm]
+    epj = epj_records(pos, vel, mass, r_out, r_search, ids=d["id"][perm])
+    L = build_lists(pos, mass, r_search, P.theta, P.n_leaf_limit, P.n_group_limit)
+    ni = np.diff(L["i_off"]).astype(np.int64)
+    n_epep, n_epsp = int((ni * np.diff(L["j_off"])).sum()), int((ni * np.diff(L["s_off"])).sum())
+    flops = EPEP_FLOPS * n_epep + EPSP_FLOPS * n_epsp
+    lib = _lib.host_lib()
+    from gplum_gb300 import autotune
+    autotune.load(lib)
+    sf = soft.SoftForce(P, precision=0)
+    sf.upload_particles(epj)
+    sf.upload_lists(L)
+    stream = torch.cuda.ExternalStream(sf.stream())
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def timed(k, precision):
+        soft.configure(P, precision=precision)
+        ms = []
+        for _ in range(k):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                sf.run(emit_candidates=True)
+                e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return ms
+
+    timed(3, 0)
+    ms = float(np.mean(timed(10, 0)))
+    ms64 = float(np.mean(timed(2, 1)))
+    soft.configure(P, precision=0)
+    peak = ctypes.c_double()
+    _lib.check(lib.p3t_probe_fma_peak(0, ctypes.byref(peak)), "fp32 peak probe")
+
+    def pinned(nbytes):
+        return torch.empty(nbytes, dtype=torch.uint8, pin_memory=True).numpy()
+
+    h_epj = pinned(epj.nbytes).view(epj.dtype)
+    h_epj[:] = epj
+    h_L = {"n_group": L["n_group"]}
+    for k in ("i_off", "i_idx", "j_off", "j_idx", "s_off", "s_idx", "spj"):
+        h_L[k] = pinned(L[k].nbytes).view(L[k].dtype)
+        h_L[k][:] = L[k]
+    h_force = pinned(len(epj) * FORCE_DTYPE.itemsize).view(FORCE_DTYPE)
+    soft.soft_force_host(P, h_epj, h_L, out=h_force)
+    e2e = []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        soft.soft_force_host(P, h_epj, h_L, out=h_force)
+        e2e.append(time.perf_counter() - t0)
+    achieved = flops / (ms * 1e-3) / 1e12
+    out = {"workload": "soft force alone, 1048576-body disk 0.5-1.5 AU, m=1e-10, theta=0.5, n_group_limit=256, "
+                       "quadrupole SPJ, tree (Morton) order, L2 flushed between launches",
+           "ms_per_pass": ms, "passes_per_s": 1e3 / ms, "epep_pairs": n_epep, "epsp_pairs": n_epsp,
+           "interactions_per_s": (n_epep + n_epsp) / (ms * 1e-3),
+           "fp64_form_ms": ms64,
+           "roofline": {"kernel": "soft_mixed_kernel", "bound": "fp32", "achieved": achieved, "peak": peak.value,
+                        "unit": "TFLOP/s", "frac": achieved / peak.value,
+                        "peak_source": "measured (FP32 FMA microbenchmark p3t_probe_fma_peak)",
+                        "traffic": SOFT_TRAFFIC_BYTES, "traffic_source": SOFT_TRAFFIC_SOURCE},
+           "e2e_passes_per_s": 1.0 / float(np.median(e2e))}
+    try:
+        v, sample, cores = cpu_soft_reference(L, epj, P, budget_s=cpu_budget_s)
+        out["cpu_functor_port"] = {"passes_per_s": v, "cores": cores, "sample": sample}
+    except Exception as e:  # the oracle is test infrastructure: report, do not fail the line
+        out["cpu_functor_port"] = {"error": repr(e)}
+    return out
+
+
+def cpu_soft_reference(L, epj, P, budget_s=5.0):
+    """GPLUM's FP32 functors (oracle restatement) on the host cores over a
+    sample of the groups, scaled to the full pass by pair flops."""
     from gplum_gb300.layout import cleared_forces
     from gplum_gb300.soft import epi_records
     from oracle import harness as H
 
-    harness_sys = H.CpuSystem("orc", P)  # sets the oracle's parameters
-    lib = harness_sys.lib
-    threads = threads or os.cpu_count()
+    H.CpuSystem("orc", P)
+    lib = H.load("orc")
+    threads = os.cpu_count()
     epi = epi_records(epj)
     ng = L["n_group"]
     vp = ctypes.c_void_p
@@ -271,14 +444,73 @@ def cpu_reference(L, epj, P, budget_s=20.0, threads=None):
     groups = rng.choice(ng, size=max(1, int(frac * ng)), replace=False)
     t = run(groups)
     ni = np.diff(L["i_off"]).astype(np.int64)
-    work = lambda gs: float((ni[gs] * (EPEP_FLOPS * np.diff(L["j_off"])[gs] + EPSP_FLOPS * np.diff(L["s_off"])[gs])).sum())
+    work = lambda gs: float((ni[gs] * (EPEP_FLOPS * np.diff(L["j_off"])[gs] +
+                                       EPSP_FLOPS * np.diff(L["s_off"])[gs])).sum())
     step_s = t * work(np.arange(ng)) / work(groups)
-    return 1.0 / step_s, f"{len(groups)} of {ng} groups ({t:.1f} s), scaled to the full step by pair flops", threads
+    return 1.0 / step_s, f"{len(groups)} of {ng} groups ({t:.1f} s), scaled to the full pass by pair flops", threads
+
+
+def long_run(workload, steps, form="mixed", schedule="learned", a_frag=0.0):
+    """A run of `steps` tree steps through p3t_tree_step: wall time, hard
+    launch time, collisions and the largest |dE/E| (GPLUM's calcEnergyError
+    with the dissipated energy, src/energy.h:65-67)."""
+    from gplum_gb300.disk import P3TParams, disk_1m_embryos, disk_8m
+
+    P = P3TParams(n_group_limit=256)
+    disk = disk_1m_embryos() if workload == "embryos" else disk_8m()
+    g = new_system(form, P)
+    if schedule == "size":
+        g.lib.p3t_set_schedule(0)
+    if a_frag > 0:
+        g.set_fragmentation(a_frag)
+    g.load(disk)
+    g.set_r_planet()
+    t0 = time.perf_counter()
+    e0 = g.startup()
+    edisp, de_max, ncol, hard_ms = 0.0, 0.0, 0, 0.0
+    for istep in range(1, steps + 1):
+        r = g.tree_step(istep)
+        edisp += r["edisp"]
+        ncol += r["n_col"]
+        hard_ms += g.step_phases_ms()["hard"]
+        de_max = max(de_max, abs((r["energy"][0] - e0[0] - edisp) / e0[0]))
+    wall = time.perf_counter() - t0
+    pos = g.get("pos")
+    out = {"steps": steps, "form": form, "queue": schedule if form == "mixed" else "size", "a_frag": a_frag,
+           "wall_s": wall, "ms_per_step": 1e3 * wall / steps, "hard_s": hard_ms * 1e-3, "collisions": ncol,
+           "n_initial": len(disk["mass"]), "n_final": g.n, "max_abs_dE_over_E": de_max,
+           "final_state_checksum": float(np.sum(pos * np.arange(1, 4))) + float(np.sum(g.get("id")))}
+    g.lib.p3t_set_fragmentation(0.0, 10, 9.426627927538057e-12, 0)
+    return out
+
+
+def cpu_step_baseline(disk, P, steps):
+    """GPLUM's whole tree step on the host cores: the CPU restatement (oracle)
+    with the project's host tree, OpenMP over bodies and clusters as GPLUM's
+    loops are; start-up not timed.  Returns (s per step, CALC_WTIME split)."""
+    from oracle import harness as H
+
+    s = H.CpuSystem("orc", P)
+    lf = H.tree_lists_fn(P)
+    H.p3t_init(s, disk, lf)
+    clock = {}
+    t0 = time.perf_counter()
+    for istep in range(1, steps + 1):
+        H.p3t_step(s, istep, lf, clock=clock)
+    return (time.perf_counter() - t0) / steps, {k: 1e3 * v / steps for k, v in clock.items()}
+
+
+def config(extra=None):
+    c = {"workload": WORKLOAD, "n_bodies": N_BODIES, "theta": 0.5, "n_group_limit": 256, "n_leaf_limit": 8,
+         "hard_queue": "learned cost model (gplum_gb300/sched_model.npz)", "launch_shapes": "gplum_gb300/tuning.json",
+         "l2": "state larger than L2 (0.34 GB resident; soft lists and hard state re-read every step)",
+         "parallelism": "replicas"}
+    if extra:
+        c.update(extra)
+    return c
 
 
 def max_over_ranks(x, world):
-    """The largest x over the ranks (every rank receives it); x itself on one
-    rank.  NCCL tensors live on the rank's GPU, gloo tensors on the host."""
     if world <= 1:
         return x
     import torch
@@ -296,155 +528,108 @@ def replica_rate(ms_step, world):
     return world * 1e3 / ms_step
 
 
+# ---------------------------------------------------------------------------
 def reference_arm(args, rank, world):
+    """GPLUM's whole tree step by the CPU restatement on all host cores, on
+    the same disk: start-up untimed, W warm-up steps, K timed steps."""
     if rank != 0:
         return
-    P, epj, L = workload()
-    steps_s = []
+    from gplum_gb300.disk import P3TParams, disk_1m_hard
+    from oracle import harness as H
+
+    P = P3TParams(n_group_limit=256)
+    s = H.CpuSystem("orc", P)
+    lf = H.tree_lists_fn(P)
+    H.p3t_init(s, disk_1m_hard(N_BODIES), lf)
+    istep = 0
     for _ in range(args.warmup):
-        cpu_reference(L, epj, P, budget_s=2.0)
+        istep += 1
+        H.p3t_step(s, istep, lf)
+    clock, t = {}, []
     for _ in range(args.steps):
-        v, sample, cores = cpu_reference(L, epj, P, budget_s=max(2.0, 60.0 / max(args.steps, 1)))
-        steps_s.append(v)
-    v = float(np.mean(steps_s))
+        istep += 1
+        t0 = time.perf_counter()
+        H.p3t_step(s, istep, lf, clock=clock)
+        t.append(time.perf_counter() - t0)
+    ms = 1e3 * float(np.mean(t))
+    v = 1e3 / ms
+    cores = os.cpu_count()
     print(json.dumps({
-        "impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s",
-        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 displacements)",
-        "data": "synthetic seeded disk", "config": config(L),
-        "cpu_baseline": {"value": v, "unit": "steps/s", "cores": cores, "kind": "port", "sample": sample},
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 soft force (FP64 displacements), f64 elsewhere",
+        "data": "synthetic seeded disk", "config": config(),
+        "phases_ms": {k: 1e3 * x / args.steps for k, x in clock.items()},
+        "cpu_baseline": {"value": v, "unit": "steps/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} whole tree steps of the same disk after {args.warmup} warm-up "
+                                   "steps (start-up untimed); GPLUM's arithmetic restated in oracle/ (pinned bit "
+                                   "for bit to GPLUM's headers), the project's host tree for FDPS"},
         "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}), flush=True)
 
 
 def gpu_arm(args, rank, world):
     import torch
 
-    from gplum_gb300 import _lib, soft
-    from gplum_gb300.layout import EPJ_DTYPE, FORCE_DTYPE
+    from gplum_gb300 import _lib
+    from gplum_gb300.disk import P3TParams, disk_1m_hard
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    P, epj, L = workload()
-    n_epep, n_epsp = pair_counts(L)
-    flops = EPEP_FLOPS * n_epep + EPSP_FLOPS * n_epsp
-    lib = _lib.host_lib()
-
-    from gplum_gb300 import autotune
-
-    tuning = autotune.load(lib)  # work split chosen by gplum_gb300/autotune.py on this workload
-    sf = soft.SoftForce(P, precision=0)
-    sf.upload_particles(epj)
-    sf.upload_lists(L)
-    stream = torch.cuda.ExternalStream(sf.stream())
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-
-    def timed_steps(k, precision):
-        soft.configure(P, precision=precision)
-        ms = []
-        for _ in range(k):
-            with torch.cuda.stream(stream):
-                flush.zero_()
-                e0 = torch.cuda.Event(enable_timing=True)
-                e1 = torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
-                sf.run(emit_candidates=True)
-                e1.record(stream)
-            e1.synchronize()
-            ms.append(e0.elapsed_time(e1))
-        return ms
-
-    for _ in range(max(3, args.warmup)):
-        sf.run(emit_candidates=True)
-    sf.synchronize()
-    _lib.check(lib.p3t_status(), "warm-up")
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    with ClockSampler() as clk:
-        ms = timed_steps(args.steps, 0)
-        torch.cuda.synchronize()
-    clocks = clk.summary()
-    st = lib.p3t_status()
-    if st not in (0,):
-        raise RuntimeError(f"soft kernel reported status {st}")
-    ms_step = float(np.mean(ms))
-    ms_step = max_over_ranks(ms_step, world)
+    P = P3TParams(n_group_limit=256)
+    disk = disk_1m_hard(N_BODIES)
+    warmup = max(3, args.warmup)
+    g, mixed = run_form("mixed", P, disk, warmup, args.steps, world, clocks=True, roofline=True)
+    lib = g.lib
+    ms_step = max_over_ranks(mixed["ms_per_step"], world)
     value = replica_rate(ms_step, world)
-
-    # plain FP64 form of the same kernel (the accuracy / speed baseline)
-    ms64 = float(np.mean(timed_steps(2, 1)))
-    soft.configure(P, precision=0)
-
-    # FP32 pipe peak of this GPU (project microbenchmark)
-    peak, peak64 = ctypes.c_double(), ctypes.c_double()
-    _lib.check(lib.p3t_probe_fma_peak(0, ctypes.byref(peak)), "fp32 peak probe")
+    peak64 = ctypes.c_double()
     _lib.check(lib.p3t_probe_fma_peak(1, ctypes.byref(peak64)), "fp64 peak probe")
-    achieved = flops / (ms_step * 1e-3) / 1e12
-    achieved64 = flops / (ms64 * 1e-3) / 1e12
-
-    # end to end through the C ABI with pinned host buffers
-    def pinned(nbytes):
-        return torch.empty(nbytes, dtype=torch.uint8, pin_memory=True).numpy()
-
-    h_epj = pinned(epj.nbytes).view(EPJ_DTYPE)
-    h_epj[:] = epj
-    h_L = {"n_group": L["n_group"]}
-    for k in ("i_off", "i_idx", "j_off", "j_idx", "s_off", "s_idx", "spj"):
-        h_L[k] = pinned(L[k].nbytes).view(L[k].dtype)
-        h_L[k][:] = L[k]
-    h_force = pinned(len(epj) * FORCE_DTYPE.itemsize).view(FORCE_DTYPE)
-    soft.soft_force_host(P, h_epj, h_L, out=h_force)
-    e2e = []
-    for _ in range(max(2, min(args.steps, 5))):
-        t0 = time.perf_counter()
-        soft.soft_force_host(P, h_epj, h_L, out=h_force)
-        e2e.append(time.perf_counter() - t0)
-    h2d = epj.nbytes + sum(L[k].nbytes for k in ("i_off", "i_idx", "j_off", "j_idx", "s_off", "s_idx", "spj"))
-    d2h = h_force.nbytes
-
+    roof = hard_roofline(mixed.pop("hard"), peak64.value)
+    acc = soft_accuracy(g, P)
+    e2e = e2e_steps(g, mixed["istep"], max(3, min(args.steps, 20)))
+    del g
+    _, plain = run_form("plain", P, disk, warmup, args.steps, world)
     if rank != 0:
         return
     out = {
-        "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 displacements, compensated sums)",
-        "data": "synthetic seeded disk", "config": config(L, {"epep_pairs": n_epep, "epsp_pairs": n_epsp}),
-        "fp64_form": {"ms_per_step": ms64, "steps_per_s": 1e3 / ms64, "mixed_speedup": ms64 / ms_step,
-                      "achieved_tflops": achieved64, "fp64_peak_tflops": peak64.value},
-        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
-                     "frac": achieved / peak.value, "peak_source": "measured (FP32 FMA microbenchmark)",
-                     "flops_per_step": flops,
-                     # DRAM bytes read + written by one launch of the pair kernel, from the
-                     # ncu capture summarised in profiles/soft_mixed_kernel_1m_disk.md
-                     "traffic": SOFT_TRAFFIC_BYTES, "traffic_source": "ncu, profiles/soft_mixed_kernel_1m_disk.md"},
-        "interactions_per_s": (n_epep + n_epsp) / (ms_step * 1e-3),
-        "e2e": {"value": 1.0 / float(np.median(e2e)), "unit": "steps/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h)},
-        # per step: position splits, superparticle pack, pair kernel
-        "gpu_launches": 3 * args.steps,
-        "soft_tiles": tuning["soft_tiles"] if tuning else [128, 64, 32],
-        "soft_ctas_per_sm": tuning.get("soft_occ", 5) if tuning else 5,
-        "clocks": clocks,
+        "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 soft force with FP64 displacements and compensated sums; f64 hard "
+                                      "part, correction, drift and energy",
+        "data": "synthetic seeded disk",
+        "config": config({"n_collisions_timed": mixed["collisions"]}),
+        "fp64_form": {"value": 1e3 / plain["ms_per_step"], "unit": "steps/s", "ms_per_step": plain["ms_per_step"],
+                      "mixed_speedup": plain["ms_per_step"] / ms_step, "phases_ms": plain["phases_ms"],
+                      "dE_over_E_max": plain["dE_over_E_max"], "collisions": plain["collisions"],
+                      "form": "FP64 soft kernel, one cluster per thread/warp/CTA, size queue order"},
+        "phases_ms": mixed["phases_ms"], "wall_ms_per_step": mixed["wall_ms_per_step"],
+        "roofline": roof,
+        "accuracy": {"soft_force": acc, "dE_over_E_max_timed_steps": mixed["dE_over_E_max"],
+                     "dE_over_E_max_fp64_form": plain["dE_over_E_max"]},
+        "e2e": e2e,
+        "gpu_launches": mixed["launches"],
+        "clocks": mixed.get("clocks"),
     }
-    if not args.skip_step:
+    if world == 1 and not args.no_extras:
+        from gplum_gb300.disk import P3TParams as PP
         try:
-            mixed = p3t_step_measure(0)
-            plain = p3t_step_measure(1, steps=1, hard_mode=1, learned=False)
-            out["p3t_step"] = {"workload": "hard-part disk, 1048576 bodies, 0.95-1.05 AU, m=7e-11, "
-                                           "rms e=6h, rms i=3h, theta=0.5, n_group_limit=256",
-                               "mixed_batched": mixed, "plain_fp64": plain,
-                               "device_speedup": plain["device_ms_per_step"] / mixed["device_ms_per_step"],
-                               "hard_speedup": plain["phases_ms"]["hard"] / mixed["phases_ms"]["hard"]}
-            cpu_s, cpu_phases = cpu_step_baseline()
-            out["p3t_step"]["cpu_baseline"] = {"value": 1.0 / cpu_s, "unit": "steps/s", "cores": os.cpu_count(),
-                                               "kind": "port", "sample": "1 tree step, same disk and host tree",
-                                               "phases_ms": cpu_phases}
-        except Exception as e:
-            out["p3t_step"] = {"error": repr(e)}
-    try:
-        v, sample, cores = cpu_reference(L, epj, P, budget_s=15.0)
-        out["cpu_baseline"] = {"value": v, "unit": "steps/s", "cores": cores, "kind": "port", "sample": sample}
-    except Exception as e:  # the oracle is test infrastructure; report, do not fail the GPU line
-        out["cpu_baseline"] = {"value": None, "unit": "steps/s", "cores": 0, "kind": "port", "sample": str(e)}
+            cpu_s, cpu_ph = cpu_step_baseline(disk, PP(n_group_limit=256), steps=2)
+            out["cpu_baseline"] = {"value": 1.0 / cpu_s, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
+                                   "sample": "2 whole tree steps of the same disk (start-up untimed), GPLUM's "
+                                             "arithmetic restated in oracle/ with the project's host tree",
+                                   "phases_ms": cpu_ph}
+        except Exception as e:  # the oracle is test infrastructure: report, do not fail the line
+            out["cpu_baseline"] = {"value": None, "unit": "steps/s", "cores": 0, "kind": "port", "sample": repr(e)}
+        for key, fn in (("soft_pass", lambda: soft_pass()),
+                        ("embryo_1000_learned", lambda: long_run("embryos", 1000, a_frag=0.5)),
+                        ("embryo_1000_size", lambda: long_run("embryos", 1000, schedule="size", a_frag=0.5)),
+                        ("disk8m_200_mixed", lambda: long_run("disk8m", 200)),
+                        ("disk8m_20_plain_fp64", lambda: long_run("disk8m", 20, form="plain"))):
+            if args.only_extra and key not in args.only_extra:
+                continue
+            try:
+                out[key] = fn()
+            except Exception as e:
+                out[key] = {"error": repr(e)}
     print(json.dumps(out), flush=True)
 
 
@@ -452,18 +637,19 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--skip-step", action="store_true", help="skip the whole-step measurement")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the CPU baseline, the soft pass alone, the embryo and the large-disk runs")
+    ap.add_argument("--only-extra", nargs="*", default=None, help="run only these extras")
     ap.add_argument("--step-only", type=int, default=0, metavar="N",
-                    help="only run one whole device step on the N-body hard-part disk and print its phases "
+                    help="start-up and one timed step of the mixed form on the N-body disk, phases printed "
                          "(a small case for profiling the step's kernels)")
-    ap.add_argument("--hard-mode", type=int, default=0, choices=[0, 1],
-                    help="with --step-only: 0 bundled hard launch (default), 1 one cluster per thread/warp/CTA")
     args = ap.parse_args()
     if args.step_only:
-        print(json.dumps(p3t_step_measure(0, steps=1, n=args.step_only, hard_mode=args.hard_mode,
-                                          learned=args.hard_mode == 0)))
+        from gplum_gb300.disk import P3TParams, disk_1m_hard
+        _, r = run_form("mixed", P3TParams(n_group_limit=256), disk_1m_hard(args.step_only), 1, 1, 1)
+        print(json.dumps(r))
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

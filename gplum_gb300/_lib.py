@@ -93,7 +93,23 @@ SIGNATURES = {
     "p3t_energy": (I, [VP]),
     "p3t_merge": (I, [VP]),
     "p3t_soft_force_noalloc": (I, [I, VP, I, VP, VP, VP, VP, VP, VP, VP, I, D, I, VP, VP]),
+    "p3t_startup": (I, [VP, VP]),
+    "p3t_tree_step": (I, [I, VP]),
+    "p3t_step_phases_ms": (I, [VP]),
+    "p3t_state_put_fpgrav": (I, [I, VP, ctypes.c_longlong]),
+    "p3t_state_get_fpgrav": (I, [VP, I]),
+    "p3t_set_hard_step_cap": (I, [I]),
+    "p3t_hard_launch_stats": (I, [VP, VP, VP]),
+    "p3t_launch_count": (ctypes.c_ulonglong, []),
 }
+
+# include/gplum_p3t.h: kernel status bits of the entry points that return a count
+COUNT_STATUS_BASE = 65536
+
+
+def status_bits(r):
+    """The kernel status bits a count-returning entry point reported (0 if none)."""
+    return -r - COUNT_STATUS_BASE if r <= -COUNT_STATUS_BASE else 0
 
 
 def lib_path():

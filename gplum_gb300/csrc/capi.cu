@@ -72,6 +72,27 @@ int grow_host(void **p, size_t *cap, size_t bytes) {
     return 0;
 }
 
+int check_csr(int n_group, const int *off) {
+    if (n_group < 0) return ST_BAD_INDEX;
+    if (n_group == 0) return (off && off[0] != 0) ? ST_BAD_INDEX : 0;
+    if (!off || off[0] != 0) return ST_BAD_INDEX;
+    for (int g = 0; g < n_group; g++)
+        if (off[g + 1] < off[g]) return ST_BAD_INDEX;
+    return 0;
+}
+
+int check_lists(int n_group, const int *i_off, const int *i_idx, const int *j_off, const int *j_idx,
+                const int *s_off, const int *s_idx, const void *spj, int n_spj) {
+    int r = 0;
+    if (n_spj < 0 || (n_spj > 0 && !spj)) return ST_BAD_INDEX;
+    if ((r = check_csr(n_group, i_off)) || (r = check_csr(n_group, j_off)) || (r = check_csr(n_group, s_off)))
+        return r;
+    if (n_group == 0) return 0;
+    if ((i_off[n_group] > 0 && !i_idx) || (j_off[n_group] > 0 && !j_idx) || (s_off[n_group] > 0 && !s_idx))
+        return ST_BAD_INDEX;
+    return 0;
+}
+
 int read_status(Context *c) {
     int h = 0;
     cudaError_t e = cudaMemcpyAsync(&h, c->status, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
@@ -224,7 +245,14 @@ using namespace p3t;
     Context *c = ctx_get(0);              \
     if (!c) return -(int)cudaErrorNoDevice;
 
+namespace p3t {
+unsigned long long g_launch_count = 0;
+int g_soft_shape[4] = {128, 64, 32, 5};
+}
+
 extern "C" {
+
+unsigned long long p3t_launch_count(void) { return __atomic_load_n(&p3t::g_launch_count, __ATOMIC_RELAXED); }
 
 int p3t_init(int device) {
     Context *c = ctx_get(device);
@@ -255,16 +283,16 @@ int p3t_set_soft_tiles(int t_ipt2, int t_s1, int t_s2) {
     CTX_OR_FAIL(c);
     if (t_s2 < 0 || t_s2 > 32 || t_s1 < t_s2 || t_s1 > 64 || t_ipt2 < t_s1 || (t_ipt2 > 128 && t_ipt2 != 256))
         return ST_BAD_INDEX;
-    c->tiles[0] = t_ipt2;
-    c->tiles[1] = t_s1;
-    c->tiles[2] = t_s2;
+    c->tiles[0] = g_soft_shape[0] = t_ipt2;
+    c->tiles[1] = g_soft_shape[1] = t_s1;
+    c->tiles[2] = g_soft_shape[2] = t_s2;
     return 0;
 }
 
 int p3t_set_soft_occupancy(int ctas_per_sm) {
     CTX_OR_FAIL(c);
     if (ctas_per_sm < 4 || ctas_per_sm > 6) return ST_BAD_INDEX;
-    c->soft_occ = ctas_per_sm;
+    c->soft_occ = g_soft_shape[3] = ctas_per_sm;
     return 0;
 }
 
@@ -294,8 +322,8 @@ int p3t_status(void) {
 
 // ---- device-resident soft force ---------------------------------------------
 int p3t_upload_particles(int n, const void *epj) {
-    CTX_OR_FAIL(c);
     if (n < 0 || (n > 0 && !epj)) return ST_BAD_INDEX;
+    CTX_OR_FAIL(c);
     DevSet &d = c->res;
     int r = 0;
     if ((r = d.epj_stage.reserve(n)) || (r = d.ptcl.reserve(n)) || (r = d.mass.reserve(n)) ||
@@ -311,8 +339,8 @@ int p3t_upload_particles(int n, const void *epj) {
 
 int p3t_upload_lists(int n_group, const int *i_off, const int *i_idx, const int *j_off, const int *j_idx,
                      const int *s_off, const int *s_idx, const void *spj, int n_spj) {
+    if (const int e = check_lists(n_group, i_off, i_idx, j_off, j_idx, s_off, s_idx, spj, n_spj)) return e;
     CTX_OR_FAIL(c);
-    if (n_group < 0 || n_spj < 0) return ST_BAD_INDEX;
     DevSet &d = c->res;
     const long long ni = n_group ? i_off[n_group] : 0, nj = n_group ? j_off[n_group] : 0,
                     ns = n_group ? s_off[n_group] : 0;
@@ -375,10 +403,9 @@ int p3t_download_forces(void *force, int n) {
 int p3t_soft_force_host(int n, const void *epj, int n_group, const int *i_off, const int *i_idx, const int *j_off,
                         const int *j_idx, const int *s_off, const int *s_idx, const void *spj, int n_spj,
                         void *force) {
+    if (n < 0 || (n > 0 && (!epj || !force))) return ST_BAD_INDEX;
+    if (const int e = check_lists(n_group, i_off, i_idx, j_off, j_idx, s_off, s_idx, spj, n_spj)) return e;
     CTX_OR_FAIL(c);
-    if (n < 0 || n_group < 0 || n_spj < 0 || (n > 0 && (!epj || !force)) ||
-        (n_group > 0 && (!i_off || !j_off || !s_off)))
-        return ST_BAD_INDEX;
     DevSet &d = c->res;
     const long long ni = n_group ? i_off[n_group] : 0, nj = n_group ? j_off[n_group] : 0,
                     ns = n_group ? s_off[n_group] : 0;

@@ -630,10 +630,10 @@ static int radix_sort(Context *c, DTree &T, unsigned long long *&key, int *&idx,
     int r = 0;
     if ((r = T.hist.reserve(256 * (size_t)nblk)) || (r = T.hoff.reserve(256 * (size_t)nblk + 1))) return r;
     for (int shift = 0; shift < bits; shift += 8) {
-        k_radix_hist<<<nblk, 256, 0, c->stream>>>(key, n, shift, nblk, T.hist.p);
+        { P3T_COUNT_LAUNCH(); k_radix_hist<<<nblk, 256, 0, c->stream>>>(key, n, shift, nblk, T.hist.p); }
         int tot = 0;
         if ((r = g_eng.scan(T.hist.p, T.hoff.p, 256 * nblk, &tot))) return r;
-        k_radix_scatter<<<nblk, 256, 0, c->stream>>>(key, idx, n, shift, nblk, T.hoff.p, key2, idx2);
+        { P3T_COUNT_LAUNCH(); k_radix_scatter<<<nblk, 256, 0, c->stream>>>(key, idx, n, shift, nblk, T.hoff.p, key2, idx2); }
         std::swap(key, key2);
         std::swap(idx, idx2);
     }
@@ -686,28 +686,28 @@ static int device_tree(Context *c, double theta, int n_leaf_limit, int n_group_l
         (r = T.gmark.reserve(n)) || (r = T.gflag.reserve(n)) || (r = T.gpos.reserve(n)))
         return r;
     // 1. root cube, keys, sort
-    k_bbox_partial<<<pb, 256, 0, c->stream>>>(E.S.pos, n, T.part.p);
-    k_bbox_root<<<1, 256, 0, c->stream>>>(T.part.p, pb, T.root.p);
-    k_keys<<<nblocks(n), 256, 0, c->stream>>>(E.S.pos, n, T.root.p, T.key.p, T.idx.p);
+    { P3T_COUNT_LAUNCH(); k_bbox_partial<<<pb, 256, 0, c->stream>>>(E.S.pos, n, T.part.p); }
+    { P3T_COUNT_LAUNCH(); k_bbox_root<<<1, 256, 0, c->stream>>>(T.part.p, pb, T.root.p); }
+    { P3T_COUNT_LAUNCH(); k_keys<<<nblocks(n), 256, 0, c->stream>>>(E.S.pos, n, T.root.p, T.key.p, T.idx.p); }
     unsigned long long *key = T.key.p, *key2 = T.key2.p;
     int *idx = T.idx.p, *idx2 = T.idx2.p;
     if ((r = radix_sort(c, T, key, idx, key2, idx2, n, 64))) return r;  // 8 passes: back in T.key / T.idx
     // 2. levels
     if ((r = grow_nodes(c, T, (size_t)n / 4 + 1024))) return r;
-    k_root_node<<<nblocks(n), 256, 0, c->stream>>>(T.nd.p, T.parent.p, T.root.p, n, limit, T.enode.p);
+    { P3T_COUNT_LAUNCH(); k_root_node<<<nblocks(n), 256, 0, c->stream>>>(T.nd.p, T.parent.p, T.root.p, n, limit, T.enode.p); }
     T.level_start.assign(1, 0);
     int base = 1;
     int *en = T.enode.p, *en2 = T.enode2.p;
     for (int level = 0; level < 21; level++) {
-        k_lvl_heads<<<nblocks(n), 256, 0, c->stream>>>(key, en, T.nd.p, n, 3 * (20 - level), T.head.p);
+        { P3T_COUNT_LAUNCH(); k_lvl_heads<<<nblocks(n), 256, 0, c->stream>>>(key, en, T.nd.p, n, 3 * (20 - level), T.head.p); }
         int m = 0;
         if ((r = E.scan(T.head.p, T.hs.p, n, &m))) return r;
         if (m == 0) break;
         if ((r = grow_nodes(c, T, (size_t)base + m))) return r;
         T.level_start.push_back(base);
-        k_lvl_make<<<nblocks(n), 256, 0, c->stream>>>(en, T.head.p, T.hs.p, n, base, T.nd.p, T.parent.p, en2);
-        k_lvl_count<<<nblocks(m), 256, 0, c->stream>>>(base, m, T.nd.p, T.parent.p);
-        k_lvl_split<<<nblocks(n), 256, 0, c->stream>>>(n, level + 1, limit, T.nd.p, en2);
+        { P3T_COUNT_LAUNCH(); k_lvl_make<<<nblocks(n), 256, 0, c->stream>>>(en, T.head.p, T.hs.p, n, base, T.nd.p, T.parent.p, en2); }
+        { P3T_COUNT_LAUNCH(); k_lvl_count<<<nblocks(m), 256, 0, c->stream>>>(base, m, T.nd.p, T.parent.p); }
+        { P3T_COUNT_LAUNCH(); k_lvl_split<<<nblocks(n), 256, 0, c->stream>>>(n, level + 1, limit, T.nd.p, en2); }
         std::swap(en, en2);
         base += m;
     }
@@ -717,20 +717,20 @@ static int device_tree(Context *c, double theta, int n_leaf_limit, int n_group_l
     // 3. moments, deepest level first
     for (int L = (int)T.level_start.size() - 2; L >= 0; L--) {
         const int lo = T.level_start[L], hi = T.level_start[L + 1];
-        k_moments<<<nblocks(hi - lo, 128), 128, 0, c->stream>>>(lo, hi, T.nd.p, d.spj.p, idx, E.S.pos, E.S.mass,
-                                                                E.S.r_search);
+        { P3T_COUNT_LAUNCH(); k_moments<<<nblocks(hi - lo, 128), 128, 0, c->stream>>>(lo, hi, T.nd.p, d.spj.p, idx, E.S.pos, E.S.mass,
+                                                                E.S.r_search); }
     }
     // 4. groups in Morton order
     cudaMemsetAsync(T.gmark.p, 0, n * sizeof(int), c->stream);
-    k_group_mark<<<nblocks(base), 256, 0, c->stream>>>(base, T.nd.p, T.parent.p, n_group_limit, T.gmark.p);
-    k_group_flag<<<nblocks(n), 256, 0, c->stream>>>(T.gmark.p, n, T.gflag.p);
+    { P3T_COUNT_LAUNCH(); k_group_mark<<<nblocks(base), 256, 0, c->stream>>>(base, T.nd.p, T.parent.p, n_group_limit, T.gmark.p); }
+    { P3T_COUNT_LAUNCH(); k_group_flag<<<nblocks(n), 256, 0, c->stream>>>(T.gmark.p, n, T.gflag.p); }
     int ng = 0;
     if ((r = E.scan(T.gflag.p, T.gpos.p, n, &ng))) return r;
     T.n_groups = ng;
     if ((r = T.gnode.reserve(ng + 1)) || (r = d.i_off.reserve(ng + 1)) || (r = d.j_off.reserve(ng + 1)) ||
         (r = d.s_off.reserve(ng + 1)) || (r = d.i_idx.reserve(n)))
         return r;
-    k_group_fill<<<nblocks(n), 256, 0, c->stream>>>(T.gmark.p, T.gpos.p, n, ng, T.gnode.p, d.i_off.p);
+    { P3T_COUNT_LAUNCH(); k_group_fill<<<nblocks(n), 256, 0, c->stream>>>(T.gmark.p, T.gpos.p, n, ng, T.gnode.p, d.i_off.p); }
     cudaMemcpyAsync(d.i_idx.p, idx, n * sizeof(int), cudaMemcpyDeviceToDevice, c->stream);
     // 5. walks: the top levels in pre-order (host, from the node table), then
     // (group, top node) pairs: open tests, counts, offsets, entries
@@ -780,27 +780,27 @@ static int device_tree(Context *c, double theta, int n_leaf_limit, int n_group_l
         int *tflag = T.pc.p + 4 * np, *tpos = T.pc.p + 5 * np;
         const int wb = (int)std::min<long long>((np + 127) / 128, 1LL << 30);
         if ((r = T.nf.reserve(T.n_nodes))) return r;
-        k_node_f32<<<nblocks(T.n_nodes), 256, 0, c->stream>>>(T.nd.p, T.n_nodes, T.nf.p);
+        { P3T_COUNT_LAUNCH(); k_node_f32<<<nblocks(T.n_nodes), 256, 0, c->stream>>>(T.nd.p, T.n_nodes, T.nf.p); }
         const float th2f = (float)(theta * theta);
-        k_walk_open<<<wb, 128, 0, c->stream>>>(T.nd.p, T.nf.p, T.gnode.p, ng, top_d, ntop, theta * theta, th2f,
-                                               T.ostat.p);
-        k_walk_class<<<wb, 128, 0, c->stream>>>(T.nd.p, top_d, anc_d, lvl_d, np, ntop, depth, T.ostat.p, idx, 0, jc,
-                                                sc, tflag, nullptr, nullptr, nullptr, nullptr);
+        { P3T_COUNT_LAUNCH(); k_walk_open<<<wb, 128, 0, c->stream>>>(T.nd.p, T.nf.p, T.gnode.p, ng, top_d, ntop, theta * theta, th2f,
+                                               T.ostat.p); }
+        { P3T_COUNT_LAUNCH(); k_walk_class<<<wb, 128, 0, c->stream>>>(T.nd.p, top_d, anc_d, lvl_d, np, ntop, depth, T.ostat.p, idx, 0, jc,
+                                                sc, tflag, nullptr, nullptr, nullptr, nullptr); }
         int ntask = 0;
         if ((r = E.scan(tflag, tpos, (int)np, &ntask)) || (r = T.tasks.reserve(ntask + 1))) return r;
-        k_task_list<<<wb, 128, 0, c->stream>>>(tflag, tpos, np, T.tasks.p);
-        k_walk_tasks<<<nblocks(ntask, 128), 128, 0, c->stream>>>(T.nd.p, T.nf.p, T.gnode.p, top_d, ntop, T.tasks.p,
+        { P3T_COUNT_LAUNCH(); k_task_list<<<wb, 128, 0, c->stream>>>(tflag, tpos, np, T.tasks.p); }
+        { P3T_COUNT_LAUNCH(); k_walk_tasks<<<nblocks(ntask, 128), 128, 0, c->stream>>>(T.nd.p, T.nf.p, T.gnode.p, top_d, ntop, T.tasks.p,
                                                                  ntask, theta * theta, th2f, idx, 0, jc, sc, nullptr,
-                                                                 nullptr, nullptr, nullptr, c->status);
+                                                                 nullptr, nullptr, nullptr, c->status); }
         int nj = 0, ns = 0;
         if ((r = E.scan(jc, jo, (int)np, &nj)) || (r = E.scan(sc, so, (int)np, &ns))) return r;
-        k_walk_group_off<<<nblocks(ng + 1), 256, 0, c->stream>>>(jo, so, ng, ntop, nj, ns, d.j_off.p, d.s_off.p);
+        { P3T_COUNT_LAUNCH(); k_walk_group_off<<<nblocks(ng + 1), 256, 0, c->stream>>>(jo, so, ng, ntop, nj, ns, d.j_off.p, d.s_off.p); }
         if ((r = d.j_idx.reserve(nj)) || (r = d.s_idx.reserve(ns))) return r;
-        k_walk_class<<<wb, 128, 0, c->stream>>>(T.nd.p, top_d, anc_d, lvl_d, np, ntop, depth, T.ostat.p, idx, 1, jc,
-                                                sc, tflag, jo, so, d.j_idx.p, d.s_idx.p);
-        k_walk_tasks<<<nblocks(ntask, 128), 128, 0, c->stream>>>(T.nd.p, T.nf.p, T.gnode.p, top_d, ntop, T.tasks.p,
+        { P3T_COUNT_LAUNCH(); k_walk_class<<<wb, 128, 0, c->stream>>>(T.nd.p, top_d, anc_d, lvl_d, np, ntop, depth, T.ostat.p, idx, 1, jc,
+                                                sc, tflag, jo, so, d.j_idx.p, d.s_idx.p); }
+        { P3T_COUNT_LAUNCH(); k_walk_tasks<<<nblocks(ntask, 128), 128, 0, c->stream>>>(T.nd.p, T.nf.p, T.gnode.p, top_d, ntop, T.tasks.p,
                                                                  ntask, theta * theta, th2f, idx, 1, jc, sc, jo, so,
-                                                                 d.j_idx.p, d.s_idx.p, c->status);
+                                                                 d.j_idx.p, d.s_idx.p, c->status); }
     }
     // 6. the soft kernel's launch order (the bodies' key buffers and the
     // group-scan scratch are free by now)
@@ -808,7 +808,7 @@ static int device_tree(Context *c, double theta, int n_leaf_limit, int n_group_l
     if (ng > 0) {
         unsigned long long *k1 = T.key.p, *k2 = T.key2.p;
         int *i1 = T.gflag.p, *i2 = T.head.p;
-        k_group_weight<<<nblocks(ng), 256, 0, c->stream>>>(ng, d.i_off.p, d.j_off.p, d.s_off.p, k1, i1);
+        { P3T_COUNT_LAUNCH(); k_group_weight<<<nblocks(ng), 256, 0, c->stream>>>(ng, d.i_off.p, d.j_off.p, d.s_off.p, k1, i1); }
         if ((r = radix_sort(c, T, k1, i1, k2, i2, ng, 64))) return r;
         cudaMemcpyAsync(d.order.p, i1, ng * sizeof(int), cudaMemcpyDeviceToDevice, c->stream);
     }

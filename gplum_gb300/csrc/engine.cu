@@ -86,7 +86,7 @@ int Engine::scan(const int32_t *in, int32_t *out, int n, int32_t *total) {
         int32_t *bscan = tmp + blocks;
         tmp += 2 * blocks;
         lv.push_back({cur_in, cur_out, bsum, cn});
-        k_scan_block<<<blocks, 1024, 0, c->stream>>>(cur_in, cur_out, bsum, cn);
+        { P3T_COUNT_LAUNCH(); k_scan_block<<<blocks, 1024, 0, c->stream>>>(cur_in, cur_out, bsum, cn); }
         if (blocks <= 1) break;
         cur_in = bsum;
         cur_out = bscan;
@@ -94,7 +94,7 @@ int Engine::scan(const int32_t *in, int32_t *out, int n, int32_t *total) {
     }
     for (int L = (int)lv.size() - 2; L >= 0; L--) {
         const int blocks = (lv[L].n + 1023) / 1024;
-        k_scan_add<<<blocks, 1024, 0, c->stream>>>(lv[L].out, lv[L + 1].out, lv[L].n);
+        { P3T_COUNT_LAUNCH(); k_scan_add<<<blocks, 1024, 0, c->stream>>>(lv[L].out, lv[L + 1].out, lv[L].n); }
     }
     if (total) {
         // total = out[n-1] + in[n-1]
@@ -676,7 +676,7 @@ int soft_run_state() {
         int32_t *mx = g_eng.counters.p + 2;
         cudaMemsetAsync(mx, 0, sizeof(int32_t), c->stream);
         const int n = c->res_n;
-        k_max_number<<<(n + 255) / 256, 256, 0, c->stream>>>(c->res.force.p, n, mx);
+        { P3T_COUNT_LAUNCH(); k_max_number<<<(n + 255) / 256, 256, 0, c->stream>>>(c->res.force.p, n, mx); }
         int h = 0;
         if ((r = d2h(c, &h, mx, sizeof(int)))) return r;
         int cap = c->cand_cap;
@@ -756,8 +756,8 @@ int Engine::load(int n, const long long *id, const double *mass, const double *r
         cudaMemsetAsync(p, 0, (size_t)n * sizeof(double), c->stream);
     for (int32_t *p : {S.number, S.rank, S.n_cluster, S.dead, S.merged, S.nbr_n})
         cudaMemsetAsync(p, 0, (size_t)n * sizeof(int32_t), c->stream);
-    k_fill_i32<<<nb(n), 256, 0, c->stream>>>(S.id_max, n, -1);
-    k_fill_i32<<<nb(n), 256, 0, c->stream>>>(S.id_min, n, INT32_MAX_);
+    { P3T_COUNT_LAUNCH(); k_fill_i32<<<nb(n), 256, 0, c->stream>>>(S.id_max, n, -1); }
+    { P3T_COUNT_LAUNCH(); k_fill_i32<<<nb(n), 256, 0, c->stream>>>(S.id_min, n, INT32_MAX_); }
     cudaMemcpyAsync(S.id_cluster, S.id, n * sizeof(int64_t), cudaMemcpyDeviceToDevice, c->stream);
     n_clusters = 0;
     frag_lo = frag_hi = n;
@@ -773,7 +773,7 @@ int Engine::pack_soft() {
     if ((r = d.ptcl.reserve(S.n)) || (r = d.force.reserve(S.n)) || (r = d.acc64.reserve(S.n)) ||
         (r = d.mass.reserve(S.n)) || (r = d.r_out.reserve(S.n)) || (r = d.r_search.reserve(S.n)))
         return r;
-    k_pack_state<<<nb(S.n), 256, 0, c->stream>>>(S, d.ptcl.p);
+    { P3T_COUNT_LAUNCH(); k_pack_state<<<nb(S.n), 256, 0, c->stream>>>(S, d.ptcl.p); }
     cudaMemcpyAsync(d.mass.p, S.mass, S.n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
     cudaMemcpyAsync(d.r_out.p, S.r_out, S.n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
     cudaMemcpyAsync(d.r_search.p, S.r_search, S.n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
@@ -792,37 +792,37 @@ int Engine::correct(int initial) {
     const int cap = c->cand_cap;
     const ForceRec *F = c->res.force.p;
     const int32_t *cand = c->res.cand.p;
-    k_corr_list<false><<<nb(S.n, 128), 128, 0, c->stream>>>(S, F, cand, cap, pair_n.p, nullptr, nullptr, nullptr,
-                                                            c->status);
+    { P3T_COUNT_LAUNCH(); k_corr_list<false><<<nb(S.n, 128), 128, 0, c->stream>>>(S, F, cand, cap, pair_n.p, nullptr, nullptr, nullptr,
+                                                            c->status); }
     int32_t np = 0;
     if ((r = scan(pair_n.p, pair_base.p, S.n, &np))) return r;
     if ((r = pair_i.reserve(np)) || (r = pair_j.reserve(np)) || (r = pair_terms.reserve(np))) return r;
-    k_corr_list<true><<<nb(S.n, 128), 128, 0, c->stream>>>(S, F, cand, cap, nullptr, pair_base.p, pair_i.p,
-                                                           pair_j.p, c->status);
+    { P3T_COUNT_LAUNCH(); k_corr_list<true><<<nb(S.n, 128), 128, 0, c->stream>>>(S, F, cand, cap, nullptr, pair_base.p, pair_i.p,
+                                                           pair_j.p, c->status); }
     if (np > 0) {
         if (initial)
-            k_corr_pairs<true><<<nb(np, 128), 128, 0, c->stream>>>(S, P, np, pair_i.p, pair_j.p, pair_terms.p);
+            { P3T_COUNT_LAUNCH(); k_corr_pairs<true><<<nb(np, 128), 128, 0, c->stream>>>(S, P, np, pair_i.p, pair_j.p, pair_terms.p); }
         else
-            k_corr_pairs<false><<<nb(np, 128), 128, 0, c->stream>>>(S, P, np, pair_i.p, pair_j.p, pair_terms.p);
+            { P3T_COUNT_LAUNCH(); k_corr_pairs<false><<<nb(np, 128), 128, 0, c->stream>>>(S, P, np, pair_i.p, pair_j.p, pair_terms.p); }
     }
     if (initial)
-        k_correct<true><<<nb(S.n, 128), 128, 0, c->stream>>>(S, P, F, cap, pair_base.p, pair_n.p, pair_j.p,
-                                                             pair_terms.p, counters.p, c->status);
+        { P3T_COUNT_LAUNCH(); k_correct<true><<<nb(S.n, 128), 128, 0, c->stream>>>(S, P, F, cap, pair_base.p, pair_n.p, pair_j.p,
+                                                             pair_terms.p, counters.p, c->status); }
     else
-        k_correct<false><<<nb(S.n, 128), 128, 0, c->stream>>>(S, P, F, cap, pair_base.p, pair_n.p, pair_j.p,
-                                                              pair_terms.p, counters.p, c->status);
-    if (initial) k_copy3<<<nb(3 * S.n), 256, 0, c->stream>>>(S.acc_d, S.acc_d_new, S.n);
+        { P3T_COUNT_LAUNCH(); k_correct<false><<<nb(S.n, 128), 128, 0, c->stream>>>(S, P, F, cap, pair_base.p, pair_n.p, pair_j.p,
+                                                              pair_terms.p, counters.p, c->status); }
+    if (initial) { P3T_COUNT_LAUNCH(); k_copy3<<<nb(3 * S.n), 256, 0, c->stream>>>(S.acc_d, S.acc_d_new, S.n); }
     return cuda_status(cudaGetLastError());
 }
 
 int Engine::cluster() {
     int r = cmin.reserve(S.n);
     if (r) return r;
-    k_iota<<<nb(S.n), 256, 0, c->stream>>>(S.label, S.n);
-    k_fill_i64<<<nb(S.n), 256, 0, c->stream>>>(cmin.p, S.n, (int64_t)0x7fffffffffffffffLL);
-    k_union<<<nb(S.n), 256, 0, c->stream>>>(S, c->cand_cap, c->status);
-    k_compress<<<nb(S.n), 256, 0, c->stream>>>(S, cmin.p);
-    k_apply_label<<<nb(S.n), 256, 0, c->stream>>>(S, cmin.p);
+    { P3T_COUNT_LAUNCH(); k_iota<<<nb(S.n), 256, 0, c->stream>>>(S.label, S.n); }
+    { P3T_COUNT_LAUNCH(); k_fill_i64<<<nb(S.n), 256, 0, c->stream>>>(cmin.p, S.n, (int64_t)0x7fffffffffffffffLL); }
+    { P3T_COUNT_LAUNCH(); k_union<<<nb(S.n), 256, 0, c->stream>>>(S, c->cand_cap, c->status); }
+    { P3T_COUNT_LAUNCH(); k_compress<<<nb(S.n), 256, 0, c->stream>>>(S, cmin.p); }
+    { P3T_COUNT_LAUNCH(); k_apply_label<<<nb(S.n), 256, 0, c->stream>>>(S, cmin.p); }
     return cuda_status(cudaGetLastError());
 }
 
@@ -833,25 +833,25 @@ int Engine::make_list() {
         (r = cl_cnt.reserve(n + 1)) || (r = cl_off.reserve(n + 1)) || (r = cl_fill.reserve(n + 1)) ||
         (r = members_tmp.reserve(n)) || (r = members.reserve(n)))
         return r;
-    k_fill_i32<<<nb(n), 256, 0, c->stream>>>(head.p, n, 0x7fffffff);
-    k_head<<<nb(n), 256, 0, c->stream>>>(S, head.p);
-    k_head_flag<<<nb(n), 256, 0, c->stream>>>(S, head.p, flag.p);
+    { P3T_COUNT_LAUNCH(); k_fill_i32<<<nb(n), 256, 0, c->stream>>>(head.p, n, 0x7fffffff); }
+    { P3T_COUNT_LAUNCH(); k_head<<<nb(n), 256, 0, c->stream>>>(S, head.p); }
+    { P3T_COUNT_LAUNCH(); k_head_flag<<<nb(n), 256, 0, c->stream>>>(S, head.p, flag.p); }
     int32_t nc = 0;
     if ((r = scan(flag.p, cidx.p, n, &nc))) return r;
     n_clusters = nc;
     cudaMemsetAsync(cl_cnt.p, 0, (nc + 1) * sizeof(int32_t), c->stream);
     cudaMemsetAsync(cl_fill.p, 0, (nc + 1) * sizeof(int32_t), c->stream);
-    k_member_count<<<nb(n), 256, 0, c->stream>>>(S, head.p, cidx.p, cl_of.p, cl_cnt.p);
+    { P3T_COUNT_LAUNCH(); k_member_count<<<nb(n), 256, 0, c->stream>>>(S, head.p, cidx.p, cl_of.p, cl_cnt.p); }
     int32_t nm = 0;
     if (nc > 0 && (r = scan(cl_cnt.p, cl_off.p, nc, &nm))) return r;
     n_members = nm;
-    k_member_fill<<<nb(n), 256, 0, c->stream>>>(S, cl_of.p, cl_off.p, cl_fill.p, members_tmp.p);
-    if (nc > 0) k_member_sort<<<nb(nc * 32), 256, 0, c->stream>>>(nc, cl_off.p, cl_cnt.p, members_tmp.p, members.p);
+    { P3T_COUNT_LAUNCH(); k_member_fill<<<nb(n), 256, 0, c->stream>>>(S, cl_of.p, cl_off.p, cl_fill.p, members_tmp.p); }
+    if (nc > 0) { P3T_COUNT_LAUNCH(); k_member_sort<<<nb(nc * 32), 256, 0, c->stream>>>(nc, cl_off.p, cl_cnt.p, members_tmp.p, members.p); }
     return cuda_status(cudaGetLastError());
 }
 
 int Engine::kick() {
-    k_kick<<<nb(S.n), 256, 0, c->stream>>>(S, 0.5 * c->params[3]);
+    { P3T_COUNT_LAUNCH(); k_kick<<<nb(S.n), 256, 0, c->stream>>>(S, 0.5 * c->params[3]); }
     return cuda_status(cudaGetLastError());
 }
 
@@ -859,8 +859,8 @@ int Engine::energy(double *out5) {
     const int blocks = nb(S.n);
     int r = 0;
     if ((r = epart.reserve(4 * (size_t)blocks + 8))) return r;
-    k_energy_partial<<<blocks, 256, 0, c->stream>>>(S, epart.p);
-    k_energy_final<<<1, 256, 0, c->stream>>>(epart.p, blocks, epart.p + 4 * blocks);
+    { P3T_COUNT_LAUNCH(); k_energy_partial<<<blocks, 256, 0, c->stream>>>(S, epart.p); }
+    { P3T_COUNT_LAUNCH(); k_energy_final<<<1, 256, 0, c->stream>>>(epart.p, blocks, epart.p + 4 * blocks); }
     cudaMemcpyAsync(out5, epart.p + 4 * blocks, 5 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
     return cuda_status(cudaStreamSynchronize(c->stream));
 }
@@ -875,7 +875,7 @@ int Engine::cutoff_radii() {
     int *cnt = icnt.p, *cntp = icnt.p + NBIN;
     const double init[2] = {0., 1.7976931348623157e308};
     cudaMemcpyAsync(mm, init, 2 * sizeof(double), cudaMemcpyHostToDevice, c->stream);
-    k_rminmax<<<nb(S.n), 256, 0, c->stream>>>(S, mm);
+    { P3T_COUNT_LAUNCH(); k_rminmax<<<nb(S.n), 256, 0, c->stream>>>(S, mm); }
     double h[2];
     cudaMemcpyAsync(h, mm, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
     if ((r = cuda_status(cudaStreamSynchronize(c->stream)))) return r;
@@ -883,9 +883,9 @@ int Engine::cutoff_radii() {
     const double r_max = std::sqrt(h[0]) * 1.01;
     const double r_min = std::sqrt(h[1]) * 0.99;
     const double dr = (r_max - r_min) / NBIN, drinv = 1. / dr;
-    k_vdisp_partial<<<nblk, VD_T, 0, c->stream>>>(S, r_min, drinv, P.m_sun, part, cntp);
-    k_vdisp_bins<<<1, 32, 0, c->stream>>>(part, cntp, nblk, vd, cnt);
-    k_radii<<<nb(S.n), 256, 0, c->stream>>>(S, P, r_min, dr, drinv, vd, cnt);
+    { P3T_COUNT_LAUNCH(); k_vdisp_partial<<<nblk, VD_T, 0, c->stream>>>(S, r_min, drinv, P.m_sun, part, cntp); }
+    { P3T_COUNT_LAUNCH(); k_vdisp_bins<<<1, 32, 0, c->stream>>>(part, cntp, nblk, vd, cnt); }
+    { P3T_COUNT_LAUNCH(); k_radii<<<nb(S.n), 256, 0, c->stream>>>(S, P, r_min, dr, drinv, vd, cnt); }
     return cuda_status(cudaGetLastError());
 }
 
@@ -895,14 +895,14 @@ int Engine::merge(double *edisp) {
     if ((r = keep.reserve(n)) || (r = kpos.reserve(n)) || (r = et.reserve(2 * (size_t)n + 1)) ||
         (r = tflag.reserve(n)) || (r = tpos.reserve(n)))
         return r;
-    k_fill_i32<<<nb(n), 256, 0, c->stream>>>(keep.p, n, 1);
-    k_merge_targets<<<nb(n), 256, 0, c->stream>>>(S, cl_of.p, cl_off.p, cl_cnt.p, members.p, keep.p, et.p,
-                                                    tflag.p, frag_lo, frag_hi, frag_cl.p);
+    { P3T_COUNT_LAUNCH(); k_fill_i32<<<nb(n), 256, 0, c->stream>>>(keep.p, n, 1); }
+    { P3T_COUNT_LAUNCH(); k_merge_targets<<<nb(n), 256, 0, c->stream>>>(S, cl_of.p, cl_off.p, cl_cnt.p, members.p, keep.p, et.p,
+                                                    tflag.p, frag_lo, frag_hi, frag_cl.p); }
     int32_t nt = 0;
     if ((r = scan(tflag.p, tpos.p, n, &nt))) return r;
     double *tl = et.p + n;
-    k_gather_targets<<<nb(n), 256, 0, c->stream>>>(et.p, tflag.p, tpos.p, n, tl);
-    k_sum_ordered<<<1, 32, 0, c->stream>>>(tl, nt, et.p + 2 * (size_t)n);
+    { P3T_COUNT_LAUNCH(); k_gather_targets<<<nb(n), 256, 0, c->stream>>>(et.p, tflag.p, tpos.p, n, tl); }
+    { P3T_COUNT_LAUNCH(); k_sum_ordered<<<1, 32, 0, c->stream>>>(tl, nt, et.p + 2 * (size_t)n); }
     double e = 0.;
     cudaMemcpyAsync(&e, et.p + 2 * (size_t)n, sizeof(double), cudaMemcpyDeviceToHost, c->stream);
     int32_t nk = 0;
@@ -922,7 +922,7 @@ int Engine::compact(int n, int nk) {
         using T2 = std::remove_pointer_t<decltype(fld)>;
         T2 *tmp = (T2 *)compact_tmp.p;
         cudaMemcpyAsync(tmp, fld, (size_t)n * w * sizeof(T2), cudaMemcpyDeviceToDevice, c->stream);
-        k_compact<T2><<<nb(n), 256, 0, c->stream>>>(tmp, fld, keep.p, kpos.p, n, w);
+        { P3T_COUNT_LAUNCH(); k_compact<T2><<<nb(n), 256, 0, c->stream>>>(tmp, fld, keep.p, kpos.p, n, w); }
         return cuda_status(cudaGetLastError());
     };
     for (double *f : {S.mass, S.r_planet, S.f, S.phi, S.phi_d, S.phi_s, S.r_out, S.r_out_inv, S.r_search, S.v_disp,
@@ -984,15 +984,15 @@ int Engine::remove(double r_max, double r_min, double *edisp, int *n_removed) {
     if ((r = keep.reserve(n)) || (r = kpos.reserve(n)) || (r = tflag.reserve(n)) || (r = tpos.reserve(n)) ||
         (r = et.reserve(2)))
         return r;
-    k_remove_flag<<<nb(n), 256, 0, c->stream>>>(S, r_max * r_max, r_min * r_min, keep.p, tflag.p);
+    { P3T_COUNT_LAUNCH(); k_remove_flag<<<nb(n), 256, 0, c->stream>>>(S, r_max * r_max, r_min * r_min, keep.p, tflag.p); }
     int32_t nr = 0;
     if ((r = scan(tflag.p, tpos.p, n, &nr))) return r;
     *n_removed = nr;
     *edisp = 0.;
     if (nr == 0) return 0;
     if ((r = members_tmp.reserve(std::max(n, nr)))) return r;
-    k_remove_list<<<nb(n), 256, 0, c->stream>>>(tflag.p, tpos.p, n, members_tmp.p);
-    k_remove_energy<<<1, 32, 0, c->stream>>>(S, params(), members_tmp.p, nr, et.p);
+    { P3T_COUNT_LAUNCH(); k_remove_list<<<nb(n), 256, 0, c->stream>>>(tflag.p, tpos.p, n, members_tmp.p); }
+    { P3T_COUNT_LAUNCH(); k_remove_energy<<<1, 32, 0, c->stream>>>(S, params(), members_tmp.p, nr, et.p); }
     if ((r = d2h(c, edisp, et.p, sizeof(double)))) return r;
     int32_t nk = 0;
     if ((r = scan(keep.p, kpos.p, n, &nk))) return r;
@@ -1166,6 +1166,7 @@ int p3t_remove_out_of_boundary(double r_max, double r_min, double *edisp) {
     if (!g_eng.c) return -(int)cudaErrorNoDevice;
     int nr = 0;
     int r = g_eng.remove(r_max, r_min, edisp, &nr);
+    if (r > 0) return P3T_COUNT_STATUS(r);
     return r ? r : nr;
 }
 

@@ -99,6 +99,8 @@ struct HardArgs {
     int32_t *n_frags;    // fragments made so far
     int frag_base, frag_cap;  // hard slots frag_base + k hold fragment k
     int wide;                 // bundle form: clusters above BCAP_MAIN in k_hard_wide (1) or run_cluster (0)
+    int max_steps;            // block steps a cluster may take in one tree step (ST_ITER_CAP beyond)
+    unsigned long long *live; // optional [2]: pair terms evaluated (predicted/corrected, full), bundle form
 };
 
 // ---- FPHard::predict / correct / calcDeltat, src/particle.h:1183-1314 ----
@@ -712,7 +714,7 @@ __device__ void run_cluster(const HardArgs &A, int c, const Team<TEAM> &tm) {
     int steps = 0;
     long long work = 0;
     while (time < A.t_end) {
-        if (++steps > MAX_BLOCK_STEPS) {
+        if (++steps > A.max_steps) {
             if (rank == 0) atomicOr(A.status, ST_ITER_CAP);
             break;
         }
@@ -1180,6 +1182,7 @@ struct HardBufs {
     DevBuf<FragRec> frags;
     DevBuf<int32_t> n_frags, fgslot, fidx;
     DevBuf<long long> fmap;
+    DevBuf<unsigned long long> live;  // [2] pair terms evaluated by the last launch
     Hard H;
     int cap = 0;
     int reserve(int m) {
@@ -1222,6 +1225,45 @@ static int g_wide = 0;        // clusters above the bundle capacity: wide lone b
 static int g_bcap = 256, g_bocc = 2;  // bundle member slots and CTAs per SM (256/2, 128/3, 128/4)
 static FragParams g_frag = {0., 9.426627927538057e-12, 10, 0, 0ULL};  // off (a_frag = 0)
 static int g_frag_cap = 0;  // fragment slots of the current launch
+static int g_max_steps = MAX_BLOCK_STEPS;  // block-step cap per cluster and tree step
+// events around the last cluster launch (k_hard_bundles / k_hard_clusters) on
+// the library stream, and whether they hold a launch
+static cudaEvent_t g_ev_launch[2] = {nullptr, nullptr};
+static bool g_launch_timed = false;
+static int g_last_nc = 0;  // clusters of the last launch (its cost log and sizes stay valid until the next)
+
+// Sums over the last launch's clusters: {sum of active x member pair sweeps,
+// sum of n (n - 1) x block steps, sum of sweeps / n (active members over block
+// steps), largest block-step count, sum of n x block steps (predictions)};
+// one block.
+__global__ void k_cost_sums(const long long *__restrict__ cost, const int32_t *__restrict__ cnt, int nc,
+                            double *out) {
+    __shared__ double s0[512], s1[512], s2[512], s3[512], s4[512];
+    double a = 0., b = 0., d = 0., m = 0., e = 0.;
+    for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+        const double st = (double)cost[2 * c], w = (double)cost[2 * c + 1], n = (double)max(cnt[c], 1);
+        a += w;
+        b += n * (n - 1.) * st;
+        d += w / n;
+        m = fmax(m, st);
+        e += n * st;
+    }
+    s0[threadIdx.x] = a; s1[threadIdx.x] = b; s2[threadIdx.x] = d; s3[threadIdx.x] = m; s4[threadIdx.x] = e;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            s0[threadIdx.x] += s0[threadIdx.x + o];
+            s1[threadIdx.x] += s1[threadIdx.x + o];
+            s2[threadIdx.x] += s2[threadIdx.x + o];
+            s3[threadIdx.x] = fmax(s3[threadIdx.x], s3[threadIdx.x + o]);
+            s4[threadIdx.x] += s4[threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[0] = s0[0]; out[1] = s1[0]; out[2] = s2[0]; out[3] = s3[0]; out[4] = s4[0];
+    }
+}
 
 // Fragments made by a launch join the particle system (addFragment2ParticleSystem,
 // src/hard.h:858-943): the r-th new body is the fragment in hard slot
@@ -1363,9 +1405,11 @@ int p3t_hard_enqueue(void) {
     g_frag_cap = (g_frag.a_frag > 0.) ? std::max(1024, g_frag.n_frag_max * 4096) : 0;
     if ((r = B.reserve(E.n_members + g_frag_cap)) || (r = B.order.reserve(nc)) || (r = B.queue.reserve(3)) ||
         (r = B.n_cols.reserve(1)) || (r = B.cl_edisp.reserve(2 * (size_t)nc + 2)) ||
-        (r = B.cols.reserve(4096)) || (r = B.frags.reserve(g_frag_cap + 1)) || (r = B.n_frags.reserve(1)))
+        (r = B.cols.reserve(4096)) || (r = B.frags.reserve(g_frag_cap + 1)) || (r = B.n_frags.reserve(1)) ||
+        (r = B.live.reserve(2)))
         return r;
     cudaMemsetAsync(B.n_frags.p, 0, sizeof(int32_t), c->stream);
+    cudaMemsetAsync(B.live.p, 0, 2 * sizeof(unsigned long long), c->stream);
     // schedule, on the device: clusters binned by tier (bundle mode: above
     // the bundle capacity first; tier mode: CTA >= g_cta_min > warp >=
     // g_warp_min > thread), then by priority (the caller's, the learned cost
@@ -1389,11 +1433,11 @@ int p3t_hard_enqueue(void) {
         int heavy_key = 2147483647;
         if (prio && (int)g_prio.size() != nc && g_heavy > 0.f)
             heavy_key = std::min(ORDER_NB - 1, (int)((g_heavy - pmin) * pscale));
-        k_order_bins<<<(nc + 255) / 256, 256, 0, c->stream>>>(E.cl_cnt.p, prio, nc, g_hard_mode, g_bcap, g_warp_min, g_cta_min,
+        { P3T_COUNT_LAUNCH(); k_order_bins<<<(nc + 255) / 256, 256, 0, c->stream>>>(E.cl_cnt.p, prio, nc, g_hard_mode, g_bcap, g_warp_min, g_cta_min,
                                                               pmin, pscale, heavy_key, B.bin.p, B.hist.p,
-                                                              B.ntier.p + 3);
-        k_order_scan<<<1, 1024, 0, c->stream>>>(B.hist.p, B.ntier.p);
-        k_order_scatter<<<(nc + 255) / 256, 256, 0, c->stream>>>(B.bin.p, nc, B.hist.p, B.order.p);
+                                                              B.ntier.p + 3); }
+        { P3T_COUNT_LAUNCH(); k_order_scan<<<1, 1024, 0, c->stream>>>(B.hist.p, B.ntier.p); }
+        { P3T_COUNT_LAUNCH(); k_order_scatter<<<(nc + 255) / 256, 256, 0, c->stream>>>(B.bin.p, nc, B.hist.p, B.order.p); }
         if ((r = cuda_status(cudaGetLastError()))) return r;
     }
     g_prio.clear();
@@ -1415,6 +1459,8 @@ int p3t_hard_integrate(int istep) {
     const int nc = E.n_clusters;
     if (g_enqueued != nc) return ST_BAD_INDEX;
     g_enqueued = -1;
+    g_launch_timed = false;
+    g_last_nc = nc;
     int r = 0;
     const Params P = E.params();
     if (nc > 0) {
@@ -1444,6 +1490,12 @@ int p3t_hard_integrate(int istep) {
         A.frag_base = E.n_members;
         A.frag_cap = g_frag_cap;
         A.wide = g_wide;
+        A.max_steps = g_max_steps;
+        A.live = B.live.p;
+        if (!g_ev_launch[0] && ((r = cuda_status(cudaEventCreate(&g_ev_launch[0]))) ||
+                                (r = cuda_status(cudaEventCreate(&g_ev_launch[1])))))
+            return r;
+        g_launch_timed = false;
         int sms = 152;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
         if (g_hard_mode == 0) {
@@ -1477,24 +1529,30 @@ int p3t_hard_integrate(int istep) {
                 if ((r = cuda_status(cudaEventRecord(ev_ready, c->stream))) ||
                     (r = cuda_status(cudaStreamWaitEvent(s_wide, ev_ready, 0))))
                     return r;
-                k_hard_wide<<<std::max(1, sms / 16), BT, smem_w, s_wide>>>(A);
+                { P3T_COUNT_LAUNCH(); k_hard_wide<<<std::max(1, sms / 16), BT, smem_w, s_wide>>>(A); }
                 if ((r = cuda_status(cudaGetLastError()))) return r;
             }
             // persistent: g_bocc CTAs per SM (fewer when there are few clusters)
             const int blocks = std::max(1, std::min(sms * g_bocc, (nc + 3) / 4));
+            if ((r = cuda_status(cudaEventRecord(g_ev_launch[0], c->stream)))) return r;
             if (g_bcap == 256)
-                k_hard_bundles<256, 2><<<blocks, bundle_threads(256), smem, c->stream>>>(A);
+                { P3T_COUNT_LAUNCH(); k_hard_bundles<256, 2><<<blocks, bundle_threads(256), smem, c->stream>>>(A); }
             else if (g_bocc == 3)
-                k_hard_bundles<128, 3><<<blocks, BT, smem, c->stream>>>(A);
+                { P3T_COUNT_LAUNCH(); k_hard_bundles<128, 3><<<blocks, BT, smem, c->stream>>>(A); }
             else
-                k_hard_bundles<128, 4><<<blocks, BT, smem, c->stream>>>(A);
+                { P3T_COUNT_LAUNCH(); k_hard_bundles<128, 4><<<blocks, BT, smem, c->stream>>>(A); }
             if ((r = cuda_status(cudaGetLastError()))) return r;
+            if ((r = cuda_status(cudaEventRecord(g_ev_launch[1], c->stream)))) return r;
+            g_launch_timed = true;
             if (A.wide && ((r = cuda_status(cudaEventRecord(ev_done, s_wide))) ||
                            (r = cuda_status(cudaStreamWaitEvent(c->stream, ev_done, 0)))))
                 return r;
         } else {
             const int blocks = std::max(1, std::min(sms * 2, (nc + 3) / 4));
-            k_hard_clusters<<<blocks, 128, 0, c->stream>>>(A);
+            if ((r = cuda_status(cudaEventRecord(g_ev_launch[0], c->stream)))) return r;
+            { P3T_COUNT_LAUNCH(); k_hard_clusters<<<blocks, 128, 0, c->stream>>>(A); }
+            if ((r = cuda_status(cudaEventRecord(g_ev_launch[1], c->stream)))) return r;
+            g_launch_timed = true;
         }
         if ((r = cuda_status(cudaGetLastError()))) return r;
     }
@@ -1504,7 +1562,7 @@ int p3t_hard_integrate(int istep) {
     I.t0 = (istep - 1) * P.dt_tree;
     I.t1 = istep * P.dt_tree;
     I.status = c->status;
-    if (E.S.n > 0) k_isolated<<<(E.S.n + 127) / 128, 128, 0, c->stream>>>(I);
+    if (E.S.n > 0) { P3T_COUNT_LAUNCH(); k_isolated<<<(E.S.n + 127) / 128, 128, 0, c->stream>>>(I); }
     return cuda_status(cudaGetLastError());
 }
 
@@ -1597,9 +1655,9 @@ int p3t_hard_fetch(int col_cap, long long *col_pairs, double *edisp) {
         if ((r = h2d(c, B.fgslot.p, gs.data(), nfr * sizeof(int))) || (r = h2d(c, B.fidx.p, ord.data(), nfr * sizeof(int))) ||
             (map.size() && (r = h2d(c, B.fmap.p, map.data(), map.size() * sizeof(long long)))))
             return r;
-        k_frag_append<<<(nfr + 127) / 128, 128, 0, c->stream>>>(E.S, B.H, B.frags.p, B.fgslot.p, B.fidx.p, nfr, n0,
-                                                                B.fmap.p, nmap, E.frag_cl.p);
-        k_frag_ids<<<(n0 + 255) / 256, 256, 0, c->stream>>>(E.S, n0, B.fmap.p, nmap);
+        { P3T_COUNT_LAUNCH(); k_frag_append<<<(nfr + 127) / 128, 128, 0, c->stream>>>(E.S, B.H, B.frags.p, B.fgslot.p, B.fidx.p, nfr, n0,
+                                                                B.fmap.p, nmap, E.frag_cl.p); }
+        { P3T_COUNT_LAUNCH(); k_frag_ids<<<(n0 + 255) / 256, 256, 0, c->stream>>>(E.S, n0, B.fmap.p, nmap); }
         if ((r = cuda_status(cudaGetLastError()))) return r;
         E.S.n = n0 + nfr;
         E.frag_lo = n0;
@@ -1607,7 +1665,7 @@ int p3t_hard_fetch(int col_cap, long long *col_pairs, double *edisp) {
         if ((r = cuda_status(cudaStreamSynchronize(c->stream)))) return r;
     }
     int st = read_status(c);
-    if (st) return st;
+    if (st) return P3T_COUNT_STATUS(st);
     return ncol;
 }
 
@@ -1648,8 +1706,44 @@ int p3t_collisions_write(const char *path, int append) {
 
 int p3t_hard(int istep, int col_cap, long long *col_pairs, double *edisp) {
     int r = p3t_hard_enqueue();
-    if (r || (r = p3t_hard_integrate(istep))) return r;
+    if (r || (r = p3t_hard_integrate(istep))) return r > 0 ? P3T_COUNT_STATUS(r) : r;
     return p3t_hard_fetch(col_cap, col_pairs, edisp);
+}
+
+int p3t_set_hard_step_cap(int max_block_steps) {
+    if (max_block_steps < 1 || max_block_steps > MAX_BLOCK_STEPS) return -(int)cudaErrorInvalidValue;
+    g_max_steps = max_block_steps;
+    return 0;
+}
+
+int p3t_hard_launch_stats(double *launch_ms, long long *pairs3, double *sums5) {
+    Engine &E = g_eng;
+    if (!E.c) return -(int)cudaErrorNoDevice;
+    int r = 0;
+    if (launch_ms) {
+        float ms = 0.f;
+        if (g_launch_timed && (r = cuda_status(cudaEventSynchronize(g_ev_launch[1])))) return r;
+        if (g_launch_timed && (r = cuda_status(cudaEventElapsedTime(&ms, g_ev_launch[0], g_ev_launch[1])))) return r;
+        *launch_ms = g_launch_timed ? (double)ms : 0.;
+    }
+    if (pairs3) {
+        unsigned long long v[2] = {0ULL, 0ULL};
+        if (g_hb.live.p && (r = d2h(E.c, v, g_hb.live.p, sizeof(v)))) return r;
+        pairs3[0] = (long long)v[0];
+        pairs3[1] = (long long)v[1];
+        pairs3[2] = (g_hard_mode == 0) ? 1 : 0;  // counted by the bundle form only
+    }
+    if (sums5) {
+        double h[5] = {0., 0., 0., 0., 0.};
+        if (g_last_nc > 0 && g_hb.cost.p && E.cl_cnt.p) {
+            static DevBuf<double> buf;
+            if ((r = buf.reserve(5))) return r;
+            { P3T_COUNT_LAUNCH(); k_cost_sums<<<1, 512, 0, E.c->stream>>>(g_hb.cost.p, E.cl_cnt.p, g_last_nc, buf.p); }
+            if ((r = cuda_status(cudaGetLastError())) || (r = d2h(E.c, h, buf.p, sizeof h))) return r;
+        }
+        for (int k = 0; k < 5; k++) sums5[k] = h[k];
+    }
+    return 0;
 }
 
 }  // extern "C"

@@ -288,6 +288,7 @@ __device__ void bundle_pairs(const HardArgs &A, BundleSmem<BCAP> &B, int mode, i
     const float *xi32 = (mode == 1) ? B.xp32 : B.pos32;
     const float *xj32 = (mode == 0) ? B.pos32 : B.xp32;
     int ring_n = 0;
+    long long n_live = 0;
     for (int base = 0; base < total; base += BT) {
         const int f = base + tid;
         int live = 0, e = 0;
@@ -319,6 +320,7 @@ __device__ void bundle_pairs(const HardArgs &A, BundleSmem<BCAP> &B, int mode, i
         const int off = bscan<BT>(live, B.ws, cnt);
         if (live) B.ring[ring_n + off] = e;
         ring_n += cnt;
+        n_live += cnt;
         __syncthreads();
         if (ring_n >= BT) {
             bundle_drain(A.P, B, mode, BT);
@@ -329,6 +331,7 @@ __device__ void bundle_pairs(const HardArgs &A, BundleSmem<BCAP> &B, int mode, i
         }
     }
     if (ring_n > 0) bundle_drain(A.P, B, mode, ring_n);
+    if (A.live && tid == 0) atomicAdd(&A.live[mode == 0 ? 1 : 0], (unsigned long long)n_live);
 }
 
 // sun force and the accumulated pair sums of the targets to the state of
@@ -837,8 +840,8 @@ __device__ void bundle_step(const HardArgs &A, BundleSmem<BCAP> &B) {
     __syncthreads();
     FOR_CLUSTERS(k) {
         const double time = bitsd(B.c_key[k]);
-        if (time < A.t_end && B.c_steps[k] >= MAX_BLOCK_STEPS) atomicOr(A.status, ST_ITER_CAP);
-        if (!(time < A.t_end) || B.c_steps[k] >= MAX_BLOCK_STEPS) {
+        if (time < A.t_end && B.c_steps[k] >= A.max_steps) atomicOr(A.status, ST_ITER_CAP);
+        if (!(time < A.t_end) || B.c_steps[k] >= A.max_steps) {
             B.c_flags[k] |= CF_FIN;
             B.any = 1;
         }
@@ -1009,7 +1012,7 @@ __global__ void __launch_bounds__(BT, 1) k_hard_wide(HardArgs A) {
             bundle_finalize(A, B, 0, nt, 2);
         }
         // bundle_step advances the cluster by one block step; it retires when done
-        for (int it = 0; it < MAX_BLOCK_STEPS + 8; it++) {
+        for (int it = 0; it < A.max_steps + 8; it++) {
             bundle_step(A, B);
             if (B.any) bundle_retire(A, B);
             if (B.ncl == 0) break;

@@ -14,11 +14,14 @@
 // Those arrays exist once per GPU that loads this library and stay allocated
 // until the process exits (P3T_NOALLOC_MAX_BODIES x 80 B = 5 MiB,
 // P3T_NOALLOC_MAX_SPJ x 64 B = 4 MiB, plus one status word).  Their device addresses are looked up once per device, on
-// that device's first call (cudaGetSymbolAddress with the device current), so
-// the first call on a device should happen before any stream capture.  Every
-// call shares the arrays: calls that overlap on the GPU (different streams,
-// or several host threads) race on them and must be serialised by the
-// caller.
+// that device's first call (cudaGetSymbolAddress with the device current).
+// A call waits for its stream (it reads the status word back to the host), so
+// it cannot be made on a stream that is being captured into a CUDA graph.
+// Every call shares the arrays: calls that overlap on the GPU (different
+// streams, or several host threads) race on them and must be serialised by
+// the caller.  The caller's CSR offsets are checked on the device before any
+// list is read through them (status bit 2); list entries out of range are
+// clamped by the kernel and reported the same way.
 #include <cstdio>
 #include <mutex>
 
@@ -90,6 +93,20 @@ __global__ void k_noalloc_pack(const p3t::EPJRec *__restrict__ in, int n, p3t::S
     out[i] = r;
 }
 
+// The caller's CSR offsets, checked on the device before any list is read:
+// each starts at 0 and never decreases, and the i lists hold at most n
+// entries.  A violation sets status bit 2 (list index out of range).
+__global__ void k_noalloc_check(const int *__restrict__ i_off, const int *__restrict__ j_off,
+                                const int *__restrict__ s_off, int n_group, int n, int *status) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g > n_group) return;
+    bool bad = false;
+    if (g == 0) bad = i_off[0] != 0 || j_off[0] != 0 || s_off[0] != 0;
+    else bad = i_off[g] < i_off[g - 1] || j_off[g] < j_off[g - 1] || s_off[g] < s_off[g - 1];
+    if (g == n_group) bad = bad || i_off[g] > n;
+    if (bad) atomicOr(status, p3t::ST_BAD_INDEX);
+}
+
 }  // namespace
 
 extern "C" int p3t_soft_force_noalloc(int n, const void *epj, int n_group, const int *i_off, const int *i_idx,
@@ -112,6 +129,9 @@ extern "C" int p3t_soft_force_noalloc(int n, const void *epj, int n_group, const
     }
     if (n_group < 0 || n_spj < 0 || (trace_mode != 0 && trace_mode != 1)) return -(int)cudaErrorInvalidValue;
     if (n == 0 || n_group == 0) return 0;
+    // every buffer the kernels will read or write must be there
+    if (!epj || !force || !i_off || !i_idx || !j_off || !j_idx || !s_off || !s_idx || (n_spj > 0 && !spj))
+        return -(int)cudaErrorInvalidValue;
     DeviceScratch *s = nullptr;
     int r = scratch_for_current_device(&s);
     if (r) return r;
@@ -119,7 +139,17 @@ extern "C" int p3t_soft_force_noalloc(int n, const void *epj, int n_group, const
     // the status word keeps the previous call's value: clear it
     cudaError_t e = cudaMemsetAsync(s->status, 0, sizeof(int), st);
     if (e != cudaSuccess) return -(int)e;
-    k_noalloc_pack<<<(n + 255) / 256, 256, 0, st>>>((const p3t::EPJRec *)epj, n, s->bodies);
+    // the offsets first: no list is read through a malformed one
+    { P3T_COUNT_LAUNCH(); k_noalloc_check<<<(n_group + 256) / 256, 256, 0, st>>>(i_off, j_off, s_off, n_group, n, s->status); }
+    if ((e = cudaGetLastError()) != cudaSuccess) return -(int)e;
+    {
+        int h = 0;
+        if ((e = cudaMemcpyAsync(&h, s->status, sizeof(int), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+            (e = cudaStreamSynchronize(st)) != cudaSuccess)
+            return -(int)e;
+        if (h) return h;
+    }
+    { P3T_COUNT_LAUNCH(); k_noalloc_pack<<<(n + 255) / 256, 256, 0, st>>>((const p3t::EPJRec *)epj, n, s->bodies); }
     if ((e = cudaGetLastError()) != cudaSuccess) return -(int)e;
     p3t::SoftArgs A{};
     A.i_off = i_off;
@@ -148,6 +178,11 @@ extern "C" int p3t_soft_force_noalloc(int n, const void *epj, int n_group, const
     A.jsplit = s->split;
     A.isplit = s->split;
     A.spjp = s->spj;
+    // the launch shape the setters chose (the same as the allocating path's)
+    A.t_ipt2 = p3t::g_soft_shape[0];
+    A.t_s1 = p3t::g_soft_shape[1];
+    A.t_s2 = p3t::g_soft_shape[2];
+    A.occ = p3t::g_soft_shape[3];
     if ((e = launch_soft(A, 0, false, st)) != cudaSuccess) return -(int)e;
     int h = 0;
     if ((e = cudaMemcpyAsync(&h, s->status, sizeof(int), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return -(int)e;

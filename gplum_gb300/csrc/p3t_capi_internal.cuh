@@ -108,6 +108,13 @@ struct Context {
 extern Context *g_ctx;
 Context *ctx_get(int device);
 int read_status(Context *c);
+// Host checks of caller lists before any copy or kernel: CSR offsets start at
+// 0 and never decrease; index arrays and records are present where the
+// offsets say there are entries.  ST_BAD_INDEX otherwise.  (GPLUM trusts
+// FDPS's lists; a C caller here can hand any pointer.)
+int check_csr(int n_group, const int *off);
+int check_lists(int n_group, const int *i_off, const int *i_idx, const int *j_off, const int *j_idx,
+                const int *s_off, const int *s_idx, const void *spj, int n_spj);
 // Async host->device copy; pinned sources go straight to the DMA engine,
 // pageable ones through the context's pinned staging buffer.
 int h2d(Context *c, void *dst, const void *src, size_t bytes);

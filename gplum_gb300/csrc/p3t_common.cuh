@@ -57,6 +57,11 @@ enum : int {
 
 constexpr int INT32_MAX_ = 2147483647;
 
+// Host-side count of the library's kernel launches (p3t_launch_count): every
+// <<<...>>> launch site of the library is preceded by P3T_COUNT_LAUNCH().
+extern unsigned long long g_launch_count;
+#define P3T_COUNT_LAUNCH() ((void)__atomic_fetch_add(&::p3t::g_launch_count, 1ULL, __ATOMIC_RELAXED))
+
 // 4 doubles, 16-byte aligned (the FP64 form's {ax, ay, az, phi} record)
 struct __align__(16) D4 {
     double x, y, z, w;

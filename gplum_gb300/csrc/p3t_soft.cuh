@@ -63,6 +63,11 @@ struct SoftArgs {
     SpjPack *spjp;
 };
 
+// The soft launch shape last set through p3t_set_soft_tiles /
+// p3t_set_soft_occupancy: {t_ipt2, t_s1, t_s2, occ}, process-wide, for entry
+// points that run without the library context (p3t_soft_force_noalloc).
+extern int g_soft_shape[4];
+
 cudaError_t launch_pack_epj(const EPJRec *in, int n, SoftPtcl *out, double *mass, double *r_out, double *r_search,
                             cudaStream_t st);
 cudaError_t launch_pack_epi(const EPIRec *in, int n, SoftPtcl *out, double *r_out, double *r_search, cudaStream_t st);

@@ -247,11 +247,11 @@ static int feature_rows(Context *c, int nc, float *X) {
     Sched &M = g_sched;
     int r = 0;
     if ((r = M.red.reserve(3 * (size_t)nc + 3))) return r;
-    k_feat_init<<<(nc + 255) / 256, 256, 0, c->stream>>>(nc, M.red.p);
+    { P3T_COUNT_LAUNCH(); k_feat_init<<<(nc + 255) / 256, 256, 0, c->stream>>>(nc, M.red.p); }
     if (E.S.n > 0)
-        k_feat_bodies<<<(E.S.n + 255) / 256, 256, 0, c->stream>>>(E.S, E.cl_of.p, E.cand_cap_alloc,
-                                                                    E.params().dt_tree, M.red.p);
-    k_feat_rows<<<(nc + 255) / 256, 256, 0, c->stream>>>(M.red.p, E.cl_cnt.p, nc, (float)E.params().dt_tree, X);
+        { P3T_COUNT_LAUNCH(); k_feat_bodies<<<(E.S.n + 255) / 256, 256, 0, c->stream>>>(E.S, E.cl_of.p, E.cand_cap_alloc,
+                                                                    E.params().dt_tree, M.red.p); }
+    { P3T_COUNT_LAUNCH(); k_feat_rows<<<(nc + 255) / 256, 256, 0, c->stream>>>(M.red.p, E.cl_cnt.p, nc, (float)E.params().dt_tree, X); }
     return cuda_status(cudaGetLastError());
 }
 
@@ -262,7 +262,7 @@ const float *sched_priority(Context *c, int nc, float *pmin, float *pscale) {
     if (M.mode != 1 || !M.ready || nc <= 0) return nullptr;
     if (M.X.reserve(4 * (size_t)nc) || M.pred.reserve(nc)) return nullptr;
     if (feature_rows(c, nc, M.X.p)) return nullptr;
-    k_mlp_predict<<<(nc + 127) / 128, 128, 0, c->stream>>>(M.P.p, M.norm_d.p, M.X.p, nc, M.pred.p);
+    { P3T_COUNT_LAUNCH(); k_mlp_predict<<<(nc + 127) / 128, 128, 0, c->stream>>>(M.P.p, M.norm_d.p, M.X.p, nc, M.pred.p); }
     if (cudaGetLastError() != cudaSuccess) return nullptr;
     *pmin = 0.f;  // predictions are log2(1 + block steps): 1/256 resolution
     *pscale = 256.f;
@@ -313,8 +313,8 @@ static int grad_launch(Context *c, int b0, int nb, const int *idx_dev, float *lo
     const int nblk = std::max(1, std::min((nb + GT - 1) / GT, sms * 4));
     int r = 0;
     if ((r = M.partial.reserve((size_t)nblk * MLP_NG)) || (r = M.g.reserve(MLP_NG))) return r;
-    k_mlp_grad<<<nblk, GT, 0, c->stream>>>(M.P.p, M.Xn.p, M.Yn.p, idx_dev, b0, nb, M.partial.p);
-    k_mlp_reduce<<<(MLP_NG + 255) / 256, 256, 0, c->stream>>>(M.partial.p, nblk, 1.f / (float)nb, M.g.p, loss_acc);
+    { P3T_COUNT_LAUNCH(); k_mlp_grad<<<nblk, GT, 0, c->stream>>>(M.P.p, M.Xn.p, M.Yn.p, idx_dev, b0, nb, M.partial.p); }
+    { P3T_COUNT_LAUNCH(); k_mlp_reduce<<<(MLP_NG + 255) / 256, 256, 0, c->stream>>>(M.partial.p, nblk, 1.f / (float)nb, M.g.p, loss_acc); }
     return cuda_status(cudaGetLastError());
 }
 
@@ -366,7 +366,7 @@ int p3t_mlp_predict(const float *x, int n, float *out) {
     int r = 0;
     if ((r = M.X.reserve(4 * (size_t)n)) || (r = M.pred.reserve(n))) return r;
     if ((r = h2d(c, M.X.p, x, 4 * (size_t)n * sizeof(float)))) return r;
-    k_mlp_predict<<<(n + 127) / 128, 128, 0, c->stream>>>(M.P.p, M.norm_d.p, M.X.p, n, M.pred.p);
+    { P3T_COUNT_LAUNCH(); k_mlp_predict<<<(n + 127) / 128, 128, 0, c->stream>>>(M.P.p, M.norm_d.p, M.X.p, n, M.pred.p); }
     if ((r = cuda_status(cudaGetLastError()))) return r;
     return d2h(c, out, M.pred.p, n * sizeof(float));
 }
@@ -431,8 +431,8 @@ int p3t_mlp_train(const float *x, const float *y, int n, int epochs, int batch, 
             if ((r = grad_launch(c, b0, nb, M.idx.p, M.loss.p))) return r;
             p1 *= b1;
             p2 *= b2;
-            k_mlp_adam<<<(MLP_NP + 255) / 256, 256, 0, c->stream>>>(M.P.p, M.g.p, M.m.p, M.v.p, lr, b1, b2, 1e-8f,
-                                                                      (float)(1. - p1), (float)(1. - p2));
+            { P3T_COUNT_LAUNCH(); k_mlp_adam<<<(MLP_NP + 255) / 256, 256, 0, c->stream>>>(M.P.p, M.g.p, M.m.p, M.v.p, lr, b1, b2, 1e-8f,
+                                                                      (float)(1. - p1), (float)(1. - p2)); }
         }
         float l = 0.f;
         if ((r = cuda_status(cudaMemcpyAsync(&l, M.loss.p, sizeof(float), cudaMemcpyDeviceToHost, c->stream))) ||

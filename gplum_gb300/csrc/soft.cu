@@ -708,20 +708,20 @@ __global__ void iota_kernel(int *out, int n, int base) {
 
 cudaError_t launch_pack_epi(const EPIRec *in, int n, SoftPtcl *out, double *r_out, double *r_search, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    pack_epi_kernel<<<(n + 255) / 256, 256, 0, st>>>(in, n, out, r_out, r_search);
+    { P3T_COUNT_LAUNCH(); pack_epi_kernel<<<(n + 255) / 256, 256, 0, st>>>(in, n, out, r_out, r_search); }
     return cudaGetLastError();
 }
 
 cudaError_t launch_iota(int *out, int n, int base, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    iota_kernel<<<(n + 255) / 256, 256, 0, st>>>(out, n, base);
+    { P3T_COUNT_LAUNCH(); iota_kernel<<<(n + 255) / 256, 256, 0, st>>>(out, n, base); }
     return cudaGetLastError();
 }
 
 cudaError_t launch_pack_epj(const EPJRec *in, int n, SoftPtcl *out, double *mass, double *r_out, double *r_search,
                             cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    pack_epj_kernel<<<(n + 255) / 256, 256, 0, st>>>(in, n, out, mass, r_out, r_search);
+    { P3T_COUNT_LAUNCH(); pack_epj_kernel<<<(n + 255) / 256, 256, 0, st>>>(in, n, out, mass, r_out, r_search); }
     return cudaGetLastError();
 }
 
@@ -824,18 +824,18 @@ cudaError_t launch_soft(const SoftArgs &Ain, int precision, bool emit, cudaStrea
             A.isplit = m.isplit;
         }
         if (same) A.isplit = A.jsplit;
-        if (A.n_ptcl > 0) split_kernel<<<(A.n_ptcl + 255) / 256, 256, 0, st>>>(A.ptcl, A.n_ptcl, A.jsplit);
+        if (A.n_ptcl > 0) { P3T_COUNT_LAUNCH(); split_kernel<<<(A.n_ptcl + 255) / 256, 256, 0, st>>>(A.ptcl, A.n_ptcl, A.jsplit); }
         if (!same && A.n_iptcl > 0)
-            split_kernel<<<(A.n_iptcl + 255) / 256, 256, 0, st>>>(A.iptcl, A.n_iptcl, A.isplit);
+            { P3T_COUNT_LAUNCH(); split_kernel<<<(A.n_iptcl + 255) / 256, 256, 0, st>>>(A.iptcl, A.n_iptcl, A.isplit); }
         if (A.n_spj > 0)
-            spj_pack_kernel<<<(A.n_spj + 255) / 256, 256, 0, st>>>(A.spj, A.n_spj, A.eps2, A.trace_mode, A.spjp);
+            { P3T_COUNT_LAUNCH(); spj_pack_kernel<<<(A.n_spj + 255) / 256, 256, 0, st>>>(A.spj, A.n_spj, A.eps2, A.trace_mode, A.spjp); }
         const int occ = A.occ ? A.occ : 5;
 #define P3T_SOFT_MIXED(OCC)                                                  \
     do {                                                                     \
         if (emit)                                                            \
-            soft_mixed_kernel<true, OCC><<<A.n_group, SB, 0, st>>>(A);       \
+            { P3T_COUNT_LAUNCH(); soft_mixed_kernel<true, OCC><<<A.n_group, SB, 0, st>>>(A); }       \
         else                                                                 \
-            soft_mixed_kernel<false, OCC><<<A.n_group, SB, 0, st>>>(A);      \
+            { P3T_COUNT_LAUNCH(); soft_mixed_kernel<false, OCC><<<A.n_group, SB, 0, st>>>(A); }      \
     } while (0)
         if (occ == 4)
             P3T_SOFT_MIXED(4);
@@ -846,9 +846,9 @@ cudaError_t launch_soft(const SoftArgs &Ain, int precision, bool emit, cudaStrea
 #undef P3T_SOFT_MIXED
     } else {
         if (emit)
-            soft_f64_kernel<true><<<A.n_group, SB, 0, st>>>(A);
+            { P3T_COUNT_LAUNCH(); soft_f64_kernel<true><<<A.n_group, SB, 0, st>>>(A); }
         else
-            soft_f64_kernel<false><<<A.n_group, SB, 0, st>>>(A);
+            { P3T_COUNT_LAUNCH(); soft_f64_kernel<false><<<A.n_group, SB, 0, st>>>(A); }
     }
     return cudaGetLastError();
 }

@@ -31,6 +31,7 @@ int functor_call(const void *epi, int ni, const void *epj, int nj, const void *s
     Context *c = ctx_get(0);
     if (!c) return -(int)cudaErrorNoDevice;
     if (ni <= 0) return 0;
+    if (!epi || !force || nj < 0 || ns < 0 || (nj > 0 && !epj) || (ns > 0 && !spj)) return ST_BAD_INDEX;
     DevSet &d = g_fun;
     int r = 0;
     if ((r = d.epi_stage.reserve(ni)) || (r = d.iptcl.reserve(ni)) || (r = d.i_r_out.reserve(ni)) ||
@@ -78,6 +79,18 @@ WalkSlot *slot_for(Context *c, int tag) {
     WalkSlot &w = c->walk[tag % MAX_TAGS];
     if (!w.done && cudaEventCreateWithFlags(&w.done, cudaEventDisableTiming) != cudaSuccess) return nullptr;
     return &w;
+}
+
+// Per-walk counts of a dispatch: non-negative, with a record pointer where a
+// count is positive, and totals that fit the int offsets.
+int check_walks(int n_walk, const int *cnt, const void *const *ptr) {
+    if (n_walk < 0 || (n_walk > 0 && !cnt)) return ST_BAD_INDEX;
+    long long tot = 0;
+    for (int k = 0; k < n_walk; k++) {
+        if (cnt[k] < 0 || (cnt[k] > 0 && (!ptr || !ptr[k]))) return ST_BAD_INDEX;
+        tot += cnt[k];
+    }
+    return tot > 2147483647LL ? ST_BAD_INDEX : 0;
 }
 
 // Common tail of both dispatch forms: kernel, download, event.
@@ -140,6 +153,10 @@ int p3t_epsp(const void *epi, int ni, const void *spj, int nj, void *force) {
 
 int p3t_soft_dispatch(int tag, int n_walk, const void **epi, const int *n_epi, const void **epj, const int *n_epj,
                       const void **spj, const int *n_spj) {
+    int e = 0;
+    if ((e = check_walks(n_walk, n_epi, epi)) || (e = check_walks(n_walk, n_epj, epj)) ||
+        (e = check_walks(n_walk, n_spj, spj)))
+        return e;
     Context *c = ctx_get(0);
     if (!c) return -(int)cudaErrorNoDevice;
     WalkSlot *ws = slot_for(c, tag);
@@ -194,6 +211,12 @@ int p3t_soft_dispatch(int tag, int n_walk, const void **epi, const int *n_epi, c
 int p3t_soft_dispatch_index(int tag, int n_walk, const void **epi, const int *n_epi, const int **id_epj,
                             const int *n_epj, const int **id_spj, const int *n_spj, const void *epj, int n_epj_tot,
                             const void *spj, int n_spj_tot, int send_flag) {
+    int e = 0;
+    if ((e = check_walks(n_walk, n_epi, epi)) || (e = check_walks(n_walk, n_epj, (const void *const *)id_epj)) ||
+        (e = check_walks(n_walk, n_spj, (const void *const *)id_spj)))
+        return e;
+    if (send_flag && (n_epj_tot < 0 || n_spj_tot < 0 || (n_epj_tot > 0 && !epj) || (n_spj_tot > 0 && !spj)))
+        return ST_BAD_INDEX;
     Context *c = ctx_get(0);
     if (!c) return -(int)cudaErrorNoDevice;
     WalkSlot *ws = slot_for(c, tag);

@@ -14,6 +14,24 @@ from . import _lib
 from .soft import configure
 
 VP = ctypes.c_void_p
+# phases of p3t_step_phases_ms (include/gplum_p3t.h P3T_PH_*)
+STEP_PHASES = ("kick1", "cluster", "hard", "tree_soft", "correct", "kick2", "energy", "merge", "remove", "reforce")
+
+
+class LoopParams(ctypes.Structure):
+    """p3t_loop_params_t"""
+    _fields_ = [("theta", ctypes.c_double), ("n_leaf_limit", ctypes.c_int), ("n_group_limit", ctypes.c_int),
+                ("reset_step", ctypes.c_int), ("r_max", ctypes.c_double), ("r_min", ctypes.c_double)]
+
+
+class StepResult(ctypes.Structure):
+    """p3t_step_result_t"""
+    _fields_ = [("n_col", ctypes.c_int), ("n_removed", ctypes.c_int), ("n_body", ctypes.c_int),
+                ("reforced", ctypes.c_int), ("n_clusters", ctypes.c_int), ("n_isolated", ctypes.c_int),
+                ("energy", ctypes.c_double * 5), ("edisp", ctypes.c_double),
+                ("edisp_hard", ctypes.c_double * 2)]
+
+
 VEC_FIELDS = {"pos": 0, "vel": 1, "acc": 2, "acc_d": 3, "jerk_d": 4, "acc_s": 5, "jerk_s": 6}
 SCALAR_FIELDS = {"phi": 10, "phi_d": 11, "phi_s": 12, "mass": 13, "r_out": 14, "r_search": 15, "dt": 16,
                  "acc0": 17, "time": 18, "r_planet": 19, "v_disp": 20, "r_out_inv": 21, "f": 22}
@@ -119,7 +137,9 @@ class GpuSystem:
         ed = np.zeros(2)
         nc = self.lib.p3t_hard(istep, col_cap, cols.ctypes.data_as(VP), ed.ctypes.data_as(VP))
         if nc < 0:
-            raise RuntimeError(f"p3t_hard failed with status {nc}")
+            bits = _lib.status_bits(nc)
+            raise RuntimeError(f"p3t_hard failed: kernel status bits {bits}" if bits else
+                               f"p3t_hard failed with status {nc}")
         return cols[:2 * min(nc, col_cap)].reshape(-1, 2), ed
 
     def set_fragmentation(self, a_frag, n_frag=10, m_min=9.426627927538057e-12, seed=0):
@@ -212,6 +232,69 @@ class GpuSystem:
         if n < 0:
             raise RuntimeError(f"p3t_remove_out_of_boundary failed with status {n}")
         return n, e.value
+
+    # the whole tree step as one native call (include/gplum_p3t.h p3t_tree_step)
+    def startup(self, reset_step=1024, r_max=40.0, r_min=0.1):
+        """Cutoff radii and two passes of soft force + correctForceLongInitial
+        (src/main_p3t.cpp:289-364); returns the initial energy."""
+        P = self.params
+        lp = LoopParams(P.theta, P.n_leaf_limit, P.n_group_limit, reset_step, r_max, r_min)
+        e = np.zeros(5)
+        self._chk(self.lib.p3t_startup(ctypes.byref(lp), e.ctypes.data_as(VP)), "p3t_startup")
+        return e
+
+    def tree_step(self, istep):
+        """One tree step (src/main_p3t.cpp:423-717) in the library; returns
+        the p3t_step_result_t fields as a dict."""
+        res = StepResult()
+        self._chk(self.lib.p3t_tree_step(istep, ctypes.byref(res)), "p3t_tree_step")
+        return {"n_col": res.n_col, "n_removed": res.n_removed, "n_body": res.n_body, "reforced": res.reforced,
+                "n_clusters": res.n_clusters, "n_isolated": res.n_isolated, "energy": np.array(res.energy[:]),
+                "edisp": res.edisp, "edisp_hard": np.array(res.edisp_hard[:])}
+
+    def step_phases_ms(self):
+        """Device time of each phase of the last tree_step (CUDA events)."""
+        ms = np.zeros(len(STEP_PHASES), np.float32)
+        self._chk(self.lib.p3t_step_phases_ms(ms.ctypes.data_as(VP)), "p3t_step_phases_ms")
+        return dict(zip(STEP_PHASES, ms.astype(float).tolist()))
+
+    def collisions(self):
+        """(impactor id, target id) of the last hard part's collisions, in
+        collision-list order."""
+        from .collisions import records
+        return np.array([(r.id_imp, r.id_tar) for r in records(self.lib)], np.int64).reshape(-1, 2)
+
+    def put_fpgrav(self, records, id_next=-1):
+        """The state from an array of GPLUM FPGrav records (layout.FPGRAV_DTYPE)."""
+        self._chk(self.lib.p3t_state_put_fpgrav(len(records), records.ctypes.data_as(VP), int(id_next)),
+                  "p3t_state_put_fpgrav")
+
+    def get_fpgrav(self, out=None):
+        """The state as an array of GPLUM FPGrav records (into `out` when it
+        is large enough)."""
+        from .layout import FPGRAV_DTYPE
+        n = self.n
+        if out is None or len(out) < n:
+            out = np.zeros(n, FPGRAV_DTYPE)
+        m = self.lib.p3t_state_get_fpgrav(out.ctypes.data_as(VP), len(out))
+        if m < 0:
+            raise RuntimeError(f"p3t_state_get_fpgrav failed with status {m}")
+        return out[:m]
+
+    def hard_launch_stats(self):
+        """The last cluster launch: dict of its device time (ms), the pair
+        terms it evaluated in predicted/corrected passes and in full-force
+        passes (counted by the bundle form), and sums over its clusters
+        (pair sweeps, n(n-1) x block steps, active members over block steps,
+        largest block-step count, member predictions)."""
+        ms = ctypes.c_double(0.0)
+        p = np.zeros(3, np.int64)
+        sm = np.zeros(5)
+        self._chk(self.lib.p3t_hard_launch_stats(ctypes.byref(ms), p.ctypes.data_as(VP), sm.ctypes.data_as(VP)),
+                  "p3t_hard_launch_stats")
+        return {"ms": ms.value, "live_pc": int(p[0]), "live_full": int(p[1]), "counted": bool(p[2]),
+                "sweeps": float(sm[0]), "coll_pairs": float(sm[1]), "active": float(sm[2]),
+                "max_block_steps": int(sm[3]), "predictions": float(sm[4])}
 
     def counts(self):
         a, b = ctypes.c_int(), ctypes.c_int()

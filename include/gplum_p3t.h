@@ -6,6 +6,10 @@
  *   1 neighbour-candidate table overflow   2 list index out of range
  *   4 iteration cap reached                8 queue / pair buffer overflow
  *   16 cluster larger than the hard kernel's capacity
+ * Entry points that return a count (p3t_hard, p3t_hard_fetch,
+ * p3t_remove_out_of_boundary) report kernel status bits as
+ * P3T_COUNT_STATUS(bits) = -(65536 + bits), below every CUDA and file error
+ * code; P3T_STATUS_BITS(r) gives the bits back (0 for any other value).
  * There is no CPU fallback: without a usable CUDA device every compute entry
  * point returns a negative status.
  *
@@ -20,6 +24,9 @@
  */
 #ifndef GPLUM_P3T_H
 #define GPLUM_P3T_H
+
+#define P3T_COUNT_STATUS(bits) (-(65536 + (bits)))
+#define P3T_STATUS_BITS(r) ((r) <= -65536 ? -(r)-65536 : 0)
 
 #ifdef __cplusplus
 extern "C" {
@@ -276,6 +283,74 @@ int p3t_merge(double *edisp);
  * the energy they take with them.  Returns how many left. */
 int p3t_remove_out_of_boundary(double r_max, double r_min, double *edisp);
 
+/* ---- the whole tree step -------------------------------------------------------
+ * GPLUM's main loop (src/main_p3t.cpp:289-364 start-up, :423-717 one step)
+ * on the device-resident state, each call running its phases in the loop's
+ * order: kick, createNeighborCluster + makeList, HardSystem::timeIntegrate
+ * with the collisions, the soft force and correctForceLong, kick,
+ * Energy::calcEnergy, MergeParticle, removeParticlesOutOfBoundary and, after
+ * a collision or removal or every reset_step steps, setCutoffRadii + soft
+ * force + correctForceLongInitial + energy.  The hard launch follows
+ * p3t_set_hard_mode / p3t_set_schedule; the soft force p3t_set_options.
+ * There is no single counterpart in GPLUM: these replace its loop body for
+ * a driver that keeps the particles on the device. */
+typedef struct {
+    double theta;                    /* tree opening angle (parameter.dat theta) */
+    int n_leaf_limit, n_group_limit; /* FDPS tree limits (parameter.dat) */
+    int reset_step;                  /* re-force every reset_step steps (parameter.dat reset_step) */
+    double r_max, r_min;             /* removal boundaries (parameter.dat r_max, r_min) */
+} p3t_loop_params_t;
+typedef struct {
+    int n_col;           /* collisions of the step (pairs: p3t_collision_records) */
+    int n_removed;       /* bodies removed outside [r_min, r_max] */
+    int n_body;          /* bodies after the step */
+    int reforced;        /* 1 if the re-force pass ran */
+    int n_clusters;      /* neighbour clusters of the hard part (HardSystem's count) */
+    int n_isolated;      /* bodies without neighbours (Kepler drift or sun-only Hermite) */
+    double energy[5];    /* Energy::calcEnergy after the step: etot, ekin, ephi_sun, ephi, ephi_d */
+    double edisp;        /* energy dissipated in the step: collisions, merges, removals */
+    double edisp_hard[2];/* of which the hard part's collisions {total, hard part} */
+} p3t_step_result_t;
+/* phases of p3t_step_phases_ms, in step order */
+enum {
+    P3T_PH_KICK1, P3T_PH_CLUSTER, P3T_PH_HARD, P3T_PH_SOFT, P3T_PH_CORRECT, P3T_PH_KICK2, P3T_PH_ENERGY,
+    P3T_PH_MERGE, P3T_PH_REMOVE, P3T_PH_REFORCE, P3T_STEP_PHASES
+};
+/* Start-up after p3t_state_load (and p3t_set_r_planet where the radii come
+ * from the masses): cutoff radii, then two passes of soft force +
+ * correctForceLongInitial; energy5 (may be NULL) receives the initial
+ * energy.  lp (NULL: keep the last, initially theta 0.5, 8, 256, 1024, 40,
+ * 0.1) sets the loop parameters for the steps that follow. */
+int p3t_startup(const p3t_loop_params_t *lp, double *energy5);
+/* Tree step istep (1, 2, ...): returns 0 or a status (kernel bits
+ * positive, CUDA errors negative) and fills *out (may be NULL). */
+int p3t_tree_step(int istep, p3t_step_result_t *out);
+/* Device time (ms) of each phase of the last p3t_tree_step, from CUDA events
+ * on the library stream: P3T_STEP_PHASES floats; their sum is the step. */
+int p3t_step_phases_ms(float *ms);
+/* The state to and from a host array of GPLUM FPGrav records (344 bytes
+ * each, ParticleSystem<FPGrav>'s element; src/particle.h:93-170,404-500),
+ * one copy each way.  put replaces the state's bodies and every field the
+ * step carries (no start-up reset; the neighbour lists of the last
+ * correction stay with the library, so a caller that changes the body set
+ * runs p3t_startup again); id_next (< 0: unchanged) raises the next
+ * particle id.  get writes n records (cap >= n) and returns n. */
+int p3t_state_put_fpgrav(int n, const void *records, long long id_next);
+int p3t_state_get_fpgrav(void *records, int cap);
+/* Block steps one cluster may take in one tree step (default and maximum
+ * 1048576); a cluster that reaches it stops there and the launch reports
+ * status bit 4.  No counterpart in GPLUM. */
+int p3t_set_hard_step_cap(int max_block_steps);
+/* The last hard launch: device time (ms) of the cluster kernel from CUDA
+ * events around it on the library stream; pairs3 = {pair terms evaluated in
+ * the predicted/corrected passes, in full-force passes, 1 if the launch
+ * counted them (bundle form) else 0}; sums5 = over its clusters {sum of
+ * active x member pair sweeps, sum of n (n - 1) x block steps, sum of active
+ * members over block steps, largest block-step count, sum of n x block steps
+ * (member predictions)}.  Valid until the next hard call (merges and removals
+ * in between do not change them).  Any pointer may be NULL. */
+int p3t_hard_launch_stats(double *launch_ms, long long *pairs3, double *sums5);
+
 /* ---- soft force without allocation ---------------------------------------------
  * No counterpart in GPLUM.  For callers that cannot allocate device memory
  * (their device memory comes from another runtime's arena or pool, or their
@@ -291,10 +366,16 @@ int p3t_remove_out_of_boundary(double r_max, double r_min, double *edisp);
  * (5 MiB), P3T_NOALLOC_MAX_SPJ packed superparticles (4 MiB), held by every
  * GPU that loads the library until the process exits, and a status word.
  * n above P3T_NOALLOC_MAX_BODIES or n_spj above P3T_NOALLOC_MAX_SPJ is
- * rejected with -cudaErrorInvalidValue and a message on stderr.  The first call on a device looks up the static
- * array's device address, so make it before any stream capture.  All calls
- * share the scratch: calls that overlap on the GPU race and must be
- * serialised by the caller. */
+ * rejected with -cudaErrorInvalidValue and a message on stderr, and so are
+ * null buffers.  The first call on a device looks up the static arrays'
+ * device addresses.  Every call waits for its stream (it reads the status
+ * word back), so it cannot be made on a stream under CUDA-graph capture.  The
+ * offsets are checked on the device before any list is read (each starts at
+ * 0 and never decreases; i_off[n_group] <= n): a violation returns status 2
+ * and runs no force kernel; out-of-range list entries are clamped and also
+ * return 2.  All calls share the scratch: calls that overlap on the GPU race
+ * and must be serialised by the caller.  The launch shape is the one
+ * p3t_set_soft_tiles / p3t_set_soft_occupancy set. */
 #define P3T_NOALLOC_MAX_BODIES 65536
 #define P3T_NOALLOC_MAX_SPJ 65536
 int p3t_soft_force_noalloc(int n, const void *epj, int n_group, const int *i_off, const int *i_idx,
@@ -385,6 +466,9 @@ int p3t_collisions_write(const char *path, int append);
  * FP64 (fp64 = 1) or packed FP32 pairs (fp64 = 2, fma.rn.f32x2): the roofline denominators of the soft (FP32-pipe) and
  * hard (FP64-pipe) kernels.  No counterpart in GPLUM. */
 int p3t_probe_fma_peak(int fp64, double *tflops);
+/* Kernel launches the library has made since it was loaded (every launch
+ * site counts; the peak probe above excepted).  No counterpart in GPLUM. */
+unsigned long long p3t_launch_count(void);
 
 #ifdef __cplusplus
 }

@@ -19,6 +19,8 @@
 #include <numeric>
 #include <vector>
 
+#include <omp.h>
+
 #include "ngb_grid.h"
 #include "p3t_oracle.h"
 
@@ -1527,7 +1529,7 @@ void orc_soft_force(int n_group, const int *i_off, const int *i_idx, const int *
     std::vector<FORCE> f(n);
     orc_export_ep(ei.data(), ej.data());
     orc_soft_lists(0, 0, n_group, i_off, i_idx, j_off, j_idx, s_off, s_idx, ei.data(), ej.data(), spj_all,
-                   f.data(), nullptr, nullptr, 8);
+                   f.data(), nullptr, nullptr, omp_get_max_threads());
     for (int i = 0; i < n; i++) {
         S[i].acc = v3(f[i].acc[0], f[i].acc[1], f[i].acc[2]);
         S[i].phi = f[i].phi;
