@@ -57,6 +57,7 @@ SIGNATURES = {
     "p3t_correct": (I, [I]),
     "p3t_neighbor_counts": (I, [VP, VP]),
     "p3t_neighbor_list": (I, [I, VP, I]),
+    "p3t_neighbor_pairs": (I, [VP, ctypes.c_longlong]),
     "p3t_cluster_label": (I, []),
     "p3t_cluster_lists": (I, [VP, VP, VP]),
     "p3t_hard": (I, [I, I, VP, VP]),

@@ -330,6 +330,31 @@ __global__ void k_copy3(double *dst, const double *src, int n) {
     if (i < 3 * n) dst[i] = src[i];
 }
 
+// NeighborList::pair_list (src/neighbor.h:635-670): the local pairs (i, j),
+// i < j, j a neighbour of i, by i and then in neighbour-list order.
+__global__ void k_pair_count(State S, int cap, int32_t *cnt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.n) return;
+    const int m = S.nbr_n[i];
+    int c = 0;
+    for (int t = 0; t < m; t++) c += (i < S.nbr[(size_t)i * cap + t]) ? 1 : 0;
+    cnt[i] = c;
+}
+__global__ void k_pair_fill(State S, int cap, const int32_t *base, int32_t *out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.n) return;
+    const int m = S.nbr_n[i];
+    int k = base[i];
+    for (int t = 0; t < m; t++) {
+        const int j = S.nbr[(size_t)i * cap + t];
+        if (i < j) {
+            out[2 * k] = i;
+            out[2 * k + 1] = j;
+            k++;
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // cluster labelling, src/neighbor.h:800-839: connected components of the
 // local pairs (i < j, j a neighbour of i), each labelled with the minimum
@@ -1189,6 +1214,26 @@ int p3t_neighbor_list(int i, int *out, int cap) {
     m = std::min(m, cap);
     if (m > 0) d2h(g_eng.c, out, g_eng.S.nbr + (size_t)i * c->cand_cap, m * sizeof(int));
     return m;
+}
+
+int p3t_neighbor_pairs(int *out, long long cap) {
+    Engine &E = g_eng;
+    if (!E.c) return -(int)cudaErrorNoDevice;
+    if (cap < 0 || (cap > 0 && !out)) return -(int)cudaErrorInvalidValue;
+    const int n = E.S.n;
+    int r = 0;
+    if ((r = E.tflag.reserve(n)) || (r = E.tpos.reserve(n))) return r;
+    { P3T_COUNT_LAUNCH(); k_pair_count<<<nb(n), 256, 0, E.c->stream>>>(E.S, E.c->cand_cap, E.tflag.p); }
+    int32_t np = 0;
+    if ((r = E.scan(E.tflag.p, E.tpos.p, n, &np))) return r;
+    if (cap >= np && np > 0) {
+        if ((r = E.members_tmp.reserve(2 * (size_t)np))) return r;
+        { P3T_COUNT_LAUNCH(); k_pair_fill<<<nb(n), 256, 0, E.c->stream>>>(E.S, E.c->cand_cap, E.tpos.p, E.members_tmp.p); }
+        if ((r = cuda_status(cudaGetLastError())) ||
+            (r = d2h(E.c, out, E.members_tmp.p, 2 * (size_t)np * sizeof(int32_t))))
+            return r;
+    }
+    return np;
 }
 
 int p3t_cluster_label(void) {

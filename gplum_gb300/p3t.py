@@ -108,14 +108,16 @@ class GpuSystem:
         return out[:max(m, 0)]
 
     def pairs(self):
-        """(i, j) with i < j, j a neighbour of i (NeighborList::pair_list)."""
-        num = self.get("number")
-        out = []
-        for i in np.nonzero(num)[0]:
-            for j in self.neighbor_ids_local(int(i)):
-                if i < j:
-                    out.append((int(i), int(j)))
-        return np.array(out, dtype=np.int32).reshape(-1, 2)
+        """(i, j) with i < j, j a neighbour of i (NeighborList::pair_list),
+        ordered by i and then j."""
+        m = self.lib.p3t_neighbor_pairs(None, 0)
+        if m < 0:
+            raise RuntimeError(f"p3t_neighbor_pairs failed with status {m}")
+        out = np.zeros((max(m, 1), 2), np.int32)
+        m2 = self.lib.p3t_neighbor_pairs(out.ctypes.data_as(VP), m)
+        if m2 != m:
+            raise RuntimeError(f"p3t_neighbor_pairs returned {m2}, expected {m}")
+        return out[:m]
 
     def cluster(self):
         self._chk(self.lib.p3t_cluster_label(), "p3t_cluster_label")

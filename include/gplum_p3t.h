@@ -25,6 +25,31 @@
 #ifndef GPLUM_P3T_H
 #define GPLUM_P3T_H
 
+/* The records as C structs (the layouts above, no padding): a C caller can
+ * use these; GPLUM passes its own classes, which have the same layout. */
+typedef struct {
+    int id_local, myrank;
+    double pos[3], r_out, r_search;
+} p3t_epi_t;
+typedef struct {
+    int id_local, myrank;
+    double pos[3], r_out, r_search;
+    long long id;
+    double mass, vel[3], acc_d[3];
+} p3t_epj_t;
+typedef struct {
+    double mass, pos[3], xx, yy, zz, xy, xz, yz;
+} p3t_spj_t;
+typedef struct {
+    float acc[3], phi;
+    int number, rank, id_max, id_min;
+} p3t_force_t;
+#ifdef __cplusplus
+static_assert(sizeof(p3t_epi_t) == 48 && sizeof(p3t_epj_t) == 112 && sizeof(p3t_spj_t) == 80 &&
+                  sizeof(p3t_force_t) == 32,
+              "record layouts");
+#endif
+
 #define P3T_COUNT_STATUS(bits) (-(65536 + (bits)))
 #define P3T_STATUS_BITS(r) ((r) <= -65536 ? -(r)-65536 : 0)
 
@@ -171,6 +196,11 @@ int p3t_correct_and_search(int initial);
 int p3t_neighbor_counts(int *n_ngb_tot, int *n_with_ngb);
 /* Neighbour local indices of body i (returns their count, at most cap). */
 int p3t_neighbor_list(int i, int *out, int cap);
+/* NeighborList::pair_list (src/neighbor.h:635-670) of the last correction:
+ * the local pairs (i, j), i < j, j a neighbour of i, ordered by i and then
+ * by neighbour-list order (ascending j), as int[2] each.  Returns the pair
+ * count; the pairs are written when cap >= that count. */
+int p3t_neighbor_pairs(int *out, long long cap);
 /* NeighborList::createNeighborCluster (src/neighbor.h:800-839) followed by
  * HardSystem::makeList (src/hard.h:321-438). */
 int p3t_cluster_label(void);

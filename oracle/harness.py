@@ -51,6 +51,16 @@ def ref_available():
     return os.path.exists(REF_SO)
 
 
+def ref_source_dir():
+    """GPLUM's src/ directory the reference build was compiled from (None
+    where there is no reference build)."""
+    p = os.path.join(HERE, "_ref", "ref_src.txt")
+    if not os.path.exists(p):
+        return None
+    d = open(p).read().strip()
+    return d if d and os.path.isdir(d) else None
+
+
 def _ptr(a, t):
     return a.ctypes.data_as(t)
 

@@ -1422,6 +1422,53 @@ void orc_load(int n, const long long *id, const double *mass, const double *r_pl
         if (i == 0 || p.id + 1 > ID_NEXT) ID_NEXT = p.id + 1;
     }
 }
+// GPLUM's FPGrav record (src/particle.h:93-170,404-500; the build with
+// individual cutoffs, quadrupole moments and collisions): 344 bytes.
+struct FPGravRec {
+    int32_t id_local, myrank;
+    double pos[3], r_out, r_search;
+    int64_t id;
+    double mass, vel[3], acc_d[3], acc[3], acc_s[3], jerk_d[3], jerk_s[3], acc_gd[3];
+    double phi, phi_d, phi_s, v_disp, r_out_inv, time, dt, acc0, r_planet, f;
+    int32_t number, rank, id_max, id_min;
+    int64_t id_cluster;
+    int32_t n_cluster;
+    uint8_t in_domain, is_sent, is_dead, is_merged;
+};
+static_assert(sizeof(FPGravRec) == 344, "FPGrav record");
+
+// The whole state from FPGrav records (every field the step carries); the
+// neighbour lists of the last correction are kept.  id_next < 0: unchanged.
+void orc_put_fpgrav(int n, const void *records, long long id_next) {
+    const FPGravRec *r = (const FPGravRec *)records;
+    S.assign(n, Ptcl());
+    for (int i = 0; i < n; i++) {
+        Ptcl &p = S[i];
+        const FPGravRec &q = r[i];
+        std::memset((void *)&p, 0, sizeof(Ptcl));
+        p.id = q.id;
+        p.mass = q.mass;
+        p.r_planet = q.r_planet;
+        p.f = q.f;
+        p.pos = v3(q.pos[0], q.pos[1], q.pos[2]);
+        p.vel = v3(q.vel[0], q.vel[1], q.vel[2]);
+        p.acc = v3(q.acc[0], q.acc[1], q.acc[2]);
+        p.acc_d = v3(q.acc_d[0], q.acc_d[1], q.acc_d[2]);
+        p.jerk_d = v3(q.jerk_d[0], q.jerk_d[1], q.jerk_d[2]);
+        p.acc_s = v3(q.acc_s[0], q.acc_s[1], q.acc_s[2]);
+        p.jerk_s = v3(q.jerk_s[0], q.jerk_s[1], q.jerk_s[2]);
+        p.phi = q.phi; p.phi_d = q.phi_d; p.phi_s = q.phi_s;
+        p.r_out = q.r_out; p.r_out_inv = q.r_out_inv; p.r_search = q.r_search; p.v_disp = q.v_disp;
+        p.time = q.time; p.dt = q.dt; p.acc0 = q.acc0;
+        p.number = q.number; p.rank = q.rank; p.id_max = q.id_max; p.id_min = q.id_min;
+        p.id_cluster = q.id_cluster;
+        p.n_cluster = q.n_cluster;
+        p.dead = q.is_dead != 0;
+        p.merged = q.is_merged != 0;
+        p.id_local = i;
+    }
+    if (id_next >= 0) ID_NEXT = id_next;
+}
 int orc_n() { return (int)S.size(); }
 
 void orc_get_f64(int field, double *out) {

@@ -99,6 +99,7 @@ def test_hard_step_from_identical_states(gpu):
         np.testing.assert_array_equal(g.get("id_cluster"), orc.get("id_cluster"))
         sync_state(orc, g)
         g.set("id", orc.get("id"))
+        iso = orc.get("number") == 0  # isolated bodies: Kepler drift
         c1, e1 = orc.hard(istep)
         c2, e2 = g.hard(istep)
         np.testing.assert_array_equal(c2, c1)
@@ -111,7 +112,12 @@ def test_hard_step_from_identical_states(gpu):
             assert np.abs(a - b).max() <= 1e-9 * np.abs(b).max(), k
         np.testing.assert_array_equal(g.get("dead"), orc.get("dead"))
         np.testing.assert_array_equal(g.get("n_cluster"), orc.get("n_cluster"))
+        # block steps equal on every cluster member; an isolated body's step
+        # (calcDeltatInitial after the Kepler drift, src/hermite.h:787-815) can
+        # differ where CUDA's sin/cos/atan2 and glibc's round a drifted
+        # position differently in the last bit
         dtg, dto = g.get("dt"), orc.get("dt")
+        assert not ((dtg != dto) & ~iso).any()
         assert (dtg == dto).mean() > 0.999
         np.testing.assert_array_equal(g.get("time"), orc.get("time"))
         # finish the step identically on both (oracle state copied over);
