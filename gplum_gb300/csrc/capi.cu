@@ -31,7 +31,15 @@ Context *ctx_get(int device) {
     if (cudaSetDevice(device) != cudaSuccess) return nullptr;
     Context *c = new Context();
     c->device = device;
-    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    // the library stream one step below the highest priority: the hard
+    // part's side launches that must hold SMs from the start (the lone form)
+    // take the highest, so the CTA dispatcher places theirs before the
+    // persistent bundle CTAs; work queued beside it at the lowest (the
+    // isolated bodies' drift) only takes SMs the step's own launches leave free
+    int prio_lo = 0, prio_hi = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+    const int prio = (prio_hi < prio_lo) ? prio_hi + 1 : prio_hi;
+    if (cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, prio) != cudaSuccess) {
         delete c;
         return nullptr;
     }

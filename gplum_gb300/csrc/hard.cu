@@ -17,6 +17,9 @@
 namespace p3t {
 
 constexpr int MAX_BLOCK_STEPS = 1 << 20;  // per cluster and tree step
+// lone form: clusters of at most this many members (larger ones run faster in
+// a bundle CTA's 256 threads than in the lone CTA's 128)
+constexpr int LONE_NMAX = 64;
 
 // Per-member working copy of one cluster (FPHard fields), indexed by the
 // member's slot in the cluster lists.
@@ -656,10 +659,24 @@ __device__ __forceinline__ long long global_ns() {
     return (long long)t;
 }
 
-// timeIntegrate_multi, src/hermite.h:224-479, for cluster c by a team.
+// Progress of one cluster's integration (uniform across the team except
+// `work`, which each team member counts for its own members).
+struct ClusterRun {
+    double time = 0.;
+    int steps = 0, n_col = 0;
+    double ed = 0., edd = 0.;
+    long long work = 0;
+    long long t_start = 0;
+};
+
+// timeIntegrate_multi, src/hermite.h:224-479, for cluster c by a team, in
+// three parts: load (FPHard from FPGrav, the prefilter, the first full
+// force), the block-step loop from run.time on, and the finish (last full
+// force, write-back, logs).  The lone-cluster form (hard_lone.cuh) runs its
+// own block steps and hands a cluster to cluster_loop at its first
+// collision.
 template <int TEAM>
-__device__ void run_cluster(const HardArgs &A, int c, const Team<TEAM> &tm) {
-    const long long t_start = (A.times && tm.rank == 0) ? global_ns() : 0;
+__device__ void cluster_load(const HardArgs &A, int c, const Team<TEAM> &tm, Pre &pre) {
     const Params &P = A.P;
     const Hard &H = A.H;
     const int rank = tm.rank;
@@ -687,7 +704,6 @@ __device__ void run_cluster(const HardArgs &A, int c, const Team<TEAM> &tm) {
     // extent; the prefilter only skips pairs beyond twice a cutoff radius, so
     // it is exact whenever that error bound is below a quarter of the
     // smallest radius it is compared with (1e-6 (D + 0.05 AU) below).
-    Pre pre;
     {
         const V3 r0 = ld3(A.S.pos, A.members[o]);
         pre.ref[0] = r0.x; pre.ref[1] = r0.y; pre.ref[2] = r0.z;
@@ -708,11 +724,19 @@ __device__ void run_cluster(const HardArgs &A, int c, const Team<TEAM> &tm) {
     tm.sync();
     for (int k = rank; k < n; k += TEAM) hard_force(P, H, o, n, o + k, 0, pre);
     tm.sync();
-    int n_col = 0;
-    double ed = 0., edd = 0.;
-    double time = 0.;
-    int steps = 0;
-    long long work = 0;
+}
+
+template <int TEAM>
+__device__ void cluster_loop(const HardArgs &A, int c, const Team<TEAM> &tm, const Pre &pre, ClusterRun &run) {
+    const Params &P = A.P;
+    const Hard &H = A.H;
+    const int rank = tm.rank;
+    const int o = A.off[c], n = A.cnt[c];
+    int n_col = run.n_col;
+    double ed = run.ed, edd = run.edd;
+    double time = run.time;
+    int steps = run.steps;
+    long long work = run.work;
     while (time < A.t_end) {
         if (++steps > A.max_steps) {
             if (rank == 0) atomicOr(A.status, ST_ITER_CAP);
@@ -857,6 +881,21 @@ __device__ void run_cluster(const HardArgs &A, int c, const Team<TEAM> &tm) {
             if (!H.dead[o + k]) tmin = dmin(tmin, H.th[o + k]);
         time = tm.min(tmin);
     }
+    run.n_col = n_col;
+    run.ed = ed;
+    run.edd = edd;
+    run.time = time;
+    run.steps = steps;
+    run.work = work;
+}
+
+template <int TEAM>
+__device__ void cluster_finish(const HardArgs &A, int c, const Team<TEAM> &tm, const Pre &pre, const ClusterRun &run) {
+    const Params &P = A.P;
+    const Hard &H = A.H;
+    const int rank = tm.rank;
+    const int o = A.off[c], n = A.cnt[c];
+    const int n_col = run.n_col;
     tm.sync();
     for (int k = rank; k < n; k += TEAM) hard_force(P, H, o, n, o + k, 0, pre);
     tm.sync();
@@ -878,17 +917,27 @@ __device__ void run_cluster(const HardArgs &A, int c, const Team<TEAM> &tm) {
         A.S.n_cluster[i] = n;
     }
     // per-cluster cost log: block steps and active-body x member pair sweeps
-    if (A.cost) atomicAdd((unsigned long long *)&A.cost[2 * c + 1], (unsigned long long)work);
+    if (A.cost) atomicAdd((unsigned long long *)&A.cost[2 * c + 1], (unsigned long long)run.work);
     if (rank == 0) {
-        A.cl_edisp[2 * c] = (n_col > 0) ? ed : 0.;
-        A.cl_edisp[2 * c + 1] = (n_col > 0) ? edd : 0.;
-        if (A.cost) A.cost[2 * c] = steps;
+        A.cl_edisp[2 * c] = (n_col > 0) ? run.ed : 0.;
+        A.cl_edisp[2 * c + 1] = (n_col > 0) ? run.edd : 0.;
+        if (A.cost) A.cost[2 * c] = run.steps;
         if (A.times) {
-            A.times[2 * c] = t_start;
+            A.times[2 * c] = run.t_start;
             A.times[2 * c + 1] = global_ns();
         }
     }
     tm.sync();
+}
+
+template <int TEAM>
+__device__ void run_cluster(const HardArgs &A, int c, const Team<TEAM> &tm) {
+    ClusterRun run;
+    run.t_start = (A.times && tm.rank == 0) ? global_ns() : 0;
+    Pre pre;
+    cluster_load(A, c, tm, pre);
+    cluster_loop(A, c, tm, pre, run);
+    cluster_finish(A, c, tm, pre, run);
 }
 
 // One persistent launch: clusters of >= cta_min members one per CTA, then
@@ -941,6 +990,7 @@ __global__ void __launch_bounds__(128, 2) k_hard_clusters(HardArgs A) {
 }  // namespace p3t
 
 #include "hard_bundle.cuh"
+#include "hard_lone.cuh"
 
 namespace p3t {
 
@@ -1100,21 +1150,26 @@ __global__ void k_isolated(IsoArgs A) {
 constexpr int ORDER_NB = 4096;
 
 __global__ void k_order_bins(const int32_t *cnt, const float *prio, int nc, int mode, int main_cap, int warp_min, int cta_min,
-                             float pmin, float pscale, int heavy_key, int32_t *bin, int32_t *hist, int32_t *n_heavy) {
+                             float pmin, float pscale, int heavy_key, int lone_key, int32_t *bin, int32_t *hist,
+                             int32_t *n_heavy) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nc) return;
     const int n = cnt[k];
-    const int tier = (mode == 0) ? (n > main_cap ? 0 : 1) : (n >= cta_min ? 0 : (n >= warp_min ? 1 : 2));
     int key = n < ORDER_NB - 1 ? n : ORDER_NB - 1;
     if (prio) {
         const float v = (prio[k] - pmin) * pscale;
         key = (v >= 0.f) ? (v < (float)(ORDER_NB - 1) ? (int)v : ORDER_NB - 1) : 0;  // NaN -> 0
     }
+    // bundle form: tier 0 above the bundle's slots, tier 2 the lone form
+    // (predicted longest chains of at most LONE_NMAX members), tier 1 the rest
+    const int tier = (mode == 0) ? (n > main_cap ? 0 : ((key >= lone_key && n <= LONE_NMAX) ? 2 : 1))
+                                 : (n >= cta_min ? 0 : (n >= warp_min ? 1 : 2));
     const int b = tier * ORDER_NB + (ORDER_NB - 1 - key);
     bin[k] = b;
     atomicAdd(&hist[b], 1);
-    // bundle form: clusters predicted to take long chains of block steps run
-    // alone in a CTA first (they head tier 1, the order being by prediction)
+    // bundle form: the other clusters predicted to take long chains of block
+    // steps run alone in a bundle CTA first (they head tier 1, the order
+    // being by prediction)
     if (mode == 0 && tier == 1 && key >= heavy_key) atomicAdd(n_heavy, 1);
 }
 
@@ -1226,6 +1281,10 @@ static int g_bcap = 256, g_bocc = 2;  // bundle member slots and CTAs per SM (25
 static FragParams g_frag = {0., 9.426627927538057e-12, 10, 0, 0ULL};  // off (a_frag = 0)
 static int g_frag_cap = 0;  // fragment slots of the current launch
 static int g_max_steps = MAX_BLOCK_STEPS;  // block-step cap per cluster and tree step
+// lone form: clusters predicted to take at least 2^g_lone - 1 block steps, on
+// g_lone_ctas CTAs of their own (0: off)
+static float g_lone = 0.f;
+static int g_lone_ctas = 0;
 // events around the last cluster launch (k_hard_bundles / k_hard_clusters) on
 // the library stream, and whether they hold a launch
 static cudaEvent_t g_ev_launch[2] = {nullptr, nullptr};
@@ -1403,7 +1462,7 @@ int p3t_hard_enqueue(void) {
     int r = 0;
     if (g_frag.a_frag > 0. && g_hard_mode != 0) return ST_BAD_INDEX;  // fragments need the bundle form
     g_frag_cap = (g_frag.a_frag > 0.) ? std::max(1024, g_frag.n_frag_max * 4096) : 0;
-    if ((r = B.reserve(E.n_members + g_frag_cap)) || (r = B.order.reserve(nc)) || (r = B.queue.reserve(3)) ||
+    if ((r = B.reserve(E.n_members + g_frag_cap)) || (r = B.order.reserve(nc)) || (r = B.queue.reserve(4)) ||
         (r = B.n_cols.reserve(1)) || (r = B.cl_edisp.reserve(2 * (size_t)nc + 2)) ||
         (r = B.cols.reserve(4096)) || (r = B.frags.reserve(g_frag_cap + 1)) || (r = B.n_frags.reserve(1)) ||
         (r = B.live.reserve(2)))
@@ -1429,12 +1488,16 @@ int p3t_hard_enqueue(void) {
         } else {
             prio = sched_priority(c, nc, &pmin, &pscale);
         }
-        // heavy clusters: learned prediction of log2(1 + block steps) >= g_heavy
-        int heavy_key = 2147483647;
+        // heavy clusters: learned prediction of log2(1 + block steps) >= g_heavy;
+        // lone ones: >= g_lone (the lone form is perfect accretion only)
+        int heavy_key = 2147483647, lone_key = 2147483647;
         if (prio && (int)g_prio.size() != nc && g_heavy > 0.f)
             heavy_key = std::min(ORDER_NB - 1, (int)((g_heavy - pmin) * pscale));
+        if (prio && (int)g_prio.size() != nc && g_lone > 0.f && g_lone_ctas > 0 && g_frag.a_frag <= 0. &&
+            g_hard_mode == 0)
+            lone_key = std::max(0, std::min(ORDER_NB - 1, (int)((g_lone - pmin) * pscale)));
         { P3T_COUNT_LAUNCH(); k_order_bins<<<(nc + 255) / 256, 256, 0, c->stream>>>(E.cl_cnt.p, prio, nc, g_hard_mode, g_bcap, g_warp_min, g_cta_min,
-                                                              pmin, pscale, heavy_key, B.bin.p, B.hist.p,
+                                                              pmin, pscale, heavy_key, lone_key, B.bin.p, B.hist.p,
                                                               B.ntier.p + 3); }
         { P3T_COUNT_LAUNCH(); k_order_scan<<<1, 1024, 0, c->stream>>>(B.hist.p, B.ntier.p); }
         { P3T_COUNT_LAUNCH(); k_order_scatter<<<(nc + 255) / 256, 256, 0, c->stream>>>(B.bin.p, nc, B.hist.p, B.order.p); }
@@ -1443,7 +1506,7 @@ int p3t_hard_enqueue(void) {
     g_prio.clear();
     if ((r = B.cost.reserve(2 * (size_t)nc + 2)) || (r = B.times.reserve(2 * (size_t)nc + 2))) return r;
     cudaMemsetAsync(B.cost.p, 0, (2 * (size_t)nc + 2) * sizeof(long long), c->stream);
-    cudaMemsetAsync(B.queue.p, 0, 3 * sizeof(int32_t), c->stream);
+    cudaMemsetAsync(B.queue.p, 0, 4 * sizeof(int32_t), c->stream);
     cudaMemsetAsync(B.n_cols.p, 0, sizeof(int32_t), c->stream);
     g_enqueued = nc;
     return cuda_status(cudaGetLastError());
@@ -1463,6 +1526,25 @@ int p3t_hard_integrate(int istep) {
     g_last_nc = nc;
     int r = 0;
     const Params P = E.params();
+    // The isolated bodies' drift (k_isolated) touches only bodies outside
+    // every cluster, so it runs beside the cluster launch, queued after it on
+    // a stream of the lowest priority: its blocks take the SMs the cluster
+    // launch leaves in its tail, and the library stream waits for both.  Its
+    // blocks reserve ISO_SMEM of shared memory they do not use, so none lands
+    // beside a lone-form CTA (whose FP64 chain it would slow).
+    static cudaStream_t s_iso = nullptr;
+    static cudaEvent_t ev_iso_ready = nullptr, ev_iso_done = nullptr;
+    constexpr int ISO_SMEM = 96 * 1024;
+    if (!s_iso) {
+        int lo = 0, hi = 0;
+        if ((r = cuda_status(cudaDeviceGetStreamPriorityRange(&lo, &hi))) ||
+            (r = cuda_status(cudaStreamCreateWithPriority(&s_iso, cudaStreamNonBlocking, lo))) ||
+            (r = cuda_status(cudaEventCreateWithFlags(&ev_iso_ready, cudaEventDisableTiming))) ||
+            (r = cuda_status(cudaEventCreateWithFlags(&ev_iso_done, cudaEventDisableTiming))) ||
+            (r = cuda_status(cudaFuncSetAttribute(k_isolated, cudaFuncAttributeMaxDynamicSharedMemorySize, ISO_SMEM))))
+            return r;
+    }
+    if (E.S.n > 0 && (r = cuda_status(cudaEventRecord(ev_iso_ready, c->stream)))) return r;
     if (nc > 0) {
         HardArgs A;
         A.S = E.S;
@@ -1500,8 +1582,8 @@ int p3t_hard_integrate(int istep) {
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
         if (g_hard_mode == 0) {
             static bool attr = false;
-            static cudaStream_t s_wide = nullptr;
-            static cudaEvent_t ev_ready = nullptr, ev_done = nullptr;
+            static cudaStream_t s_wide = nullptr, s_lone = nullptr;
+            static cudaEvent_t ev_ready = nullptr, ev_done = nullptr, ev_lone = nullptr;
             const int smem_w = (int)sizeof(BundleSmem<BCAP_WIDE>);
             const int smem = g_bcap == 128 ? (int)sizeof(BundleSmem<128>) : (int)sizeof(BundleSmem<256>);
             if (!attr) {
@@ -1516,25 +1598,42 @@ int p3t_hard_integrate(int istep) {
                                                           (int)sizeof(BundleSmem<128>)))) ||
                     (r = cuda_status(cudaFuncSetAttribute(k_hard_wide, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                           smem_w))) ||
-                    (r = cuda_status(cudaStreamCreateWithFlags(&s_wide, cudaStreamNonBlocking))) ||
+                    (r = cuda_status(cudaFuncSetAttribute(k_hard_lone, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                          (int)sizeof(LoneSmem)))) ||
+                    (r = cuda_status(cudaStreamCreateWithPriority(&s_lone, cudaStreamNonBlocking, -1000))) ||
+                    (r = cuda_status(cudaEventCreateWithFlags(&ev_lone, cudaEventDisableTiming))) ||
+                    (r = cuda_status(cudaStreamCreateWithPriority(&s_wide, cudaStreamNonBlocking, -1000))) ||
                     (r = cuda_status(cudaEventCreateWithFlags(&ev_ready, cudaEventDisableTiming))) ||
                     (r = cuda_status(cudaEventCreateWithFlags(&ev_done, cudaEventDisableTiming))))
                     return r;
                 attr = true;
             }
-            // the clusters above BCAP_MAIN bodies on a second stream, started
-            // first so that they hold SMs from the beginning (a handful of CTAs;
-            // they leave at once when there are none)
+            // the lone clusters and the clusters above BCAP_MAIN bodies on
+            // streams of their own, started first so that they hold SMs from the
+            // beginning (a handful of CTAs; they leave at once when there are none)
+            const bool lone = g_lone > 0.f && g_lone_ctas > 0 && g_frag.a_frag <= 0.;
+            if ((r = cuda_status(cudaEventRecord(g_ev_launch[0], c->stream)))) return r;
+            if (A.wide || lone) {
+                if ((r = cuda_status(cudaEventRecord(ev_ready, c->stream)))) return r;
+            }
+            if (lone) {
+                // The lone CTAs must hold their SMs before the persistent
+                // bundle CTAs fill every SM: the queue is complete when the
+                // library stream has drained, and the lone kernel is then
+                // submitted first, with no dependency left to resolve.
+                if ((r = cuda_status(cudaStreamSynchronize(c->stream)))) return r;
+                { P3T_COUNT_LAUNCH(); k_hard_lone<<<g_lone_ctas, LT, sizeof(LoneSmem), s_lone>>>(A); }
+                if ((r = cuda_status(cudaGetLastError())) || (r = cuda_status(cudaEventRecord(ev_lone, s_lone))))
+                    return r;
+            }
             if (A.wide) {
-                if ((r = cuda_status(cudaEventRecord(ev_ready, c->stream))) ||
-                    (r = cuda_status(cudaStreamWaitEvent(s_wide, ev_ready, 0))))
+                if ((r = cuda_status(cudaStreamWaitEvent(s_wide, ev_ready, 0))))
                     return r;
                 { P3T_COUNT_LAUNCH(); k_hard_wide<<<std::max(1, sms / 16), BT, smem_w, s_wide>>>(A); }
                 if ((r = cuda_status(cudaGetLastError()))) return r;
             }
             // persistent: g_bocc CTAs per SM (fewer when there are few clusters)
             const int blocks = std::max(1, std::min(sms * g_bocc, (nc + 3) / 4));
-            if ((r = cuda_status(cudaEventRecord(g_ev_launch[0], c->stream)))) return r;
             if (g_bcap == 256)
                 { P3T_COUNT_LAUNCH(); k_hard_bundles<256, 2><<<blocks, bundle_threads(256), smem, c->stream>>>(A); }
             else if (g_bocc == 3)
@@ -1542,11 +1641,13 @@ int p3t_hard_integrate(int istep) {
             else
                 { P3T_COUNT_LAUNCH(); k_hard_bundles<128, 4><<<blocks, BT, smem, c->stream>>>(A); }
             if ((r = cuda_status(cudaGetLastError()))) return r;
-            if ((r = cuda_status(cudaEventRecord(g_ev_launch[1], c->stream)))) return r;
-            g_launch_timed = true;
             if (A.wide && ((r = cuda_status(cudaEventRecord(ev_done, s_wide))) ||
                            (r = cuda_status(cudaStreamWaitEvent(c->stream, ev_done, 0)))))
                 return r;
+            if (lone && (r = cuda_status(cudaStreamWaitEvent(c->stream, ev_lone, 0)))) return r;
+            // the launch's time spans all three forms
+            if ((r = cuda_status(cudaEventRecord(g_ev_launch[1], c->stream)))) return r;
+            g_launch_timed = true;
         } else {
             const int blocks = std::max(1, std::min(sms * 2, (nc + 3) / 4));
             if ((r = cuda_status(cudaEventRecord(g_ev_launch[0], c->stream)))) return r;
@@ -1556,13 +1657,19 @@ int p3t_hard_integrate(int istep) {
         }
         if ((r = cuda_status(cudaGetLastError()))) return r;
     }
-    IsoArgs I;
-    I.S = E.S;
-    I.P = P;
-    I.t0 = (istep - 1) * P.dt_tree;
-    I.t1 = istep * P.dt_tree;
-    I.status = c->status;
-    if (E.S.n > 0) { P3T_COUNT_LAUNCH(); k_isolated<<<(E.S.n + 127) / 128, 128, 0, c->stream>>>(I); }
+    if (E.S.n > 0) {
+        IsoArgs I;
+        I.S = E.S;
+        I.P = P;
+        I.t0 = (istep - 1) * P.dt_tree;
+        I.t1 = istep * P.dt_tree;
+        I.status = c->status;
+        if ((r = cuda_status(cudaStreamWaitEvent(s_iso, ev_iso_ready, 0)))) return r;
+        { P3T_COUNT_LAUNCH(); k_isolated<<<(E.S.n + 127) / 128, 128, ISO_SMEM, s_iso>>>(I); }
+        if ((r = cuda_status(cudaGetLastError())) || (r = cuda_status(cudaEventRecord(ev_iso_done, s_iso))) ||
+            (r = cuda_status(cudaStreamWaitEvent(c->stream, ev_iso_done, 0))))
+            return r;
+    }
     return cuda_status(cudaGetLastError());
 }
 
@@ -1708,6 +1815,13 @@ int p3t_hard(int istep, int col_cap, long long *col_pairs, double *edisp) {
     int r = p3t_hard_enqueue();
     if (r || (r = p3t_hard_integrate(istep))) return r > 0 ? P3T_COUNT_STATUS(r) : r;
     return p3t_hard_fetch(col_cap, col_pairs, edisp);
+}
+
+int p3t_set_hard_lone(float log2_steps, int ctas) {
+    if (ctas < 0 || ctas > 4096 || !(log2_steps >= 0.f)) return -(int)cudaErrorInvalidValue;
+    g_lone = log2_steps;
+    g_lone_ctas = ctas;
+    return 0;
 }
 
 int p3t_set_hard_step_cap(int max_block_steps) {

@@ -246,6 +246,19 @@ int p3t_set_hard_wide(int on);
  * (default), 128/3 or 128/4 (clusters above the slot count go to the wide
  * or one-per-CTA form).  Results are bit-identical; set by the autotuner. */
 int p3t_set_hard_bundle(int member_slots, int ctas_per_sm);
+/* Bundle form with the learned order: clusters whose predicted
+ * log2(1 + block steps) is at least log2_steps and that have at most 64
+ * members run in the lone form -- each alone on a CTA of 128 threads that
+ * holds the whole cluster in shared memory and owns its SM, `ctas` such CTAs
+ * submitted before the bundle launch -- which shortens a block step's chain
+ * of FP64 operations (the longest chains of block steps set the launch's
+ * span).  Perfect accretion only (with fragmentation the clusters stay in the
+ * bundles); a lone cluster that collides continues in the one-cluster-per-CTA
+ * form.  log2_steps = 0 or ctas = 0: off (the default: the SMs it holds cost
+ * the bundles more throughput than its shorter chains gain at 1M bodies).
+ * Results are bit-identical.  ctas in [0, 4096].  No counterpart in GPLUM's
+ * interface. */
+int p3t_set_hard_lone(float log2_steps, int ctas);
 /* KOMINAMI fragmentation of the collision outcome (src/collisionB.h:7-93;
  * Collision::a_frag, N_frag, Collision0::m_min of parameter.dat).  a_frag = 0
  * (the default) is perfect accretion.  A collision makes

@@ -86,3 +86,37 @@ def test_bundles_match_tiers_bitwise(gpu, n, f, seed, mfac):
     b = forms[0]
     if f > 1.0:
         assert len(b[0]) > 0
+
+
+# the lone form (one cluster per CTA, the whole cluster in shared memory) for
+# the clusters the learned model predicts to run longest: with a threshold of
+# 0.5 every cluster goes there, with 3.0 the head of the queue; collisions
+# (f > 1) hand a cluster to the one-cluster-per-team loop mid-integration
+@pytest.mark.parametrize("n,f,seed", [(65536, 1.0, 5), (65536, 40.0, 6), (8192, 200.0, 7)])
+def test_lone_form_matches_tiers_bitwise(gpu, n, f, seed):
+    from gplum_gb300 import scheduler
+
+    g = prepared(n, f, seed)
+    off, _ = g.cluster_lists()
+    nc = len(off) - 1
+    assert g.lib.p3t_state_snapshot(0) == 0
+    scheduler.load(lib=g.lib)
+    assert g.lib.p3t_set_schedule(1) == 0
+    try:
+        t = run(g, 1, nc)
+        forms = []
+        for thr, ctas in ((0.5, 152), (3.0, 16)):
+            assert g.lib.p3t_set_hard_lone(thr, ctas) == 0
+            forms.append(run(g, 0, nc))
+    finally:
+        g.lib.p3t_set_hard_lone(0.0, 0)
+        g.lib.p3t_set_schedule(0)
+        g.lib.p3t_set_hard_mode(0)
+    for b in forms:
+        np.testing.assert_array_equal(b[0], t[0])
+        assert b[1].tobytes() == t[1].tobytes()
+        for k in FIELDS:
+            assert b[2][k].tobytes() == t[2][k].tobytes(), k
+        np.testing.assert_array_equal(b[3], t[3])
+    if f > 1.0:
+        assert len(forms[0][0]) > 0
