@@ -17,9 +17,6 @@
 namespace p3t {
 
 constexpr int MAX_BLOCK_STEPS = 1 << 20;  // per cluster and tree step
-// lone form: clusters of at most this many members (larger ones run faster in
-// a bundle CTA's 256 threads than in the lone CTA's 128)
-constexpr int LONE_NMAX = 64;
 
 // Per-member working copy of one cluster (FPHard fields), indexed by the
 // member's slot in the cluster lists.
@@ -103,6 +100,7 @@ struct HardArgs {
     int frag_base, frag_cap;  // hard slots frag_base + k hold fragment k
     int wide;                 // bundle form: clusters above BCAP_MAIN in k_hard_wide (1) or run_cluster (0)
     int max_steps;            // block steps a cluster may take in one tree step (ST_ITER_CAP beyond)
+    int lone_in;              // bundle form: the lone tier runs in the bundle CTAs (1) or in k_hard_lone (0)
     unsigned long long *live; // optional [2]: pair terms evaluated (predicted/corrected, full), bundle form
 };
 
@@ -673,8 +671,8 @@ struct ClusterRun {
 // three parts: load (FPHard from FPGrav, the prefilter, the first full
 // force), the block-step loop from run.time on, and the finish (last full
 // force, write-back, logs).  The lone-cluster form (hard_lone.cuh) runs its
-// own block steps and hands a cluster to cluster_loop at its first
-// collision.
+// own block steps and hands each block step that has a collision to
+// cluster_loop (one_step).
 template <int TEAM>
 __device__ void cluster_load(const HardArgs &A, int c, const Team<TEAM> &tm, Pre &pre) {
     const Params &P = A.P;
@@ -727,7 +725,8 @@ __device__ void cluster_load(const HardArgs &A, int c, const Team<TEAM> &tm, Pre
 }
 
 template <int TEAM>
-__device__ void cluster_loop(const HardArgs &A, int c, const Team<TEAM> &tm, const Pre &pre, ClusterRun &run) {
+__device__ void cluster_loop(const HardArgs &A, int c, const Team<TEAM> &tm, const Pre &pre, ClusterRun &run,
+                             bool one_step = false) {
     const Params &P = A.P;
     const Hard &H = A.H;
     const int rank = tm.rank;
@@ -880,6 +879,7 @@ __device__ void cluster_loop(const HardArgs &A, int c, const Team<TEAM> &tm, con
         for (int k = rank; k < n; k += TEAM)
             if (!H.dead[o + k]) tmin = dmin(tmin, H.th[o + k]);
         time = tm.min(tmin);
+        if (one_step) break;
     }
     run.n_col = n_col;
     run.ed = ed;
@@ -989,8 +989,8 @@ __global__ void __launch_bounds__(128, 2) k_hard_clusters(HardArgs A) {
 
 }  // namespace p3t
 
-#include "hard_bundle.cuh"
 #include "hard_lone.cuh"
+#include "hard_bundle.cuh"
 
 namespace p3t {
 
@@ -1150,8 +1150,8 @@ __global__ void k_isolated(IsoArgs A) {
 constexpr int ORDER_NB = 4096;
 
 __global__ void k_order_bins(const int32_t *cnt, const float *prio, int nc, int mode, int main_cap, int warp_min, int cta_min,
-                             float pmin, float pscale, int heavy_key, int lone_key, int32_t *bin, int32_t *hist,
-                             int32_t *n_heavy) {
+                             float pmin, float pscale, int heavy_key, int lone_key, int lone_nmax, int32_t *bin,
+                             int32_t *hist, int32_t *n_heavy) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nc) return;
     const int n = cnt[k];
@@ -1161,8 +1161,8 @@ __global__ void k_order_bins(const int32_t *cnt, const float *prio, int nc, int 
         key = (v >= 0.f) ? (v < (float)(ORDER_NB - 1) ? (int)v : ORDER_NB - 1) : 0;  // NaN -> 0
     }
     // bundle form: tier 0 above the bundle's slots, tier 2 the lone form
-    // (predicted longest chains of at most LONE_NMAX members), tier 1 the rest
-    const int tier = (mode == 0) ? (n > main_cap ? 0 : ((key >= lone_key && n <= LONE_NMAX) ? 2 : 1))
+    // (predicted longest chains of at most lone_nmax members), tier 1 the rest
+    const int tier = (mode == 0) ? (n > main_cap ? 0 : ((key >= lone_key && n <= lone_nmax) ? 2 : 1))
                                  : (n >= cta_min ? 0 : (n >= warp_min ? 1 : 2));
     const int b = tier * ORDER_NB + (ORDER_NB - 1 - key);
     bin[k] = b;
@@ -1281,8 +1281,8 @@ static int g_bcap = 256, g_bocc = 2;  // bundle member slots and CTAs per SM (25
 static FragParams g_frag = {0., 9.426627927538057e-12, 10, 0, 0ULL};  // off (a_frag = 0)
 static int g_frag_cap = 0;  // fragment slots of the current launch
 static int g_max_steps = MAX_BLOCK_STEPS;  // block-step cap per cluster and tree step
-// lone form: clusters predicted to take at least 2^g_lone - 1 block steps, on
-// g_lone_ctas CTAs of their own (0: off)
+// lone form: clusters predicted to take at least 2^g_lone - 1 block steps (0:
+// off), on g_lone_ctas CTAs of their own (0: in the bundle CTAs)
 static float g_lone = 0.f;
 static int g_lone_ctas = 0;
 // events around the last cluster launch (k_hard_bundles / k_hard_clusters) on
@@ -1493,12 +1493,11 @@ int p3t_hard_enqueue(void) {
         int heavy_key = 2147483647, lone_key = 2147483647;
         if (prio && (int)g_prio.size() != nc && g_heavy > 0.f)
             heavy_key = std::min(ORDER_NB - 1, (int)((g_heavy - pmin) * pscale));
-        if (prio && (int)g_prio.size() != nc && g_lone > 0.f && g_lone_ctas > 0 && g_frag.a_frag <= 0. &&
-            g_hard_mode == 0)
+        if (prio && (int)g_prio.size() != nc && g_lone > 0.f && g_frag.a_frag <= 0. && g_hard_mode == 0)
             lone_key = std::max(0, std::min(ORDER_NB - 1, (int)((g_lone - pmin) * pscale)));
         { P3T_COUNT_LAUNCH(); k_order_bins<<<(nc + 255) / 256, 256, 0, c->stream>>>(E.cl_cnt.p, prio, nc, g_hard_mode, g_bcap, g_warp_min, g_cta_min,
-                                                              pmin, pscale, heavy_key, lone_key, B.bin.p, B.hist.p,
-                                                              B.ntier.p + 3); }
+                                                              pmin, pscale, heavy_key, lone_key, LCAP, B.bin.p,
+                                                              B.hist.p, B.ntier.p + 3); }
         { P3T_COUNT_LAUNCH(); k_order_scan<<<1, 1024, 0, c->stream>>>(B.hist.p, B.ntier.p); }
         { P3T_COUNT_LAUNCH(); k_order_scatter<<<(nc + 255) / 256, 256, 0, c->stream>>>(B.bin.p, nc, B.hist.p, B.order.p); }
         if ((r = cuda_status(cudaGetLastError()))) return r;
@@ -1546,7 +1545,7 @@ int p3t_hard_integrate(int istep) {
     }
     if (E.S.n > 0 && (r = cuda_status(cudaEventRecord(ev_iso_ready, c->stream)))) return r;
     if (nc > 0) {
-        HardArgs A;
+        HardArgs A{};
         A.S = E.S;
         A.P = P;
         A.H = B.H;
@@ -1585,21 +1584,28 @@ int p3t_hard_integrate(int istep) {
             static cudaStream_t s_wide = nullptr, s_lone = nullptr;
             static cudaEvent_t ev_ready = nullptr, ev_done = nullptr, ev_lone = nullptr;
             const int smem_w = (int)sizeof(BundleSmem<BCAP_WIDE>);
-            const int smem = g_bcap == 128 ? (int)sizeof(BundleSmem<128>) : (int)sizeof(BundleSmem<256>);
+            static_assert(sizeof(LoneSmem<bundle_threads(256)>) <= sizeof(BundleSmem<256>) &&
+                              sizeof(LoneSmem<BT>) <= 200 * 1024 && sizeof(LoneSmem<LONE_T>) <= LONE_EXCL_SMEM,
+                          "lone state fits the shared memory it borrows");
+            // the lone tier in the bundle CTAs: k_hard_lone with no CTAs of its own
+            const bool lone = g_lone > 0.f && g_frag.a_frag <= 0.;
+            A.lone_in = (lone && g_lone_ctas == 0) ? 1 : 0;
+            int smem = g_bcap == 128 ? (int)sizeof(BundleSmem<128>) : (int)sizeof(BundleSmem<256>);
+            if (A.lone_in && g_bcap == 128) smem = std::max(smem, (int)sizeof(LoneSmem<BT>));
             if (!attr) {
                 if ((r = cuda_status(cudaFuncSetAttribute(k_hard_bundles<256, 2>,
                                                           cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                           (int)sizeof(BundleSmem<256>)))) ||
-                    (r = cuda_status(cudaFuncSetAttribute(k_hard_bundles<128, 3>,
-                                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                          (int)sizeof(BundleSmem<128>)))) ||
-                    (r = cuda_status(cudaFuncSetAttribute(k_hard_bundles<128, 4>,
-                                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                          (int)sizeof(BundleSmem<128>)))) ||
+                    (r = cuda_status(cudaFuncSetAttribute(
+                         k_hard_bundles<128, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)std::max(sizeof(BundleSmem<128>), sizeof(LoneSmem<BT>))))) ||
+                    (r = cuda_status(cudaFuncSetAttribute(
+                         k_hard_bundles<128, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)std::max(sizeof(BundleSmem<128>), sizeof(LoneSmem<BT>))))) ||
                     (r = cuda_status(cudaFuncSetAttribute(k_hard_wide, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                           smem_w))) ||
                     (r = cuda_status(cudaFuncSetAttribute(k_hard_lone, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                          (int)sizeof(LoneSmem)))) ||
+                                                          LONE_EXCL_SMEM))) ||
                     (r = cuda_status(cudaStreamCreateWithPriority(&s_lone, cudaStreamNonBlocking, -1000))) ||
                     (r = cuda_status(cudaEventCreateWithFlags(&ev_lone, cudaEventDisableTiming))) ||
                     (r = cuda_status(cudaStreamCreateWithPriority(&s_wide, cudaStreamNonBlocking, -1000))) ||
@@ -1611,18 +1617,18 @@ int p3t_hard_integrate(int istep) {
             // the lone clusters and the clusters above BCAP_MAIN bodies on
             // streams of their own, started first so that they hold SMs from the
             // beginning (a handful of CTAs; they leave at once when there are none)
-            const bool lone = g_lone > 0.f && g_lone_ctas > 0 && g_frag.a_frag <= 0.;
+            const bool lone_k = lone && g_lone_ctas > 0;
             if ((r = cuda_status(cudaEventRecord(g_ev_launch[0], c->stream)))) return r;
-            if (A.wide || lone) {
+            if (A.wide || lone_k) {
                 if ((r = cuda_status(cudaEventRecord(ev_ready, c->stream)))) return r;
             }
-            if (lone) {
+            if (lone_k) {
                 // The lone CTAs must hold their SMs before the persistent
                 // bundle CTAs fill every SM: the queue is complete when the
                 // library stream has drained, and the lone kernel is then
                 // submitted first, with no dependency left to resolve.
                 if ((r = cuda_status(cudaStreamSynchronize(c->stream)))) return r;
-                { P3T_COUNT_LAUNCH(); k_hard_lone<<<g_lone_ctas, LT, sizeof(LoneSmem), s_lone>>>(A); }
+                { P3T_COUNT_LAUNCH(); k_hard_lone<<<g_lone_ctas, LONE_T, LONE_EXCL_SMEM, s_lone>>>(A); }
                 if ((r = cuda_status(cudaGetLastError())) || (r = cuda_status(cudaEventRecord(ev_lone, s_lone))))
                     return r;
             }
@@ -1644,7 +1650,7 @@ int p3t_hard_integrate(int istep) {
             if (A.wide && ((r = cuda_status(cudaEventRecord(ev_done, s_wide))) ||
                            (r = cuda_status(cudaStreamWaitEvent(c->stream, ev_done, 0)))))
                 return r;
-            if (lone && (r = cuda_status(cudaStreamWaitEvent(c->stream, ev_lone, 0)))) return r;
+            if (lone_k && (r = cuda_status(cudaStreamWaitEvent(c->stream, ev_lone, 0)))) return r;
             // the launch's time spans all three forms
             if ((r = cuda_status(cudaEventRecord(g_ev_launch[1], c->stream)))) return r;
             g_launch_timed = true;

@@ -1032,8 +1032,8 @@ __global__ void __launch_bounds__(bundle_threads(BCAP), OCC) k_hard_bundles(Hard
     __shared__ long long red_l[BT / 32];
     __shared__ int q_sh;
     const int tid = threadIdx.x;
+    const Team<BT> tm{tid, red_d, red_l};
     if (!A.wide) {
-        Team<BT> tm{tid, red_d, red_l};
         for (int guard = 0; guard < (1 << 30); guard++) {
             if (tid == 0) q_sh = atomicAdd(&A.queue[0], 1);
             __syncthreads();
@@ -1041,6 +1041,25 @@ __global__ void __launch_bounds__(bundle_threads(BCAP), OCC) k_hard_bundles(Hard
             __syncthreads();
             if (q >= A.n_tier[0]) break;
             run_cluster<BT>(A, A.order[q], tm);
+        }
+    }
+    // the lone tier: each cluster integrated alone by the whole CTA, the
+    // bundle's shared memory holding its state (the predicted longest chains
+    // start first, beside bundles on the other CTA slots of the SM)
+    if (A.lone_in) {
+        LoneSmem<BT> &L = *reinterpret_cast<LoneSmem<BT> *>(bundle_smem);
+        for (int guard = 0; guard < (1 << 30); guard++) {
+            if (tid == 0) q_sh = atomicAdd(&A.queue[3], 1);
+            __syncthreads();
+            const int q = q_sh;
+            __syncthreads();
+            if (q >= A.n_tier[2]) break;
+            const int c = A.order[A.n_tier[0] + A.n_tier[1] + q];
+            if (A.cnt[c] > LCAP) {  // the lone tier holds at most LCAP members
+                if (tid == 0) atomicOr(A.status, ST_CLUSTER_TOO_BIG);
+                continue;
+            }
+            lone_cluster<BT>(A, c, L, tm, red_d);
         }
     }
     if (tid == 0) {

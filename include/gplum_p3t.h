@@ -232,32 +232,20 @@ int p3t_set_hard_tiers(int warp_min, int cta_min);
  * Both give identical results.  No counterpart in GPLUM's interface. */
 int p3t_set_hard_mode(int mode);
 /* Bundle form with the learned order: clusters whose predicted
- * log2(1 + block steps) is at least log2_steps run first, each alone in a
- * CTA, so the longest chains of block steps do not wait on a full bundle
- * (default 5.5, about 45 block steps; set by the autotuner; 0 turns it
- * off).  Results do not depend on it. */
-int p3t_set_hard_heavy(float log2_steps);
-/* Bundle form: the clusters above the bundle's member slots run in a second, concurrent
- * launch as lone bundles of up to 512 slots (1) or one cluster per CTA
- * inside the main launch (0, default).  Results are bit-identical; set by the
- * autotuner. */
-int p3t_set_hard_wide(int on);
-/* Bundle form: member slots per bundle and resident CTAs per SM -- 256/2
- * (default), 128/3 or 128/4 (clusters above the slot count go to the wide
- * or one-per-CTA form).  Results are bit-identical; set by the autotuner. */
-int p3t_set_hard_bundle(int member_slots, int ctas_per_sm);
-/* Bundle form with the learned order: clusters whose predicted
  * log2(1 + block steps) is at least log2_steps and that have at most 64
- * members run in the lone form -- each alone on a CTA of 128 threads that
- * holds the whole cluster in shared memory and owns its SM, `ctas` such CTAs
- * submitted before the bundle launch -- which shortens a block step's chain
- * of FP64 operations (the longest chains of block steps set the launch's
- * span).  Perfect accretion only (with fragmentation the clusters stay in the
- * bundles); a lone cluster that collides continues in the one-cluster-per-CTA
- * form.  log2_steps = 0 or ctas = 0: off (the default: the SMs it holds cost
- * the bundles more throughput than its shorter chains gain at 1M bodies).
- * Results are bit-identical.  ctas in [0, 4096].  No counterpart in GPLUM's
- * interface. */
+ * members run in the lone form -- each integrated alone by one CTA that holds
+ * the whole cluster in shared memory for all its block steps, with the
+ * independent parts of a block step (members x components, target x partner
+ * pair terms, the sun force, the two time-step criteria) spread over the
+ * CTA's threads -- which shortens a block step's chain of FP64 operations
+ * (the longest chains of block steps set the launch's span).  ctas = 0: the
+ * lone clusters run first in the bundle kernel's own CTAs (256 threads, beside
+ * bundles on the SM's other CTA slot); ctas > 0: in a kernel of that many
+ * 128-thread CTAs of their own, each holding a whole SM.  Perfect accretion
+ * only (with fragmentation the clusters stay in the bundles); a lone cluster
+ * that collides continues in the one-cluster-per-CTA form.  log2_steps = 0:
+ * off (the default).  Results are bit-identical.  ctas in [0, 4096].  No
+ * counterpart in GPLUM's interface. */
 int p3t_set_hard_lone(float log2_steps, int ctas);
 /* KOMINAMI fragmentation of the collision outcome (src/collisionB.h:7-93;
  * Collision::a_frag, N_frag, Collision0::m_min of parameter.dat).  a_frag = 0

@@ -89,9 +89,11 @@ def test_bundles_match_tiers_bitwise(gpu, n, f, seed, mfac):
 
 
 # the lone form (one cluster per CTA, the whole cluster in shared memory) for
-# the clusters the learned model predicts to run longest: with a threshold of
-# 0.5 every cluster goes there, with 3.0 the head of the queue; collisions
-# (f > 1) hand a cluster to the one-cluster-per-team loop mid-integration
+# the clusters the learned model predicts to run longest, in CTAs of its own
+# (ctas > 0) and inside the bundle kernel's CTAs (ctas = 0): with a threshold
+# of 0.5 every cluster of at most 64 members goes there, with 3.0 the head of
+# the queue; collisions (f > 1) hand a cluster to the one-cluster-per-team loop
+# mid-integration
 @pytest.mark.parametrize("n,f,seed", [(65536, 1.0, 5), (65536, 40.0, 6), (8192, 200.0, 7)])
 def test_lone_form_matches_tiers_bitwise(gpu, n, f, seed):
     from gplum_gb300 import scheduler
@@ -105,7 +107,7 @@ def test_lone_form_matches_tiers_bitwise(gpu, n, f, seed):
     try:
         t = run(g, 1, nc)
         forms = []
-        for thr, ctas in ((0.5, 152), (3.0, 16)):
+        for thr, ctas in ((0.5, 152), (3.0, 16), (0.5, 0), (3.0, 0)):
             assert g.lib.p3t_set_hard_lone(thr, ctas) == 0
             forms.append(run(g, 0, nc))
     finally:
