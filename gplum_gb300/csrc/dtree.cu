@@ -580,6 +580,186 @@ __global__ void k_walk_tasks(const TNode *nd, const TNodeF *nf, const int *gnode
     }
 }
 
+// ---- the walk as one CTA per group, breadth first --------------------------------------------
+// The host builder's depth-first walk emits, in visiting order, one SPJ entry
+// per unopened cell and the bodies of every opened leaf.  The same sequence
+// comes out of a breadth-first sweep that keeps a frontier of items in that
+// order: each round replaces every still-untested cell by its verdict -- an
+// unopened cell or an opened leaf stays as a final item, an opened inner cell
+// gives way to its children in child order -- so that after the last round
+// the frontier is the depth-first output sequence.  All the CTA's threads
+// test the frontier's cells at once (the subtree walks of one thread each
+// ran at ~3 active lanes per instruction).  Items: node << 2 | kind.
+constexpr int BFS_T = 128;
+constexpr int BFS_CAP = 4096;  // frontier items per group (more: the group takes the task walk)
+enum : int { FI_PEND = 0, FI_SPJ = 1, FI_EPJ = 2 };
+
+// exclusive block-wide prefix of v over BFS_T threads (all threads call)
+__device__ __forceinline__ int bfs_scan(int v, int *ws, int &total) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[w] = x;
+    __syncthreads();
+    int off = 0, tot = 0;
+#pragma unroll
+    for (int k = 0; k < BFS_T / 32; k++) {
+        const int c = ws[k];
+        off += (k < w) ? c : 0;
+        tot += c;
+    }
+    __syncthreads();
+    total = tot;
+    return off + x - v;
+}
+
+// count pass: the final frontier of group g (blockIdx.x) into store[off[g] ..
+// off[g] + len[g]) and its EPJ / SPJ entry counts; a frontier above BFS_CAP
+// items or a full store sets *overflow (the lists then come from the task walk)
+__global__ void __launch_bounds__(BFS_T) k_walk_bfs(const TNode *nd, const TNodeF *nf, const int *gnode, int ng,
+                                                    double theta2, float theta2f, int *jc, int *sc, int *len,
+                                                    long long *off, int *store, unsigned long long *cursor,
+                                                    long long store_cap, int *overflow) {
+    __shared__ int buf[2][BFS_CAP];
+    __shared__ int ws[BFS_T / 32];
+    __shared__ long long s_base;
+    const int g = blockIdx.x, tid = threadIdx.x;
+    if (g >= ng) return;
+    const int gn = gnode[g];
+    float fil[3], fih[3], fol[3], foh[3];
+    {
+        const TNodeF &G = nf[gn];
+        for (int d = 0; d < 3; d++) {
+            fil[d] = G.ilo[d];
+            fih[d] = G.ihi[d];
+            fol[d] = G.olo[d];
+            foh[d] = G.ohi[d];
+        }
+    }
+    if (tid == 0) buf[0][0] = (0 << 2) | FI_PEND;  // the root
+    __syncthreads();
+    int cur = 0, n = 1;
+    bool over = false, pend = true;
+    for (int round = 0; pend && round < 64; round++) {
+        int run = 0, grown = 0;
+        for (int base = 0; base < n; base += BFS_T) {
+            const int q = base + tid;
+            int item = 0, cnt = 0, kind = FI_SPJ, nch = 0, c0 = 0;
+            if (q < n) {
+                item = buf[cur][q];
+                kind = item & 3;
+                cnt = 1;
+                if (kind == FI_PEND) {
+                    const int c = item >> 2;
+                    const TNodeF &Q = nf[c];
+                    int o = open3(Q, fil, fih, fol, foh, theta2f);
+                    if (o == 0) {
+                        const TNode &Gd = nd[gn];
+                        o = cell_open(nd[c], Gd.ilo, Gd.ihi, Gd.olo, Gd.ohi, theta2) ? 1 : -1;
+                    }
+                    if (o < 0) {
+                        kind = FI_SPJ;
+                    } else if (Q.nchild == 0) {
+                        kind = FI_EPJ;
+                    } else {
+                        nch = Q.nchild;
+                        c0 = Q.child0;
+                        cnt = nch;
+                    }
+                    item = (c << 2) | kind;
+                }
+            }
+            int tot = 0;
+            const int o = run + bfs_scan(cnt, ws, tot);
+            if (q < n && o + cnt <= BFS_CAP) {
+                if (nch) {
+                    for (int k = 0; k < nch; k++) buf[cur ^ 1][o + k] = ((c0 + k) << 2) | FI_PEND;
+                } else {
+                    buf[cur ^ 1][o] = item;
+                }
+            }
+            grown += __syncthreads_or(nch > 0);
+            run += tot;
+        }
+        if (run > BFS_CAP) {
+            over = true;
+            break;
+        }
+        cur ^= 1;
+        n = run;
+        pend = grown > 0;
+        __syncthreads();
+    }
+    if (pend && !over) over = true;  // deeper than 64 rounds
+    if (!over) {
+        int nj = 0, ns = 0;
+        for (int q = tid; q < n; q += BFS_T) {
+            const int it = buf[cur][q];
+            if ((it & 3) == FI_EPJ) nj += nf[it >> 2].count;
+            else ns += 1;
+        }
+        int tj = 0, ts = 0;
+        bfs_scan(nj, ws, tj);
+        bfs_scan(ns, ws, ts);
+        if (tid == 0) {
+            const long long b = (long long)atomicAdd(cursor, (unsigned long long)n);
+            s_base = b;
+            if (b + n > store_cap) atomicOr(overflow, 1);
+            jc[g] = tj;
+            sc[g] = ts;
+            len[g] = n;
+            off[g] = b;
+        }
+        __syncthreads();
+        const long long b = s_base;
+        if (b + n <= store_cap)
+            for (int q = tid; q < n; q += BFS_T) store[b + q] = buf[cur][q];
+    } else if (tid == 0) {
+        atomicOr(overflow, 1);
+        jc[g] = 0;
+        sc[g] = 0;
+        len[g] = 0;
+        off[g] = 0;
+    }
+}
+
+// fill pass: group g's entries from its stored frontier, in frontier order
+__global__ void __launch_bounds__(BFS_T) k_walk_bfs_fill(const TNodeF *nf, int ng, const int *len, const long long *off,
+                                                         const int *store, const int *order, const int *j_off,
+                                                         const int *s_off, int *j_idx, int *s_idx) {
+    __shared__ int ws[BFS_T / 32];
+    const int g = blockIdx.x, tid = threadIdx.x;
+    if (g >= ng) return;
+    const int n = len[g];
+    const int *fr = store + off[g];
+    int jrun = j_off[g], srun = s_off[g];
+    for (int base = 0; base < n; base += BFS_T) {
+        const int q = base + tid;
+        int it = 0, nj = 0, ns = 0, first = 0;
+        if (q < n) {
+            it = fr[q];
+            if ((it & 3) == FI_EPJ) {
+                const TNodeF &Q = nf[it >> 2];
+                nj = Q.count;
+                first = Q.first;
+            } else {
+                ns = 1;
+            }
+        }
+        int tj = 0, ts = 0;
+        const int oj = jrun + bfs_scan(nj, ws, tj);
+        const int os = srun + bfs_scan(ns, ws, ts);
+        for (int k = 0; k < nj; k++) j_idx[oj + k] = order[first + k];
+        if (ns) s_idx[os] = it >> 2;
+        jrun += tj;
+        srun += ts;
+    }
+}
+
 __global__ void k_task_list(const int *flag, const int *pos, long long np, int *tasks) {
     const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (p < np && flag[p]) tasks[pos[p]] = (int)p;
@@ -616,12 +796,18 @@ struct DTree {
     DevBuf<TNodeF> nf;
     DevBuf<int> top, pc, tasks;
     DevBuf<unsigned char> ostat;
+    DevBuf<int> bjc, bsc, blen, bstore, bover;  // breadth-first walk
+    DevBuf<long long> boff;
+    DevBuf<unsigned long long> bcur;
+    long long bstore_cap = 1LL << 24;
     size_t node_cap = 0;
     std::vector<int> level_start;
     int n_nodes = 0, n_groups = 0;
 };
 static DTree g_dt;
 static int g_walk_depth = 3;  // levels above the walk's task split
+static int g_walk_bfs = 1;    // walk form: breadth first per group (1) or subtree tasks (0)
+static int g_walk_last = -1;  // the form the last build's lists came from
 
 // (key, idx) sorted in place by key, stably (8 passes of 8 bits over `bits`)
 static int radix_sort(Context *c, DTree &T, unsigned long long *&key, int *&idx, unsigned long long *&key2,
@@ -732,9 +918,44 @@ static int device_tree(Context *c, double theta, int n_leaf_limit, int n_group_l
         return r;
     { P3T_COUNT_LAUNCH(); k_group_fill<<<nblocks(n), 256, 0, c->stream>>>(T.gmark.p, T.gpos.p, n, ng, T.gnode.p, d.i_off.p); }
     cudaMemcpyAsync(d.i_idx.p, idx, n * sizeof(int), cudaMemcpyDeviceToDevice, c->stream);
-    // 5. walks: the top levels in pre-order (host, from the node table), then
-    // (group, top node) pairs: open tests, counts, offsets, entries
-    {
+    // 5. walks: breadth first, one CTA per group; if a frontier outgrows its
+    // CTA (or the frontier store), the task walk below
+    if ((r = T.nf.reserve(T.n_nodes))) return r;
+    { P3T_COUNT_LAUNCH(); k_node_f32<<<nblocks(T.n_nodes), 256, 0, c->stream>>>(T.nd.p, T.n_nodes, T.nf.p); }
+    bool walked = false;
+    if (g_walk_bfs && ng > 0) {
+        if ((r = T.bjc.reserve(ng)) || (r = T.bsc.reserve(ng)) || (r = T.blen.reserve(ng)) ||
+            (r = T.boff.reserve(ng)) || (r = T.bover.reserve(1)) || (r = T.bcur.reserve(1)) ||
+            (r = T.bstore.reserve((size_t)T.bstore_cap)))
+            return r;
+        cudaMemsetAsync(T.bover.p, 0, sizeof(int), c->stream);
+        cudaMemsetAsync(T.bcur.p, 0, sizeof(unsigned long long), c->stream);
+        { P3T_COUNT_LAUNCH(); k_walk_bfs<<<ng, BFS_T, 0, c->stream>>>(T.nd.p, T.nf.p, T.gnode.p, ng, theta * theta,
+                                                                  (float)(theta * theta), T.bjc.p, T.bsc.p, T.blen.p,
+                                                                  T.boff.p, T.bstore.p, T.bcur.p, T.bstore_cap,
+                                                                  T.bover.p); }
+        int over = 0;
+        unsigned long long used = 0;
+        int nj = 0, ns = 0;
+        if ((r = E.scan(T.bjc.p, d.j_off.p, ng, &nj)) || (r = E.scan(T.bsc.p, d.s_off.p, ng, &ns)) ||
+            (r = d2h(c, &over, T.bover.p, sizeof(int))) || (r = d2h(c, &used, T.bcur.p, sizeof(used))))
+            return r;
+        if (!over) {
+            if ((r = h2d(c, d.j_off.p + ng, &nj, sizeof(int))) || (r = h2d(c, d.s_off.p + ng, &ns, sizeof(int))) ||
+                (r = d.j_idx.reserve(nj)) || (r = d.s_idx.reserve(ns)))
+                return r;
+            { P3T_COUNT_LAUNCH(); k_walk_bfs_fill<<<ng, BFS_T, 0, c->stream>>>(T.nf.p, ng, T.blen.p, T.boff.p, T.bstore.p,
+                                                                           idx, d.j_off.p, d.s_off.p, d.j_idx.p,
+                                                                           d.s_idx.p); }
+            walked = true;
+        } else if ((long long)used > T.bstore_cap) {
+            T.bstore_cap = (long long)(used + used / 4);  // room for the next build
+        }
+    }
+    g_walk_last = walked ? 1 : 0;
+    // the task walk: the top levels in pre-order (host, from the node table),
+    // then (group, top node) pairs: open tests, counts, offsets, entries
+    if (!walked) {
         const int nlev = (int)T.level_start.size() - 1;
         const int depth = std::min(g_walk_depth, nlev - 1);
         const int ntop_nodes = T.level_start[depth + 1];
@@ -779,8 +1000,6 @@ static int device_tree(Context *c, double theta, int n_leaf_limit, int n_group_l
         int *jc = T.pc.p, *sc = T.pc.p + np, *jo = T.pc.p + 2 * np, *so = T.pc.p + 3 * np;
         int *tflag = T.pc.p + 4 * np, *tpos = T.pc.p + 5 * np;
         const int wb = (int)std::min<long long>((np + 127) / 128, 1LL << 30);
-        if ((r = T.nf.reserve(T.n_nodes))) return r;
-        { P3T_COUNT_LAUNCH(); k_node_f32<<<nblocks(T.n_nodes), 256, 0, c->stream>>>(T.nd.p, T.n_nodes, T.nf.p); }
         const float th2f = (float)(theta * theta);
         { P3T_COUNT_LAUNCH(); k_walk_open<<<wb, 128, 0, c->stream>>>(T.nd.p, T.nf.p, T.gnode.p, ng, top_d, ntop, theta * theta, th2f,
                                                T.ostat.p); }
@@ -824,6 +1043,14 @@ static int device_tree(Context *c, double theta, int n_leaf_limit, int n_group_l
 using namespace p3t;
 
 extern "C" {
+
+int p3t_set_walk(int form) {
+    if (form != 0 && form != 1) return -(int)cudaErrorInvalidValue;
+    g_walk_bfs = form;
+    return 0;
+}
+
+int p3t_walk_last(void) { return g_walk_last; }
 
 int p3t_state_tree(double theta, int n_leaf_limit, int n_group_limit) {
     Context *c = ctx_get(0);

@@ -247,6 +247,15 @@ int p3t_set_hard_mode(int mode);
  * off (the default).  Results are bit-identical.  ctas in [0, 4096].  No
  * counterpart in GPLUM's interface. */
 int p3t_set_hard_lone(float log2_steps, int ctas);
+/* Walk form of the device tree's interaction lists: 1 (default) breadth
+ * first, one CTA per group, every thread testing cells of the group's
+ * frontier; 0 the subtree tasks of one thread each.  Both emit the host
+ * builder's depth-first lists entry for entry (a group whose frontier
+ * outgrows its CTA takes form 0).  No counterpart in GPLUM's interface. */
+int p3t_set_walk(int form);
+/* The walk form the last device tree's lists came from (1 breadth first, 0
+ * tasks), -1 before the first build. */
+int p3t_walk_last(void);
 /* KOMINAMI fragmentation of the collision outcome (src/collisionB.h:7-93;
  * Collision::a_frag, N_frag, Collision0::m_min of parameter.dat).  a_frag = 0
  * (the default) is perfect accretion.  A collision makes

@@ -46,11 +46,17 @@ CASES = [
 ]
 
 
+@pytest.mark.parametrize("walk", [1, 0], ids=["breadth-first", "tasks"])
 @pytest.mark.parametrize("name,mk,ngl", CASES)
-def test_device_lists_equal_host_lists(gpu, name, mk, ngl):
+def test_device_lists_equal_host_lists(gpu, name, mk, ngl, walk):
     g, P = prepared(mk(), ngl)
     H = host_lists(g, P)
-    D = g.tree_lists(build=True)
+    assert g.lib.p3t_set_walk(walk) == 0
+    try:
+        D = g.tree_lists(build=True)
+        assert g.lib.p3t_walk_last() == walk
+    finally:
+        g.lib.p3t_set_walk(1)
     assert D["n_group"] == H["n_group"]
     for k in ("i_off", "i_idx", "j_off", "j_idx", "s_off"):
         np.testing.assert_array_equal(D[k], H[k], err_msg=k)
@@ -83,3 +89,21 @@ def test_soft_force_from_device_lists(gpu, name, mk, ngl):
         np.testing.assert_array_equal(fd[k], fh[k], err_msg=k)
     assert rel_err(fd["acc"].astype(np.float64), fh["acc"].astype(np.float64)).max() < 1e-6
     assert (np.abs(fd["phi"] - fh["phi"]) / np.abs(fh["phi"])).max() < 1e-6
+
+
+# both walk forms on the 1M-body hard-part disk: the same lists, entry for entry
+def test_walk_forms_agree_at_1m(gpu):
+    from gplum_gb300.disk import disk_1m_hard
+
+    g, P = prepared(disk_1m_hard(1048576), 256)
+    out = []
+    try:
+        for walk in (1, 0):
+            assert g.lib.p3t_set_walk(walk) == 0
+            out.append(g.tree_lists(build=True))
+            assert g.lib.p3t_walk_last() == walk
+    finally:
+        g.lib.p3t_set_walk(1)
+    a, b = out
+    for k in ("i_off", "i_idx", "j_off", "j_idx", "s_off", "s_idx"):
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
