@@ -25,8 +25,10 @@
 // the upper three levels) tasks taken in pre-order, each walking its subtree
 // with the host builder's stack discipline (count, then fill), so the
 // concatenated lists equal the host builder's entry for entry (SPJ entries
-// name the same cells; node numbers are in level order here).  The lists go straight into
-// the resident soft-force buffers.  Compiled with -fmad=false so the box and
+// name the same cells; node numbers are in level order here).  By default the
+// walk is breadth first instead, one CTA per group over an order-keeping
+// frontier (k_walk_bfs), giving the same lists; the task walk is its
+// fallback.  The lists go straight into the resident soft-force buffers.  Compiled with -fmad=false so the box and
 // opening arithmetic rounds as the host builder's (-ffp-contract=off).
 #include <algorithm>
 #include <cstdint>
