@@ -261,17 +261,20 @@ __global__ void k_lvl_split(int n, int level, int limit, const TNode *nd, int *e
 }
 
 // ---- moments and boxes, bottom-up -------------------------------------------------------
-__global__ void k_moments(int lo, int hi, TNode *nd, SPJRec *spj, const int *order, const double *pos,
-                          const double *mass, const double *rs) {
-    const int c = lo + blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= hi) return;
+// Node c's moments and boxes: a leaf sums its bodies in key order (the host
+// builder's sums), an inner node combines its children in child order by the
+// parallel-axis rule.  Children are read through L2 (ld.cg): they may have
+// been written by other CTAs of the same launch.
+__device__ void node_moments(int c, TNode *nd, SPJRec *spj, const int *order, const double *pos, const double *mass,
+                             const double *rs) {
     TNode &N = nd[c];
+    const int nchild = __ldcg(&N.nchild), child0 = __ldcg(&N.child0);
     double m = 0., cx = 0., cy = 0., cz = 0., q[6] = {0., 0., 0., 0., 0., 0.};
     double ilo[3] = {1e300, 1e300, 1e300}, ihi[3] = {-1e300, -1e300, -1e300};
     double olo[3] = {1e300, 1e300, 1e300}, ohi[3] = {-1e300, -1e300, -1e300};
-    if (N.nchild == 0) {
-        // the host builder's sums, in key order
-        for (int k = N.first; k < N.first + N.count; k++) {
+    if (nchild == 0) {
+        const int first = N.first, count = N.count;
+        for (int k = first; k < first + count; k++) {
             const int p = order[k];
             const double x = pos[3 * p], y = pos[3 * p + 1], z = pos[3 * p + 2], mp = mass[p];
             m += mp;
@@ -292,25 +295,25 @@ __global__ void k_moments(int lo, int hi, TNode *nd, SPJRec *spj, const int *ord
             cy /= m;
             cz /= m;
         }
-        for (int k = N.first; k < N.first + N.count; k++) {
+        for (int k = first; k < first + count; k++) {
             const int p = order[k];
             const double dx = pos[3 * p] - cx, dy = pos[3 * p + 1] - cy, dz = pos[3 * p + 2] - cz, mp = mass[p];
             q[0] += mp * dx * dx; q[1] += mp * dy * dy; q[2] += mp * dz * dz;
             q[3] += mp * dx * dy; q[4] += mp * dx * dz; q[5] += mp * dy * dz;
         }
     } else {
-        for (int j = 0; j < N.nchild; j++) {
-            const int ch = N.child0 + j;
-            const double mc = spj[ch].mass;
+        for (int j = 0; j < nchild; j++) {
+            const int ch = child0 + j;
+            const double mc = __ldcg(&spj[ch].mass);
             m += mc;
-            cx += mc * spj[ch].pos[0];
-            cy += mc * spj[ch].pos[1];
-            cz += mc * spj[ch].pos[2];
+            cx += mc * __ldcg(&spj[ch].pos[0]);
+            cy += mc * __ldcg(&spj[ch].pos[1]);
+            cz += mc * __ldcg(&spj[ch].pos[2]);
             for (int d = 0; d < 3; d++) {
-                ilo[d] = fmin(ilo[d], nd[ch].ilo[d]);
-                ihi[d] = fmax(ihi[d], nd[ch].ihi[d]);
-                olo[d] = fmin(olo[d], nd[ch].olo[d]);
-                ohi[d] = fmax(ohi[d], nd[ch].ohi[d]);
+                ilo[d] = fmin(ilo[d], __ldcg(&nd[ch].ilo[d]));
+                ihi[d] = fmax(ihi[d], __ldcg(&nd[ch].ihi[d]));
+                olo[d] = fmin(olo[d], __ldcg(&nd[ch].olo[d]));
+                ohi[d] = fmax(ohi[d], __ldcg(&nd[ch].ohi[d]));
             }
         }
         if (m != 0.) {
@@ -318,11 +321,14 @@ __global__ void k_moments(int lo, int hi, TNode *nd, SPJRec *spj, const int *ord
             cy /= m;
             cz /= m;
         }
-        for (int j = 0; j < N.nchild; j++) {
-            const SPJRec &S = spj[N.child0 + j];
-            const double dx = S.pos[0] - cx, dy = S.pos[1] - cy, dz = S.pos[2] - cz, mc = S.mass;
-            q[0] += S.xx + mc * dx * dx; q[1] += S.yy + mc * dy * dy; q[2] += S.zz + mc * dz * dz;
-            q[3] += S.xy + mc * dx * dy; q[4] += S.xz + mc * dx * dz; q[5] += S.yz + mc * dy * dz;
+        for (int j = 0; j < nchild; j++) {
+            const SPJRec *S = spj + child0 + j;
+            const double mc = __ldcg(&S->mass);
+            const double dx = __ldcg(&S->pos[0]) - cx, dy = __ldcg(&S->pos[1]) - cy, dz = __ldcg(&S->pos[2]) - cz;
+            q[0] += __ldcg(&S->xx) + mc * dx * dx; q[1] += __ldcg(&S->yy) + mc * dy * dy;
+            q[2] += __ldcg(&S->zz) + mc * dz * dz;
+            q[3] += __ldcg(&S->xy) + mc * dx * dy; q[4] += __ldcg(&S->xz) + mc * dx * dz;
+            q[5] += __ldcg(&S->yz) + mc * dy * dz;
         }
     }
     for (int d = 0; d < 3; d++) {
@@ -340,6 +346,35 @@ __global__ void k_moments(int lo, int hi, TNode *nd, SPJRec *spj, const int *ord
     S.pos[1] = cy;
     S.pos[2] = cz;
     S.xx = q[0]; S.yy = q[1]; S.zz = q[2]; S.xy = q[3]; S.xz = q[4]; S.yz = q[5];
+}
+
+// one level (nodes lo..hi-1) per launch, deepest level first
+__global__ void k_moments(int lo, int hi, TNode *nd, SPJRec *spj, const int *order, const double *pos,
+                          const double *mass, const double *rs) {
+    const int c = lo + blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= hi) return;
+    node_moments(c, nd, spj, order, pos, mass, rs);
+}
+
+// the whole tree in one launch: every leaf from its bodies, then up its
+// ancestors while it is the last child of the parent to finish (a counter per
+// node; the fence before the count publishes the child, the one after it
+// orders the parent's reads of its siblings)
+__global__ void k_moments_up(int nn, TNode *nd, SPJRec *spj, const int *parent, int *arrived, const int *order,
+                             const double *pos, const double *mass, const double *rs) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nn || nd[c].nchild != 0) return;
+    node_moments(c, nd, spj, order, pos, mass, rs);
+    for (int guard = 0; guard < 64; guard++) {
+        const int p = parent[c];
+        if (p < 0) break;
+        __threadfence();
+        const int k = atomicAdd(&arrived[p], 1);
+        if (k != __ldcg(&nd[p].nchild) - 1) break;
+        __threadfence();
+        node_moments(p, nd, spj, order, pos, mass, rs);
+        c = p;
+    }
 }
 
 // ---- groups ---------------------------------------------------------------------------------
@@ -799,6 +834,7 @@ struct DTree {
     DevBuf<int> top, pc, tasks;
     DevBuf<unsigned char> ostat;
     DevBuf<int> bjc, bsc, blen, bstore, bover;  // breadth-first walk
+    DevBuf<int> arrived;                        // one-launch moments
     DevBuf<long long> boff;
     DevBuf<unsigned long long> bcur;
     long long bstore_cap = 1LL << 24;
@@ -810,6 +846,7 @@ static DTree g_dt;
 static int g_walk_depth = 3;  // levels above the walk's task split
 static int g_walk_bfs = 1;    // walk form: breadth first per group (1) or subtree tasks (0)
 static int g_walk_last = -1;  // the form the last build's lists came from
+static int g_moments_up = 1;  // moments in one launch (1) or one launch per level (0)
 
 // (key, idx) sorted in place by key, stably (8 passes of 8 bits over `bits`)
 static int radix_sort(Context *c, DTree &T, unsigned long long *&key, int *&idx, unsigned long long *&key2,
@@ -902,11 +939,19 @@ static int device_tree(Context *c, double theta, int n_leaf_limit, int n_group_l
     T.level_start.push_back(base);
     T.n_nodes = base;
     if ((r = d.spj.reserve(base))) return r;
-    // 3. moments, deepest level first
-    for (int L = (int)T.level_start.size() - 2; L >= 0; L--) {
-        const int lo = T.level_start[L], hi = T.level_start[L + 1];
-        { P3T_COUNT_LAUNCH(); k_moments<<<nblocks(hi - lo, 128), 128, 0, c->stream>>>(lo, hi, T.nd.p, d.spj.p, idx, E.S.pos, E.S.mass,
-                                                                E.S.r_search); }
+    // 3. moments, bottom-up in one launch (or one launch per level, deepest first)
+    if (g_moments_up) {
+        if ((r = T.arrived.reserve(base))) return r;
+        cudaMemsetAsync(T.arrived.p, 0, base * sizeof(int), c->stream);
+        { P3T_COUNT_LAUNCH(); k_moments_up<<<nblocks(base, 128), 128, 0, c->stream>>>(base, T.nd.p, d.spj.p, T.parent.p,
+                                                                                  T.arrived.p, idx, E.S.pos,
+                                                                                  E.S.mass, E.S.r_search); }
+    } else {
+        for (int L = (int)T.level_start.size() - 2; L >= 0; L--) {
+            const int lo = T.level_start[L], hi = T.level_start[L + 1];
+            { P3T_COUNT_LAUNCH(); k_moments<<<nblocks(hi - lo, 128), 128, 0, c->stream>>>(lo, hi, T.nd.p, d.spj.p, idx, E.S.pos, E.S.mass,
+                                                                    E.S.r_search); }
+        }
     }
     // 4. groups in Morton order
     cudaMemsetAsync(T.gmark.p, 0, n * sizeof(int), c->stream);
@@ -1047,8 +1092,9 @@ using namespace p3t;
 extern "C" {
 
 int p3t_set_walk(int form) {
-    if (form != 0 && form != 1) return -(int)cudaErrorInvalidValue;
-    g_walk_bfs = form;
+    if (form < 0 || form > 3) return -(int)cudaErrorInvalidValue;
+    g_walk_bfs = form & 1;
+    g_moments_up = (form >> 1) ^ 1;
     return 0;
 }
 

@@ -247,11 +247,14 @@ int p3t_set_hard_mode(int mode);
  * off (the default).  Results are bit-identical.  ctas in [0, 4096].  No
  * counterpart in GPLUM's interface. */
 int p3t_set_hard_lone(float log2_steps, int ctas);
-/* Walk form of the device tree's interaction lists: 1 (default) breadth
- * first, one CTA per group, every thread testing cells of the group's
- * frontier; 0 the subtree tasks of one thread each.  Both emit the host
- * builder's depth-first lists entry for entry (a group whose frontier
- * outgrows its CTA takes form 0).  No counterpart in GPLUM's interface. */
+/* Device tree forms.  Bit 0, the walk of the interaction lists: 1 (default)
+ * breadth first, one CTA per group, every thread testing cells of the
+ * group's frontier; 0 the subtree tasks of one thread each.  Both emit the
+ * host builder's depth-first lists entry for entry (a group whose frontier
+ * outgrows its CTA takes the task walk).  Bit 1, the moments: 0 (default) one
+ * launch that climbs from every leaf while it is its parent's last child to
+ * finish, 1 one launch per level; the same values.  No counterpart in GPLUM's
+ * interface. */
 int p3t_set_walk(int form);
 /* The walk form the last device tree's lists came from (1 breadth first, 0
  * tasks), -1 before the first build. */

@@ -91,19 +91,22 @@ def test_soft_force_from_device_lists(gpu, name, mk, ngl):
     assert (np.abs(fd["phi"] - fh["phi"]) / np.abs(fh["phi"])).max() < 1e-6
 
 
-# both walk forms on the 1M-body hard-part disk: the same lists, entry for entry
+# both walk forms and both moment forms (form bit 1: one launch per level) on
+# the 1M-body hard-part disk: the same lists entry for entry, the same cells
 def test_walk_forms_agree_at_1m(gpu):
     from gplum_gb300.disk import disk_1m_hard
 
     g, P = prepared(disk_1m_hard(1048576), 256)
     out = []
     try:
-        for walk in (1, 0):
-            assert g.lib.p3t_set_walk(walk) == 0
+        for form in (1, 0, 3):
+            assert g.lib.p3t_set_walk(form) == 0
             out.append(g.tree_lists(build=True))
-            assert g.lib.p3t_walk_last() == walk
+            assert g.lib.p3t_walk_last() == form & 1
     finally:
         g.lib.p3t_set_walk(1)
-    a, b = out
-    for k in ("i_off", "i_idx", "j_off", "j_idx", "s_off", "s_idx"):
-        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+    a = out[0]
+    for b in out[1:]:
+        for k in ("i_off", "i_idx", "j_off", "j_idx", "s_off", "s_idx"):
+            np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+        assert a["spj"].tobytes() == b["spj"].tobytes()
