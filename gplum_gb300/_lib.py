@@ -75,6 +75,8 @@ SIGNATURES = {
     "p3t_set_hard_lone": (I, [ctypes.c_float, I]),
     "p3t_set_walk": (I, [I]),
     "p3t_walk_last": (I, []),
+    "p3t_set_hard_profile": (I, [I]),
+    "p3t_hard_phase_cycles": (I, [VP, I]),
     "p3t_id_next": (ctypes.c_longlong, []),
     "p3t_mlp_set": (I, [VP, VP]),
     "p3t_mlp_get": (I, [VP, VP]),

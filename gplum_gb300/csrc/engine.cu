@@ -528,7 +528,8 @@ __global__ void k_rminmax(State S, double *mm) {
     }
 }
 constexpr int NBIN = 32;
-constexpr int VD_T = 64;
+constexpr int VD_T = 96;
+constexpr int VD_BLOCKS_PER_SM = 6;
 __global__ void k_vdisp_partial(State S, double r_min, double drinv, double m_sun, double *part, int *cntp) {
     __shared__ double sv[NBIN][VD_T];
     __shared__ int sc[NBIN][VD_T];
@@ -556,12 +557,22 @@ __global__ void k_vdisp_partial(State S, double r_min, double drinv, double m_su
         cntp[blockIdx.x * NBIN + threadIdx.x] = c;
     }
 }
+// the bins' sums over the partials: 32 slices of the partials per bin, then
+// the slices in order (one block of 32 x 32 threads)
 __global__ void k_vdisp_bins(const double *part, const int *cntp, int nblk, double *vd, int *cnt) {
-    const int b = threadIdx.x;
-    if (b >= NBIN) return;
+    __shared__ double ss[32][NBIN + 1];
+    __shared__ int sn[32][NBIN + 1];
+    const int b = threadIdx.x & (NBIN - 1), sl = threadIdx.x / NBIN;
     double s = 0.;
     int c = 0;
-    for (int k = 0; k < nblk; k++) { s += part[k * NBIN + b]; c += cntp[k * NBIN + b]; }
+    for (int k = sl; k < nblk; k += 32) { s += part[k * NBIN + b]; c += cntp[k * NBIN + b]; }
+    ss[sl][b] = s;
+    sn[sl][b] = c;
+    __syncthreads();
+    if (sl) return;
+    s = 0.;
+    c = 0;
+    for (int k = 0; k < 32; k++) { s += ss[k][b]; c += sn[k][b]; }
     vd[b] = (c > 0) ? sqrt(s / c) : 0.;
     cnt[b] = c;
 }
@@ -625,8 +636,12 @@ __global__ void k_radii(State S, Params P, double r_min, double dr, double drinv
     const double ecccosu = 1. - r / ax;
     const double eccsinu2 = rv * rv / (P.m_sun * ax);
     if (!(sqrt(ecccosu * ecccosu + eccsinu2) < 0.6)) ax = r;
-    const double rHill = pow(S.mass[i] / (3. * P.m_sun), 1. / 3.) * ax;
-    const double r_out_i = dmax(P.R_cut0 * pow(ax, -P.p_cut) * rHill, P.R_cut1 * v_disp * P.dt_tree);
+    // the cube root GPLUM takes as pow(x, 1/3.), by cbrt (within 1 ulp of it,
+    // at a sixth of its cost)
+    const double rHill = cbrt(S.mass[i] / (3. * P.m_sun)) * ax;
+    // pow(ax, -0) is 1 for every ax
+    const double fac = (P.p_cut == 0.) ? 1. : pow(ax, -P.p_cut);
+    const double r_out_i = dmax(P.R_cut0 * fac * rHill, P.R_cut1 * v_disp * P.dt_tree);
     double ro = dmax(r_out_i, P.r_cut_min);
     if (P.r_cut_max > 0.) ro = dmin(P.r_cut_max, ro);
     S.r_out[i] = ro;
@@ -933,7 +948,9 @@ int Engine::energy(double *out5) {
 int Engine::cutoff_radii() {
     const Params P = params();
     int r = 0;
-    const int nblk = 152;
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    const int nblk = sms * VD_BLOCKS_PER_SM;
     if ((r = epart.reserve(2 + 2 * NBIN + (size_t)nblk * NBIN)) || (r = icnt.reserve(NBIN + (size_t)nblk * NBIN)))
         return r;
     double *mm = epart.p, *vd = epart.p + 2, *part = epart.p + 2 + 2 * NBIN;
@@ -949,7 +966,7 @@ int Engine::cutoff_radii() {
     const double r_min = std::sqrt(h[1]) * 0.99;
     const double dr = (r_max - r_min) / NBIN, drinv = 1. / dr;
     { P3T_COUNT_LAUNCH(); k_vdisp_partial<<<nblk, VD_T, 0, c->stream>>>(S, r_min, drinv, P.m_sun, part, cntp); }
-    { P3T_COUNT_LAUNCH(); k_vdisp_bins<<<1, 32, 0, c->stream>>>(part, cntp, nblk, vd, cnt); }
+    { P3T_COUNT_LAUNCH(); k_vdisp_bins<<<1, 32 * NBIN, 0, c->stream>>>(part, cntp, nblk, vd, cnt); }
     { P3T_COUNT_LAUNCH(); k_radii<<<nb(S.n), 256, 0, c->stream>>>(S, P, r_min, dr, drinv, vd, cnt); }
     return cuda_status(cudaGetLastError());
 }

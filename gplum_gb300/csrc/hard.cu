@@ -17,6 +17,12 @@
 namespace p3t {
 
 constexpr int MAX_BLOCK_STEPS = 1 << 20;  // per cluster and tree step
+// phases of the bundle form's loop, for its optional clock counts (the order
+// of p3t_hard_phase_cycles)
+enum : int {
+    HP_LONE, HP_ADMIT, HP_TS, HP_PREDICT, HP_DETECT, HP_ACTIVE, HP_PAIRS, HP_FINAL, HP_CORRECT, HP_DT, HP_COLLIDE,
+    HP_TIME, HP_RETIRE, HP_N
+};
 
 // Per-member working copy of one cluster (FPHard fields), indexed by the
 // member's slot in the cluster lists.
@@ -101,6 +107,7 @@ struct HardArgs {
     int wide;                 // bundle form: clusters above BCAP_MAIN in k_hard_wide (1) or run_cluster (0)
     int max_steps;            // block steps a cluster may take in one tree step (ST_ITER_CAP beyond)
     int lone_in;              // bundle form: the lone tier runs in the bundle CTAs (1) or in k_hard_lone (0)
+    unsigned long long *phase_cycles;  // optional [HP_N]: clock cycles per phase of the bundle loop, all CTAs
     unsigned long long *live; // optional [2]: pair terms evaluated (predicted/corrected, full), bundle form
 };
 
@@ -130,21 +137,25 @@ __device__ __forceinline__ void correct(const Hard &H, int s, double Dt) {
     st3(H.pos, s, ld3(H.xp, s) + 1.6666666666666667e-2 * Dt2 * (5. * A2 + 3. * 1.1666666666666667e-3 * A3));
     st3(H.vel, s, ld3(H.vp, s) + 8.3333333333333333e-2 * Dt * (4. * A2 + 3. * A3));
 }
-__device__ __forceinline__ void dt_hermite(const Params &P, const Hard &H, int s) {
-    double dt_next = dmin(2. * H.dt[s], 0.5 * P.dt_tree);
-    const double dt_1 = dmin(dt4th(P.eta, P.alpha2, H.acc0[s], ld3(H.acc_d, s), ld3(H.jerk_d, s), ld3(H.a2_d, s),
-                                   ld3(H.a3_d, s)),
-                             dt4th(P.eta_sun, P.alpha2, 0., ld3(H.acc_s, s), ld3(H.jerk_s, s), ld3(H.a2_s, s),
-                                   ld3(H.a3_s, s)));
-    const double time = H.th[s];
+// the next time step from the current one, the member's time and dt_1, the
+// smaller of its two criteria (the rest of FPHard::calcDeltat)
+__device__ __forceinline__ double dt_next_hermite(const Params &P, double time, double dt, double dt_1) {
+    double dt_next = dmin(2. * dt, 0.5 * P.dt_tree);
     double rem = rem_pow2(time, dt_next);
     for (int k = 0; rem != 0.0 && k < 1100; k++) {
         dt_next *= 0.5;
         rem = rem_pow2(time, dt_next);
     }
-    for (int k = 0; dt_1 < dt_next && 0.5 * H.dt[s] < dt_next && k < 1100; k++) dt_next *= 0.5;
+    for (int k = 0; dt_1 < dt_next && 0.5 * dt < dt_next && k < 1100; k++) dt_next *= 0.5;
     if (dt_next < 2. * P.dt_min) dt_next = P.dt_min;
-    H.dt[s] = dt_next;
+    return dt_next;
+}
+__device__ __forceinline__ void dt_hermite(const Params &P, const Hard &H, int s) {
+    const double dt_1 = dmin(dt4th(P.eta, P.alpha2, H.acc0[s], ld3(H.acc_d, s), ld3(H.jerk_d, s), ld3(H.a2_d, s),
+                                   ld3(H.a3_d, s)),
+                             dt4th(P.eta_sun, P.alpha2, 0., ld3(H.acc_s, s), ld3(H.jerk_s, s), ld3(H.a2_s, s),
+                                   ld3(H.a3_s, s)));
+    H.dt[s] = dt_next_hermite(P, H.th[s], H.dt[s], dt_1);
 }
 
 // ---- pair sums over a cluster, src/gravity_hard.h:203-367 -------------------
@@ -1238,6 +1249,7 @@ struct HardBufs {
     DevBuf<int32_t> n_frags, fgslot, fidx;
     DevBuf<long long> fmap;
     DevBuf<unsigned long long> live;  // [2] pair terms evaluated by the last launch
+    DevBuf<unsigned long long> phase;  // [HP_N] clock cycles per bundle phase (when profiled)
     Hard H;
     int cap = 0;
     int reserve(int m) {
@@ -1283,6 +1295,7 @@ static int g_frag_cap = 0;  // fragment slots of the current launch
 static int g_max_steps = MAX_BLOCK_STEPS;  // block-step cap per cluster and tree step
 // lone form: clusters predicted to take at least 2^g_lone - 1 block steps (0:
 // off), on g_lone_ctas CTAs of their own (0: in the bundle CTAs)
+static int g_hard_profile = 0;  // per-phase clock counts of the bundle loop
 static float g_lone = 0.f;
 static int g_lone_ctas = 0;
 // events around the last cluster launch (k_hard_bundles / k_hard_clusters) on
@@ -1469,6 +1482,10 @@ int p3t_hard_enqueue(void) {
         return r;
     cudaMemsetAsync(B.n_frags.p, 0, sizeof(int32_t), c->stream);
     cudaMemsetAsync(B.live.p, 0, 2 * sizeof(unsigned long long), c->stream);
+    if (g_hard_profile) {
+        if ((r = B.phase.reserve(HP_N))) return r;
+        cudaMemsetAsync(B.phase.p, 0, HP_N * sizeof(unsigned long long), c->stream);
+    }
     // schedule, on the device: clusters binned by tier (bundle mode: above
     // the bundle capacity first; tier mode: CTA >= g_cta_min > warp >=
     // g_warp_min > thread), then by priority (the caller's, the learned cost
@@ -1573,6 +1590,7 @@ int p3t_hard_integrate(int istep) {
         A.wide = g_wide;
         A.max_steps = g_max_steps;
         A.live = B.live.p;
+        A.phase_cycles = g_hard_profile ? B.phase.p : nullptr;
         if (!g_ev_launch[0] && ((r = cuda_status(cudaEventCreate(&g_ev_launch[0]))) ||
                                 (r = cuda_status(cudaEventCreate(&g_ev_launch[1])))))
             return r;
@@ -1828,6 +1846,22 @@ int p3t_set_hard_lone(float log2_steps, int ctas) {
     g_lone = log2_steps;
     g_lone_ctas = ctas;
     return 0;
+}
+
+int p3t_set_hard_profile(int on) {
+    g_hard_profile = on ? 1 : 0;
+    return 0;
+}
+
+int p3t_hard_phase_cycles(unsigned long long *out, int n) {
+    if (!out || n < HP_N) return -(int)cudaErrorInvalidValue;
+    Context *c = ctx_get(0);
+    if (!c) return -(int)cudaErrorNoDevice;
+    if (!g_hard_profile || !g_hb.phase.p) {
+        for (int k = 0; k < HP_N; k++) out[k] = 0;
+        return 0;
+    }
+    return d2h(c, out, g_hb.phase.p, HP_N * sizeof(unsigned long long));
 }
 
 int p3t_set_hard_step_cap(int max_block_steps) {

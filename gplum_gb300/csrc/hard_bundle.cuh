@@ -98,7 +98,19 @@ struct BundleSmem {
     int pend_c[BCLAIM], pend_n[BCLAIM];
     int ws[NT / 32];
     int used, ncl, fresh_k, fresh_p, n_sv, n_pend, i_pend, exhausted, any, grew, phase;
+    long long ph_acc[HP_N], ph_t;  // optional per-phase clock counts (thread 0)
 };
+
+// the end of a phase of the bundle loop (after its barrier): thread 0 adds
+// the clock cycles since the last mark to the phase's count
+#define HP_MARK(id)                                            \
+    do {                                                       \
+        if (A.phase_cycles && threadIdx.x == 0) {              \
+            const long long t_ = clock64();                    \
+            B.ph_acc[id] += t_ - B.ph_t;                       \
+            B.ph_t = t_;                                       \
+        }                                                      \
+    } while (0)
 
 __device__ __forceinline__ unsigned long long dbits(double x) {
     return (unsigned long long)__double_as_longlong(x);
@@ -682,6 +694,7 @@ __device__ void bundle_step(const HardArgs &A, BundleSmem<BCAP> &B) {
     }
     if (threadIdx.x == 0) B.n_sv = 0;
     __syncthreads();
+    HP_MARK(HP_TS);
     // predict every member
     FOR_SLOTS(p) {
         const int g = B.gslot[p], k = B.cl[p];
@@ -692,6 +705,7 @@ __device__ void bundle_step(const HardArgs &A, BundleSmem<BCAP> &B) {
         st32b(B, B.xp32, p, xp, k);
     }
     __syncthreads();
+    HP_MARK(HP_PREDICT);
     // collisionDetermination, src/hermite.h:98-196
     bundle_detect(A, B, false);
     __syncthreads();
@@ -714,6 +728,7 @@ __device__ void bundle_step(const HardArgs &A, BundleSmem<BCAP> &B) {
         B.c_flags[k] = fl;
     }
     __syncthreads();
+    HP_MARK(HP_DETECT);
     // the active set (every alive member on a collision) and the twins of
     // active merged members
     FOR_SLOTS(p) {
@@ -734,20 +749,51 @@ __device__ void bundle_step(const HardArgs &A, BundleSmem<BCAP> &B) {
     }
     __syncthreads();
     const int nt = bundle_list(B, MF_TGT);
+    HP_MARK(HP_ACTIVE);
     bundle_pairs(A, B, 1, nt);
+    HP_MARK(HP_PAIRS);
     bundle_finalize(A, B, 1, nt, 1);
+    HP_MARK(HP_FINAL);
     for (int it = 0; it < 2; it++) {
-        for (int i = threadIdx.x; i < nt; i += BT) {
-            const int s = B.tgt[i], g = B.gslot[s], k = B.cl[s];
-            correct(H, g, B.c_ts[k] - H.th[g]);
-            const V3 x = ld3(H.pos, g);
-            st3(B.pos, s, x);
-            st3(B.vel, s, ld3(H.vel, g));
-            st32b(B, B.pos32, s, x, k);
+        // FPHard::correct, one thread per (target, component): correct()'s
+        // arithmetic component by component
+        for (int i = threadIdx.x; i < 3 * nt; i += BT) {
+            const int t = i / 3, d = i - 3 * t;
+            const int s = B.tgt[t], g = B.gslot[s], k = B.cl[s];
+            const int gd = 3 * g + d;
+            // every input first (one round trip to the state of record)
+            const double th = H.th[g], as = H.acc_s[gd], a0s = H.a0_s[gd], j0s = H.j0_s[gd], js = H.jerk_s[gd];
+            const double ad = H.acc_d[gd], a0d = H.a0_d[gd], j0d = H.j0_d[gd], jd = H.jerk_d[gd];
+            const double xp = H.xp[gd], vp = H.vp[gd];
+            const double Dt = B.c_ts[k] - th;
+            const double Dt2 = Dt * Dt, Di = 1. / Dt, Di2 = Di * Di, Di3 = Di2 * Di;
+            const double Am_s = as - a0s, J0_s = Dt * j0s, J1_s = Dt * js;
+            const double A2_s = 3. * Am_s - (J1_s + 2. * J0_s);
+            const double A3_s = -2. * Am_s + (J1_s + J0_s);
+            H.a2_s[gd] = 2. * Di2 * (A2_s + 3. * A3_s);
+            H.a3_s[gd] = 6. * Di3 * A3_s;
+            const double Am_d = ad - a0d, J0_d = j0d * Dt, J1_d = jd * Dt;
+            const double A2_d = 3. * Am_d - (J1_d + 2. * J0_d);
+            const double A3_d = -2. * Am_d + (J1_d + J0_d);
+            H.a2_d[gd] = 2. * (A2_d + 3. * A3_d) * Di2;
+            H.a3_d[gd] = 6. * A3_d * Di3;
+            const double A2 = A2_s + A2_d, A3 = A3_s + A3_d;
+            const double x = xp + 1.6666666666666667e-2 * Dt2 * (5. * A2 + 3. * 1.1666666666666667e-3 * A3);
+            const double v = vp + 8.3333333333333333e-2 * Dt * (4. * A2 + 3. * A3);
+            H.pos[gd] = x;
+            H.vel[gd] = v;
+            B.pos[3 * s + d] = x;
+            B.vel[3 * s + d] = v;
+            const float u = (float)(x - B.c_ref[3 * k + d]);
+            B.pos32[3 * s + d] = u;
+            if (!(fabsf(u) < B.c_E32[k])) atomicOr(&B.c_flags[k], CF_EXACT);
         }
         __syncthreads();
+        HP_MARK(HP_CORRECT);
         bundle_pairs(A, B, 2, nt);
+        HP_MARK(HP_PAIRS);
         bundle_finalize(A, B, 2, nt, 1);
+        HP_MARK(HP_FINAL);
     }
     for (int i = threadIdx.x; i < nt; i += BT) {
         const int s = B.tgt[i], g = B.gslot[s], k = B.cl[s];
@@ -761,6 +807,7 @@ __device__ void bundle_step(const HardArgs &A, BundleSmem<BCAP> &B) {
     }
     if (threadIdx.x == 0) B.any = 0;
     __syncthreads();
+    HP_MARK(HP_DT);
     // collisions: one thread per colliding cluster
     if (threadIdx.x == 0) B.grew = 0;
     __syncthreads();
@@ -830,6 +877,7 @@ __device__ void bundle_step(const HardArgs &A, BundleSmem<BCAP> &B) {
         }
         __syncthreads();
     }
+    HP_MARK(HP_COLLIDE);
     // getSystemTime, src/hermite.h:25-35
     FOR_CLUSTERS(k) B.c_key[k] = dbits(1.e10);
     __syncthreads();
@@ -847,6 +895,7 @@ __device__ void bundle_step(const HardArgs &A, BundleSmem<BCAP> &B) {
         }
     }
     __syncthreads();
+    HP_MARK(HP_TIME);
 }
 
 // final forces, write-back and removal of the finished clusters
@@ -1032,6 +1081,7 @@ __global__ void __launch_bounds__(bundle_threads(BCAP), OCC) k_hard_bundles(Hard
     __shared__ long long red_l[BT / 32];
     __shared__ int q_sh;
     const int tid = threadIdx.x;
+    const long long t_k0 = A.phase_cycles ? clock64() : 0;
     const Team<BT> tm{tid, red_d, red_l};
     if (!A.wide) {
         for (int guard = 0; guard < (1 << 30); guard++) {
@@ -1069,6 +1119,9 @@ __global__ void __launch_bounds__(bundle_threads(BCAP), OCC) k_hard_bundles(Hard
         B.i_pend = 0;
         B.exhausted = 0;
         B.phase = 0;
+        for (int k = 0; k < HP_N; k++) B.ph_acc[k] = 0;
+        B.ph_t = clock64();
+        B.ph_acc[HP_LONE] = B.ph_t - t_k0;  // the clusters above the slots, the lone tier
     }
     __syncthreads();
     for (int guard = 0; guard < (1 << 30); guard++) {
@@ -1085,9 +1138,13 @@ __global__ void __launch_bounds__(bundle_threads(BCAP), OCC) k_hard_bundles(Hard
             bundle_pairs(A, B, 0, nt);
             bundle_finalize(A, B, 0, nt, 2);
         }
+        HP_MARK(HP_ADMIT);
         bundle_step(A, B);
         if (B.any) bundle_retire(A, B);
+        HP_MARK(HP_RETIRE);
     }
+    if (A.phase_cycles && tid == 0)
+        for (int k = 0; k < HP_N; k++) atomicAdd(&A.phase_cycles[k], (unsigned long long)B.ph_acc[k]);
 }
 
 #undef FOR_SLOTS

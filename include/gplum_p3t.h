@@ -256,6 +256,16 @@ int p3t_set_hard_lone(float log2_steps, int ctas);
  * finish, 1 one launch per level; the same values.  No counterpart in GPLUM's
  * interface. */
 int p3t_set_walk(int form);
+/* Per-phase clock counts of the bundle form's loop (off by default; on, each
+ * CTA's thread 0 reads the SM clock at the barriers that end the phases):
+ * p3t_hard_phase_cycles writes, summed over the CTAs of the last launch, the
+ * cycles of: 0 clusters above the slots and the lone tier, 1 admission
+ * (claim, load, first force), 2 block time, 3 prediction, 4 collision
+ * detection, 5 active set, 6 pair terms, 7 their sums, 8 correction, 9 time
+ * steps, 10 collisions, 11 system time, 12 retirement; n >= 13.  No
+ * counterpart in GPLUM's interface (its CALC_WTIME timers are per call). */
+int p3t_set_hard_profile(int on);
+int p3t_hard_phase_cycles(unsigned long long *out, int n);
 /* The walk form the last device tree's lists came from (1 breadth first, 0
  * tasks), -1 before the first build. */
 int p3t_walk_last(void);
