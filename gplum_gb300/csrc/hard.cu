@@ -21,7 +21,7 @@ constexpr int MAX_BLOCK_STEPS = 1 << 20;  // per cluster and tree step
 // of p3t_hard_phase_cycles)
 enum : int {
     HP_LONE, HP_ADMIT, HP_TS, HP_PREDICT, HP_DETECT, HP_ACTIVE, HP_PAIRS, HP_FINAL, HP_CORRECT, HP_DT, HP_COLLIDE,
-    HP_TIME, HP_RETIRE, HP_N
+    HP_TIME, HP_RETIRE, HP_DRAIN, HP_N
 };
 
 // Per-member working copy of one cluster (FPHard fields), indexed by the

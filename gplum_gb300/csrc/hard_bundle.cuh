@@ -51,6 +51,7 @@
 namespace p3t {
 
 constexpr int BT = 128;      // threads of a bundle (one CTA) unless bundle_threads says otherwise
+constexpr int BPT = 4;       // (target, partner) items a thread tests per round of bundle_pairs
 constexpr int BCAP_MAIN = 256;  // member slots of a bundle
 constexpr int BCAP_WIDE = 512;  // member slots of the wide form (clusters of 257..512 bodies, one at a time)
 // clusters in a bundle at once: half its member slots, at most one per thread
@@ -77,7 +78,7 @@ struct BundleSmem {
     float pos32[3 * BCAP], xp32[3 * BCAP], roi32[BCAP], fr32[BCAP];
     int gslot[BCAP];
     int pfx[BCAP + 1];
-    int ring[2 * NT];
+    int ring[(BPT + 1) * NT];  // live pair items: a round's BPT per thread beyond a part drain
     int seg[NT + 1];
     short tgt[BCAP], cl[BCAP], owner[BCAP];
     unsigned char dead[BCAP], merged[BCAP], flag[BCAP];
@@ -237,19 +238,19 @@ __device__ __forceinline__ void pair_terms(const Params &P, const BundleSmem<BCA
 
 // terms of ring[0..m), then in-order addition into the targets' accumulators
 template <int BCAP>
-__device__ void bundle_drain(const Params &P, BundleSmem<BCAP> &B, int mode, int m) {
+__device__ void bundle_drain(const Params &P, BundleSmem<BCAP> &B, const int *ring, int mode, int m) {
     constexpr int BT = BundleSmem<BCAP>::NT;
     const int q = threadIdx.x;
     int sq = -1;
     if (q < m) {
-        const int e = B.ring[q];
+        const int e = ring[q];
         sq = e >> 16;
         double o[7];
         pair_terms(P, B, mode, sq, e & 0xffff, o);
 #pragma unroll
         for (int c = 0; c < 7; c++) B.term[c * BT + q] = o[c];
     }
-    const int head = (q < m) && (q == 0 || (B.ring[q - 1] >> 16) != sq);
+    const int head = (q < m) && (q == 0 || (ring[q - 1] >> 16) != sq);
     int nseg;
     const int off = bscan<BT>(head, B.ws, nseg);
     if (head) B.seg[off] = q;
@@ -259,7 +260,7 @@ __device__ void bundle_drain(const Params &P, BundleSmem<BCAP> &B, int mode, int
     for (int it = q; it < ncomp * nseg; it += BT) {
         const int j = it / ncomp, c = it - ncomp * j;
         const int a = B.seg[j], b = B.seg[j + 1];
-        const int s = B.ring[a] >> 16;
+        const int s = ring[a] >> 16;
         double acc = B.acc[c * BCAP + s];
         for (int k = a; k < b; k++) acc += B.term[c * BT + k];
         B.acc[c * BCAP + s] = acc;
@@ -299,50 +300,76 @@ __device__ void bundle_pairs(const HardArgs &A, BundleSmem<BCAP> &B, int mode, i
     }
     const float *xi32 = (mode == 1) ? B.xp32 : B.pos32;
     const float *xj32 = (mode == 0) ? B.pos32 : B.xp32;
+    // rounds of BPT consecutive items per thread (the ring stays in (target,
+    // partner) order); full drains of BT items as the ring fills
     int ring_n = 0;
     long long n_live = 0;
-    for (int base = 0; base < total; base += BT) {
-        const int f = base + tid;
-        int live = 0, e = 0;
-        if (f < total) {
+    for (int base = 0; base < total; base += BPT * BT) {
+        const int f0 = base + BPT * tid;
+        int e[BPT], nl = 0;
+        unsigned lv = 0u;
+        if (f0 < total) {
             int lo = 0, hi = nt - 1;
             while (lo < hi) {
                 const int mid = (lo + hi + 1) >> 1;
-                if (B.pfx[mid] <= f) lo = mid;
+                if (B.pfx[mid] <= f0) lo = mid;
                 else hi = mid - 1;
             }
-            const int s = B.tgt[lo], k = B.cl[s];
-            const int t = B.c_off[k] + (f - B.pfx[lo]);
-            if (B.id[s] != B.id[t]) {
-                if (!(B.c_flags[k] & CF_EXACT)) {
-                    const float rf = fminf(B.roi32[s], B.roi32[t]);
-                    live = d2_32(xi32, s, xj32, t) * (rf * rf) <= B.c_thrf[k];
-                } else {
-                    const V3 xi = ld3((mode == 1) ? B.xp : B.pos, s);
-                    const V3 dr = ld3((mode == 0) ? B.pos : B.xp, t) - xi;
-                    double dr2 = dot(dr, dr);
-                    dr2 += A.P.eps2;
-                    const double r = dmin(B.roi[s], B.roi[t]);
-                    live = !(dr2 * r * r > 1.000001);
+#pragma unroll
+            for (int u = 0; u < BPT; u++) {
+                const int f = f0 + u;
+                e[u] = 0;
+                if (f >= total) continue;
+                while (B.pfx[lo + 1] <= f) lo++;
+                const int s = B.tgt[lo], k = B.cl[s];
+                const int t = B.c_off[k] + (f - B.pfx[lo]);
+                int live = 0;
+                if (B.id[s] != B.id[t]) {
+                    if (!(B.c_flags[k] & CF_EXACT)) {
+                        const float rf = fminf(B.roi32[s], B.roi32[t]);
+                        live = d2_32(xi32, s, xj32, t) * (rf * rf) <= B.c_thrf[k];
+                    } else {
+                        const V3 xi = ld3((mode == 1) ? B.xp : B.pos, s);
+                        const V3 dr = ld3((mode == 0) ? B.pos : B.xp, t) - xi;
+                        double dr2 = dot(dr, dr);
+                        dr2 += A.P.eps2;
+                        const double r = dmin(B.roi[s], B.roi[t]);
+                        live = !(dr2 * r * r > 1.000001);
+                    }
                 }
+                e[u] = (s << 16) | t;
+                lv |= (unsigned)live << u;
+                nl += live;
             }
-            e = (s << 16) | t;
         }
         int cnt;
-        const int off = bscan<BT>(live, B.ws, cnt);
-        if (live) B.ring[ring_n + off] = e;
+        int off = ring_n + bscan<BT>(nl, B.ws, cnt);
+#pragma unroll
+        for (int u = 0; u < BPT; u++)
+            if ((lv >> u) & 1u) B.ring[off++] = e[u];
         ring_n += cnt;
         n_live += cnt;
         __syncthreads();
-        if (ring_n >= BT) {
-            bundle_drain(A.P, B, mode, BT);
-            const int rest = ring_n - BT;
-            if (tid < rest) B.ring[tid] = B.ring[BT + tid];
+        int head = 0;
+        while (ring_n - head >= BT) {
+            const long long t0 = (A.phase_cycles && tid == 0) ? clock64() : 0;
+            bundle_drain(A.P, B, B.ring + head, mode, BT);
+            if (A.phase_cycles && tid == 0) B.ph_acc[HP_DRAIN] += clock64() - t0;
+            head += BT;
+        }
+        if (head > 0) {
+            // the rest (fewer than BT items, at or beyond BT) to the front
+            const int rest = ring_n - head;
+            if (tid < rest) B.ring[tid] = B.ring[head + tid];
             ring_n = rest;
             __syncthreads();
         }
     }
-    if (ring_n > 0) bundle_drain(A.P, B, mode, ring_n);
+    if (ring_n > 0) {
+        const long long t0 = (A.phase_cycles && tid == 0) ? clock64() : 0;
+        bundle_drain(A.P, B, B.ring, mode, ring_n);
+        if (A.phase_cycles && tid == 0) B.ph_acc[HP_DRAIN] += clock64() - t0;
+    }
     if (A.live && tid == 0) atomicAdd(&A.live[mode == 0 ? 1 : 0], (unsigned long long)n_live);
 }
 

@@ -262,7 +262,8 @@ int p3t_set_walk(int form);
  * cycles of: 0 clusters above the slots and the lone tier, 1 admission
  * (claim, load, first force), 2 block time, 3 prediction, 4 collision
  * detection, 5 active set, 6 pair terms, 7 their sums, 8 correction, 9 time
- * steps, 10 collisions, 11 system time, 12 retirement; n >= 13.  No
+ * steps, 10 collisions, 11 system time, 12 retirement, 13 of which (in
+ * 1, 6, 12) the pair-term drains; n >= 14.  No
  * counterpart in GPLUM's interface (its CALC_WTIME timers are per call). */
 int p3t_set_hard_profile(int on);
 int p3t_hard_phase_cycles(unsigned long long *out, int n);
