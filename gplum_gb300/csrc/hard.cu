@@ -1288,7 +1288,7 @@ static double g_edisp[2] = {0., 0.};
 static int g_warp_min = 8, g_cta_min = 64;
 static int g_hard_mode = 0;  // 0: bundles, 1: thread/warp/CTA tiers
 static float g_heavy = 5.5f;  // predicted log2(1 + block steps) from which a cluster runs alone (0: never)
-static int g_wide = 0;        // clusters above the bundle capacity: wide lone bundles (1) or one per CTA (0)
+static int g_wide = 1;        // clusters above the bundle capacity: wide lone bundles (1) or one per CTA (0)
 static int g_bcap = 256, g_bocc = 2;  // bundle member slots and CTAs per SM (256/2, 128/3, 128/4)
 static FragParams g_frag = {0., 9.426627927538057e-12, 10, 0, 0ULL};  // off (a_frag = 0)
 static int g_frag_cap = 0;  // fragment slots of the current launch
@@ -1600,8 +1600,9 @@ int p3t_hard_integrate(int istep) {
         if (g_hard_mode == 0) {
             static bool attr = false;
             static cudaStream_t s_wide = nullptr, s_lone = nullptr;
-            static cudaEvent_t ev_ready = nullptr, ev_done = nullptr, ev_lone = nullptr;
+            static cudaEvent_t ev_done = nullptr, ev_lone = nullptr;
             const int smem_w = (int)sizeof(BundleSmem<BCAP_WIDE>);
+            static_assert(sizeof(BundleSmem<BCAP_WIDE>) <= 200 * 1024, "the wide bundle fits an SM");
             static_assert(sizeof(LoneSmem<bundle_threads(256)>) <= sizeof(BundleSmem<256>) &&
                               sizeof(LoneSmem<BT>) <= 200 * 1024 && sizeof(LoneSmem<LONE_T>) <= LONE_EXCL_SMEM,
                           "lone state fits the shared memory it borrows");
@@ -1627,7 +1628,6 @@ int p3t_hard_integrate(int istep) {
                     (r = cuda_status(cudaStreamCreateWithPriority(&s_lone, cudaStreamNonBlocking, -1000))) ||
                     (r = cuda_status(cudaEventCreateWithFlags(&ev_lone, cudaEventDisableTiming))) ||
                     (r = cuda_status(cudaStreamCreateWithPriority(&s_wide, cudaStreamNonBlocking, -1000))) ||
-                    (r = cuda_status(cudaEventCreateWithFlags(&ev_ready, cudaEventDisableTiming))) ||
                     (r = cuda_status(cudaEventCreateWithFlags(&ev_done, cudaEventDisableTiming))))
                     return r;
                 attr = true;
@@ -1635,25 +1635,28 @@ int p3t_hard_integrate(int istep) {
             // the lone clusters and the clusters above BCAP_MAIN bodies on
             // streams of their own, started first so that they hold SMs from the
             // beginning (a handful of CTAs; they leave at once when there are none)
-            const bool lone_k = lone && g_lone_ctas > 0;
+            bool lone_k = lone && g_lone_ctas > 0;
             if ((r = cuda_status(cudaEventRecord(g_ev_launch[0], c->stream)))) return r;
+            // The wide and lone CTAs must hold their SMs before the persistent
+            // bundle CTAs fill every SM (with a cross-stream event the bundle
+            // kernel was dispatched first): the queue is complete when the
+            // library stream has drained; its tier sizes then give the wide
+            // grid, and both kernels are submitted before the bundle kernel
+            // with no dependency left to resolve.
+            int wide_ctas = 0;
             if (A.wide || lone_k) {
-                if ((r = cuda_status(cudaEventRecord(ev_ready, c->stream)))) return r;
+                int nt[3] = {0, 0, 0};
+                if ((r = d2h(c, nt, B.ntier.p, sizeof(nt)))) return r;  // synchronizes the stream
+                wide_ctas = A.wide ? std::min(nt[0], std::max(1, sms / 16)) : 0;
+                if (nt[2] == 0) lone_k = false;
             }
             if (lone_k) {
-                // The lone CTAs must hold their SMs before the persistent
-                // bundle CTAs fill every SM: the queue is complete when the
-                // library stream has drained, and the lone kernel is then
-                // submitted first, with no dependency left to resolve.
-                if ((r = cuda_status(cudaStreamSynchronize(c->stream)))) return r;
                 { P3T_COUNT_LAUNCH(); k_hard_lone<<<g_lone_ctas, LONE_T, LONE_EXCL_SMEM, s_lone>>>(A); }
                 if ((r = cuda_status(cudaGetLastError())) || (r = cuda_status(cudaEventRecord(ev_lone, s_lone))))
                     return r;
             }
-            if (A.wide) {
-                if ((r = cuda_status(cudaStreamWaitEvent(s_wide, ev_ready, 0))))
-                    return r;
-                { P3T_COUNT_LAUNCH(); k_hard_wide<<<std::max(1, sms / 16), BT, smem_w, s_wide>>>(A); }
+            if (wide_ctas > 0) {
+                { P3T_COUNT_LAUNCH(); k_hard_wide<<<wide_ctas, WT, smem_w, s_wide>>>(A); }
                 if ((r = cuda_status(cudaGetLastError()))) return r;
             }
             // persistent: g_bocc CTAs per SM (fewer when there are few clusters)
@@ -1665,8 +1668,8 @@ int p3t_hard_integrate(int istep) {
             else
                 { P3T_COUNT_LAUNCH(); k_hard_bundles<128, 4><<<blocks, BT, smem, c->stream>>>(A); }
             if ((r = cuda_status(cudaGetLastError()))) return r;
-            if (A.wide && ((r = cuda_status(cudaEventRecord(ev_done, s_wide))) ||
-                           (r = cuda_status(cudaStreamWaitEvent(c->stream, ev_done, 0)))))
+            if (wide_ctas > 0 && ((r = cuda_status(cudaEventRecord(ev_done, s_wide))) ||
+                                  (r = cuda_status(cudaStreamWaitEvent(c->stream, ev_done, 0)))))
                 return r;
             if (lone_k && (r = cuda_status(cudaStreamWaitEvent(c->stream, ev_lone, 0)))) return r;
             // the launch's time spans all three forms

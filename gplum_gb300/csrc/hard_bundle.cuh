@@ -59,7 +59,7 @@ __host__ __device__ constexpr int bmaxcl(int cap) { return cap / 2 < 128 ? cap /
 // threads of a bundle of `cap` member slots: one per slot for the main
 // 256-slot form (8 warps; twice the warps per SM of 128 at 2 CTAs per SM,
 // for the FP64 dependency chains), 128 for the others
-__host__ __device__ constexpr int bundle_threads(int cap) { return cap == 256 ? 256 : 128; }
+__host__ __device__ constexpr int bundle_threads(int cap) { return cap == 256 ? 256 : (cap == 512 ? 512 : 128); }
 constexpr int BSURV = 64;    // colliding-pair candidates kept per block step
 constexpr int BCLAIM = 8;    // clusters claimed from the queue at a time
 
@@ -1046,14 +1046,15 @@ __device__ void bundle_retire(const HardArgs &A, BundleSmem<BCAP> &B) {
 // (fragment room included) as a lone wide bundle, the lane-dense form, larger
 // ones in the one-cluster-per-CTA form.  Same arithmetic, bit for bit, as
 // every other form.
-__global__ void __launch_bounds__(BT, 1) k_hard_wide(HardArgs A) {
+constexpr int WT = bundle_threads(BCAP_WIDE);  // threads of a wide CTA (it holds its SM)
+__global__ void __launch_bounds__(WT, 1) k_hard_wide(HardArgs A) {
     extern __shared__ __align__(16) unsigned char bundle_smem[];
     BundleSmem<BCAP_WIDE> &B = *reinterpret_cast<BundleSmem<BCAP_WIDE> *>(bundle_smem);
-    __shared__ double red_d[4];
-    __shared__ long long red_l[4];
+    __shared__ double red_d[WT / 32];
+    __shared__ long long red_l[WT / 32];
     __shared__ int q_sh;
     const int tid = threadIdx.x;
-    Team<128> tm{tid, red_d, red_l};
+    Team<WT> tm{tid, red_d, red_l};
     const int room = (A.frag.a_frag > 0.) ? 2 * A.frag.n_frag_max : 0;
     for (int guard = 0; guard < (1 << 30); guard++) {
         if (tid == 0) q_sh = atomicAdd(&A.queue[0], 1);
@@ -1064,7 +1065,7 @@ __global__ void __launch_bounds__(BT, 1) k_hard_wide(HardArgs A) {
         const int c = A.order[q];
         const int n = A.cnt[c];
         if (n + room > BCAP_WIDE) {
-            run_cluster<128>(A, c, tm);
+            run_cluster<WT>(A, c, tm);
             continue;
         }
         if (tid == 0) {
