@@ -577,19 +577,20 @@ __global__ void k_vdisp_bins(const double *part, const int *cntp, int nblk, doub
     cnt[b] = c;
 }
 // The Gaussian weights w_b = exp(-t_b^2), t_b = (r_min + (b + 1/2) dr - r) / dr
-// (src/particle.h:1443-1456): directly for the RB bins on either side of the
-// nearest one, and from there outwards by w_{b+1} = w_b exp(-2 t_b - 1),
-// w_{b-1} = w_b exp(2 t_b - 1), whose factors shrink by e^-2 per bin (t_b
-// steps by one).  Those bins weigh below exp(-(RB + 1/2)^2) ~ 5e-6 of the
-// nearest, so the recurrence's relative error (a few 1e-15) stays below
-// 1e-20 of the sums; the sums come out within a few ulp of the bin-by-bin
-// exp (11 exps a body instead of 32).
-constexpr int RB = 3;
+// (src/particle.h:1443-1456): by the bin-by-bin FP64 exp for the RB bins on
+// either side of the body's own, in FP32 beyond (their weights are below
+// exp(-(RB + 1/2)^2) ~ 1e-13 of the nearest, so FP32's 1e-6 relative error
+// there stays below 1e-19 of the sums); the sums come out within a few ulp
+// of the bin-by-bin FP64 arithmetic at a third of its FP64 work.
+constexpr int RB = 5;
 __global__ void k_radii(State S, Params P, double r_min, double dr, double drinv, const double *vd, const int *cnt) {
     __shared__ double s_vd[NBIN], s_on[NBIN];
+    __shared__ float s_vdf[NBIN], s_onf[NBIN];
     if (threadIdx.x < NBIN) {
         s_vd[threadIdx.x] = vd[threadIdx.x];
         s_on[threadIdx.x] = (cnt[threadIdx.x] > 0) ? 1. : 0.;
+        s_vdf[threadIdx.x] = (float)vd[threadIdx.x];
+        s_onf[threadIdx.x] = (cnt[threadIdx.x] > 0) ? 1.f : 0.f;
     }
     __syncthreads();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -607,27 +608,17 @@ __global__ void k_radii(State S, Params P, double r_min, double dr, double drinv
         vs += s_vd[b] * ex;
         ws += s_on[b] * ex;
     }
-    const double e2 = exp(-2.);
-    if (hi < NBIN - 1) {
-        const double t = (r_min + (hi + 0.5) * dr - rc) * drinv;
-        double w = exp(-t * t), g = exp(-2. * t - 1.);
-        for (int b = hi + 1; b < NBIN; b++) {
-            w *= g;
-            g *= e2;
-            vs += s_vd[b] * w;
-            ws += s_on[b] * w;
-        }
+    const float xf = (float)x;
+    float vsf = 0.f, wsf = 0.f;
+    for (int b = 0; b < NBIN; b++) {
+        if (b >= lo && b <= hi) continue;
+        const float t = ((float)b + 0.5f) - xf;
+        const float w = expf(-t * t);
+        vsf += s_vdf[b] * w;
+        wsf += s_onf[b] * w;
     }
-    if (lo > 0) {
-        const double t = (r_min + (lo + 0.5) * dr - rc) * drinv;
-        double w = exp(-t * t), h = exp(2. * t - 1.);
-        for (int b = lo - 1; b >= 0; b--) {
-            w *= h;
-            h *= e2;
-            vs += s_vd[b] * w;
-            ws += s_on[b] * w;
-        }
-    }
+    vs += (double)vsf;
+    ws += (double)wsf;
     const double v_disp = vs / ws;
     S.v_disp[i] = v_disp;
     const double r = sqrt(dot(pos, pos));

@@ -469,6 +469,378 @@ __global__ void __launch_bounds__(SB, OCC) soft_mixed_kernel(SoftArgs A) {
     }
 }
 
+// the mixed kernel's staging: pipelined (1) or gather-then-compute (0, the
+// default: at 1M bodies 1.046 ms per pass against 1.062 pipelined -- with six
+// CTAs per SM the gather's latency is already hidden, and the FMA pipe, not
+// the staging, bounds the pass)
+int g_soft_pipe = 0;
+
+// --------------------------------------------------------------------------
+// mixed precision, pipelined staging
+//
+// The same arithmetic, in the same order, as group_mixed with one i per
+// thread; only the staging of the tiles differs.  There the CTA gathered a
+// tile (global loads, FP64 shifts, shared stores), met a barrier, computed it
+// and met a second barrier, so the gather's latency stood between every two
+// tiles.  Here the EP-EP tiles and then the EP-SP tiles form one sequence: a
+// thread copies the records of its entry of tile t + 2 into a raw staging
+// slot with cp.async while the CTA computes tile t, and converts tile t + 1
+// from the raw slot into the second tile buffer at the start of tile t's
+// turn -- one barrier per tile, the global latency behind a tile of pair
+// work.  A thread reads back only the raw slot it copied itself.
+struct __align__(16) RawEntry {
+    float4 v[5];  // EP-EP: SoftSplit (v[0..1]), SoftPtcl (v[2..4]); EP-SP: SpjPack (v[0..3])
+};
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+struct PipeSmem {
+    MixedTile T[2];
+    RawEntry raw[TM];  // also the sub-block reduction's space at the end of a group
+    float4 sI[SB];
+    int4 sQ[SB];
+};
+
+// list entry e of tile t (EP-EP tiles first): its record copies started;
+// returns the particle / superparticle index, -1 for padding
+__device__ __forceinline__ int pipe_issue(const SoftArgs &A, int t, int Tep, int j0, int nj, int s0, int ns, int e,
+                                          RawEntry &R) {
+    if (t < Tep) {
+        const int k = t * TM + e;
+        if (k >= nj) return -1;
+        int p = A.j_idx[j0 + k];
+        if ((unsigned)p >= (unsigned)A.n_ptcl) { atomicOr(A.status, ST_BAD_INDEX); p = 0; }
+        const float4 *sp = reinterpret_cast<const float4 *>(A.jsplit + p);
+        const float4 *rp = reinterpret_cast<const float4 *>(A.ptcl + p);
+        cp_async16(&R.v[0], sp);
+        cp_async16(&R.v[1], sp + 1);
+        cp_async16(&R.v[2], rp);
+        cp_async16(&R.v[3], rp + 1);
+        cp_async16(&R.v[4], rp + 2);
+        return p;
+    }
+    const int k = (t - Tep) * TM + e;
+    if (k >= ns) return -1;
+    int q = A.s_idx[s0 + k];
+    if ((unsigned)q >= (unsigned)A.n_spj) { atomicOr(A.status, ST_BAD_INDEX); q = 0; }
+    const float4 *qp = reinterpret_cast<const float4 *>(A.spjp + q);
+    cp_async16(&R.v[0], qp);
+    cp_async16(&R.v[1], qp + 1);
+    cp_async16(&R.v[2], qp + 2);
+    cp_async16(&R.v[3], qp + 3);
+    return q;
+}
+
+// entry e of tile t from its raw slot into tile buffer T (group_mixed's staging arithmetic)
+template <bool EMIT>
+__device__ __forceinline__ void pipe_convert(int t, int Tep, int e, int p, const RawEntry &R, MixedTile &T, double ox,
+                                             double oy, double oz, const SoftSplit &o) {
+    if (t < Tep) {
+        if (p >= 0) {
+            const SoftSplit &sp = *reinterpret_cast<const SoftSplit *>(&R.v[0]);
+            const SoftPtcl &r = *reinterpret_cast<const SoftPtcl *>(&R.v[2]);
+            const double x = r.x, y = r.y, z = r.z;
+            const float rs2 = r.rs2;
+            put2(T.a, e, 0, -sp.xh); put2(T.a, e, 1, -sp.yh);
+            put2(T.b, e, 0, -sp.zh); put2(T.b, e, 1, sp.m);
+            put2(T.c, e, 0, -sp.xl); put2(T.c, e, 1, -sp.yl);
+            put2(T.d, e, 0, -sp.zl); put2(T.d, e, 1, sp.ro2);
+            reinterpret_cast<float *>(T.e)[e] = 1.01f * rs2;
+            T.r[e] = make_float4(__double2float_rn(x - ox), __double2float_rn(y - oy), __double2float_rn(z - oz), rs2);
+            T.q[e] = make_int2(r.id_local, r.rank);
+            if (EMIT) T.idx[e] = p;
+        } else {  // padding: massless, far away, never flagged
+            put2(T.a, e, 0, -1.0e18f); put2(T.a, e, 1, -1.0e18f);
+            put2(T.b, e, 0, -1.0e18f); put2(T.b, e, 1, 0.f);
+            put2(T.c, e, 0, 0.f); put2(T.c, e, 1, 0.f);
+            put2(T.d, e, 0, 0.f); put2(T.d, e, 1, 0.f);
+            reinterpret_cast<float *>(T.e)[e] = 0.f;
+            T.r[e] = make_float4(1.0e18f, 1.0e18f, 1.0e18f, 0.f);
+            T.q[e] = make_int2(-1, -1);
+        }
+        return;
+    }
+    if (p >= 0) {
+        const float4 p0 = R.v[0], p1 = R.v[1], p2 = R.v[2], p3 = R.v[3];
+        put2(T.a, e, 0, __fadd_rn(__fsub_rn(o.xh, p0.x), __fsub_rn(o.xl, p1.x)));
+        put2(T.a, e, 1, __fadd_rn(__fsub_rn(o.yh, p0.y), __fsub_rn(o.yl, p1.y)));
+        put2(T.b, e, 0, __fadd_rn(__fsub_rn(o.zh, p0.z), __fsub_rn(o.zl, p1.z)));
+        put2(T.b, e, 1, p0.w);
+        put2(T.c, e, 0, p2.x);
+        put2(T.c, e, 1, p2.y);
+        put2(T.d, e, 0, p2.z);
+        put2(T.d, e, 1, p1.w);
+        put2(T.f, e, 0, p2.w);
+        put2(T.f, e, 1, p3.x);
+        reinterpret_cast<float *>(T.e)[e] = p3.y;
+    } else {  // padding: massless, far away
+        put2(T.a, e, 0, -1.0e18f); put2(T.a, e, 1, -1.0e18f);
+        put2(T.b, e, 0, -1.0e18f); put2(T.b, e, 1, 0.f);
+        put2(T.c, e, 0, 0.f); put2(T.c, e, 1, 0.f);
+        put2(T.d, e, 0, 0.f); put2(T.d, e, 1, 0.f);
+        put2(T.f, e, 0, 0.f); put2(T.f, e, 1, 0.f);
+        reinterpret_cast<float *>(T.e)[e] = 0.f;
+    }
+}
+
+template <int S, bool EMIT, int UNR>
+__device__ __forceinline__ void group_mixed_pipe(const SoftArgs &A, int g, int ib, int ni, PipeSmem &M, int *scnt) {
+    constexpr int W = SB / S;
+    const int tid = threadIdx.x;
+    const int sub = tid / W, lane = tid % W;
+    const int i0 = A.i_off[g];
+    const int j0 = A.j_off[g], nj = A.j_off[g + 1] - j0;
+    const int s0 = A.s_off[g], ns = A.s_off[g + 1] - s0;
+    const float eps2 = A.eps2;
+    const float2 eps2_2 = dup2(eps2);
+
+    int p_first = A.i_idx[i0];
+    if ((unsigned)p_first >= (unsigned)A.n_iptcl) { atomicOr(A.status, ST_BAD_INDEX); p_first = 0; }
+    const double ox = A.iptcl[p_first].x, oy = A.iptcl[p_first].y, oz = A.iptcl[p_first].z;
+    const SoftSplit o = A.isplit[p_first];
+
+    // the i-particle of this thread (group_mixed with IPT = 1)
+    float xh, yh, zh, xl, yl, zl, xf, yf, zf, ro2i, thi;
+    const int li = lane;
+    bool vi = li < ni;
+    float ahx = 0.f, alx = 0.f, ahy = 0.f, aly = 0.f, ahz = 0.f, alz = 0.f, ahp = 0.f, alp = 0.f;
+    int ngb = 0, rk = 0, idmax = -1, idmin = INT32_MAX_;
+    {
+        int p = vi ? A.i_idx[i0 + ib + li] : p_first;
+        if ((unsigned)p >= (unsigned)A.n_iptcl) { atomicOr(A.status, ST_BAD_INDEX); p = 0; vi = false; }
+        const SoftPtcl r = A.iptcl[p];
+        const SoftSplit sp = A.isplit[p];
+        xf = __double2float_rn(r.x - ox);
+        yf = __double2float_rn(r.y - oy);
+        zf = __double2float_rn(r.z - oz);
+        M.sI[tid] = make_float4(xf, yf, zf, r.rs2);
+        M.sQ[tid] = make_int4(r.id_local, r.rank, p, 0);
+        xh = sp.xh; yh = sp.yh; zh = sp.zh;
+        xl = sp.xl; yl = sp.yl; zl = sp.zl;
+        ro2i = r.ro2;
+    }
+    const bool wact = (lane & ~31) < ni;
+    if (EMIT) {
+        for (int t = tid; t < ni; t += SB) scnt[t] = 0;
+    }
+    {
+        float L = 0.f, rmin2 = 3.0e38f;
+        if (vi) {
+            L = fmaxf(fabsf(xf), fmaxf(fabsf(yf), fabsf(zf)));
+            rmin2 = M.sI[tid].w;
+        }
+        const bool pre_ok = __syncthreads_and(L * L <= 4.0e8f * rmin2) != 0;
+        thi = pre_ok ? 1.01f * M.sI[tid].w : 3.0e38f;
+    }
+    const float2 c15 = dup2(1.5f), cm05 = dup2(-0.5f);
+    const float2 c05 = dup2(-0.5f), c25 = dup2(-2.5f);
+
+    const int Tep = (nj + TM - 1) / TM, Tn = Tep + (ns + TM - 1) / TM;
+    RawEntry &R = M.raw[tid];
+    int pn = -1;
+    if (Tn > 0) {
+        pn = pipe_issue(A, 0, Tep, j0, nj, s0, ns, tid, R);
+        cp_async_commit();
+        cp_async_wait_all();
+        pipe_convert<EMIT>(0, Tep, tid, pn, R, M.T[0], ox, oy, oz, o);
+    }
+    if (Tn > 1) {
+        pn = pipe_issue(A, 1, Tep, j0, nj, s0, ns, tid, R);
+        cp_async_commit();
+    }
+    __syncthreads();
+    for (int t = 0; t < Tn; t++) {
+        const int cur = t & 1;
+        if (t + 1 < Tn) {
+            cp_async_wait_all();
+            pipe_convert<EMIT>(t + 1, Tep, tid, pn, R, M.T[cur ^ 1], ox, oy, oz, o);
+        }
+        if (t + 2 < Tn) {
+            pn = pipe_issue(A, t + 2, Tep, j0, nj, s0, ns, tid, R);
+            cp_async_commit();
+        }
+        const MixedTile &T = M.T[cur];
+        const int jb = sub * (TM / S);
+        if (t < Tep) {
+            // ---- EP-EP ----
+            const int nt = min(TM, nj - t * TM);
+            const int je = wact ? min(jb + TM / S, (nt + 15) & ~15) : jb;
+            for (int c0 = jb; c0 < je; c0 += CHUNK) {
+                const int nq = min(CHUNK, je - c0) >> 1;
+                float2 tx = dup2(0.f), ty = dup2(0.f), tz = dup2(0.f), tp = dup2(0.f);
+                unsigned nm = 0u;
+#pragma unroll UNR
+                for (int q = 0; q < nq; q++) {
+                    const int pq = (c0 >> 1) + q;
+                    const float4 a = T.a[pq], b = T.b[pq], c = T.c[pq], d = T.d[pq];
+                    const float2 e = T.e[pq];
+                    const float2 rx = __fadd2_rn(__fadd2_rn(dup2(xh), lo2(a)), __fadd2_rn(dup2(xl), lo2(c)));
+                    const float2 ry = __fadd2_rn(__fadd2_rn(dup2(yh), hi2(a)), __fadd2_rn(dup2(yl), hi2(c)));
+                    const float2 rz = __fadd2_rn(__fadd2_rn(dup2(zh), lo2(b)), __fadd2_rn(dup2(zl), lo2(d)));
+                    const float2 r2f = __ffma2_rn(rx, rx, __ffma2_rn(ry, ry, __ffma2_rn(rz, rz, eps2_2)));
+                    const float2 r2 = make_float2(fmaxf(r2f.x, fmaxf(ro2i, d.z)), fmaxf(r2f.y, fmaxf(ro2i, d.w)));
+                    float2 ri = rsqrt2(r2);
+                    ri = __fmul2_rn(ri, __ffma2_rn(__fmul2_rn(cm05, r2), __fmul2_rn(ri, ri), c15));
+                    const float2 mr = __fmul2_rn(hi2(b), ri);
+                    const float2 mr3 = __fmul2_rn(mr, __fmul2_rn(ri, ri));
+                    tx = __ffma2_rn(mr3, rx, tx);
+                    ty = __ffma2_rn(mr3, ry, ty);
+                    tz = __ffma2_rn(mr3, rz, tz);
+                    tp = __fadd2_rn(tp, mr);
+                    if (r2f.x < fmaxf(thi, e.x)) nm |= 1u << (2 * q);
+                    if (r2f.y < fmaxf(thi, e.y)) nm |= 2u << (2 * q);
+                }
+                fold(ahx, alx, tx.x + tx.y);
+                fold(ahy, aly, ty.x + ty.y);
+                fold(ahz, alz, tz.x + tz.y);
+                fold(ahp, alp, tp.x + tp.y);
+                unsigned m = vi ? nm : 0u;
+                if (m) {
+                    const float4 me = M.sI[tid];
+                    const int4 mq = M.sQ[tid];
+                    do {
+                        const int jj = c0 + __ffs(m) - 1;
+                        m &= m - 1;
+                        const float4 rr = T.r[jj];
+                        const float hx = __fsub_rn(me.x, rr.x);
+                        const float hy = __fsub_rn(me.y, rr.y);
+                        const float hz = __fsub_rn(me.z, rr.z);
+                        const float r2r =
+                            __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(hx, hx), __fmul_rn(hy, hy)), __fmul_rn(hz, hz)), eps2);
+                        if (r2r < fmaxf(me.w, rr.w)) {
+                            const int2 qq = T.q[jj];
+                            const int idj = qq.x, rkj = qq.y;
+                            if (mq.x != idj || mq.y != rkj) {
+                                ngb += 1;
+                                rk += abs(mq.y - rkj);
+                                idmax = max(idmax, idj);
+                                idmin = min(idmin, idj);
+                                if (EMIT) {
+                                    const int slot = atomicAdd(&scnt[li], 1);
+                                    if (slot < A.cand_cap)
+                                        A.cand[(size_t)mq.z * A.cand_cap + slot] = T.idx[jj];
+                                    else
+                                        atomicOr(A.status, ST_CAND_OVERFLOW);
+                                }
+                            }
+                        }
+                    } while (m);
+                }
+            }
+        } else {
+            // ---- EP-SP (quadrupole) ----
+            if (t == Tep) {  // origin-relative FP32 coordinates of the i-particle
+                xf = __fadd_rn(__fsub_rn(xh, o.xh), __fsub_rn(xl, o.xl));
+                yf = __fadd_rn(__fsub_rn(yh, o.yh), __fsub_rn(yl, o.yl));
+                zf = __fadd_rn(__fsub_rn(zh, o.zh), __fsub_rn(zl, o.zl));
+            }
+            const int nt = min(TM, ns - (t - Tep) * TM);
+            const int je = wact ? min(jb + TM / S, (nt + 15) & ~15) : jb;
+            for (int c0 = jb; c0 < je; c0 += CHUNK) {
+                const int nq = min(CHUNK, je - c0) >> 1;
+                float2 tx = dup2(0.f), ty = dup2(0.f), tz = dup2(0.f), tp = dup2(0.f);
+#pragma unroll 4
+                for (int q = 0; q < nq; q++) {
+                    const int pq = (c0 >> 1) + q;
+                    const float4 a = T.a[pq], b = T.b[pq], c = T.c[pq], d = T.d[pq], f = T.f[pq];
+                    const float2 e = T.e[pq];
+                    const float2 rx = __fadd2_rn(dup2(xf), lo2(a));
+                    const float2 ry = __fadd2_rn(dup2(yf), hi2(a));
+                    const float2 rz = __fadd2_rn(dup2(zf), lo2(b));
+                    const float2 r2 = __ffma2_rn(rx, rx, __ffma2_rn(ry, ry, __ffma2_rn(rz, rz, eps2_2)));
+                    const float2 ri = rsqrt2(r2);
+                    const float2 r2i = __fmul2_rn(ri, ri);
+                    const float2 r3i = __fmul2_rn(r2i, ri);
+                    const float2 r4i = __fmul2_rn(r2i, r2i);
+                    const float2 r5i = __fmul2_rn(r2i, r3i);
+                    const float2 qrx = __ffma2_rn(lo2(c), rx, __ffma2_rn(lo2(f), ry, __fmul2_rn(e, rz)));
+                    const float2 qry = __ffma2_rn(hi2(c), ry, __ffma2_rn(hi2(f), rz, __fmul2_rn(lo2(f), rx)));
+                    const float2 qrz = __ffma2_rn(lo2(d), rz, __ffma2_rn(e, rx, __fmul2_rn(hi2(f), ry)));
+                    const float2 nrqr = __ffma2_rn(qrx, rx, __ffma2_rn(qry, ry, __ffma2_rn(qrz, rz, hi2(d))));
+                    const float2 nrqr4 = __fmul2_rn(nrqr, r4i);
+                    const float2 meff = __ffma2_rn(c05, nrqr4, hi2(b));
+                    const float2 meff3 = __fmul2_rn(__ffma2_rn(c25, nrqr4, hi2(b)), r3i);
+                    tx = __ffma2_rn(r5i, qrx, __ffma2_rn(meff3, rx, tx));
+                    ty = __ffma2_rn(r5i, qry, __ffma2_rn(meff3, ry, ty));
+                    tz = __ffma2_rn(r5i, qrz, __ffma2_rn(meff3, rz, tz));
+                    tp = __ffma2_rn(meff, ri, tp);
+                }
+                fold(ahx, alx, tx.x + tx.y);
+                fold(ahy, aly, ty.x + ty.y);
+                fold(ahz, alz, tz.x + tz.y);
+                fold(ahp, alp, tp.x + tp.y);
+            }
+        }
+        __syncthreads();
+    }
+    // ---- combine sub-blocks in a fixed order and write ForceGrav ----
+    if (S > 1) {
+        float *redf = reinterpret_cast<float *>(M.raw);
+        int *redi = reinterpret_cast<int *>(redf + SB * 8);
+        float *f = redf + tid * 8;
+        f[0] = ahx; f[1] = alx; f[2] = ahy; f[3] = aly;
+        f[4] = ahz; f[5] = alz; f[6] = ahp; f[7] = alp;
+        int *q = redi + tid * 4;
+        q[0] = ngb; q[1] = rk; q[2] = idmax; q[3] = idmin;
+        __syncthreads();
+        if (sub == 0) {
+            for (int s2 = 1; s2 < S; s2++) {
+                const float *h = redf + (tid + s2 * W) * 8;
+                const int *c = redi + (tid + s2 * W) * 4;
+                fold(ahx, alx, h[0]); alx += h[1];
+                fold(ahy, aly, h[2]); aly += h[3];
+                fold(ahz, alz, h[4]); alz += h[5];
+                fold(ahp, alp, h[6]); alp += h[7];
+                ngb += c[0]; rk += c[1];
+                idmax = max(idmax, c[2]); idmin = min(idmin, c[3]);
+            }
+        }
+    }
+    if (sub == 0 && vi) {
+        ForceRec &orec = A.force[M.sQ[tid].z];
+        ForceRec r;
+        if (A.accumulate) {
+            r = orec;
+        } else {
+            r.acc[0] = r.acc[1] = r.acc[2] = r.phi = 0.f;
+            r.number = 0; r.rank = 0; r.id_max = -1; r.id_min = INT32_MAX_;
+        }
+        r.acc[0] -= ahx + alx;
+        r.acc[1] -= ahy + aly;
+        r.acc[2] -= ahz + alz;
+        r.phi -= ahp + alp;
+        r.number += ngb;
+        r.rank += rk;
+        r.id_max = max(idmax, r.id_max);
+        r.id_min = min(idmin, r.id_min);
+        orec = r;
+    }
+}
+
+template <bool EMIT, int OCC>
+__global__ void __launch_bounds__(SB, OCC) soft_mixed_pipe_kernel(SoftArgs A) {
+    __shared__ PipeSmem M;
+    __shared__ int scnt[EMIT ? SB : 1];
+    const int g = A.group_order ? A.group_order[blockIdx.x] : blockIdx.x;
+    const int ni_all = A.i_off[g + 1] - A.i_off[g];
+    constexpr int UNR = OCC <= 4 ? 8 : 2;
+    for (int ib = 0; ib < ni_all; ib += SB) {
+        const int ni = min(SB, ni_all - ib);
+        if (ni > A.t_s1)
+            group_mixed_pipe<1, EMIT, UNR>(A, g, ib, ni, M, scnt);
+        else if (ni > A.t_s2)
+            group_mixed_pipe<2, EMIT, UNR>(A, g, ib, ni, M, scnt);
+        else
+            group_mixed_pipe<4, EMIT, UNR>(A, g, ib, ni, M, scnt);
+        __syncthreads();
+    }
+}
+
 // --------------------------------------------------------------------------
 // plain FP64
 template <int S, int IPT, bool EMIT>
@@ -830,12 +1202,13 @@ cudaError_t launch_soft(const SoftArgs &Ain, int precision, bool emit, cudaStrea
         if (A.n_spj > 0)
             { P3T_COUNT_LAUNCH(); spj_pack_kernel<<<(A.n_spj + 255) / 256, 256, 0, st>>>(A.spj, A.n_spj, A.eps2, A.trace_mode, A.spjp); }
         const int occ = A.occ ? A.occ : 5;
-#define P3T_SOFT_MIXED(OCC)                                                  \
-    do {                                                                     \
-        if (emit)                                                            \
-            { P3T_COUNT_LAUNCH(); soft_mixed_kernel<true, OCC><<<A.n_group, SB, 0, st>>>(A); }       \
-        else                                                                 \
-            { P3T_COUNT_LAUNCH(); soft_mixed_kernel<false, OCC><<<A.n_group, SB, 0, st>>>(A); }      \
+#define P3T_SOFT_MIXED(OCC)                                                                               \
+    do {                                                                                                  \
+        P3T_COUNT_LAUNCH();                                                                               \
+        if (g_soft_pipe && emit) soft_mixed_pipe_kernel<true, OCC><<<A.n_group, SB, 0, st>>>(A);        \
+        else if (g_soft_pipe) soft_mixed_pipe_kernel<false, OCC><<<A.n_group, SB, 0, st>>>(A);          \
+        else if (emit) soft_mixed_kernel<true, OCC><<<A.n_group, SB, 0, st>>>(A);                       \
+        else soft_mixed_kernel<false, OCC><<<A.n_group, SB, 0, st>>>(A);                                \
     } while (0)
         if (occ == 4)
             P3T_SOFT_MIXED(4);
@@ -854,3 +1227,8 @@ cudaError_t launch_soft(const SoftArgs &Ain, int precision, bool emit, cudaStrea
 }
 
 }  // namespace p3t
+
+extern "C" int p3t_set_soft_pipe(int on) {
+    p3t::g_soft_pipe = on ? 1 : 0;
+    return 0;
+}

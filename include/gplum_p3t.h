@@ -87,6 +87,13 @@ int p3t_set_soft_tiles(int t_ipt2, int t_s1, int t_s2);
  * per SM it is compiled for: 4, 5 (default) or 6.  Set by the autotuner;
  * results do not depend on it. */
 int p3t_set_soft_occupancy(int ctas_per_sm);
+/* Staging of the mixed soft kernel's tiles: 1 pipelined -- each thread
+ * copies the records of its entry two tiles ahead with cp.async and converts
+ * the next tile into a second buffer while the CTA computes the current one,
+ * one barrier per tile; 0 (default, 1.5 % faster at 1M bodies) gather,
+ * barrier, compute, barrier.  Bit-identical results.  No counterpart in
+ * GPLUM's interface. */
+int p3t_set_soft_pipe(int on);
 /* The library's CUDA stream (cudaStream_t) for callers that order their own
  * work or timing events after the library's launches. */
 void *p3t_stream(void);

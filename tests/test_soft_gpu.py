@@ -263,3 +263,30 @@ def test_work_splits_agree(gpu, tiles):
     assert lib.p3t_set_soft_tiles(40, 64, 32) != 0  # invalid: t_ipt2 < t_s1
     assert lib.p3t_set_soft_tiles(200, 64, 32) != 0  # invalid: neither <= 128 nor 256
     assert lib.p3t_set_soft_occupancy(3) != 0
+
+
+@pytest.mark.parametrize("ngl,tiles", [(256, (128, 64, 32)), (64, (128, 64, 32)), (256, (256, 32, 0))])
+def test_pipelined_staging_bit_identical(gpu, ngl, tiles):
+    """The pipelined staging (records copied two tiles ahead, one barrier per
+    tile) against gather-then-compute: the same ForceGrav records bit for
+    bit, with and without candidate emission, in every work split."""
+    P, d, s = prepared_state(n=20000, seed=9, ecc_hill=3.0, inc_hill=1.5, params=P3TParams(n_group_limit=ngl))
+    epi, epj = records(s)
+    L = lists_for(s, P)
+    sf = soft.SoftForce(P, precision=0)
+    sf.upload_particles(epj)
+    sf.upload_lists(L)
+    lib = sf.lib
+    out = {}
+    try:
+        assert lib.p3t_set_soft_tiles(*tiles) == 0
+        for pipe in (0, 1):
+            assert lib.p3t_set_soft_pipe(pipe) == 0
+            for emit in (False, True):
+                sf.run(emit_candidates=emit)
+                out[pipe, emit] = sf.download().copy()
+    finally:
+        lib.p3t_set_soft_pipe(0)
+        lib.p3t_set_soft_tiles(128, 64, 32)
+    for emit in (False, True):
+        assert out[1, emit].tobytes() == out[0, emit].tobytes()
