@@ -261,6 +261,7 @@ __global__ void k_lvl_split(int n, int level, int limit, const TNode *nd, int *e
 }
 
 // ---- moments and boxes, bottom-up -------------------------------------------------------
+constexpr int LEAF_B = 8;  // bodies of a leaf loaded at once (leaves hold at most n_leaf_limit = 8)
 // Node c's moments and boxes: a leaf sums its bodies in key order (the host
 // builder's sums), an inner node combines its children in child order by the
 // parallel-axis rule.  Children are read through L2 (ld.cg): they may have
@@ -274,20 +275,29 @@ __device__ void node_moments(int c, TNode *nd, SPJRec *spj, const int *order, co
     double olo[3] = {1e300, 1e300, 1e300}, ohi[3] = {-1e300, -1e300, -1e300};
     if (nchild == 0) {
         const int first = N.first, count = N.count;
-        for (int k = first; k < first + count; k++) {
-            const int p = order[k];
-            const double x = pos[3 * p], y = pos[3 * p + 1], z = pos[3 * p + 2], mp = mass[p];
-            m += mp;
-            cx += mp * x;
-            cy += mp * y;
-            cz += mp * z;
-            const double r = 1.1 * rs[p];
-            const double v[3] = {x, y, z};
-            for (int d = 0; d < 3; d++) {
-                ilo[d] = fmin(ilo[d], v[d] - 0.);
-                ihi[d] = fmax(ihi[d], v[d] + 0.);
-                olo[d] = fmin(olo[d], v[d] - r);
-                ohi[d] = fmax(ohi[d], v[d] + r);
+        // in blocks of LEAF_B bodies, every load of a block issued before its
+        // sums (the sums stay in key order)
+        for (int k0 = first; k0 < first + count; k0 += LEAF_B) {
+            int pb[LEAF_B];
+#pragma unroll
+            for (int u = 0; u < LEAF_B; u++) pb[u] = (k0 + u < first + count) ? order[k0 + u] : -1;
+#pragma unroll
+            for (int u = 0; u < LEAF_B; u++) {
+                const int p = pb[u];
+                if (p < 0) break;
+                const double x = pos[3 * p], y = pos[3 * p + 1], z = pos[3 * p + 2], mp = mass[p];
+                m += mp;
+                cx += mp * x;
+                cy += mp * y;
+                cz += mp * z;
+                const double r = 1.1 * rs[p];
+                const double v[3] = {x, y, z};
+                for (int d = 0; d < 3; d++) {
+                    ilo[d] = fmin(ilo[d], v[d] - 0.);
+                    ihi[d] = fmax(ihi[d], v[d] + 0.);
+                    olo[d] = fmin(olo[d], v[d] - r);
+                    ohi[d] = fmax(ohi[d], v[d] + r);
+                }
             }
         }
         if (m != 0.) {
@@ -295,14 +305,23 @@ __device__ void node_moments(int c, TNode *nd, SPJRec *spj, const int *order, co
             cy /= m;
             cz /= m;
         }
-        for (int k = first; k < first + count; k++) {
-            const int p = order[k];
-            const double dx = pos[3 * p] - cx, dy = pos[3 * p + 1] - cy, dz = pos[3 * p + 2] - cz, mp = mass[p];
-            q[0] += mp * dx * dx; q[1] += mp * dy * dy; q[2] += mp * dz * dz;
-            q[3] += mp * dx * dy; q[4] += mp * dx * dz; q[5] += mp * dy * dz;
+        for (int k0 = first; k0 < first + count; k0 += LEAF_B) {
+            int pb[LEAF_B];
+#pragma unroll
+            for (int u = 0; u < LEAF_B; u++) pb[u] = (k0 + u < first + count) ? order[k0 + u] : -1;
+#pragma unroll
+            for (int u = 0; u < LEAF_B; u++) {
+                const int p = pb[u];
+                if (p < 0) break;
+                const double dx = pos[3 * p] - cx, dy = pos[3 * p + 1] - cy, dz = pos[3 * p + 2] - cz, mp = mass[p];
+                q[0] += mp * dx * dx; q[1] += mp * dy * dy; q[2] += mp * dz * dz;
+                q[3] += mp * dx * dy; q[4] += mp * dx * dz; q[5] += mp * dy * dz;
+            }
         }
     } else {
-        for (int j = 0; j < nchild; j++) {
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            if (j >= nchild) break;
             const int ch = child0 + j;
             const double mc = __ldcg(&spj[ch].mass);
             m += mc;
@@ -321,7 +340,9 @@ __device__ void node_moments(int c, TNode *nd, SPJRec *spj, const int *order, co
             cy /= m;
             cz /= m;
         }
-        for (int j = 0; j < nchild; j++) {
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            if (j >= nchild) break;
             const SPJRec *S = spj + child0 + j;
             const double mc = __ldcg(&S->mass);
             const double dx = __ldcg(&S->pos[0]) - cx, dy = __ldcg(&S->pos[1]) - cy, dz = __ldcg(&S->pos[2]) - cz;
@@ -856,8 +877,7 @@ static int radix_sort(Context *c, DTree &T, unsigned long long *&key, int *&idx,
     if ((r = T.hist.reserve(256 * (size_t)nblk)) || (r = T.hoff.reserve(256 * (size_t)nblk + 1))) return r;
     for (int shift = 0; shift < bits; shift += 8) {
         { P3T_COUNT_LAUNCH(); k_radix_hist<<<nblk, 256, 0, c->stream>>>(key, n, shift, nblk, T.hist.p); }
-        int tot = 0;
-        if ((r = g_eng.scan(T.hist.p, T.hoff.p, 256 * nblk, &tot))) return r;
+        if ((r = g_eng.scan(T.hist.p, T.hoff.p, 256 * nblk, nullptr))) return r;  // stream-ordered, no host wait
         { P3T_COUNT_LAUNCH(); k_radix_scatter<<<nblk, 256, 0, c->stream>>>(key, idx, n, shift, nblk, T.hoff.p, key2, idx2); }
         std::swap(key, key2);
         std::swap(idx, idx2);
