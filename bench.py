@@ -58,7 +58,7 @@ HARD_FLOPS_PC, HARD_FLOPS_FULL, HARD_FLOPS_MEMBER, HARD_FLOPS_PREDICT = 77, 120,
 EPEP_FLOPS, EPSP_FLOPS = 32, 70  # per soft pair
 # DRAM bytes (read + write) per launch from the ncu captures summarised in
 # profiles/ (the bench cannot read DRAM counters itself)
-HARD_TRAFFIC_BYTES = 6.63e9
+HARD_TRAFFIC_BYTES = 3.53e9  # 868 MB at 262,144 bodies scaled by pair terms (57.45 M / 14.15 M)
 HARD_TRAFFIC_SOURCE = "ncu, profiles/k_hard_bundles_1m_hard_disk.md"
 SOFT_TRAFFIC_BYTES = 195.0e6
 SOFT_TRAFFIC_SOURCE = "ncu, profiles/soft_mixed_kernel_1m_disk.md"
