@@ -112,14 +112,23 @@ struct HardArgs {
 };
 
 // ---- FPHard::predict / correct / calcDeltat, src/particle.h:1183-1314 ----
-__device__ __forceinline__ void predict(const Hard &H, int s, double Dt) {
+// the predicted position and velocity also come back to the caller (no
+// reload of what was just stored)
+__device__ __forceinline__ void predict(const Hard &H, int s, double Dt, V3 &xp, V3 &vp) {
     const V3 pos = ld3(H.pos, s), vel = ld3(H.vel, s), as = ld3(H.acc_s, s), js = ld3(H.jerk_s, s),
              ad = ld3(H.acc_d, s), jd = ld3(H.jerk_d, s);
-    st3(H.x0, s, pos); st3(H.v0, s, vel); st3(H.a0_s, s, as); st3(H.j0_s, s, js); st3(H.j0_d, s, jd);
+    // FPHard's x0 and v0 (the step's start) are never read here: not stored
+    st3(H.a0_s, s, as); st3(H.j0_s, s, js); st3(H.j0_d, s, jd);
     st3(H.a0_d, s, ad);
     const V3 a = as + ad, j = js + jd;
-    st3(H.xp, s, pos + Dt * (vel + Dt * (0.5 * a + 1.6666666666666667e-1 * Dt * j)));
-    st3(H.vp, s, vel + Dt * (a + Dt * 0.5 * j));
+    xp = pos + Dt * (vel + Dt * (0.5 * a + 1.6666666666666667e-1 * Dt * j));
+    vp = vel + Dt * (a + Dt * 0.5 * j);
+    st3(H.xp, s, xp);
+    st3(H.vp, s, vp);
+}
+__device__ __forceinline__ void predict(const Hard &H, int s, double Dt) {
+    V3 xp, vp;
+    predict(H, s, Dt, xp, vp);
 }
 __device__ __forceinline__ void correct(const Hard &H, int s, double Dt) {
     const double Dt2 = Dt * Dt, Di = 1. / Dt, Di2 = Di * Di, Di3 = Di2 * Di;

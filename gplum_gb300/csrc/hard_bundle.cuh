@@ -725,10 +725,10 @@ __device__ void bundle_step(const HardArgs &A, BundleSmem<BCAP> &B) {
     // predict every member
     FOR_SLOTS(p) {
         const int g = B.gslot[p], k = B.cl[p];
-        predict(H, g, B.c_ts[k] - H.th[g]);
-        const V3 xp = ld3(H.xp, g);
+        V3 xp, vp;
+        predict(H, g, B.c_ts[k] - H.th[g], xp, vp);
         st3(B.xp, p, xp);
-        st3(B.vp, p, ld3(H.vp, g));
+        st3(B.vp, p, vp);
         st32b(B, B.xp32, p, xp, k);
     }
     __syncthreads();
