@@ -75,6 +75,7 @@ SIGNATURES = {
     "p3t_set_hard_lone": (I, [ctypes.c_float, I]),
     "p3t_set_walk": (I, [I]),
     "p3t_walk_last": (I, []),
+    "p3t_set_walk_limits": (I, [I, ctypes.c_longlong]),
     "p3t_set_soft_pipe": (I, [I]),
     "p3t_set_hard_profile": (I, [I]),
     "p3t_hard_phase_cycles": (I, [VP, I]),

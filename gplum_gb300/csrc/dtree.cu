@@ -676,12 +676,12 @@ __device__ __forceinline__ int bfs_scan(int v, int *ws, int &total) {
 }
 
 // count pass: the final frontier of group g (blockIdx.x) into store[off[g] ..
-// off[g] + len[g]) and its EPJ / SPJ entry counts; a frontier above BFS_CAP
+// off[g] + len[g]) and its EPJ / SPJ entry counts; a frontier above cap (<= BFS_CAP)
 // items or a full store sets *overflow (the lists then come from the task walk)
 __global__ void __launch_bounds__(BFS_T) k_walk_bfs(const TNode *nd, const TNodeF *nf, const int *gnode, int ng,
                                                     double theta2, float theta2f, int *jc, int *sc, int *len,
                                                     long long *off, int *store, unsigned long long *cursor,
-                                                    long long store_cap, int *overflow) {
+                                                    long long store_cap, int *overflow, int cap) {
     __shared__ int buf[2][BFS_CAP];
     __shared__ int ws[BFS_T / 32];
     __shared__ long long s_base;
@@ -733,7 +733,7 @@ __global__ void __launch_bounds__(BFS_T) k_walk_bfs(const TNode *nd, const TNode
             }
             int tot = 0;
             const int o = run + bfs_scan(cnt, ws, tot);
-            if (q < n && o + cnt <= BFS_CAP) {
+            if (q < n && o + cnt <= cap) {
                 if (nch) {
                     for (int k = 0; k < nch; k++) buf[cur ^ 1][o + k] = ((c0 + k) << 2) | FI_PEND;
                 } else {
@@ -743,7 +743,7 @@ __global__ void __launch_bounds__(BFS_T) k_walk_bfs(const TNode *nd, const TNode
             grown += __syncthreads_or(nch > 0);
             run += tot;
         }
-        if (run > BFS_CAP) {
+        if (run > cap) {
             over = true;
             break;
         }
@@ -867,6 +867,7 @@ static DTree g_dt;
 static int g_walk_depth = 3;  // levels above the walk's task split
 static int g_walk_bfs = 1;    // walk form: breadth first per group (1) or subtree tasks (0)
 static int g_walk_last = -1;  // the form the last build's lists came from
+static int g_walk_cap = BFS_CAP;  // frontier items a group's CTA may hold (lower: more groups take the task walk)
 static int g_moments_up = 1;  // moments in one launch (1) or one launch per level (0)
 
 // (key, idx) sorted in place by key, stably (8 passes of 8 bits over `bits`)
@@ -1000,7 +1001,7 @@ static int device_tree(Context *c, double theta, int n_leaf_limit, int n_group_l
         { P3T_COUNT_LAUNCH(); k_walk_bfs<<<ng, BFS_T, 0, c->stream>>>(T.nd.p, T.nf.p, T.gnode.p, ng, theta * theta,
                                                                   (float)(theta * theta), T.bjc.p, T.bsc.p, T.blen.p,
                                                                   T.boff.p, T.bstore.p, T.bcur.p, T.bstore_cap,
-                                                                  T.bover.p); }
+                                                                  T.bover.p, g_walk_cap); }
         int over = 0;
         unsigned long long used = 0;
         int nj = 0, ns = 0;
@@ -1119,6 +1120,13 @@ int p3t_set_walk(int form) {
 }
 
 int p3t_walk_last(void) { return g_walk_last; }
+
+int p3t_set_walk_limits(int frontier_cap, long long store_items) {
+    if (frontier_cap < 1 || frontier_cap > BFS_CAP || store_items < 0) return -(int)cudaErrorInvalidValue;
+    g_walk_cap = frontier_cap;
+    if (store_items > 0) g_dt.bstore_cap = store_items;
+    return 0;
+}
 
 int p3t_state_tree(double theta, int n_leaf_limit, int n_group_limit) {
     Context *c = ctx_get(0);

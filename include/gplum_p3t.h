@@ -277,6 +277,12 @@ int p3t_hard_phase_cycles(unsigned long long *out, int n);
 /* The walk form the last device tree's lists came from (1 breadth first, 0
  * tasks), -1 before the first build. */
 int p3t_walk_last(void);
+/* Limits of the breadth-first walk: frontier items a group's CTA may hold
+ * (1..4096, default 4096) and items of the store that keeps the groups'
+ * final frontiers between the count and fill passes (0: unchanged; it grows
+ * by itself after an overflow).  A build that exceeds either takes the task
+ * walk for its lists (same lists).  For tests of that fallback. */
+int p3t_set_walk_limits(int frontier_cap, long long store_items);
 /* KOMINAMI fragmentation of the collision outcome (src/collisionB.h:7-93;
  * Collision::a_frag, N_frag, Collision0::m_min of parameter.dat).  a_frag = 0
  * (the default) is perfect accretion.  A collision makes

@@ -110,3 +110,26 @@ def test_walk_forms_agree_at_1m(gpu):
         for k in ("i_off", "i_idx", "j_off", "j_idx", "s_off", "s_idx"):
             np.testing.assert_array_equal(a[k], b[k], err_msg=k)
         assert a["spj"].tobytes() == b["spj"].tobytes()
+
+
+# the breadth-first walk's fallbacks: a frontier above the CTA's limit, or a
+# frontier store too small for the build, hands the build to the task walk,
+# with the same lists; the store grows by itself for the next build
+@pytest.mark.parametrize("cap,store", [(8, 0), (4096, 1000)])
+def test_walk_fallback_same_lists(gpu, cap, store):
+    name, mk, ngl = CASES[1]
+    g, P = prepared(mk(), ngl)
+    H = host_lists(g, P)
+    try:
+        assert g.lib.p3t_set_walk_limits(cap, store) == 0
+        D = g.tree_lists(build=True)
+        assert g.lib.p3t_walk_last() == 0
+        for k in ("i_off", "i_idx", "j_off", "j_idx", "s_off"):
+            np.testing.assert_array_equal(D[k], H[k], err_msg=k)
+        if store:
+            D2 = g.tree_lists(build=True)  # the store grew: breadth first again
+            assert g.lib.p3t_walk_last() == 1
+            for k in ("j_idx", "s_idx"):
+                np.testing.assert_array_equal(D2[k], D[k], err_msg=k)
+    finally:
+        g.lib.p3t_set_walk_limits(4096, 1 << 24)

@@ -107,3 +107,22 @@ def test_count_status_coding():
     assert _lib.status_bits(-(65536 + 4)) == 4
     assert _lib.status_bits(-(65536 + 18)) == 18
     assert _lib.status_bits(-700) == 0 and _lib.status_bits(3) == 0
+
+
+def test_form_setters_reject_out_of_range():
+    lib = _lib.host_lib()
+    try:
+        for bad in (-1, 4):
+            assert lib.p3t_set_walk(bad) == INVALID_VALUE
+        assert lib.p3t_set_walk(3) == 0 and lib.p3t_set_walk(1) == 0
+        for cap, store in ((0, 0), (4097, 0), (8, -1)):
+            assert lib.p3t_set_walk_limits(cap, store) == INVALID_VALUE
+        assert lib.p3t_set_walk_limits(4096, 0) == 0
+        for thr, ctas in ((-1.0, 0), (1.0, -1), (1.0, 4097)):
+            assert lib.p3t_set_hard_lone(thr, ctas) == INVALID_VALUE
+        assert lib.p3t_hard_phase_cycles(None, 14) == INVALID_VALUE
+        buf = np.zeros(4, np.uint64)
+        assert lib.p3t_hard_phase_cycles(_p(buf), 4) == INVALID_VALUE  # fewer slots than phases
+    finally:
+        lib.p3t_set_walk(1)
+        lib.p3t_set_hard_lone(0.0, 0)
