@@ -686,11 +686,35 @@ __global__ void k_sum_ordered(const double *v, int n, double *out) {
     for (int i = 0; i < n; i++) s += v[i];
     *out = s;
 }
-template <class T>
-__global__ void k_compact(const T *src, T *dst, const int32_t *keep, const int32_t *pos, int n, int w) {
+// every field of the state in one pass: field f (words 32-bit words per
+// body) gathers its kept bodies into tmp + off[f], then the compacted runs go
+// back in a second pass
+constexpr int CF_MAX = 32;
+struct CompactSet {
+    uint32_t *p[CF_MAX];
+    int words[CF_MAX];
+    long long off[CF_MAX];  // in words
+    int nf;
+};
+__global__ void k_compact_gather(CompactSet C, const int32_t *keep, const int32_t *pos, int n, uint32_t *tmp) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || !keep[i]) return;
-    for (int k = 0; k < w; k++) dst[(size_t)pos[i] * w + k] = src[(size_t)i * w + k];
+    const long long d = pos[i];
+    for (int f = 0; f < C.nf; f++) {
+        const int w = C.words[f];
+        const uint32_t *src = C.p[f] + (long long)i * w;
+        uint32_t *dst = tmp + C.off[f] + d * w;
+        for (int k = 0; k < w; k++) dst[k] = src[k];
+    }
+}
+// blockIdx.y: the field; its first nk bodies' words from the gathered run
+__global__ void k_compact_back(CompactSet C, int nk, const uint32_t *tmp) {
+    const int f = blockIdx.y;
+    const long long nw = (long long)nk * C.words[f];
+    uint32_t *dst = C.p[f];
+    const uint32_t *src = tmp + C.off[f];
+    for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < nw; j += (long long)gridDim.x * blockDim.x)
+        dst[j] = src[j];
 }
 
 // ---------------------------------------------------------------------------
@@ -990,23 +1014,26 @@ int Engine::merge(double *edisp) {
 // (kpos: their new positions, nk: how many)
 int Engine::compact(int n, int nk) {
     int r = 0;
-    if ((r = compact_tmp.reserve((size_t)n * 3 * sizeof(double)))) return r;
-    auto comp = [&](auto *fld, int w) -> int {
-        using T2 = std::remove_pointer_t<decltype(fld)>;
-        T2 *tmp = (T2 *)compact_tmp.p;
-        cudaMemcpyAsync(tmp, fld, (size_t)n * w * sizeof(T2), cudaMemcpyDeviceToDevice, c->stream);
-        { P3T_COUNT_LAUNCH(); k_compact<T2><<<nb(n), 256, 0, c->stream>>>(tmp, fld, keep.p, kpos.p, n, w); }
-        return cuda_status(cudaGetLastError());
+    CompactSet C{};
+    long long words = 0;
+    auto add = [&](void *p, int w) {
+        C.p[C.nf] = (uint32_t *)p;
+        C.words[C.nf] = w;
+        C.off[C.nf] = words;
+        words += (long long)n * w;
+        C.nf++;
     };
     for (double *f : {S.mass, S.r_planet, S.f, S.phi, S.phi_d, S.phi_s, S.r_out, S.r_out_inv, S.r_search, S.v_disp,
                       S.time, S.dt, S.acc0})
-        if ((r = comp(f, 1))) return r;
-    for (double *f : {S.pos, S.vel, S.acc, S.acc_d, S.jerk_d, S.acc_s, S.jerk_s})
-        if ((r = comp(f, 3))) return r;
-    for (int64_t *f : {S.id, S.id_cluster})
-        if ((r = comp(f, 1))) return r;
-    for (int32_t *f : {S.number, S.rank, S.id_max, S.id_min, S.n_cluster, S.dead, S.merged})
-        if ((r = comp(f, 1))) return r;
+        add(f, 2);
+    for (double *f : {S.pos, S.vel, S.acc, S.acc_d, S.jerk_d, S.acc_s, S.jerk_s}) add(f, 6);
+    for (int64_t *f : {S.id, S.id_cluster}) add(f, 2);
+    for (int32_t *f : {S.number, S.rank, S.id_max, S.id_min, S.n_cluster, S.dead, S.merged}) add(f, 1);
+    if ((r = compact_tmp.reserve((size_t)words * sizeof(uint32_t)))) return r;
+    uint32_t *tmp = (uint32_t *)compact_tmp.p;
+    { P3T_COUNT_LAUNCH(); k_compact_gather<<<nb(n), 256, 0, c->stream>>>(C, keep.p, kpos.p, n, tmp); }
+    if (nk > 0) { P3T_COUNT_LAUNCH(); k_compact_back<<<dim3(std::max(1, std::min(nb(nk), 1024)), C.nf), 256, 0, c->stream>>>(C, nk, tmp); }
+    if ((r = cuda_status(cudaGetLastError()))) return r;
     S.n = nk;
     n_clusters = 0;
     frag_lo = frag_hi = nk;
