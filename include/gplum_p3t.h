@@ -258,10 +258,10 @@ int p3t_set_hard_lone(float log2_steps, int ctas);
  * breadth first, one CTA per group, every thread testing cells of the
  * group's frontier; 0 the subtree tasks of one thread each.  Both emit the
  * host builder's depth-first lists entry for entry (a group whose frontier
- * outgrows its CTA takes the task walk).  Bit 1, the moments: 0 (default) one
- * launch that climbs from every leaf while it is its parent's last child to
- * finish, 1 one launch per level; the same values.  No counterpart in GPLUM's
- * interface. */
+ * outgrows its CTA takes the task walk).  Bit 1, the moments: 0 (default)
+ * every leaf in one launch over a compacted leaf list, then the inner nodes
+ * one level at a time; 1 all nodes one level at a time; the same values.  No
+ * counterpart in GPLUM's interface. */
 int p3t_set_walk(int form);
 /* Per-phase clock counts of the bundle form's loop (off by default; on, each
  * CTA's thread 0 reads the SM clock at the barriers that end the phases):
