@@ -1039,13 +1039,34 @@ struct IsoArgs {
     Params P;
     double t0, t1;
     int *status;
+    const int32_t *list, *count;  // the isolated bodies and how many
 };
 
-__global__ void k_isolated(IsoArgs A) {
+// the bodies outside every cluster (no neighbour), ascending: the drift's
+// threads take one each, every lane busy (a launch over all bodies left
+// nine lanes in ten idle on a disk whose bodies are mostly in clusters)
+__global__ void k_iso_flag(const int32_t *number, int n, int32_t *flag) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) flag[i] = number[i] == 0;
+}
+__global__ void k_iso_list(const int32_t *flag, const int32_t *pos, int n, int32_t *list, int32_t *count) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (flag[i]) list[pos[i]] = i;
+    if (i == n - 1) *count = pos[i] + flag[i];
+}
+
+__device__ void isolated_body(const IsoArgs &A, int i);
+// grid-stride over the list: the grid is sized from the host's count of
+// bodies outside the clusters, the device's count is the one obeyed
+__global__ void k_isolated(IsoArgs A) {
+    const int n_iso = *A.count;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n_iso; t += gridDim.x * blockDim.x)
+        isolated_body(A, A.list[t]);
+}
+__device__ void isolated_body(const IsoArgs &A, int i) {
     const State &S = A.S;
     const Params &P = A.P;
-    if (i >= S.n || S.number[i] != 0) return;
     V3 pos = ld3(S.pos, i), vel = ld3(S.vel, i);
     // getEccentricity, src/particle.h:668-681
     double ecc;
@@ -1259,6 +1280,7 @@ struct HardBufs {
     DevBuf<long long> fmap;
     DevBuf<unsigned long long> live;  // [2] pair terms evaluated by the last launch
     DevBuf<unsigned long long> phase;  // [HP_N] clock cycles per bundle phase (when profiled)
+    DevBuf<int32_t> iso;               // isolated bodies: flags, positions, list, count
     Hard H;
     int cap = 0;
     int reserve(int m) {
@@ -1569,7 +1591,15 @@ int p3t_hard_integrate(int istep) {
             (r = cuda_status(cudaFuncSetAttribute(k_isolated, cudaFuncAttributeMaxDynamicSharedMemorySize, ISO_SMEM))))
             return r;
     }
-    if (E.S.n > 0 && (r = cuda_status(cudaEventRecord(ev_iso_ready, c->stream)))) return r;
+    if (E.S.n > 0) {
+        const int n = E.S.n;
+        if ((r = g_hb.iso.reserve(3 * (size_t)n + 1))) return r;
+        int32_t *flag = g_hb.iso.p, *pos = flag + n, *list = pos + n;
+        { P3T_COUNT_LAUNCH(); k_iso_flag<<<(n + 255) / 256, 256, 0, c->stream>>>(E.S.number, n, flag); }
+        if ((r = E.scan(flag, pos, n, nullptr))) return r;
+        { P3T_COUNT_LAUNCH(); k_iso_list<<<(n + 255) / 256, 256, 0, c->stream>>>(flag, pos, n, list, list + n); }
+        if ((r = cuda_status(cudaEventRecord(ev_iso_ready, c->stream)))) return r;
+    }
     if (nc > 0) {
         HardArgs A{};
         A.S = E.S;
@@ -1700,8 +1730,12 @@ int p3t_hard_integrate(int istep) {
         I.t0 = (istep - 1) * P.dt_tree;
         I.t1 = istep * P.dt_tree;
         I.status = c->status;
+        I.list = g_hb.iso.p + 2 * (size_t)E.S.n;
+        I.count = I.list + E.S.n;
+        // the bodies outside the clusters: n - members (the device count checks it)
+        const int n_iso = std::max(1, E.S.n - E.n_members);
         if ((r = cuda_status(cudaStreamWaitEvent(s_iso, ev_iso_ready, 0)))) return r;
-        { P3T_COUNT_LAUNCH(); k_isolated<<<(E.S.n + 127) / 128, 128, ISO_SMEM, s_iso>>>(I); }
+        { P3T_COUNT_LAUNCH(); k_isolated<<<(n_iso + 127) / 128, 128, ISO_SMEM, s_iso>>>(I); }
         if ((r = cuda_status(cudaGetLastError())) || (r = cuda_status(cudaEventRecord(ev_iso_done, s_iso))) ||
             (r = cuda_status(cudaStreamWaitEvent(c->stream, ev_iso_done, 0))))
             return r;
