@@ -386,10 +386,14 @@ __global__ void k_leaf_flag(int nn, const TNode *nd, int *flag) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c < nn) flag[c] = nd[c].nchild == 0;
 }
+// leaves to the front of `list` (ascending), inner nodes to the back in
+// ascending node order (so each level's inner nodes are one run; inner node c
+// sits at nn - 1 - (c - pos[c]) counted from the back); count = leaves
 __global__ void k_leaf_list(int nn, const int *flag, const int *pos, int *list, int *count) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= nn) return;
     if (flag[c]) list[pos[c]] = c;
+    else list[nn - 1 - (c - pos[c])] = c;
     if (c == nn - 1) *count = pos[c] + flag[c];
 }
 __global__ void k_moments_leaves(const int *list, const int *count, TNode *nd, SPJRec *spj, const int *order,
@@ -398,11 +402,15 @@ __global__ void k_moments_leaves(const int *list, const int *count, TNode *nd, S
     if (t >= *count) return;
     node_moments(list[t], nd, spj, order, pos, mass, rs);
 }
-__global__ void k_moments_inner(int lo, int hi, TNode *nd, SPJRec *spj, const int *order, const double *pos,
-                                const double *mass, const double *rs) {
-    const int c = lo + blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= hi || nd[c].nchild == 0) return;
-    node_moments(c, nd, spj, order, pos, mass, rs);
+// the inner nodes of level [lo, hi): their run in the back of `list` (from
+// the leaf-position scan: inner nodes below c number c - lpos[c])
+__global__ void k_moments_inner(int lo, int hi, int nn, const int *list, const int *lpos, const int *flag, TNode *nd,
+                                SPJRec *spj, const int *order, const double *pos, const double *mass, const double *rs) {
+    const int a = lo - lpos[lo];                                 // inner nodes before the level
+    const int b = (hi < nn) ? hi - lpos[hi] : nn - (lpos[nn - 1] + flag[nn - 1]);  // ... and up to its end
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a + t >= b) return;
+    node_moments(list[nn - 1 - (a + t)], nd, spj, order, pos, mass, rs);
 }
 
 // ---- groups ---------------------------------------------------------------------------------
@@ -979,7 +987,8 @@ static int device_tree(Context *c, double theta, int n_leaf_limit, int n_group_l
                                                                                       E.S.r_search); }
         for (int L = (int)T.level_start.size() - 2; L >= 0; L--) {
             const int lo = T.level_start[L], hi = T.level_start[L + 1];
-            { P3T_COUNT_LAUNCH(); k_moments_inner<<<nblocks(hi - lo, 128), 128, 0, c->stream>>>(lo, hi, T.nd.p, d.spj.p, idx,
+            { P3T_COUNT_LAUNCH(); k_moments_inner<<<nblocks(hi - lo, 128), 128, 0, c->stream>>>(lo, hi, base, list, lpos, flag,
+                                                                                           T.nd.p, d.spj.p, idx,
                                                                                            E.S.pos, E.S.mass,
                                                                                            E.S.r_search); }
         }

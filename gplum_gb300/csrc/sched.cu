@@ -203,11 +203,15 @@ __global__ void k_feat_bodies(State S, const int32_t *cl_of, int cap, double dt_
     for (int t = 0; t < nn; t++) {
         const int j = S.nbr[(size_t)i * cap + t];
         if (j < 0 || j >= S.n) continue;
-        const double dx = S.pos[3 * j] - xi, dy = S.pos[3 * j + 1] - yi, dz = S.pos[3 * j + 2] - zi;
-        const double du = S.vel[3 * j] - ui, dv = S.vel[3 * j + 1] - vi, dw = S.vel[3 * j + 2] - wi;
-        const double r = fmin(roi, S.r_out_inv[j]);
-        sep = fminf(sep, (float)(sqrt(dx * dx + dy * dy + dz * dz) * r));
-        vr = fmaxf(vr, (float)(sqrt(du * du + dv * dv + dw * dw) * dt_tree * r));
+        // FP64 differences (positions near 1 AU, separations of 1e-4 AU), the
+        // rest in FP32: the features only order the work queue
+        const float dx = (float)(S.pos[3 * j] - xi), dy = (float)(S.pos[3 * j + 1] - yi),
+                    dz = (float)(S.pos[3 * j + 2] - zi);
+        const float du = (float)(S.vel[3 * j] - ui), dv = (float)(S.vel[3 * j + 1] - vi),
+                    dw = (float)(S.vel[3 * j + 2] - wi);
+        const float r = (float)fmin(roi, S.r_out_inv[j]);
+        sep = fminf(sep, sqrtf(dx * dx + dy * dy + dz * dz) * r);
+        vr = fmaxf(vr, sqrtf(du * du + dv * dv + dw * dw) * (float)dt_tree * r);
     }
     atomicMin(&red[3 * c], fbits(sep));
     atomicMax(&red[3 * c + 1], fbits(vr));
