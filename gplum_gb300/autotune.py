@@ -10,7 +10,9 @@ code:
   disk (0.5-1.5 AU, m = 1e-10, theta = 0.5, n_group_limit = 256);
 * the bundle form's heavy-cluster threshold (p3t_set_hard_heavy: clusters
   whose learned prediction of log2(1 + block steps) reaches it run alone in a
-  CTA first) -- timed from restored states of the hard-part disk;
+  CTA first) -- the mean hard launch over tree steps 6..25 of whole runs of
+  the hard-part disk (one restored state misjudged it: 5.5 there, 6.75 over
+  the steps, 51.3 against 47.4 ms);
 * whether the bundle form's clusters above 256 bodies run in a concurrent
   wide launch (lone bundles of up to 512 slots) or one per CTA in the main
   launch (p3t_set_hard_wide) -- timed from one restored state;
@@ -26,6 +28,7 @@ Every candidate gives the same neighbour results and forces equal to
 rounding (soft) or bit-identical results (hard); only the time differs.
 """
 import argparse
+import ctypes
 import json
 import os
 import time
@@ -96,7 +99,8 @@ def tune_tiers(g, istep=1, grid=TIER_GRID):
     return best, table
 
 
-HEAVY_GRID = (0.0, 5.5, 6.0, 6.5, 7.0, 7.5)
+HEAVY_GRID = (0.0, 5.5, 6.0, 6.5, 6.75, 7.0, 7.5)
+HEAVY_STEPS = (5, 25)  # the hard launch's mean over tree steps 6..25 after start-up
 
 
 def tune_heavy(g, istep=1, grid=HEAVY_GRID):
@@ -115,6 +119,39 @@ def tune_heavy(g, istep=1, grid=HEAVY_GRID):
     lib.p3t_state_snapshot(1)
     best = min(table, key=table.get)
     _lib.check(lib.p3t_set_hard_heavy(ctypes.c_float(best)), "p3t_set_hard_heavy")
+    return best, table
+
+
+def tune_heavy_steps(P, disk, grid=HEAVY_GRID, steps=HEAVY_STEPS):
+    """The heavy-cluster threshold by whole runs: for each threshold, start-up
+    and tree steps 1..steps[1] of `disk` with the learned order, the mean hard
+    launch over the steps after steps[0] (the distribution of chain lengths
+    changes as the disk evolves, so one state misjudges it); installs the
+    fastest.  Returns (best, {threshold: ms})."""
+    import ctypes
+
+    import numpy as np
+
+    from . import scheduler
+    from .p3t import GpuSystem
+
+    table = {}
+    for h in grid:
+        g = GpuSystem(P)
+        load(g.lib)
+        scheduler.load(lib=g.lib)
+        g.lib.p3t_set_schedule(1)
+        _lib.check(g.lib.p3t_set_hard_heavy(ctypes.c_float(h)), "p3t_set_hard_heavy")
+        g.load(disk)
+        g.set_r_planet()
+        g.startup()
+        hard = []
+        for istep in range(1, steps[1] + 1):
+            g.tree_step(istep)
+            if istep > steps[0]:
+                hard.append(g.step_phases_ms()["hard"])
+        table[h] = float(np.mean(hard))
+    best = min(table, key=table.get)
     return best, table
 
 
@@ -222,17 +259,9 @@ def main():
     heavy_best, heavy_table = None, {}
     wide_best, wide_table = tune_wide(g)
     if scheduler.load(lib=g.lib) is not None:
-        # two tree steps' states: the heavy threshold matters where predictions differ
-        for istep in (1, 2):
-            b, t = tune_heavy(g, istep)
-            for k, v in t.items():
-                heavy_table[k] = heavy_table.get(k, 0.0) + v
-            g.hard(istep)
-            g.tree_soft()
-            g.correct(False)
-            g.kick()
-            g.cluster()
-        heavy_best = keep_incumbent(min(heavy_table, key=heavy_table.get), heavy_table, prev.get("hard_heavy"))
+        heavy_best, heavy_table = tune_heavy_steps(P, d)
+        heavy_best = keep_incumbent(heavy_best, heavy_table, prev.get("hard_heavy"))
+        _lib.check(g.lib.p3t_set_hard_heavy(ctypes.c_float(heavy_best)), "p3t_set_hard_heavy")
     if "hard_bundle" in prev and "hard_wide" in prev:
         wide_best = keep_incumbent(wide_best, wide_table, tuple(prev["hard_bundle"]) + (prev["hard_wide"],))
     if "hard_tiers" in prev:

@@ -1318,7 +1318,7 @@ static std::vector<ColRec> g_cols;
 static double g_edisp[2] = {0., 0.};
 static int g_warp_min = 8, g_cta_min = 64;
 static int g_hard_mode = 0;  // 0: bundles, 1: thread/warp/CTA tiers
-static float g_heavy = 5.5f;  // predicted log2(1 + block steps) from which a cluster runs alone (0: never)
+static float g_heavy = 6.75f;  // predicted log2(1 + block steps) from which a cluster runs alone (0: never)
 static int g_wide = 1;        // clusters above the bundle capacity: wide lone bundles (1) or one per CTA (0)
 static int g_bcap = 256, g_bocc = 2;  // bundle member slots and CTAs per SM (256/2, 128/3, 128/4)
 static FragParams g_frag = {0., 9.426627927538057e-12, 10, 0, 0ULL};  // off (a_frag = 0)
