@@ -822,10 +822,33 @@ __device__ void bundle_step(const HardArgs &A, BundleSmem<BCAP> &B) {
         bundle_finalize(A, B, 2, nt, 1);
         HP_MARK(HP_FINAL);
     }
-    for (int i = threadIdx.x; i < nt; i += BT) {
-        const int s = B.tgt[i], g = B.gslot[s], k = B.cl[s];
-        H.th[g] += B.c_ts[k] - H.th[g];
-        if (!(B.c_flags[k] & CF_COL) && !B.dead[s]) dt_hermite(P, H, g);
+    // time and calcDeltat: the two criteria of a target (planets, sun) in a
+    // pair of lanes, exchanged by a shuffle; the even lane goes on with the
+    // target's time and dt_hermite's step choice
+    for (int base = 0; base < 2 * nt; base += BT) {
+        const int i = base + threadIdx.x, t = i >> 1;
+        const bool act = i < 2 * nt;
+        int s = 0, g = 0, k = 0;
+        bool upd = false;
+        double crit = 0.;
+        if (act) {
+            s = B.tgt[t];
+            g = B.gslot[s];
+            k = B.cl[s];
+            upd = !(B.c_flags[k] & CF_COL) && !B.dead[s];
+            if (upd) {
+                // one code path for both lanes (the inputs chosen by parity)
+                const bool sun = (i & 1) != 0;
+                crit = dt4th(sun ? P.eta_sun : P.eta, P.alpha2, sun ? 0. : H.acc0[g], ld3(sun ? H.acc_s : H.acc_d, g),
+                             ld3(sun ? H.jerk_s : H.jerk_d, g), ld3(sun ? H.a2_s : H.a2_d, g),
+                             ld3(sun ? H.a3_s : H.a3_d, g));
+            }
+        }
+        const double other = __shfl_xor_sync(0xffffffffu, crit, 1);
+        if (act && !(i & 1)) {
+            H.th[g] += B.c_ts[k] - H.th[g];
+            if (upd) H.dt[g] = dt_next_hermite(P, H.th[g], H.dt[g], dmin(crit, other));
+        }
     }
     __syncthreads();
     for (int i = threadIdx.x; i < nt; i += BT) {

@@ -551,10 +551,12 @@ __device__ void lone_cluster(const HardArgs &A, int c, LoneSmem<NT> &L, const Te
         const int nt = L.n_tgt;
         for (int it = tid; it < 2 * na; it += NT) {
             const int t = it >> 1, q = it & 1, s = L.tgt[t];
-            L.dtq[q][t] = q == 0 ? dt4th(P.eta, P.alpha2, L.acc0[s], lv(L.acc_d, s), lv(L.jerk_d, s), lv(L.a2_d, s),
-                                         lv(L.a3_d, s))
-                                 : dt4th(P.eta_sun, P.alpha2, 0., lv(L.acc_s, s), lv(L.jerk_s, s), lv(L.a2_s, s),
-                                         lv(L.a3_s, s));
+            // one code path for both criteria (the inputs chosen by q): lanes
+            // of a warp that took two paths would run them one after the other
+            const bool sun = q != 0;
+            L.dtq[q][t] = dt4th(sun ? P.eta_sun : P.eta, P.alpha2, sun ? 0. : L.acc0[s], lv(sun ? L.acc_s : L.acc_d, s),
+                                lv(sun ? L.jerk_s : L.jerk_d, s), lv(sun ? L.a2_s : L.a2_d, s),
+                                lv(sun ? L.a3_s : L.a3_d, s));
         }
         __syncthreads();
         for (int t = tid; t < nt; t += NT) {
