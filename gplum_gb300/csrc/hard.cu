@@ -131,7 +131,7 @@ __device__ __forceinline__ void predict(const Hard &H, int s, double Dt) {
     predict(H, s, Dt, xp, vp);
 }
 __device__ __forceinline__ void correct(const Hard &H, int s, double Dt) {
-    const double Dt2 = Dt * Dt, Di = 1. / Dt, Di2 = Di * Di, Di3 = Di2 * Di;
+    const double Dt2 = Dt * Dt, Di = recip_pow2_or_div(Dt), Di2 = Di * Di, Di3 = Di2 * Di;
     const V3 Am_s = ld3(H.acc_s, s) - ld3(H.a0_s, s), J0_s = Dt * ld3(H.j0_s, s), J1_s = Dt * ld3(H.jerk_s, s);
     const V3 A2_s = 3. * Am_s - (J1_s + 2. * J0_s);
     const V3 A3_s = -2. * Am_s + (J1_s + J0_s);
@@ -1141,7 +1141,7 @@ __device__ void isolated_body(const IsoArgs &A, int i) {
             jd = v3(0., 0., 0.);
             sun_force(P, xp, vp, as, js, nullptr);
             for (int it = 0; it < 2; it++) {
-                const double Dt = dt, Dt2 = Dt * Dt, Di = 1. / Dt, Di2 = Di * Di, Di3 = Di2 * Di;
+                const double Dt = dt, Dt2 = Dt * Dt, Di = recip_pow2_or_div(Dt), Di2 = Di * Di, Di3 = Di2 * Di;
                 const V3 Am_s = as - a0s, J0_s = Dt * j0s, J1_s = Dt * js;
                 const V3 A2_s = 3. * Am_s - (J1_s + 2. * J0_s);
                 const V3 A3_s = -2. * Am_s + (J1_s + J0_s);

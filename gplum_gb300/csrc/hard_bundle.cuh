@@ -793,7 +793,7 @@ __device__ void bundle_step(const HardArgs &A, BundleSmem<BCAP> &B) {
             const double ad = H.acc_d[gd], a0d = H.a0_d[gd], j0d = H.j0_d[gd], jd = H.jerk_d[gd];
             const double xp = H.xp[gd], vp = H.vp[gd];
             const double Dt = B.c_ts[k] - th;
-            const double Dt2 = Dt * Dt, Di = 1. / Dt, Di2 = Di * Di, Di3 = Di2 * Di;
+            const double Dt2 = Dt * Dt, Di = recip_pow2_or_div(Dt), Di2 = Di * Di, Di3 = Di2 * Di;
             const double Am_s = as - a0s, J0_s = Dt * j0s, J1_s = Dt * js;
             const double A2_s = 3. * Am_s - (J1_s + 2. * J0_s);
             const double A3_s = -2. * Am_s + (J1_s + J0_s);

@@ -269,7 +269,7 @@ __device__ void lone_correct(LoneSmem<NT> &L, const Pre &pre) {
     for (int it = threadIdx.x; it < 3 * nt; it += NT) {
         const int t = it / 3, d = it - 3 * t, s = L.tgt[t];
         const double Dt = L.ts - L.th[s];
-        const double Dt2 = Dt * Dt, Di = 1. / Dt, Di2 = Di * Di, Di3 = Di2 * Di;
+        const double Dt2 = Dt * Dt, Di = recip_pow2_or_div(Dt), Di2 = Di * Di, Di3 = Di2 * Di;
         const double Am_s = L.acc_s[d][s] - L.a0_s[d][s], J0_s = Dt * L.j0_s[d][s], J1_s = Dt * L.jerk_s[d][s];
         const double A2_s = 3. * Am_s - (J1_s + 2. * J0_s);
         const double A3_s = -2. * Am_s + (J1_s + J0_s);

@@ -93,6 +93,17 @@ __device__ __forceinline__ double dt4th(double eta, double alpha2, double acc0, 
     return (Jerk > 0.) ? eta * sqrt((Acc * Snap + Jerk2) / (Jerk * Crac + Snap2)) : 1.7976931348623157e308;
 }
 
+// 1 / x, the same double as the IEEE quotient: by the exponent alone when x
+// is a power of two (a block step's length; its reciprocal is exact), else
+// by the division
+__device__ __forceinline__ double recip_pow2_or_div(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned e = (unsigned)((b >> 52) & 0x7ff);
+    if ((b & 0x800fffffffffffffULL) == 0ULL && e != 0 && e < 0x7fe)
+        return __longlong_as_double((long long)(0x7FE0000000000000ULL - b));
+    return 1. / x;
+}
+
 // fmod(t, d) for the time-step quantisation.  d is a power of two there
 // (dt_tree, dt_min and every halving of them); then t - floor(t/d)*d is
 // computed exactly (scaling by a power of two, floor and the product are
@@ -100,10 +111,14 @@ __device__ __forceinline__ double dt4th(double eta, double alpha2, double acc0, 
 // IEEE fmod returns for t >= 0.  Any other d takes the library fmod.
 __device__ __forceinline__ double rem_pow2(double t, double d) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(d);
-    const bool pow2 = d > 0. && (b & 0x000fffffffffffffULL) == 0ULL && ((b >> 52) & 0x7ff) != 0 &&
-                      ((b >> 52) & 0x7ff) != 0x7ff;
+    const unsigned e = (unsigned)((b >> 52) & 0x7ff);
+    const bool pow2 = d > 0. && (b & 0x000fffffffffffffULL) == 0ULL && e != 0 && e < 0x7fe;
     if (!pow2 || !(t >= 0.) || t >= 1e300) return fmod(t, d);
-    return t - floor(t / d) * d;
+    // t / d as t times 1/d: for d = 2^k (normal, k < 1023) the reciprocal
+    // 2^-k is exact (its biased exponent is 2046 minus d's), and so is the
+    // product -- the same double as the quotient, without a division
+    const double rd = __longlong_as_double((long long)(0x7FE0000000000000ULL - b));
+    return t - floor(t * rd) * d;
 }
 
 // FPGrav::calcDeltatInitial, src/particle.h:886-914.  The fmod loops are
