@@ -657,7 +657,7 @@ __global__ void k_walk_tasks(const TNode *nd, const TNodeF *nf, const int *gnode
 // The host builder's depth-first walk emits, in visiting order, one SPJ entry
 // per unopened cell and the bodies of every opened leaf.  The same sequence
 // comes out of a breadth-first sweep that keeps a frontier of items in that
-// order: each round replaces every still-untested cell by its verdict -- an
+// order: each round replaces every still-untested cell by its outcome -- an
 // unopened cell or an opened leaf stays as a final item, an opened inner cell
 // gives way to its children in child order -- so that after the last round
 // the frontier is the depth-first output sequence.  All the CTA's threads
