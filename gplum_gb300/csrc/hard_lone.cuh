@@ -22,9 +22,10 @@
 // one CTA barrier.  k_hard_lone's shared memory request is large enough that
 // no bundle CTA shares its SM, so its warps have the FP64 unit to themselves.
 //
-// Collisions are rare: at the first block step that detects one, the state
-// as of that block step's start goes to the global state of record and the
-// team form's loop (cluster_loop) takes over from there.
+// Collisions are rare: a block step that detects one goes, as of its start,
+// to the global state of record, the team form's loop (cluster_loop,
+// one_step) integrates that block step, and the lone form reloads the result
+// -- dead members, merged targets and their twins included -- and goes on.
 #pragma once
 
 namespace p3t {
