@@ -1671,9 +1671,9 @@ int p3t_hard_integrate(int istep) {
                     return r;
                 attr = true;
             }
-            // the lone clusters and the clusters above BCAP_MAIN bodies on
-            // streams of their own, started first so that they hold SMs from the
-            // beginning (a handful of CTAs; they leave at once when there are none)
+            // the lone clusters (with CTAs of their own) and the clusters above
+            // BCAP_MAIN bodies on streams of their own, started first so that
+            // they hold SMs from the beginning (no launch when there are none)
             bool lone_k = lone && g_lone_ctas > 0;
             if ((r = cuda_status(cudaEventRecord(g_ev_launch[0], c->stream)))) return r;
             // The wide and lone CTAs must hold their SMs before the persistent
