@@ -239,6 +239,22 @@ int p3t_set_hard_tiers(int warp_min, int cta_min);
  * Both give identical results.  No counterpart in GPLUM's interface. */
 int p3t_set_hard_mode(int mode);
 /* Bundle form with the learned order: clusters whose predicted
+ * log2(1 + block steps) is at least log2_steps run first, each alone in a
+ * bundle CTA, so the longest chains of block steps do not wait on a full
+ * bundle (default 6.75, about 110 block steps; set by the autotuner from
+ * whole runs; 0 turns it off).  Results do not depend on it. */
+int p3t_set_hard_heavy(float log2_steps);
+/* Bundle form: the clusters above the bundle's member slots run in a second,
+ * concurrent launch as lone bundles of up to 512 slots, one per CTA of 512
+ * threads holding its SM, submitted before the bundle kernel (1, default), or
+ * one cluster per CTA inside the main launch (0).  Results are bit-identical;
+ * set by the autotuner. */
+int p3t_set_hard_wide(int on);
+/* Bundle form: member slots per bundle and resident CTAs per SM -- 256/2
+ * (default), 128/3 or 128/4 (clusters above the slot count go to the wide
+ * or one-per-CTA form).  Results are bit-identical; set by the autotuner. */
+int p3t_set_hard_bundle(int member_slots, int ctas_per_sm);
+/* Bundle form with the learned order: clusters whose predicted
  * log2(1 + block steps) is at least log2_steps and that have at most 64
  * members run in the lone form -- each integrated alone by one CTA that holds
  * the whole cluster in shared memory for all its block steps, with the
@@ -249,8 +265,9 @@ int p3t_set_hard_mode(int mode);
  * lone clusters run first in the bundle kernel's own CTAs (256 threads, beside
  * bundles on the SM's other CTA slot); ctas > 0: in a kernel of that many
  * 128-thread CTAs of their own, each holding a whole SM.  Perfect accretion
- * only (with fragmentation the clusters stay in the bundles); a lone cluster
- * that collides continues in the one-cluster-per-CTA form.  log2_steps = 0:
+ * only (with fragmentation the clusters stay in the bundles); a block step
+ * with a collision runs in the one-cluster-per-CTA form's loop and the lone
+ * form goes on from its result.  log2_steps = 0:
  * off (the default).  Results are bit-identical.  ctas in [0, 4096].  No
  * counterpart in GPLUM's interface. */
 int p3t_set_hard_lone(float log2_steps, int ctas);
