@@ -221,9 +221,11 @@ int p3t_hard(int istep, int col_cap, long long *col_pairs, double *edisp);
 /* p3t_hard in three stages (HardSystem::makeList / timeIntegrate / the
  * collision records, src/hard.h:321-438,554-829): enqueue orders the
  * clusters of the last p3t_cluster_label into the work queue and integrate
- * queues the launches for tree step istep, both without waiting; fetch
- * waits and returns the collision count with the pairs and the dissipated
- * energy as p3t_hard does. */
+ * queues the launches for tree step istep, both without waiting (except that
+ * integrate waits for the queue's tier sizes before it submits the wide form
+ * and the lone form's own kernel, so that their CTAs take SMs before the
+ * persistent bundle CTAs); fetch waits and returns the collision count with
+ * the pairs and the dissipated energy as p3t_hard does. */
 int p3t_hard_enqueue(void);
 int p3t_hard_integrate(int istep);
 int p3t_hard_fetch(int col_cap, long long *col_pairs, double *edisp);
